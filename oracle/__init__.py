@@ -1,0 +1,279 @@
+"""ctypes bindings for the CPU oracle (test infrastructure only).
+
+``Oracle`` wraps ``liboracle.so`` (the restatement in oracle.cpp) and
+``RefLib`` wraps ``_ref/libaxisref.so`` (the reference's own geometry headers
+compiled through the shim; present only where the reference checkout was
+available at build time). Only tests/, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of bench.py import this package.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_u64 = C.c_uint64
+
+
+def _mesh_args(m):
+    ll = np.ascontiguousarray(np.asarray(m.node_lonlat, dtype=np.float64).T).reshape(-1)  # LayoutLeft
+    return (m.n_nodes, ll, m.n_cells, np.ascontiguousarray(m.conn_offsets, dtype=np.int64),
+            np.ascontiguousarray(m.conn_indices, dtype=np.int64))
+
+
+class Weights:
+    """CSR weights + frac/area arrays as returned by the oracle."""
+
+    def __init__(self, n_src, n_dst, row, col, w, frac_a, frac_b, area_a, area_b, stats=None, seconds=None):
+        self.n_src, self.n_dst = n_src, n_dst
+        self.row, self.col, self.w = row, col, w
+        self.frac_a, self.frac_b, self.area_a, self.area_b = frac_a, frac_b, area_a, area_b
+        self.stats = stats or {}
+        self.seconds = seconds
+
+    @property
+    def nnz(self):
+        return int(self.w.shape[0])
+
+    def row_ptr(self):
+        rp = np.zeros(self.n_dst + 1, dtype=np.int64)
+        np.add.at(rp, self.row + 1, 1)
+        return np.cumsum(rp)
+
+
+class Oracle:
+    def __init__(self, path: str | None = None):
+        if path is None:
+            path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            from . import build as _b  # noqa: F401  (build recipe lives beside)
+            _b.build_oracle()
+        L = C.CDLL(path)
+        self.L = L
+        L.orc_num_threads.restype = C.c_int
+        L.orc_set_threads.argtypes = [C.c_int]
+        mesh = [C.c_int64, _f64p, C.c_int64, _i64p, _i64p]
+        L.orc_detect.argtypes = mesh + [_i32p, _i64p, _f64p]
+        L.orc_cell_prep.argtypes = mesh + [_f64p, _f64p, _f64p, _f32p, _i32p]
+        L.orc_clip.restype = C.c_double
+        L.orc_clip.argtypes = [_f64p, C.c_int, _f64p, C.c_int, _f64p, C.POINTER(C.c_int)]
+        L.orc_poly_area.restype = C.c_double
+        L.orc_poly_area.argtypes = [_f64p, C.c_int]
+        L.orc_morton_encode.restype = _u64
+        L.orc_morton_encode.argtypes = [C.c_uint32, C.c_uint32]
+        L.orc_normalize_coord.restype = C.c_uint32
+        L.orc_normalize_coord.argtypes = [C.c_double, C.c_double, C.c_double]
+        L.orc_morton_order.argtypes = mesh + [_i64p]
+        L.orc_conservative.restype = C.c_int
+        L.orc_conservative.argtypes = (mesh + [C.c_void_p, C.c_void_p] + mesh + [C.c_void_p, C.c_void_p]
+                                       + [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)])
+        L.orc_bilinear.restype = C.c_int
+        L.orc_bilinear.argtypes = mesh + mesh + [C.POINTER(C.c_void_p)]
+        L.orc_result_nnz.restype = C.c_int64
+        L.orc_result_nnz.argtypes = [C.c_void_p]
+        L.orc_result_stats.argtypes = [C.c_void_p, _i64p]
+        L.orc_result_copy.argtypes = [C.c_void_p, _i64p, _i64p, _f64p, _f64p, _f64p, _f64p, _f64p]
+        L.orc_result_free.argtypes = [C.c_void_p]
+        L.orc_apply_csr.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_int64, _f64p, C.c_int64, C.c_int64,
+                                    C.c_int]
+        L.orc_apply_coo_atomic.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_int64, _f64p, C.c_int64,
+                                           C.c_int64, C.c_int64]
+        L.orc_conservation.argtypes = [C.c_int64, _f64p, _f64p, _f64p, C.c_int64, _f64p, _f64p, _f64p, C.c_int,
+                                       _f64p]
+
+    def threads(self, n: int | None = None) -> int:
+        if n is not None:
+            self.L.orc_set_threads(int(n))
+        return self.L.orc_num_threads()
+
+    def detect(self, m):
+        f = np.zeros(2, np.int32)
+        d = np.zeros(2, np.int64)
+        v = np.zeros(4, np.float64)
+        self.L.orc_detect(*_mesh_args(m), f, d, v)
+        return dict(regular=bool(f[0]), rectilinear=bool(f[1]), ni=int(d[0]), nj=int(d[1]), lon_min=v[0],
+                    dlon=v[1], lat_min=v[2], dlat=v[3])
+
+    def cell_prep(self, m):
+        n = m.n_cells
+        area = np.zeros(n)
+        cc = np.zeros(3 * n)
+        cr = np.zeros(n)
+        box = np.zeros(6 * n, np.float32)
+        deg = np.zeros(n, np.int32)
+        self.L.orc_cell_prep(*_mesh_args(m), area, cc, cr, box, deg)
+        return dict(area=area, cap_c=cc.reshape(n, 3), cap_r=cr, box=box.reshape(n, 6), degen=deg)
+
+    def clip(self, subj, clipp):
+        s = np.ascontiguousarray(subj, np.float64).reshape(-1)
+        c = np.ascontiguousarray(clipp, np.float64).reshape(-1)
+        out = np.zeros(32 * 3)
+        n = C.c_int(0)
+        a = self.L.orc_clip(s, len(s) // 3, c, len(c) // 3, out, C.byref(n))
+        return a, out[: 3 * n.value].reshape(-1, 3)
+
+    def poly_area(self, xyz):
+        x = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        return self.L.orc_poly_area(x, len(x) // 3)
+
+    def morton_encode(self, x, y):
+        return int(self.L.orc_morton_encode(x, y))
+
+    def normalize_coord(self, v, lo, hi):
+        return int(self.L.orc_normalize_coord(v, lo, hi))
+
+    def morton_order(self, m):
+        p = np.zeros(m.n_cells, np.int64)
+        self.L.orc_morton_order(*_mesh_args(m), p)
+        return p
+
+    def _result(self, h, seconds):
+        nnz = self.L.orc_result_nnz(h)
+        st = np.zeros(3, np.int64)
+        self.L.orc_result_stats(h, st)
+        return nnz, st
+
+    def conservative(self, src, dst, norm_type: int = 0, unmapped: int = 1, faithful: bool = False) -> Weights:
+        h = C.c_void_p()
+        t0 = time.perf_counter()
+        rc = self.L.orc_conservative(*_mesh_args(src), None, None, *_mesh_args(dst), None, None, norm_type, unmapped,
+                                     int(faithful), C.byref(h))
+        dt = time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError(f"oracle conservative failed rc={rc}")
+        return self._collect(h, src.n_cells, dst.n_cells, dt)
+
+    def bilinear(self, src, dst) -> Weights:
+        h = C.c_void_p()
+        t0 = time.perf_counter()
+        rc = self.L.orc_bilinear(*_mesh_args(src), *_mesh_args(dst), C.byref(h))
+        dt = time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError(f"oracle bilinear failed rc={rc}")
+        return self._collect(h, src.n_cells, dst.n_cells, dt)
+
+    def _collect(self, h, n_src, n_dst, dt):
+        nnz = self.L.orc_result_nnz(h)
+        st = np.zeros(3, np.int64)
+        self.L.orc_result_stats(h, st)
+        row = np.zeros(nnz, np.int64)
+        col = np.zeros(nnz, np.int64)
+        w = np.zeros(nnz)
+        fa = np.zeros(n_src)
+        fb = np.zeros(n_dst)
+        aa = np.zeros(n_src)
+        ab = np.zeros(n_dst)
+        self.L.orc_result_copy(h, row, col, w, fa, fb, aa, ab)
+        self.L.orc_result_free(h)
+        return Weights(n_src, n_dst, row, col, w, fa, fb, aa, ab,
+                       stats=dict(box_pairs=int(st[0]), cap_pass=int(st[1]), clipped=int(st[2])), seconds=dt)
+
+    def apply_csr(self, wts: Weights, x, compensated: bool = True):
+        """x: [nrhs, n_src] float64 (row-major = one field per row)."""
+        x = np.ascontiguousarray(np.atleast_2d(x), np.float64)
+        nrhs = x.shape[0]
+        y = np.zeros((nrhs, wts.n_dst))
+        self.L.orc_apply_csr(wts.n_dst, wts.row_ptr(), np.ascontiguousarray(wts.col), np.ascontiguousarray(wts.w),
+                             x.reshape(-1), x.shape[1], y.reshape(-1), wts.n_dst, nrhs, int(compensated))
+        return y
+
+    def apply_coo_atomic(self, wts: Weights, x):
+        x = np.ascontiguousarray(np.atleast_2d(x), np.float64)
+        nrhs = x.shape[0]
+        y = np.zeros((nrhs, wts.n_dst))
+        self.L.orc_apply_coo_atomic(wts.nnz, np.ascontiguousarray(wts.row), np.ascontiguousarray(wts.col),
+                                    np.ascontiguousarray(wts.w), x.reshape(-1), x.shape[1], y.reshape(-1), wts.n_dst,
+                                    wts.n_dst, nrhs)
+        return y
+
+    def conservation(self, wts: Weights, src, dst, norm_type: int = 0):
+        out = np.zeros(4)
+        self.L.orc_conservation(wts.n_src, np.ascontiguousarray(src, np.float64), wts.area_a, wts.frac_a, wts.n_dst,
+                                np.ascontiguousarray(dst, np.float64), wts.area_b, wts.frac_b, norm_type, out)
+        return dict(src_integral=out[0], dst_integral=out[1], absolute_error=out[2], relative_error=out[3])
+
+
+class RefLib:
+    """The reference's geometry headers compiled through the shim."""
+
+    def __init__(self, path: str | None = None):
+        if path is None:
+            path = os.path.join(HERE, "_ref", "libaxisref.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = C.CDLL(path)
+        self.L = L
+        mesh = [C.c_int64, _f64p, C.c_int64, _i64p, _i64p]
+        L.ref_cell_prep.argtypes = mesh + [_f64p, _f64p, _f64p, _f32p, _i32p]
+        L.ref_detect.argtypes = mesh + [_i32p, _i64p, _f64p]
+        L.ref_morton_order.argtypes = mesh + [_i64p]
+        L.ref_morton_encode.restype = _u64
+        L.ref_morton_encode.argtypes = [C.c_uint32, C.c_uint32]
+        L.ref_normalize_coord.restype = C.c_uint32
+        L.ref_normalize_coord.argtypes = [C.c_double, C.c_double, C.c_double]
+        L.ref_clip.restype = C.c_double
+        L.ref_clip.argtypes = [_f64p, C.c_int, _f64p, C.c_int, _f64p, C.POINTER(C.c_int)]
+        L.ref_conservative.argtypes = mesh + mesh + [C.c_int64, C.POINTER(C.c_int64), _i64p, _i64p, _f64p, _f64p,
+                                                     _f64p, _f64p, _f64p]
+
+    def cell_prep(self, m):
+        n = m.n_cells
+        area = np.zeros(n)
+        cc = np.zeros(3 * n)
+        cr = np.zeros(n)
+        box = np.zeros(6 * n, np.float32)
+        deg = np.zeros(n, np.int32)
+        self.L.ref_cell_prep(*_mesh_args(m), area, cc, cr, box, deg)
+        return dict(area=area, cap_c=cc.reshape(n, 3), cap_r=cr, box=box.reshape(n, 6), degen=deg)
+
+    def detect(self, m):
+        f = np.zeros(2, np.int32)
+        d = np.zeros(2, np.int64)
+        v = np.zeros(4, np.float64)
+        self.L.ref_detect(*_mesh_args(m), f, d, v)
+        return dict(regular=bool(f[0]), rectilinear=bool(f[1]), ni=int(d[0]), nj=int(d[1]), lon_min=v[0],
+                    dlon=v[1], lat_min=v[2], dlat=v[3])
+
+    def morton_order(self, m):
+        p = np.zeros(m.n_cells, np.int64)
+        self.L.ref_morton_order(*_mesh_args(m), p)
+        return p
+
+    def morton_encode(self, x, y):
+        return int(self.L.ref_morton_encode(x, y))
+
+    def normalize_coord(self, v, lo, hi):
+        return int(self.L.ref_normalize_coord(v, lo, hi))
+
+    def clip(self, subj, clipp):
+        s = np.ascontiguousarray(subj, np.float64).reshape(-1)
+        c = np.ascontiguousarray(clipp, np.float64).reshape(-1)
+        out = np.zeros(32 * 3)
+        n = C.c_int(0)
+        a = self.L.ref_clip(s, len(s) // 3, c, len(c) // 3, out, C.byref(n))
+        return a, out[: 3 * n.value].reshape(-1, 3)
+
+    def conservative(self, src, dst) -> Weights:
+        cap = 64 * dst.n_cells + 1024
+        nnz = C.c_int64(0)
+        row = np.zeros(cap, np.int64)
+        col = np.zeros(cap, np.int64)
+        w = np.zeros(cap)
+        fa = np.zeros(src.n_cells)
+        fb = np.zeros(dst.n_cells)
+        aa = np.zeros(src.n_cells)
+        ab = np.zeros(dst.n_cells)
+        self.L.ref_conservative(*_mesh_args(src), *_mesh_args(dst), cap, C.byref(nnz), row, col, w, fa, fb, aa, ab)
+        n = nnz.value
+        if n > cap:
+            raise RuntimeError("reference result larger than buffer")
+        return Weights(src.n_cells, dst.n_cells, row[:n], col[:n], w[:n], fa, fb, aa, ab)

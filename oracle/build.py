@@ -1,0 +1,57 @@
+"""Build recipe for the CPU oracle (test infrastructure).
+
+* ``oracle/liboracle.so``      the C++ restatement in oracle.cpp (always).
+* ``oracle/_ref/libaxisref.so`` the reference's own header-only geometry code
+  compiled unchanged from the reference checkout through the host shim in
+  ``oracle/ref_shim`` plus the glue in ``ref_driver.cpp``; built only when the
+  reference checkout exists (never on machines without it).
+
+Both use ``-O2 -ffp-contract=off`` so double expressions are evaluated as
+written, like the reference's host build.
+"""
+
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_INCLUDE = "/root/reference/libs/axis/include"
+FLAGS = ["-std=c++20", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp"]
+
+
+def _needs(out: str, srcs: list[str]) -> bool:
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle.cpp")
+    out = os.path.join(HERE, "liboracle.so")
+    if force or _needs(out, [src]):
+        subprocess.check_call(["g++", *FLAGS, src, "-o", out])
+    return out
+
+
+def build_ref(force: bool = False) -> str | None:
+    if not os.path.isdir(REF_INCLUDE):
+        return None
+    src = os.path.join(HERE, "ref_driver.cpp")
+    shim = os.path.join(HERE, "ref_shim")
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libaxisref.so")
+    deps = [src] + [os.path.join(shim, f) for f in ("Kokkos_Core.hpp", "mdspan/mdspan.hpp")]
+    if force or _needs(out, deps):
+        subprocess.check_call(["g++", *[f for f in FLAGS if f != "-fopenmp"], "-I", shim, "-I", REF_INCLUDE, src,
+                               "-o", out])
+    return out
+
+
+if __name__ == "__main__":
+    force = "--force" in sys.argv
+    print(build_oracle(force))
+    print(build_ref(force))

@@ -1,0 +1,967 @@
+// CPU oracle for the AXIS regridding hot path.
+//
+// TEST INFRASTRUCTURE ONLY. This file restates, in plain C++ with OpenMP,
+// the reference algorithm of AXIS (HELM) for first-order conservative
+// great-circle weights, rectilinear bilinear weights, the CSR apply and the
+// conservation report. Only the test suite, the smoke check and the CPU
+// baseline leg of the benchmark load it (as liboracle.so through ctypes),
+// always as the checker and never as the code under test. Nothing in the
+// product library links or calls it.
+//
+// Citations use paths inside the AXIS library (libs/axis/ of HELM).
+// Build flags: -O2 -ffp-contract=off so every double expression is
+// evaluated exactly as written (no FMA contraction), matching the reference
+// built for its OpenMP host space.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+using i64 = std::int64_t;
+
+constexpr double kPi = 3.14159265358979323846;
+// deg2rad as the compile-time constant pi/180 used by the clipper-polygon
+// extraction (src/solver/weight_generator.cpp:463), the cap filter
+// (include/axis/detail/spherical_cap_filter.hpp:47) and the degenerate scan
+// (include/axis/detail/degenerate_cell_handler.hpp:205).
+constexpr double kDeg2Rad = kPi / 180.0;
+
+struct V3 {
+    double x, y, z;
+};
+
+// Operation order of include/axis/detail/spherical_clipper.hpp:39-88.
+inline double dot3(const V3 &a, const V3 &b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross3(const V3 &a, const V3 &b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline double lensq3(const V3 &v) { return v.x * v.x + v.y * v.y + v.z * v.z; }
+inline V3 normalize3(const V3 &v) {
+    double len = std::sqrt(lensq3(v));
+    if (len < 1.0e-300) return {0.0, 0.0, 0.0};
+    double inv = 1.0 / len;
+    return {v.x * inv, v.y * inv, v.z * inv};
+}
+inline V3 add3(const V3 &a, const V3 &b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+
+// Fixed-capacity polygon, pushes past the capacity are dropped
+// (spherical_clipper.hpp:100-156).
+constexpr int kCap = 32;
+struct Poly {
+    V3 v[kCap];
+    int n = 0;
+    void push(const V3 &p) {
+        if (n < kCap) v[n++] = p;
+    }
+};
+
+// Van Oosterom-Strackee fan from vertex 0, |sum| (spherical_clipper.hpp:112-137).
+double poly_area(const Poly &p) {
+    if (p.n < 3) return 0.0;
+    double total = 0.0;
+    const V3 &a = p.v[0];
+    for (int i = 1; i < p.n - 1; ++i) {
+        const V3 &b = p.v[i];
+        const V3 &c = p.v[i + 1];
+        double ab = dot3(a, b);
+        double ac = dot3(a, c);
+        double bc = dot3(b, c);
+        V3 bxc = cross3(b, c);
+        double num = dot3(a, bxc);
+        double den = 1.0 + ab + ac + bc;
+        double tri = 2.0 * std::atan2(num, den);
+        total += tri;
+    }
+    return std::fabs(total);
+}
+
+// Intersection of arc v1->v2 with the great circle (ea, eb), midpoint
+// fallback for parallel planes (spherical_clipper.hpp:265-295).
+V3 arc_cross(const V3 &v1, const V3 &v2, const V3 &ea, const V3 &eb) {
+    V3 n1 = cross3(ea, eb);
+    V3 n2 = cross3(v1, v2);
+    V3 d = cross3(n1, n2);
+    double dl = lensq3(d);
+    if (dl < 1.0e-30) return normalize3(add3(v1, v2));
+    V3 c = normalize3(d);
+    V3 mid = normalize3(add3(v1, v2));
+    if (dot3(c, mid) < 0.0) c = {-c.x, -c.y, -c.z};
+    return c;
+}
+
+// One Sutherland-Hodgman step with the inclusive eps = -1e-14
+// (spherical_clipper.hpp:301-335).
+void clip_edge(const Poly &in, const V3 &nrm, const V3 &ea, const V3 &eb, Poly &out) {
+    if (in.n < 1) return;
+    constexpr double eps = -1.0e-14;
+    for (int i = 0; i < in.n; ++i) {
+        int pi = (i + in.n - 1) % in.n;
+        const V3 &cur = in.v[i];
+        const V3 &prv = in.v[pi];
+        double dc = dot3(nrm, cur);
+        double dp = dot3(nrm, prv);
+        bool ci = dc >= eps;
+        bool pin = dp >= eps;
+        if (ci) {
+            if (!pin) out.push(arc_cross(prv, cur, ea, eb));
+            out.push(cur);
+        } else if (pin) {
+            out.push(arc_cross(prv, cur, ea, eb));
+        }
+    }
+}
+
+// Clip subject by every edge of clip_poly, skipping edges with
+// |a x b|^2 < 1e-30 (spherical_clipper.hpp:181-229).
+Poly clip_poly(const Poly &subject, const Poly &cp) {
+    Poly empty;
+    if (subject.n < 3 || cp.n < 3) return empty;
+    Poly a = subject, b;
+    for (int ci = 0; ci < cp.n; ++ci) {
+        const V3 &ea = cp.v[ci];
+        const V3 &eb = cp.v[(ci + 1) % cp.n];
+        V3 nrm = cross3(ea, eb);
+        if (lensq3(nrm) < 1.0e-30) continue;
+        b.n = 0;
+        clip_edge(a, nrm, ea, eb, b);
+        a.n = b.n;
+        for (int i = 0; i < b.n; ++i) a.v[i] = b.v[i];
+        if (a.n < 3) return empty;
+    }
+    return a;
+}
+
+double overlap_area(const Poly &src, const Poly &dst) { return poly_area(clip_poly(src, dst)); }
+
+// ─── Mesh view ──────────────────────────────────────────────────────────────
+
+struct Mesh {
+    i64 n_nodes, n_cells;
+    const double *lonlat;  // LayoutLeft [n_nodes, 2]: lon at [i], lat at [i + n_nodes]
+    const i64 *off;
+    const i64 *idx;
+    const double *areas;  // optional precomputed areas (may be null)
+    const int *mask;      // optional cell mask (may be null)
+    double lon(i64 n) const { return lonlat[n]; }
+    double lat(i64 n) const { return lonlat[n + n_nodes]; }
+};
+
+// Node xyz with the deg2rad constant: lonlat_to_xyz
+// (include/axis/detail/spherical_geometry.hpp:80-83).
+std::vector<V3> node_xyz(const Mesh &m) {
+    std::vector<V3> out(m.n_nodes);
+#pragma omp parallel for schedule(static)
+    for (i64 n = 0; n < m.n_nodes; ++n) {
+        double lo = m.lon(n) * kDeg2Rad;
+        double la = m.lat(n) * kDeg2Rad;
+        double cl = std::cos(la);
+        out[n] = {cl * std::cos(lo), cl * std::sin(lo), std::sin(la)};
+    }
+    return out;
+}
+
+Poly cell_poly(const Mesh &m, const std::vector<V3> &xyz, i64 c) {
+    Poly p;
+    for (i64 k = m.off[c]; k < m.off[c + 1]; ++k) p.push(xyz[m.idx[k]]);
+    return p;
+}
+
+// ─── Regular / rectilinear detection (include/axis/detail/regular_grid_detector.hpp:64-299)
+
+struct GridInfo {
+    bool regular = false, rectilinear = false;
+    double lon_min = 0, lon_max = 0, dlon = 0, lat_min = 0, lat_max = 0, dlat = 0;
+    i64 ni = 0, nj = 0;
+    std::vector<double> ulon, ulat;  // tolerance-unique sorted node coordinates
+};
+
+std::vector<double> unique_tol(std::vector<double> v) {
+    std::sort(v.begin(), v.end());
+    std::vector<double> u;
+    if (v.empty()) return u;
+    u.push_back(v[0]);
+    for (size_t i = 1; i < v.size(); ++i)
+        if (std::abs(v[i] - u.back()) > 1.0e-12) u.push_back(v[i]);
+    return u;
+}
+
+bool uniform(const std::vector<double> &d) {
+    if (d.empty()) return false;
+    double mn = d[0], mx = d[0], s = 0.0;
+    for (double x : d) {
+        mn = std::min(mn, x);
+        mx = std::max(mx, x);
+        s += x;
+    }
+    if (mn <= 0.0) return false;
+    double mean = s / static_cast<double>(d.size());
+    return (mx - mn) < 1.0e-10 * mean;
+}
+
+GridInfo detect(const Mesh &m) {
+    GridInfo g;
+    if (m.n_cells == 0) return g;
+    for (i64 c = 0; c < m.n_cells; ++c)
+        if (m.off[c + 1] - m.off[c] != 4) return g;
+    std::vector<double> lo(m.n_nodes), la(m.n_nodes);
+    for (i64 n = 0; n < m.n_nodes; ++n) {
+        lo[n] = m.lon(n);
+        la[n] = m.lat(n);
+    }
+    g.ulon = unique_tol(std::move(lo));
+    g.ulat = unique_tol(std::move(la));
+    if (g.ulon.size() < 2 || g.ulat.size() < 2) return g;
+    i64 ni = static_cast<i64>(g.ulon.size()) - 1, nj = static_cast<i64>(g.ulat.size()) - 1;
+    if (ni * nj != m.n_cells) return g;
+    g.rectilinear = true;
+    g.ni = ni;
+    g.nj = nj;
+    std::vector<double> dl(ni), dt(nj);
+    for (i64 i = 0; i < ni; ++i) dl[i] = g.ulon[i + 1] - g.ulon[i];
+    for (i64 j = 0; j < nj; ++j) dt[j] = g.ulat[j + 1] - g.ulat[j];
+    if (!uniform(dl) || !uniform(dt)) return g;
+    double sl = 0.0, st = 0.0;
+    for (double d : dl) sl += d;
+    for (double d : dt) st += d;
+    g.regular = true;
+    g.lon_min = g.ulon.front();
+    g.lon_max = g.ulon.back();
+    g.dlon = sl / static_cast<double>(ni);
+    g.lat_min = g.ulat.front();
+    g.lat_max = g.ulat.back();
+    g.dlat = st / static_cast<double>(nj);
+    return g;
+}
+
+// Node trig cache polygons for regular grids: vertex (i,j) at
+// (lon_min + i*dlon, lat_min + j*dlat), cell (ci,cj) = (c % ni, c / ni)
+// (include/axis/detail/trig_cache.hpp:210-289,
+//  src/solver/weight_generator.cpp:492-520).
+struct TrigCache {
+    bool valid = false;
+    i64 ni = 0, nj = 0;
+    std::vector<double> slon, clon, slat, clat;
+};
+
+TrigCache build_trig(const GridInfo &g) {
+    TrigCache t;
+    if (!g.regular || g.ni == 0 || g.nj == 0) return t;
+    t.ni = g.ni;
+    t.nj = g.nj;
+    t.slon.resize(g.ni + 1);
+    t.clon.resize(g.ni + 1);
+    t.slat.resize(g.nj + 1);
+    t.clat.resize(g.nj + 1);
+    for (i64 i = 0; i <= g.ni; ++i) {
+        double r = (g.lon_min + static_cast<double>(i) * g.dlon) * kDeg2Rad;
+        t.slon[i] = std::sin(r);
+        t.clon[i] = std::cos(r);
+    }
+    for (i64 j = 0; j <= g.nj; ++j) {
+        double r = (g.lat_min + static_cast<double>(j) * g.dlat) * kDeg2Rad;
+        t.slat[j] = std::sin(r);
+        t.clat[j] = std::cos(r);
+    }
+    t.valid = true;
+    return t;
+}
+
+Poly trig_poly(const TrigCache &t, i64 c) {
+    i64 ci = c % t.ni, cj = c / t.ni;
+    auto at = [&](i64 i, i64 j) {
+        double cl = t.clat[j];
+        return V3{cl * t.clon[i], cl * t.slon[i], t.slat[j]};
+    };
+    Poly p;
+    p.push(at(ci, cj));
+    p.push(at(ci + 1, cj));
+    p.push(at(ci + 1, cj + 1));
+    p.push(at(ci, cj + 1));
+    return p;
+}
+
+// ─── Degenerate classification (include/axis/detail/degenerate_cell_handler.hpp:115-142, 259-367)
+
+int count_unique(const Poly &p, double thr) {
+    if (p.n < 1) return 0;
+    double t2 = thr * thr;
+    int u = 1;
+    for (int i = 1; i < p.n; ++i) {
+        bool dup = false;
+        for (int j = 0; j < i; ++j) {
+            V3 d{p.v[i].x - p.v[j].x, p.v[i].y - p.v[j].y, p.v[i].z - p.v[j].z};
+            if (lensq3(d) < t2) {
+                dup = true;
+                break;
+            }
+        }
+        if (!dup) ++u;
+    }
+    return u;
+}
+
+bool arcs_cross(const V3 &a, const V3 &b, const V3 &c, const V3 &d) {
+    V3 nab = cross3(a, b);
+    double dc = dot3(nab, c), dd = dot3(nab, d);
+    if (dc * dd >= 0.0) return false;
+    V3 ncd = cross3(c, d);
+    double da = dot3(ncd, a), db = dot3(ncd, b);
+    if (da * db >= 0.0) return false;
+    return true;
+}
+
+bool self_intersecting(const Poly &p) {
+    if (p.n < 4) return false;
+    for (int i = 0; i < p.n; ++i) {
+        int in = (i + 1) % p.n;
+        for (int j = i + 2; j < p.n; ++j) {
+            int jn = (j + 1) % p.n;
+            if (jn == i) continue;
+            if (arcs_cross(p.v[i], p.v[in], p.v[j], p.v[jn])) return true;
+        }
+    }
+    return false;
+}
+
+// 0 none, 1 zero area, 2 collapsed edge, 3 self-intersecting
+int classify(const Poly &p) {
+    if (p.n < 3) return 1;
+    if (poly_area(p) < 1e-25) return 1;
+    if (count_unique(p, 1e-15) < 3) return 2;
+    if (self_intersecting(p)) return 3;
+    return 0;
+}
+
+// ─── Float AABB of src/solver/weight_generator.cpp:198-262 (lon*pi/180.0 trig)
+
+struct FBox {
+    float lo[3], hi[3];
+};
+
+std::vector<FBox> cell_boxes(const Mesh &m) {
+    std::vector<FBox> b(m.n_cells);
+#pragma omp parallel for schedule(static)
+    for (i64 c = 0; c < m.n_cells; ++c) {
+        double mn[3] = {std::numeric_limits<double>::max(), std::numeric_limits<double>::max(),
+                        std::numeric_limits<double>::max()};
+        double mx[3] = {-std::numeric_limits<double>::max(), -std::numeric_limits<double>::max(),
+                        -std::numeric_limits<double>::max()};
+        for (i64 k = m.off[c]; k < m.off[c + 1]; ++k) {
+            i64 n = m.idx[k];
+            double lo = m.lon(n) * kPi / 180.0;
+            double la = m.lat(n) * kPi / 180.0;
+            double p[3] = {std::cos(la) * std::cos(lo), std::cos(la) * std::sin(lo), std::sin(la)};
+            for (int d = 0; d < 3; ++d) {
+                mn[d] = std::min(mn[d], p[d]);
+                mx[d] = std::max(mx[d], p[d]);
+            }
+        }
+        double ext = std::max({mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]});
+        double eps = std::min(std::max(0.25 * ext, 1.0e-6), 0.02);
+        for (int d = 0; d < 3; ++d) {
+            b[c].lo[d] = static_cast<float>(mn[d] - eps);
+            b[c].hi[d] = static_cast<float>(mx[d] + eps);
+        }
+    }
+    return b;
+}
+
+inline bool boxes_meet(const FBox &a, const FBox &b) {
+    for (int d = 0; d < 3; ++d)
+        if (a.lo[d] > b.hi[d] || a.hi[d] < b.lo[d]) return false;
+    return true;
+}
+
+// Exact closed-interval box query (replaces the ArborX BVH; the candidate SET
+// is what matters, its order is set by sorting below). A sparse uniform grid
+// over [-1,1]^3 buckets the source boxes.
+struct BoxIndex {
+    double h;
+    int G;
+    std::vector<std::pair<i64, int>> cells;  // (key, src id) sorted by key
+    i64 key(int x, int y, int z) const { return (static_cast<i64>(x) * G + y) * G + z; }
+    int q(float v) const {
+        int r = static_cast<int>(std::floor((static_cast<double>(v) + 1.5) / h));
+        return std::max(0, std::min(G - 1, r));
+    }
+};
+
+BoxIndex build_index(const std::vector<FBox> &bx) {
+    BoxIndex ix;
+    std::vector<double> ext(bx.size());
+    for (size_t i = 0; i < bx.size(); ++i)
+        ext[i] = std::max({bx[i].hi[0] - bx[i].lo[0], bx[i].hi[1] - bx[i].lo[1], bx[i].hi[2] - bx[i].lo[2]});
+    double med = 0.1;
+    if (!ext.empty()) {
+        std::nth_element(ext.begin(), ext.begin() + ext.size() / 2, ext.end());
+        med = ext[ext.size() / 2];
+    }
+    ix.h = std::max(med, 3.0 / 2048.0);
+    ix.G = static_cast<int>(std::ceil(3.0 / ix.h)) + 1;
+    std::vector<std::vector<std::pair<i64, int>>> parts(1);
+#ifdef _OPENMP
+    parts.resize(omp_get_max_threads());
+#endif
+#pragma omp parallel
+    {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+#pragma omp for schedule(static)
+        for (i64 i = 0; i < static_cast<i64>(bx.size()); ++i) {
+            int x0 = ix.q(bx[i].lo[0]), x1 = ix.q(bx[i].hi[0]);
+            int y0 = ix.q(bx[i].lo[1]), y1 = ix.q(bx[i].hi[1]);
+            int z0 = ix.q(bx[i].lo[2]), z1 = ix.q(bx[i].hi[2]);
+            for (int x = x0; x <= x1; ++x)
+                for (int y = y0; y <= y1; ++y)
+                    for (int z = z0; z <= z1; ++z) parts[t].push_back({ix.key(x, y, z), static_cast<int>(i)});
+        }
+    }
+    for (auto &p : parts) ix.cells.insert(ix.cells.end(), p.begin(), p.end());
+    std::sort(ix.cells.begin(), ix.cells.end());
+    return ix;
+}
+
+void query_index(const BoxIndex &ix, const std::vector<FBox> &sb, const FBox &q, std::vector<int> &out) {
+    out.clear();
+    int x0 = ix.q(q.lo[0]), x1 = ix.q(q.hi[0]);
+    int y0 = ix.q(q.lo[1]), y1 = ix.q(q.hi[1]);
+    int z0 = ix.q(q.lo[2]), z1 = ix.q(q.hi[2]);
+    for (int x = x0; x <= x1; ++x)
+        for (int y = y0; y <= y1; ++y)
+            for (int z = z0; z <= z1; ++z) {
+                i64 k = ix.key(x, y, z);
+                auto it = std::lower_bound(ix.cells.begin(), ix.cells.end(), std::make_pair(k, -1));
+                for (; it != ix.cells.end() && it->first == k; ++it)
+                    if (boxes_meet(sb[it->second], q)) out.push_back(it->second);
+            }
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+}
+
+// ─── Spherical caps (include/axis/detail/spherical_cap_filter.hpp:85-197)
+
+struct Caps {
+    std::vector<V3> c;
+    std::vector<double> r;
+};
+
+Caps cell_caps(const Mesh &m, const std::vector<V3> &xyz) {
+    Caps k;
+    k.c.resize(m.n_cells);
+    k.r.resize(m.n_cells);
+#pragma omp parallel for schedule(static)
+    for (i64 c = 0; c < m.n_cells; ++c) {
+        i64 b = m.off[c], e = m.off[c + 1];
+        int nv = static_cast<int>(e - b);
+        if (nv < 1) {
+            k.c[c] = {0, 0, 0};
+            k.r[c] = 0.0;
+            continue;
+        }
+        double sx = 0, sy = 0, sz = 0;
+        for (i64 q = b; q < e; ++q) {
+            const V3 &p = xyz[m.idx[q]];
+            sx += p.x;
+            sy += p.y;
+            sz += p.z;
+        }
+        double inv = 1.0 / static_cast<double>(nv);
+        V3 cen = normalize3({sx * inv, sy * inv, sz * inv});
+        double mx = 0.0;
+        for (i64 q = b; q < e; ++q) {
+            double d = dot3(cen, xyz[m.idx[q]]);
+            d = std::fmin(1.0, std::fmax(-1.0, d));
+            double a = std::acos(d);
+            if (a > mx) mx = a;
+        }
+        k.c[c] = cen;
+        k.r[c] = mx;
+    }
+    return k;
+}
+
+inline bool cap_rejects(const V3 &cs, double rs, const V3 &cd, double rd) {
+    double cd_ = dot3(cs, cd);
+    cd_ = std::fmin(1.0, std::fmax(-1.0, cd_));
+    return std::acos(cd_) > (rs + rd);
+}
+
+// ─── Morton processing order (include/axis/detail/morton_sort.hpp:43-176,
+//     src/solver/weight_generator.cpp:75-125)
+
+inline std::uint64_t spread16(std::uint32_t v) {
+    std::uint64_t r = v;
+    r = (r | (r << 16)) & 0x0000FFFF0000FFFFull;
+    r = (r | (r << 8)) & 0x00FF00FF00FF00FFull;
+    r = (r | (r << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    r = (r | (r << 2)) & 0x3333333333333333ull;
+    r = (r | (r << 1)) & 0x5555555555555555ull;
+    return r;
+}
+inline std::uint64_t morton2(std::uint32_t x, std::uint32_t y) { return spread16(x) | (spread16(y) << 1); }
+inline std::uint32_t norm16(double v, double lo, double hi) {
+    constexpr std::uint32_t N = (1u << 16) - 1;
+    if (hi <= lo) return 0;
+    double t = (v - lo) / (hi - lo);
+    t = std::fmax(0.0, std::fmin(1.0, t));
+    return static_cast<std::uint32_t>(t * N);
+}
+
+std::vector<i64> morton_order(const Mesh &m) {
+    std::vector<double> cx(m.n_cells), cy(m.n_cells);
+    for (i64 c = 0; c < m.n_cells; ++c) {
+        i64 b = m.off[c], e = m.off[c + 1];
+        double sx = 0, sy = 0, sz = 0;
+        for (i64 q = b; q < e; ++q) {
+            double lo = m.lon(m.idx[q]) * kPi / 180.0;
+            double la = m.lat(m.idx[q]) * kPi / 180.0;
+            sx += std::cos(la) * std::cos(lo);
+            sy += std::cos(la) * std::sin(lo);
+            sz += std::sin(la);
+        }
+        double inv = (e - b > 0) ? 1.0 / static_cast<double>(e - b) : 0.0;
+        double ax = sx * inv, ay = sy * inv, az = sz * inv;
+        double lat = std::asin(az);
+        double lon = std::atan2(ay, ax);
+        if (lon < 0.0) lon += 2.0 * kPi;
+        cx[c] = lon * 180.0 / kPi;
+        cy[c] = lat * 180.0 / kPi;
+    }
+    std::vector<i64> perm(m.n_cells);
+    std::iota(perm.begin(), perm.end(), 0);
+    if (m.n_cells == 0) return perm;
+    // Kokkos Min/Max reducers start from their identities, so these are the
+    // true extremes (morton_sort.hpp:114-131).
+    double xlo = std::numeric_limits<double>::max(), xhi = -std::numeric_limits<double>::max();
+    double ylo = xlo, yhi = xhi;
+    for (i64 c = 0; c < m.n_cells; ++c) {
+        xlo = std::min(xlo, cx[c]);
+        xhi = std::max(xhi, cx[c]);
+        ylo = std::min(ylo, cy[c]);
+        yhi = std::max(yhi, cy[c]);
+    }
+    std::vector<std::uint64_t> key(m.n_cells);
+    for (i64 c = 0; c < m.n_cells; ++c) key[c] = morton2(norm16(cx[c], xlo, xhi), norm16(cy[c], ylo, yhi));
+    // std::sort with the reference's comparator (morton_sort.hpp:170): the
+    // same libstdc++ introsort breaks ties the same way.
+    std::sort(perm.begin(), perm.end(), [&](i64 a, i64 b) { return key[a] < key[b]; });
+    return perm;
+}
+
+}  // namespace
+
+// ─────────────────────────────────────────────────────────────────────────────
+// C ABI for ctypes
+// ─────────────────────────────────────────────────────────────────────────────
+
+struct orc_result {
+    i64 n_src = 0, n_dst = 0;
+    std::vector<i64> row, col;  // CSR order: sorted by (row, col)
+    std::vector<double> w, frac_a, frac_b, area_a, area_b;
+    i64 n_box_pairs = 0, n_cap_pass = 0, n_clipped = 0;
+    double seconds = 0.0;
+};
+
+extern "C" {
+
+int orc_num_threads() {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+// Detection report: flags[0]=regular, flags[1]=rectilinear; dims = (ni, nj);
+// vals = (lon_min, dlon, lat_min, dlat).
+int orc_detect(i64 n_nodes, const double *lonlat, i64 n_cells, const i64 *off, const i64 *idx, int *flags, i64 *dims,
+               double *vals) {
+    Mesh m{n_nodes, n_cells, lonlat, off, idx, nullptr, nullptr};
+    GridInfo g = detect(m);
+    flags[0] = g.regular;
+    flags[1] = g.rectilinear;
+    dims[0] = g.ni;
+    dims[1] = g.nj;
+    vals[0] = g.lon_min;
+    vals[1] = g.dlon;
+    vals[2] = g.lat_min;
+    vals[3] = g.dlat;
+    return 0;
+}
+
+// Per-cell products: areas, cap centroids [n,3] and radii, float boxes [n,6],
+// degenerate class.
+int orc_cell_prep(i64 n_nodes, const double *lonlat, i64 n_cells, const i64 *off, const i64 *idx, double *area,
+                  double *cap_c, double *cap_r, float *box, int *degen) {
+    Mesh m{n_nodes, n_cells, lonlat, off, idx, nullptr, nullptr};
+    auto xyz = node_xyz(m);
+    auto caps = cell_caps(m, xyz);
+    auto bx = cell_boxes(m);
+#pragma omp parallel for schedule(static)
+    for (i64 c = 0; c < n_cells; ++c) {
+        Poly p = cell_poly(m, xyz, c);
+        area[c] = poly_area(p);
+        degen[c] = classify(p);
+        cap_c[3 * c] = caps.c[c].x;
+        cap_c[3 * c + 1] = caps.c[c].y;
+        cap_c[3 * c + 2] = caps.c[c].z;
+        cap_r[c] = caps.r[c];
+        for (int d = 0; d < 3; ++d) {
+            box[6 * c + d] = bx[c].lo[d];
+            box[6 * c + 3 + d] = bx[c].hi[d];
+        }
+    }
+    return 0;
+}
+
+// Clip two polygons given as [n,3] xyz arrays; returns the overlap area and
+// writes the clipped polygon (up to 32 vertices).
+double orc_clip(const double *subj, int ns, const double *clipp, int nc, double *out_xyz, int *out_n) {
+    Poly a, b;
+    for (int i = 0; i < ns; ++i) a.push({subj[3 * i], subj[3 * i + 1], subj[3 * i + 2]});
+    for (int i = 0; i < nc; ++i) b.push({clipp[3 * i], clipp[3 * i + 1], clipp[3 * i + 2]});
+    Poly r = clip_poly(a, b);
+    if (out_xyz)
+        for (int i = 0; i < r.n; ++i) {
+            out_xyz[3 * i] = r.v[i].x;
+            out_xyz[3 * i + 1] = r.v[i].y;
+            out_xyz[3 * i + 2] = r.v[i].z;
+        }
+    if (out_n) *out_n = r.n;
+    return poly_area(r);
+}
+
+double orc_poly_area(const double *xyz, int n) {
+    Poly a;
+    for (int i = 0; i < n; ++i) a.push({xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]});
+    return poly_area(a);
+}
+
+std::uint64_t orc_morton_encode(std::uint32_t x, std::uint32_t y) { return morton2(x, y); }
+std::uint32_t orc_normalize_coord(double v, double lo, double hi) { return norm16(v, lo, hi); }
+
+int orc_morton_order(i64 n_nodes, const double *lonlat, i64 n_cells, const i64 *off, const i64 *idx, i64 *perm) {
+    Mesh m{n_nodes, n_cells, lonlat, off, idx, nullptr, nullptr};
+    auto p = morton_order(m);
+    std::copy(p.begin(), p.end(), perm);
+    return 0;
+}
+
+// First-order conservative great-circle weights:
+// WeightGenerator::generate_conservative_impl<3>
+// (src/solver/weight_generator.cpp:3304-3770) with the dispatch checks of
+// generate_conservative (:3246-3302).
+// norm_type: 0 DstArea, 1 FracArea. unmapped: 0 Error, 1 Ignore.
+// faithful = 1 runs the clip loop serially in Morton order as the reference
+// does; 0 runs it with OpenMP and merges in the same order (identical output).
+// Returns 0 ok, -2 both meshes regular/rectilinear (fast paths not restated),
+// -7 unmapped destination under Error.
+int orc_conservative(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *soff, const i64 *sidx,
+                     const double *sareas, const int *smask, i64 dn_nodes, const double *dlonlat, i64 dn_cells,
+                     const i64 *doff, const i64 *didx, const double *dareas, const int *dmask, int norm_type,
+                     int unmapped, int faithful, orc_result **out) {
+    Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, sareas, smask};
+    Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, dareas, dmask};
+    GridInfo sg = detect(S), dg = detect(D);
+    if ((sg.regular && dg.regular) || (sg.rectilinear && dg.rectilinear)) return -2;
+
+    auto sxyz = node_xyz(S), dxyz = node_xyz(D);
+    // degenerate scan
+    std::vector<char> sdeg(sn_cells), ddeg(dn_cells);
+#pragma omp parallel for schedule(static)
+    for (i64 c = 0; c < sn_cells; ++c) sdeg[c] = classify(cell_poly(S, sxyz, c)) != 0;
+#pragma omp parallel for schedule(static)
+    for (i64 c = 0; c < dn_cells; ++c) ddeg[c] = classify(cell_poly(D, dxyz, c)) != 0;
+    // candidates: every src box meeting each dst box, ascending src index
+    auto sbox = cell_boxes(S), dbox = cell_boxes(D);
+    BoxIndex ix = build_index(sbox);
+    std::vector<i64> coff(dn_cells + 1, 0);
+    std::vector<std::vector<int>> cand(dn_cells);
+#pragma omp parallel
+    {
+        std::vector<int> tmp;
+#pragma omp for schedule(dynamic, 256)
+        for (i64 j = 0; j < dn_cells; ++j) {
+            query_index(ix, sbox, dbox[j], tmp);
+            cand[j] = tmp;
+        }
+    }
+    // areas
+    std::vector<double> sarea(sn_cells), darea(dn_cells);
+#pragma omp parallel for schedule(static)
+    for (i64 c = 0; c < sn_cells; ++c) sarea[c] = sareas ? sareas[c] : poly_area(cell_poly(S, sxyz, c));
+#pragma omp parallel for schedule(static)
+    for (i64 c = 0; c < dn_cells; ++c) darea[c] = dareas ? dareas[c] : poly_area(cell_poly(D, dxyz, c));
+    auto order = morton_order(D);
+    Caps scap = cell_caps(S, sxyz), dcap = cell_caps(D, dxyz);
+    TrigCache st = build_trig(sg), dt = build_trig(dg);
+
+    auto *res = new orc_result;
+    res->n_src = sn_cells;
+    res->n_dst = dn_cells;
+    std::vector<double> fa(sn_cells, 0.0), fb(dn_cells, 0.0);
+    struct Ent {
+        i64 j, i;
+        double ov;
+    };
+    std::atomic<i64> n_box{0}, n_cap{0}, n_clip{0};
+    std::atomic<bool> unmapped_hit{false};
+
+    auto process = [&](i64 j, std::vector<Ent> &ents) {
+        if (dmask && dmask[j] == 0) return;
+        if (ddeg[j]) return;
+        double ad = darea[j];
+        if (ad <= 0.0) {
+            if (unmapped == 0) unmapped_hit = true;
+            return;
+        }
+        Poly dp = dt.valid ? trig_poly(dt, j) : cell_poly(D, dxyz, j);
+        bool has = false;
+        i64 lb = 0, lc = 0, ll = 0;
+        for (int i : cand[j]) {
+            ++lb;
+            if (smask && smask[i] == 0) continue;
+            if (sdeg[i]) continue;
+            if (sarea[i] <= 0.0) continue;
+            if (cap_rejects(scap.c[i], scap.r[i], dcap.c[j], dcap.r[j])) continue;
+            ++lc;
+            Poly sp = st.valid ? trig_poly(st, i) : cell_poly(S, sxyz, i);
+            double ov = overlap_area(sp, dp);
+            ++ll;
+            if (ov <= 0.0) continue;
+            ents.push_back({j, i, ov});
+            has = true;
+        }
+        n_box += lb;
+        n_cap += lc;
+        n_clip += ll;
+        if (!has && unmapped == 0) unmapped_hit = true;
+    };
+
+    std::vector<std::vector<Ent>> per(dn_cells);
+    if (faithful) {
+        for (i64 k = 0; k < dn_cells; ++k) process(order[k], per[k]);
+    } else {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (i64 k = 0; k < dn_cells; ++k) process(order[k], per[k]);
+    }
+    if (unmapped_hit) {
+        delete res;
+        return -7;
+    }
+    // merge in Morton order: COO order and frac sums as in :3682-3693
+    std::vector<double> wv;
+    std::vector<i64> rv, cv;
+    for (i64 k = 0; k < dn_cells; ++k)
+        for (const Ent &e : per[k]) {
+            double w = e.ov / darea[e.j];
+            w = std::max(w, 0.0);
+            wv.push_back(w);
+            rv.push_back(e.j);
+            cv.push_back(e.i);
+            fa[e.i] += e.ov / sarea[e.i];
+            fb[e.j] += e.ov / darea[e.j];
+        }
+    if (norm_type == 1)
+        for (size_t k = 0; k < wv.size(); ++k)
+            if (fb[rv[k]] > 0.0) wv[k] /= fb[rv[k]];
+    for (auto &x : fa) x = std::min(x, 1.0);
+    for (auto &x : fb) x = std::min(x, 1.0);
+    // to_csr (include/axis/solver/interpolation_matrix.hpp:180-255)
+    std::vector<i64> perm(wv.size());
+    std::iota(perm.begin(), perm.end(), 0);
+    std::sort(perm.begin(), perm.end(), [&](i64 a, i64 b) {
+        if (rv[a] != rv[b]) return rv[a] < rv[b];
+        return cv[a] < cv[b];
+    });
+    res->row.resize(perm.size());
+    res->col.resize(perm.size());
+    res->w.resize(perm.size());
+    for (size_t k = 0; k < perm.size(); ++k) {
+        res->row[k] = rv[perm[k]];
+        res->col[k] = cv[perm[k]];
+        res->w[k] = wv[perm[k]];
+    }
+    res->frac_a = std::move(fa);
+    res->frac_b = std::move(fb);
+    res->area_a = std::move(sarea);
+    res->area_b = std::move(darea);
+    res->n_box_pairs = n_box;
+    res->n_cap_pass = n_cap;
+    res->n_clipped = n_clip;
+    *out = res;
+    return 0;
+}
+
+// Rectilinear-source bilinear weights: generate_bilinear_rect_nonuniform
+// (src/solver/weight_generator_bilinear_rect_nonuniform.cpp:22-149) behind
+// the dispatch of generate_bilinear (src/solver/weight_generator.cpp:2306-2345).
+// Returns -2 when both meshes are regular (the regular fast path is not
+// restated) and -3 when the source is not rectilinear.
+int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *soff, const i64 *sidx, i64 dn_nodes,
+                 const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, orc_result **out) {
+    Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, nullptr, nullptr};
+    Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, nullptr, nullptr};
+    GridInfo sg = detect(S), dg = detect(D);
+    if (sg.regular && dg.regular) return -2;
+    if (!sg.rectilinear) return -3;
+    i64 ni = sg.ni, nj = sg.nj;
+    std::vector<double> cl(ni), ct(nj);
+    for (i64 i = 0; i < ni; ++i) cl[i] = 0.5 * (sg.ulon[i] + sg.ulon[i + 1]);
+    for (i64 j = 0; j < nj; ++j) ct[j] = 0.5 * (sg.ulat[j] + sg.ulat[j + 1]);
+    auto *res = new orc_result;
+    res->n_src = sn_cells;
+    res->n_dst = dn_cells;
+    res->row.resize(4 * dn_cells);
+    res->col.resize(4 * dn_cells);
+    res->w.resize(4 * dn_cells);
+#pragma omp parallel for schedule(static)
+    for (i64 c = 0; c < dn_cells; ++c) {
+        i64 b = D.off[c], e = D.off[c + 1];
+        double ls = 0.0, ts = 0.0;
+        for (i64 q = b; q < e; ++q) {
+            ls += D.lon(D.idx[q]);
+            ts += D.lat(D.idx[q]);
+        }
+        double ld = ls / static_cast<double>(e - b);
+        double td = ts / static_cast<double>(e - b);
+        int i = static_cast<int>(std::upper_bound(cl.begin(), cl.end(), ld) - cl.begin()) - 1;
+        int j = static_cast<int>(std::upper_bound(ct.begin(), ct.end(), td) - ct.begin()) - 1;
+        if (i < 0) i = 0;
+        if (i >= static_cast<int>(ni) - 1) i = static_cast<int>(ni) - 2;
+        if (i < 0) i = 0;
+        if (j < 0) j = 0;
+        if (j >= static_cast<int>(nj) - 1) j = static_cast<int>(nj) - 2;
+        if (j < 0) j = 0;
+        double x0 = cl[i], x1 = cl[i + 1], y0 = ct[j], y1 = ct[j + 1];
+        double tx = (ld - x0) / (x1 - x0);
+        double ty = (td - y0) / (y1 - y0);
+        tx = std::max(0.0, std::min(1.0, tx));
+        ty = std::max(0.0, std::min(1.0, ty));
+        i64 src[4] = {j * ni + i, j * ni + i + 1, (j + 1) * ni + i, (j + 1) * ni + i + 1};
+        double w[4] = {(1.0 - tx) * (1.0 - ty), tx * (1.0 - ty), (1.0 - tx) * ty, tx * ty};
+        // CSR order: columns ascending within the row (all four are distinct)
+        int ordk[4] = {0, 1, 2, 3};
+        std::sort(ordk, ordk + 4, [&](int a, int bq) { return src[a] < src[bq]; });
+        for (int k = 0; k < 4; ++k) {
+            res->row[4 * c + k] = c;
+            res->col[4 * c + k] = src[ordk[k]];
+            res->w[4 * c + k] = w[ordk[k]];
+        }
+    }
+    res->frac_a.assign(sn_cells, 1.0);
+    res->frac_b.assign(dn_cells, 1.0);
+    res->area_a.assign(sn_cells, 0.0);
+    res->area_b.assign(dn_cells, 0.0);
+    *out = res;
+    return 0;
+}
+
+i64 orc_result_nnz(const orc_result *r) { return static_cast<i64>(r->w.size()); }
+
+void orc_result_stats(const orc_result *r, i64 *stats) {
+    stats[0] = r->n_box_pairs;
+    stats[1] = r->n_cap_pass;
+    stats[2] = r->n_clipped;
+}
+
+void orc_result_copy(const orc_result *r, i64 *row, i64 *col, double *w, double *fa, double *fb, double *aa,
+                     double *ab) {
+    std::copy(r->row.begin(), r->row.end(), row);
+    std::copy(r->col.begin(), r->col.end(), col);
+    std::copy(r->w.begin(), r->w.end(), w);
+    std::copy(r->frac_a.begin(), r->frac_a.end(), fa);
+    std::copy(r->frac_b.begin(), r->frac_b.end(), fb);
+    std::copy(r->area_a.begin(), r->area_a.end(), aa);
+    std::copy(r->area_b.begin(), r->area_b.end(), ab);
+}
+
+void orc_result_free(orc_result *r) { delete r; }
+
+// CSR apply y[:, v] = S x[:, v] in FP64, rows in parallel; x/y column-major
+// with leading dims ldx/ldy (the multivector spmv of
+// include/axis/solver/apply.hpp:300-306). compensated = 1 sums each row with
+// TwoSum (an FP64 reference of higher accuracy than the plain loop).
+void orc_apply_csr(i64 n_dst, const i64 *row_ptr, const i64 *col, const double *val, const double *x, i64 ldx,
+                   double *y, i64 ldy, i64 nrhs, int compensated) {
+#pragma omp parallel for schedule(static) collapse(2)
+    for (i64 v = 0; v < nrhs; ++v)
+        for (i64 j = 0; j < n_dst; ++j) {
+            const double *xv = x + v * ldx;
+            double s = 0.0, c = 0.0;
+            for (i64 k = row_ptr[j]; k < row_ptr[j + 1]; ++k) {
+                double p = val[k] * xv[col[k]];
+                if (compensated) {
+                    // TwoProduct error via Dekker splitting is not needed for
+                    // the 1e-13 bar; TwoSum on the products suffices.
+                    double t = s + p;
+                    double bp = t - s;
+                    double e = (s - (t - bp)) + (p - bp);
+                    s = t;
+                    c += e;
+                } else {
+                    s += p;
+                }
+            }
+            y[v * ldy + j] = s + c;
+        }
+}
+
+// COO scatter-add with OpenMP atomics: the path Python batch_apply takes
+// on an uncompressed matrix (include/axis/solver/apply.hpp:315-330).
+void orc_apply_coo_atomic(i64 nnz, const i64 *row, const i64 *col, const double *val, const double *x, i64 ldx,
+                          double *y, i64 ldy, i64 n_dst, i64 nrhs) {
+#pragma omp parallel for schedule(static)
+    for (i64 q = 0; q < n_dst * nrhs; ++q) y[(q / n_dst) * ldy + q % n_dst] = 0.0;
+#pragma omp parallel for schedule(static)
+    for (i64 q = 0; q < nnz * nrhs; ++q) {
+        i64 k = q % nnz, v = q / nnz;
+        double add = val[k] * x[v * ldx + col[k]];
+#pragma omp atomic
+        y[v * ldy + row[k]] += add;
+    }
+}
+
+// Conservation report of src/solver/conservation.cpp:24-96.
+// out = (src_integral, dst_integral, absolute_error, relative_error).
+void orc_conservation(i64 n_src, const double *src, const double *area_a, const double *frac_a, i64 n_dst,
+                      const double *dst, const double *area_b, const double *frac_b, int norm_type, double *out) {
+    double si = 0.0, di = 0.0;
+    for (i64 i = 0; i < n_src; ++i) si += src[i] * area_a[i] * frac_a[i];
+    if (norm_type == 0) {
+        for (i64 j = 0; j < n_dst; ++j)
+            if (frac_b[j] != 0.0) di += dst[j] * area_b[j];
+    } else {
+        for (i64 j = 0; j < n_dst; ++j) di += dst[j] * area_b[j] * frac_b[j];
+    }
+    double ae = std::abs(si - di);
+    double den = std::max({std::abs(si), std::abs(di), std::numeric_limits<double>::epsilon()});
+    out[0] = si;
+    out[1] = di;
+    out[2] = ae;
+    out[3] = ae / den;
+}
+
+}  // extern "C"

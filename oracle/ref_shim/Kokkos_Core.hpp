@@ -1,0 +1,164 @@
+// Minimal host-only stand-in for the part of the Kokkos API that the AXIS
+// geometry headers use (View, RangePolicy, parallel_for/reduce, math
+// wrappers, mirror/deep_copy). It lets oracle/ref_driver.cpp compile the
+// reference's header-only geometry code unchanged, serially, on the host.
+// Test infrastructure: used only to build oracle/_ref/libaxisref.so.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <limits>
+#include <memory>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#define KOKKOS_FUNCTION
+#define KOKKOS_INLINE_FUNCTION inline
+#define KOKKOS_FORCEINLINE_FUNCTION inline
+#define KOKKOS_LAMBDA [=]
+
+namespace Kokkos {
+
+struct Serial {};
+struct HostSpace {
+    using execution_space = Serial;
+    using memory_space = HostSpace;
+};
+using DefaultHostExecutionSpace = Serial;
+using DefaultExecutionSpace = Serial;
+struct LayoutLeft {};
+struct LayoutRight {};
+template <unsigned N = 0>
+struct MemoryTraits {};
+constexpr unsigned Unmanaged = 1;
+
+template <class A, class B>
+struct SpaceAccessibility {
+    static constexpr bool accessible = true;
+};
+
+inline double sqrt(double x) { return std::sqrt(x); }
+inline double atan2(double y, double x) { return std::atan2(y, x); }
+inline double fabs(double x) { return std::fabs(x); }
+inline double fmin(double a, double b) { return std::fmin(a, b); }
+inline double fmax(double a, double b) { return std::fmax(a, b); }
+inline double acos(double x) { return std::acos(x); }
+inline double asin(double x) { return std::asin(x); }
+inline double cos(double x) { return std::cos(x); }
+inline double sin(double x) { return std::sin(x); }
+inline double abs(double x) { return std::fabs(x); }
+inline bool isnan(double x) { return std::isnan(x); }
+inline bool isinf(double x) { return std::isinf(x); }
+inline double nan(const char *s) { return std::nan(s); }
+
+template <class T>
+struct view_traits;
+template <class U>
+struct view_traits<U *> {
+    using value = U;
+    static constexpr int rank = 1;
+};
+template <class U>
+struct view_traits<U **> {
+    using value = U;
+    static constexpr int rank = 2;
+};
+
+// Rank-1 or rank-2 (column-major) host array with shared ownership.
+template <class DataType, class... Props>
+class View {
+   public:
+    using value_type = typename view_traits<DataType>::value;
+    using nc_value = std::remove_const_t<value_type>;
+    using memory_space = HostSpace;
+    static constexpr int Rank = view_traits<DataType>::rank;
+
+    std::shared_ptr<nc_value[]> store;
+    nc_value *ptr = nullptr;
+    std::size_t e0 = 0, e1 = 1;
+
+    View() = default;
+    View(const std::string &, std::size_t n0, std::size_t n1 = 1)
+        : store(new nc_value[n0 * n1 > 0 ? n0 * n1 : 1]()), ptr(store.get()), e0(n0), e1(Rank > 1 ? n1 : 1) {}
+    View(value_type *p, std::size_t n0, std::size_t n1 = 1) : ptr(const_cast<nc_value *>(p)), e0(n0), e1(Rank > 1 ? n1 : 1) {}
+    template <class D2, class... P2>
+    View(const View<D2, P2...> &o) : store(o.store), ptr(o.ptr), e0(o.e0), e1(o.e1) {}
+
+    value_type &operator()(std::size_t i) const { return ptr[i]; }
+    value_type &operator()(std::size_t i, std::size_t j) const { return ptr[i + j * e0]; }
+    value_type &operator[](std::size_t i) const { return ptr[i]; }
+    std::size_t extent(int d) const { return d == 0 ? e0 : (d == 1 && Rank > 1 ? e1 : 1); }
+    value_type *data() const { return ptr; }
+    std::size_t size() const { return e0 * e1; }
+};
+
+template <class V>
+V create_mirror_view(const V &v) {
+    return v;
+}
+template <class S, class V>
+V create_mirror_view_and_copy(const S &, const V &v) {
+    return v;
+}
+template <class A, class B>
+void deep_copy(const A &dst, const B &src) {
+    if constexpr (std::is_arithmetic_v<B>) {
+        for (std::size_t i = 0; i < dst.size(); ++i) dst.data()[i] = src;
+    } else {
+        if (dst.data() != src.data())
+            for (std::size_t i = 0; i < dst.size(); ++i) dst.data()[i] = src.data()[i];
+    }
+}
+
+template <class ExecSpace = Serial>
+struct RangePolicy {
+    std::size_t b, e;
+    RangePolicy(std::size_t b_, std::size_t e_) : b(b_), e(e_) {}
+};
+
+template <class T>
+struct Min {
+    T &ref;
+    explicit Min(T &r) : ref(r) {}
+    T init() const { return std::numeric_limits<T>::max(); }
+};
+template <class T>
+struct Max {
+    T &ref;
+    explicit Max(T &r) : ref(r) {}
+    T init() const { return std::numeric_limits<T>::lowest(); }
+};
+
+template <class E, class F>
+void parallel_for(const std::string &, const RangePolicy<E> &p, F f) {
+    for (std::size_t i = p.b; i < p.e; ++i) f(i);
+}
+template <class F>
+void parallel_for(const std::string &, std::size_t n, F f) {
+    for (std::size_t i = 0; i < n; ++i) f(i);
+}
+template <class E, class F, class R1, class R2>
+void parallel_reduce(const std::string &, const RangePolicy<E> &p, F f, R1 r1, R2 r2) {
+    auto a = r1.init();
+    auto b = r2.init();
+    for (std::size_t i = p.b; i < p.e; ++i) f(i, a, b);
+    r1.ref = a;
+    r2.ref = b;
+}
+template <class E, class F, class T>
+std::enable_if_t<std::is_arithmetic_v<T>> parallel_reduce(const std::string &, const RangePolicy<E> &p, F f, T &result) {
+    T s{};
+    for (std::size_t i = p.b; i < p.e; ++i) f(i, s);
+    result = s;
+}
+
+inline void fence() {}
+inline void fence(const std::string &) {}
+inline bool is_initialized() { return true; }
+inline void initialize() {}
+
+}  // namespace Kokkos
