@@ -1,0 +1,449 @@
+#!/usr/bin/env python
+"""Benchmark of the AXIS regridding hot path on one GB300.
+
+Headline workload (one "step" = one pass of the batched apply over the whole
+batch): C768 gnomonic cubed sphere (3,538,944 cells) -> 0.25 deg lat-lon
+(1,036,800 cells), first-order conservative weights generated on the GPU,
+1016 right-hand sides (8 tracers x 127 levels) of FP32 fields laid out
+[field][level][cell], each a seeded spherical-harmonic field (l <= 128) times
+a seeded lognormal(0,1) per-level scale. The apply is the split-FP32
+(hi+lo weights, compensated) SpMM; the plain FP64 SpMM on FP64 copies of the
+same fields is timed beside it. Inputs are 14.4 GB per step, larger than L2.
+
+Also reported on the same line: max/RMS relative error of both applies
+against the CPU oracle on sampled fields, the conservation errors, the
+roofline fraction against the measured HBM copy bandwidth, the end-to-end
+throughput through the host-buffer C ABI (pinned host -> device -> host every
+step), weight generation for 0.25 deg -> C384 (pairs/s), and the CPU oracle
+apply timed on this host's cores.
+
+--impl reference times the reference's CPU algorithm (the oracle port of the
+CSR apply, all host threads) on a bounded sample of fields of the same
+workload and prints the same metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "helm-project_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "regrid apply dst-vals/s (split-FP32 SpMM, C768->0.25deg, 1016 RHS)"
+UNIT = "dst-vals/s"
+N_TRACERS, N_LEVELS = 8, 127
+NRHS = N_TRACERS * N_LEVELS
+WORKLOAD = "C768->0.25deg conservative, batched split-FP32 SpMM, 1016 RHS (8 tracers x 127 levels)"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "50"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.12)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_fields(xyz_t, seed: int = 2024):
+    """[1016, n] float32 on the device: 8 SH(l<=128) tracers x lognormal level scales."""
+    import torch
+
+    from axgb import fields
+    base = fields.sh_fields(xyz_t, 128, [seed + t for t in range(N_TRACERS)])
+    rng = np.random.default_rng(seed)
+    scales = rng.lognormal(0.0, 1.0, size=(N_TRACERS, N_LEVELS))
+    X = torch.empty((NRHS, xyz_t.shape[0]), dtype=torch.float32, device=xyz_t.device)
+    for t in range(N_TRACERS):
+        sc = torch.tensor(scales[t], dtype=torch.float64, device=xyz_t.device)
+        X[t * N_LEVELS:(t + 1) * N_LEVELS] = (base[t][None, :] * sc[:, None]).to(torch.float32)
+    del base
+    return X, scales
+
+
+def rel_errors(y, ref):
+    d = np.abs(y.astype(np.float64) - ref)
+    scale = np.maximum(np.abs(ref), 1e-30)
+    return {"max_rel": float(np.max(d / scale)),
+            "max_rel_normwise": float(np.max(d) / np.max(np.abs(ref))),
+            "rms_rel": float(np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean(ref ** 2)))}
+
+
+def cpu_apply_rate(oracle, wo, X_cpu):
+    """dst-vals/s of the oracle's CSR FP64 apply (OpenMP rows) on X_cpu."""
+    t0 = time.perf_counter()
+    oracle.apply_csr(wo, X_cpu, compensated=False)
+    dt = time.perf_counter() - t0
+    return X_cpu.shape[0] * wo.n_dst / dt, dt
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from axgb import fields, grids
+    from oracle import Oracle
+    from oracle import build as obuild
+    obuild.build_oracle()
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    o.threads(cores)
+    src, dst = grids.cubed_sphere(768), grids.latlon_deg(0.25)
+    t0 = time.perf_counter()
+    wo = o.conservative(src, dst)
+    gen_s = time.perf_counter() - t0
+    xyz = grids.cell_centroids_xyz(src)
+    base = fields.sh_fields(xyz, 32, [2024]).numpy()[0]
+    sample = 16
+    rng = np.random.default_rng(2024)
+    X = np.stack([base * s for s in rng.lognormal(0, 1, sample)]).astype(np.float32).astype(np.float64)
+    for _ in range(args.warmup):
+        cpu_apply_rate(o, wo, X)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_apply_rate(o, wo, X)
+        times.append(dt)
+    ms = 1e3 * statistics.mean(times)
+    value = sample * wo.n_dst / (ms / 1e3)
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "n_src": wo.n_src, "n_dst": wo.n_dst, "nnz": wo.nnz,
+                      "nrhs_sampled": sample, "parallelism": "host threads"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{sample} of {NRHS} RHS per step, FP64 CSR row loop (OpenMP), "
+                                      f"oracle weights generated in {gen_s:.1f} s"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="axgb", choices=["axgb", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    import torch.distributed as dist
+
+    import axgb
+    from axgb import grids
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    axgb.init(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    # ── weights for the headline workload ──
+    t0 = time.perf_counter()
+    src_g, dst_g = grids.cubed_sphere(768), grids.latlon_deg(0.25)
+    t_grid = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ms, md = axgb.Mesh.from_grid(src_g), axgb.Mesh.from_grid(dst_g)
+    t_ingest = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    M = axgb.generate_weights(ms, md, {"method": "conservative"})
+    t_gen3 = time.perf_counter() - t0
+    st3 = M.stats()
+    log(f"grids {t_grid:.1f}s ingest {t_ingest:.2f}s gen C768->0.25 {t_gen3:.3f}s nnz={M.nnz} {st3}")
+
+    # ── fields ──
+    xyz = torch.tensor(grids.cell_centroids_xyz(src_g), device=dev)
+    t0 = time.perf_counter()
+    X, scales = make_fields(xyz)
+    torch.cuda.synchronize()
+    log(f"fields {time.perf_counter() - t0:.1f}s")
+    Y = torch.empty((NRHS, M.n_dst), dtype=torch.float32, device=dev)
+    M.prepare(1)
+    tile, unroll = axgb.autotune_f32split(M, X, Y)
+    launches_per_step = axgb_launches(M)
+    log(f"autotune: fields_per_pass={tile} unroll={unroll} launches/step={launches_per_step}")
+
+    stream = torch.cuda.current_stream()
+
+    def run_split():
+        axgb.apply_f32split(M, X, Y, stream=stream, fields_per_pass=tile, unroll=unroll)
+
+    for _ in range(args.warmup):
+        run_split()
+    torch.cuda.synchronize()
+    barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        run_split()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = clk.stop()
+    ms_step = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        tt = torch.tensor([ms_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_step = float(tt.item())
+    dst_vals = M.n_dst * NRHS
+    value = world * dst_vals / (ms_step / 1e3)
+    bytes_split = 4 * M.n_src * NRHS + 4 * M.n_dst * NRHS + 12 * M.nnz + 4 * (M.n_dst + 1)
+    peak, peak_kind = peaks()
+    achieved = bytes_split / (ms_step / 1e3) / 1e9
+    log(f"split: {ms_step:.3f} ms/step  {achieved:.0f} GB/s ({achieved / peak:.2%} of {peak_kind} {peak:.0f})")
+
+    # ── plain FP64 SpMM on FP64 copies of the same fields ──
+    X64 = X.to(torch.float64)
+    Y64 = torch.empty((NRHS, M.n_dst), dtype=torch.float64, device=dev)
+    M.prepare(0)
+    for _ in range(args.warmup):
+        axgb.apply_f64(M, X64, Y64, stream=stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        axgb.apply_f64(M, X64, Y64, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / args.steps
+    bytes_f64 = 8 * M.n_src * NRHS + 8 * M.n_dst * NRHS + 12 * M.nnz + 4 * (M.n_dst + 1)
+    log(f"fp64: {ms64:.3f} ms/step  {bytes_f64 / ms64 / 1e6:.0f} GB/s; split speed-up {ms64 / ms_step:.2f}x")
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_src": M.n_src, "n_dst": M.n_dst, "nnz": M.nnz, "nrhs": NRHS,
+                   "fields_per_pass": tile, "unroll": unroll, "l2": "inputs 14.4 GB per step > L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": profiled_traffic(), "peak_kind": peak_kind,
+                     "bytes_per_step": bytes_split},
+        "fp64_apply": {"ms_per_step": ms64, "GBps": bytes_f64 / ms64 / 1e6, "split_speedup": ms64 / ms_step},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+        "weightgen_c768_to_0p25": {"seconds": t_gen3, "nnz": M.nnz, "pairs_per_s": M.nnz / t_gen3,
+                                   "candidates": st3["bvh_candidates"], "gated": st3["gated_pairs"],
+                                   "stages_ms": {k: st3[k] for k in st3 if k.startswith("t_")}},
+    }
+
+    if rank == 0:
+        # ── errors and conservation against the CPU oracle ──
+        from oracle import Oracle
+        o = Oracle()
+        o.threads(os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        wo = o.conservative(src_g, dst_g)
+        t_oracle = time.perf_counter() - t0
+        csr = M.to_csr()
+        rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
+        same = M.nnz == wo.nnz and np.array_equal(rows, wo.row) and np.array_equal(csr["col"], wo.col)
+        wrel = float(np.max(np.abs(csr["val"] - wo.w) / wo.w)) if same else None
+        sample = [0, 1, 500, NRHS - 1]
+        Xs = X[sample].to(torch.float64).cpu().numpy()
+        ref = o.apply_csr(wo, Xs, compensated=True)
+        e_split = rel_errors(Y[sample].cpu().numpy(), ref)
+        e_f64 = rel_errors(Y64[sample].cpu().numpy(), ref)
+        cons_split = axgb.check_conservation(M, X[0], Y[0])
+        cons_f64 = axgb.check_conservation(M, X64[0], Y64[0])
+        # operator conservation: sum_j w_ij area_b_j = area_a_i frac_a_i
+        colsum = np.bincount(csr["col"], weights=csr["val"] * csr["area_b"][rows], minlength=M.n_src)
+        rhs = csr["area_a"] * csr["frac_a"]
+        op_cons = float(np.max(np.abs(colsum - rhs) / rhs))
+        result["parity"] = {"index_set_identical": bool(same), "weights_max_rel": wrel,
+                            "oracle_weightgen_s": t_oracle, "split": e_split, "fp64": e_f64,
+                            "sampled_rhs": sample}
+        result["conservation"] = {"split_field_rel": cons_split["relative_error"],
+                                  "fp64_field_rel": cons_f64["relative_error"], "operator_max_rel": op_cons}
+        log("parity", result["parity"])
+        log("conservation", result["conservation"])
+        del X64, Y64
+        torch.cuda.empty_cache()
+
+        # ── end to end through the host-buffer C ABI ──
+        if not args.no_e2e:
+            result["e2e"] = e2e(M, X, args)
+        # ── weight generation for 0.25 deg -> C384 ──
+        result["weightgen_0p25_to_c384"] = weightgen_c384(md, dst_g)
+        # ── CPU baseline: oracle CSR apply on this host ──
+        if not args.no_cpu:
+            ns = 16
+            xs = X[:ns].to(torch.float64).cpu().numpy()
+            rate, dt = cpu_apply_rate(o, wo, xs)
+            result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                      "sample": f"{ns} of {NRHS} RHS, FP64 CSR row loop (OpenMP), {dt:.2f} s"}
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def axgb_launches(M):
+    # one launch per non-empty slice length class of the split layout
+    st = np.zeros(8, np.int64)
+    import ctypes
+
+    import axgb
+    axgb._check(axgb.lib().axgb_matrix_stats(M.handle, st.ctypes.data_as(ctypes.c_void_p), None))
+    return int(st[5]) if st[5] > 0 else 1
+
+
+def profiled_traffic():
+    """Per-step DRAM bytes of the apply from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "apply_split_c768_0p25_1016rhs.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_step:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def e2e(M, X, args):
+    import torch
+
+    import axgb
+    need = 4 * (M.n_src + M.n_dst) * NRHS
+    avail = 0
+    try:
+        for ln in open("/proc/meminfo"):
+            if ln.startswith("MemAvailable:"):
+                avail = int(ln.split()[1]) * 1024
+    except OSError:
+        pass
+    nrhs = NRHS
+    if avail and need > 0.6 * avail:
+        nrhs = max(8, int(NRHS * 0.6 * avail / need))
+    Xh = torch.empty((nrhs, M.n_src), dtype=torch.float32, pin_memory=True)
+    Yh = torch.empty((nrhs, M.n_dst), dtype=torch.float32, pin_memory=True)
+    Xh.copy_(X[:nrhs])
+    steps = max(3, min(args.steps, 5))
+    for _ in range(1):
+        axgb.batch_apply_host_f32split(M, Xh, Yh)
+    t = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        axgb.batch_apply_host_f32split(M, Xh, Yh)
+        t.append(time.perf_counter() - t0)
+    s = statistics.mean(t)
+    return {"value": M.n_dst * nrhs / s, "unit": UNIT, "h2d_bytes_per_step": 4 * M.n_src * nrhs,
+            "d2h_bytes_per_step": 4 * M.n_dst * nrhs, "ms_per_step": 1e3 * s, "nrhs": nrhs,
+            "api": "axgb_batch_apply_host_f32split (pinned host buffers)"}
+
+
+def weightgen_c384(md_0p25, latlon_g):
+    import torch
+
+    import axgb
+    from axgb import grids
+    c384 = grids.cubed_sphere(384)
+    t0 = time.perf_counter()
+    mc = axgb.Mesh.from_grid(c384)
+    t_ingest = time.perf_counter() - t0
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Mc = axgb.generate_weights(md_0p25, mc, {"method": "conservative"})
+        times.append(time.perf_counter() - t0)
+        st = Mc.stats()
+    tb = time.perf_counter()
+    Mb = axgb.generate_weights(md_0p25, mc, {"method": "bilinear"})
+    t_bil = time.perf_counter() - tb
+    best = min(times)
+    return {"seconds_best": best, "seconds_first": times[0], "ingest_s": t_ingest, "nnz": Mc.nnz,
+            "pairs_per_s": Mc.nnz / best, "candidates_per_s": st["gated_pairs"] / best,
+            "bvh_candidates": st["bvh_candidates"], "gated": st["gated_pairs"],
+            "stages_ms": {k: st[k] for k in st if k.startswith("t_")}, "bilinear_s": t_bil, "bilinear_nnz": Mb.nnz}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -28,23 +28,30 @@ def sh_field(xyz, lmax: int, seed: int, offset: float = 0.0, device=None, chunk:
     """Evaluate the seeded field at unit vectors ``xyz`` ([n,3]); returns a
     float64 tensor on ``device`` (default: the device of ``xyz`` if it is a
     tensor, else CPU)."""
+    return sh_fields(xyz, lmax, [seed], offset, device, chunk)[0]
+
+
+def sh_fields(xyz, lmax: int, seeds, offset: float = 0.0, device=None, chunk: int = 1 << 19) -> torch.Tensor:
+    """Several seeded fields at once: returns float64 [len(seeds), n]."""
     if not isinstance(xyz, torch.Tensor):
         xyz = torch.as_tensor(np.ascontiguousarray(xyz), dtype=torch.float64)
     if device is not None:
         xyz = xyz.to(device)
     xyz = xyz.to(torch.float64)
-    coef = torch.as_tensor(sh_coefficients(lmax, seed), dtype=torch.float64, device=xyz.device)
-    out = torch.empty(xyz.shape[0], dtype=torch.float64, device=xyz.device)
+    coef = torch.as_tensor(np.stack([sh_coefficients(lmax, s) for s in seeds]), dtype=torch.float64,
+                           device=xyz.device)
+    out = torch.empty((len(seeds), xyz.shape[0]), dtype=torch.float64, device=xyz.device)
     for s in range(0, xyz.shape[0], chunk):
-        out[s:s + chunk] = _eval_chunk(xyz[s:s + chunk], lmax, coef) + offset
+        out[:, s:s + chunk] = _eval_chunk(xyz[s:s + chunk], lmax, coef) + offset
     return out
 
 
 def _eval_chunk(p: torch.Tensor, lmax: int, coef: torch.Tensor) -> torch.Tensor:
+    """coef: [F, (lmax+1)^2] -> [F, n]."""
     z = p[:, 2].clamp(-1.0, 1.0)
     sint = torch.sqrt(torch.clamp(1.0 - z * z, min=0.0))
     phi = torch.atan2(p[:, 1], p[:, 0])
-    res = torch.zeros_like(z)
+    res = torch.zeros((coef.shape[0], z.shape[0]), dtype=z.dtype, device=z.device)
 
     def cidx(l, m):  # index of a_lm in the flat coefficient vector
         return l * l + (m + l)
@@ -53,26 +60,25 @@ def _eval_chunk(p: torch.Tensor, lmax: int, coef: torch.Tensor) -> torch.Tensor:
     for m in range(0, lmax + 1):
         if m > 0:
             pmm = pmm * (math.sqrt((2.0 * m + 1.0) / (2.0 * m)) * sint)
-        norm = 1.0 if m == 0 else math.sqrt(2.0)
-        # accumulate sum_l a_{l,+m} P_l^m and sum_l a_{l,-m} P_l^m
-        cpos = coef[cidx(m, m)] * pmm
-        cneg = coef[cidx(m, -m)] * pmm if m > 0 else None
+        # Legendre column P_l^m, l = m..lmax, as rows of a matrix
+        cols = [pmm]
         if m + 1 <= lmax:
             p_lm1 = pmm
             p_l = math.sqrt(2.0 * m + 3.0) * z * pmm
-            cpos = cpos + coef[cidx(m + 1, m)] * p_l
-            if m > 0:
-                cneg = cneg + coef[cidx(m + 1, -m)] * p_l
+            cols.append(p_l)
             for l in range(m + 2, lmax + 1):
                 a = math.sqrt((4.0 * l * l - 1.0) / (l * l - m * m))
                 b = math.sqrt(((l - 1.0) ** 2 - m * m) / (4.0 * (l - 1.0) ** 2 - 1.0))
                 p_new = a * (z * p_l - b * p_lm1)
                 p_lm1, p_l = p_l, p_new
-                cpos = cpos + coef[cidx(l, m)] * p_l
-                if m > 0:
-                    cneg = cneg + coef[cidx(l, -m)] * p_l
+                cols.append(p_l)
+        P = torch.stack(cols)  # [lmax-m+1, n]
+        ipos = [cidx(l, m) for l in range(m, lmax + 1)]
+        cpos = coef[:, ipos] @ P
         if m == 0:
             res = res + cpos
         else:
-            res = res + norm * (cpos * torch.cos(m * phi) + cneg * torch.sin(m * phi))
+            ineg = [cidx(l, -m) for l in range(m, lmax + 1)]
+            cneg = coef[:, ineg] @ P
+            res = res + math.sqrt(2.0) * (cpos * torch.cos(m * phi) + cneg * torch.sin(m * phi))
     return res

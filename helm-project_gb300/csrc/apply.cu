@@ -1,0 +1,676 @@
+// Sparse weight apply on the device: y[f] = S x[f] for fields f < nrhs,
+// fields laid out [f][cell] (the LayoutLeft (n_cells, n_vars) of
+// batch_apply, libs/axis/include/axis/solver/apply.hpp:275-343).
+//
+// Layout: 32-row sliced ELL built once per matrix from the CSR. One warp
+// owns one slice (one row per lane): it loads its row's entries (column,
+// FP64 weight or FP32 hi+lo pair) once into registers, then streams the
+// fields of its work item through them, so the matrix is read once per
+// item while the gathers of x are the only per-field traffic. Slices are
+// grouped by length class (<=8, <=16, <=32, <=64 entries) so each class
+// runs a kernel with a fixed register array; longer slices take a kernel
+// that re-reads its entries from global memory.
+//
+// Split FP32 path: weights w = hi + lo (hi = fp32(w), lo = fp32(w - hi));
+// per entry the product hi*x is split exactly (fma), lo*x is added to the
+// error term, and the running sum is carried with Knuth's TwoSum, so each
+// output is the compensated sum rounded once to FP32. Two fields are
+// processed together with packed f32x2 instructions.
+//
+// Work items are (field tile, slice), tile-major: all warps sweep the same
+// tile of fields at once, so the source values they gather stay in L2
+// between neighbouring slices. The tile width and the number of fields per
+// thread iteration are the tuning knobs (see the autotuner in api.cpp).
+#include <algorithm>
+
+#include "internal.hpp"
+
+namespace axgb {
+
+struct Batch {
+    struct Desc {
+        const int *base, *len, *rlen, *col;
+        const float *hi, *lo;
+        i64 n_rows, n_slices;
+        const float *x;
+        i64 ldx;
+        float *y;
+        i64 ldy;
+        i64 nrhs;
+        i64 tile;
+        i64 n_tiles;
+        i64 item_begin;  // first global item of this matrix
+    };
+    std::vector<std::shared_ptr<Matrix>> mats;
+    std::vector<i64> nrhs;
+    std::vector<Desc> desc;
+    DBuf<Desc> d_desc;
+    DBuf<unsigned long long> counter;
+    i64 total_items = 0;
+    int blocks = 0;
+    // graph per stream, replayed while descriptors are updated in place
+    std::map<cudaStream_t, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
+    std::vector<const void *> last_ptrs;
+    std::mutex mu;
+    ~Batch() {
+        for (auto &g : graphs) {
+            cudaGraphExecDestroy(g.second.second);
+            cudaGraphDestroy(g.second.first);
+        }
+    }
+};
+
+namespace {
+
+inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
+
+// ─── packed f32x2 helpers ──────────────────────────────────────────────────
+
+struct F2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ F2 pk(float a, float b) {
+    F2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk(F2 r, float &a, float &b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r.v)); }
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+    F2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 sub2(F2 a, F2 b) {
+    F2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) {
+    F2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+    F2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+
+// One compensated step for one field: s + c accumulates (hi + lo) * x.
+__device__ __forceinline__ void csum1(float &s, float &c, float h, float l, float x) {
+    float p = __fmul_rn(h, x);
+    float pe = __fmaf_rn(h, x, -p);
+    float q = __fmaf_rn(l, x, pe);
+    float t = __fadd_rn(s, p);
+    float bp = __fsub_rn(t, s);
+    float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(e, q));
+}
+
+// Same for two fields at once; hn = -hi (so mul gives -p exactly).
+__device__ __forceinline__ void csum2(F2 &s, F2 &c, F2 h, F2 hn, F2 l, F2 x) {
+    F2 pn = mul2(hn, x);
+    F2 pe = fma2(h, x, pn);
+    F2 q = fma2(l, x, pe);
+    F2 t = sub2(s, pn);
+    F2 bp = sub2(t, s);
+    F2 a2 = sub2(s, sub2(t, bp));
+    F2 a3 = add2(pn, bp);
+    F2 e = sub2(a2, a3);
+    s = t;
+    c = add2(c, add2(e, q));
+}
+
+struct SellArgs {
+    const int *ids;
+    i64 n_ids;
+    const int *base, *len, *rlen, *col;
+    const float *hi, *lo;
+    const double *w64;
+    i64 n_rows;
+};
+
+__device__ __forceinline__ float ldg_f(const float *p) { return __ldg(p); }
+
+// ─── split-FP32 kernel ─────────────────────────────────────────────────────
+// L > 0: entries cached in registers (slice length <= L).
+// L == 0: entries re-read from global memory (long slices).
+template <int L, int U>
+__global__ void __launch_bounds__(256) k_split(SellArgs a, const float *__restrict__ x, i64 ldx, float *__restrict__ y,
+                                               i64 ldy, i64 nrhs, i64 tile) {
+    const int lane = threadIdx.x & 31;
+    const i64 item = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const i64 n_tiles = (nrhs + tile - 1) / tile;
+    if (item >= n_tiles * a.n_ids) return;
+    const i64 t = item / a.n_ids;
+    const int sid = a.ids[item - t * a.n_ids];
+    const i64 row = static_cast<i64>(sid) * 32 + lane;
+    const int base = a.base[sid];
+    const int rl = a.rlen[static_cast<i64>(sid) * 32 + lane];
+    const i64 f0 = t * tile, f1 = min(f0 + tile, nrhs);
+    const bool store = row < a.n_rows;
+    if constexpr (L > 0) {
+        int c[L];
+        float h[L], lw[L];
+#pragma unroll
+        for (int k = 0; k < L; ++k) {
+            if (k < rl) {
+                int e = base + k * 32 + lane;
+                c[k] = a.col[e];
+                h[k] = a.hi[e];
+                lw[k] = a.lo[e];
+            } else {
+                c[k] = 0;
+                h[k] = 0.f;
+                lw[k] = 0.f;
+            }
+        }
+        i64 f = f0;
+        if constexpr (U >= 2) {
+            F2 hp[L], hn[L], lp[L];
+#pragma unroll
+            for (int k = 0; k < L; ++k) {
+                hp[k] = pk(h[k], h[k]);
+                hn[k] = pk(-h[k], -h[k]);
+                lp[k] = pk(lw[k], lw[k]);
+            }
+            for (; f + U <= f1; f += U) {
+                F2 s[U / 2], cc[U / 2];
+#pragma unroll
+                for (int u = 0; u < U / 2; ++u) {
+                    s[u] = pk(0.f, 0.f);
+                    cc[u] = pk(0.f, 0.f);
+                }
+                const float *xf = x + f * ldx;
+#pragma unroll
+                for (int k = 0; k < L; ++k) {
+                    if (k < rl) {
+#pragma unroll
+                        for (int u = 0; u < U / 2; ++u) {
+                            float xa = ldg_f(xf + (2 * u) * ldx + c[k]);
+                            float xb = ldg_f(xf + (2 * u + 1) * ldx + c[k]);
+                            csum2(s[u], cc[u], hp[k], hn[k], lp[k], pk(xa, xb));
+                        }
+                    }
+                }
+                if (store) {
+#pragma unroll
+                    for (int u = 0; u < U / 2; ++u) {
+                        F2 r = add2(s[u], cc[u]);
+                        float ra, rb;
+                        upk(r, ra, rb);
+                        y[(f + 2 * u) * ldy + row] = ra;
+                        y[(f + 2 * u + 1) * ldy + row] = rb;
+                    }
+                }
+            }
+        }
+        for (; f < f1; ++f) {
+            float s = 0.f, cc = 0.f;
+            const float *xf = x + f * ldx;
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (k < rl) csum1(s, cc, h[k], lw[k], ldg_f(xf + c[k]));
+            if (store) y[f * ldy + row] = __fadd_rn(s, cc);
+        }
+    } else {
+        for (i64 f = f0; f < f1; ++f) {
+            float s = 0.f, cc = 0.f;
+            const float *xf = x + f * ldx;
+            for (int k = 0; k < rl; ++k) {
+                int e = base + k * 32 + lane;
+                csum1(s, cc, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
+            }
+            if (store) y[f * ldy + row] = __fadd_rn(s, cc);
+        }
+    }
+}
+
+// ─── FP64 kernel ───────────────────────────────────────────────────────────
+template <int L, int U>
+__global__ void __launch_bounds__(256) k_f64(SellArgs a, const double *__restrict__ x, i64 ldx, double *__restrict__ y,
+                                             i64 ldy, i64 nrhs, i64 tile) {
+    const int lane = threadIdx.x & 31;
+    const i64 item = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const i64 n_tiles = (nrhs + tile - 1) / tile;
+    if (item >= n_tiles * a.n_ids) return;
+    const i64 t = item / a.n_ids;
+    const int sid = a.ids[item - t * a.n_ids];
+    const i64 row = static_cast<i64>(sid) * 32 + lane;
+    const int base = a.base[sid];
+    const int rl = a.rlen[static_cast<i64>(sid) * 32 + lane];
+    const i64 f0 = t * tile, f1 = min(f0 + tile, nrhs);
+    const bool store = row < a.n_rows;
+    if constexpr (L > 0) {
+        int c[L];
+        double w[L];
+#pragma unroll
+        for (int k = 0; k < L; ++k) {
+            if (k < rl) {
+                int e = base + k * 32 + lane;
+                c[k] = a.col[e];
+                w[k] = a.w64[e];
+            } else {
+                c[k] = 0;
+                w[k] = 0.0;
+            }
+        }
+        i64 f = f0;
+        for (; f + U <= f1; f += U) {
+            double s[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) s[u] = 0.0;
+            const double *xf = x + f * ldx;
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (k < rl) {
+#pragma unroll
+                    for (int u = 0; u < U; ++u) s[u] = fma(w[k], __ldg(xf + u * ldx + c[k]), s[u]);
+                }
+            if (store) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) y[(f + u) * ldy + row] = s[u];
+            }
+        }
+        for (; f < f1; ++f) {
+            double s = 0.0;
+            const double *xf = x + f * ldx;
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (k < rl) s = fma(w[k], __ldg(xf + c[k]), s);
+            if (store) y[f * ldy + row] = s;
+        }
+    } else {
+        for (i64 f = f0; f < f1; ++f) {
+            double s = 0.0;
+            const double *xf = x + f * ldx;
+            for (int k = 0; k < rl; ++k) {
+                int e = base + k * 32 + lane;
+                s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
+            }
+            if (store) y[f * ldy + row] = s;
+        }
+    }
+}
+
+// ─── layout build ──────────────────────────────────────────────────────────
+
+__global__ void k_slice_len(const int *rp, i64 n_rows, i64 n_slices, int *len) {
+    i64 s = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= n_slices) return;
+    int m = 0;
+    for (int q = 0; q < 32; ++q) {
+        i64 r = s * 32 + q;
+        if (r < n_rows) m = max(m, rp[r + 1] - rp[r]);
+    }
+    len[s] = m * 32;  // entries of the slice; scanned into base
+}
+
+__global__ void k_sell_fill(const int *rp, const int *ccol, const double *val, i64 n_rows, i64 n_slices,
+                            const int *base, const int *slen32, int *rlen, int *col, float *hi, float *lo,
+                            double *w64) {
+    i64 r = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= n_slices * 32) return;
+    i64 s = r >> 5;
+    int lane = static_cast<int>(r & 31);
+    int L = slen32[s] / 32;
+    int b = base[s];
+    int n = 0, r0 = 0;
+    if (r < n_rows) {
+        r0 = rp[r];
+        n = rp[r + 1] - r0;
+    }
+    rlen[r] = n;
+    int last = n > 0 ? ccol[r0 + n - 1] : 0;
+    for (int k = 0; k < L; ++k) {
+        int e = b + k * 32 + lane;
+        if (k < n) {
+            double w = val[r0 + k];
+            col[e] = ccol[r0 + k];
+            if (hi) {
+                float h = __double2float_rn(w);
+                hi[e] = h;
+                lo[e] = __double2float_rn(w - static_cast<double>(h));
+            }
+            if (w64) w64[e] = w;
+        } else {
+            col[e] = last;
+            if (hi) {
+                hi[e] = 0.f;
+                lo[e] = 0.f;
+            }
+            if (w64) w64[e] = 0.0;
+        }
+    }
+}
+
+void build_sell(Matrix &m, int fmt, cudaStream_t s) {
+    Sell &S = fmt == 0 ? m.sell64 : m.sell32;
+    if (S.built) return;
+    const i64 n_rows = m.n_dst;
+    const i64 n_slices = (n_rows + 31) / 32;
+    DBuf<int> slen32(n_slices), base(n_slices + 1);
+    if (n_slices > 0) {
+        k_slice_len<<<nblk(n_slices, 256), 256, 0, s>>>(m.row_ptr.p, n_rows, n_slices, slen32.p);
+        AXGB_CUDA(cudaGetLastError());
+    }
+    scan_exclusive_i32(slen32.p, base.p, n_slices, s);
+    int total = 0;
+    AXGB_CUDA(cudaMemcpy(&total, base.p + n_slices, sizeof(int), cudaMemcpyDeviceToHost));
+    S.n_slices = n_slices;
+    S.n_entries = total;
+    S.col.alloc(total);
+    S.len.alloc(n_slices);
+    S.base = std::move(base);
+    DBuf<int> rlen(n_slices * 32);
+    if (fmt == 1) {
+        S.hi.alloc(total);
+        S.lo.alloc(total);
+    } else {
+        S.w64.alloc(total);
+    }
+    if (n_slices > 0) {
+        k_sell_fill<<<nblk(n_slices * 32, 256), 256, 0, s>>>(m.row_ptr.p, m.col.p, m.val.p, n_rows, n_slices,
+                                                            S.base.p, slen32.p, rlen.p, S.col.p,
+                                                            fmt == 1 ? S.hi.p : nullptr, fmt == 1 ? S.lo.p : nullptr,
+                                                            fmt == 0 ? S.w64.p : nullptr);
+        AXGB_CUDA(cudaGetLastError());
+    }
+    // length classes on the host
+    std::vector<int> h_len(n_slices);
+    if (n_slices) AXGB_CUDA(cudaMemcpy(h_len.data(), slen32.p, sizeof(int) * n_slices, cudaMemcpyDeviceToHost));
+    const int bounds[5] = {8, 16, 32, 64, 1 << 30};
+    std::vector<std::vector<int>> cls(5);
+    for (i64 q = 0; q < n_slices; ++q) {
+        int L = h_len[q] / 32;
+        int c = 0;
+        while (L > bounds[c]) ++c;
+        cls[c].push_back(static_cast<int>(q));
+    }
+    std::vector<int> ids;
+    S.class_begin.assign(6, 0);
+    S.class_maxlen.assign(5, 0);
+    for (int c = 0; c < 5; ++c) {
+        S.class_begin[c] = static_cast<i64>(ids.size());
+        for (int q : cls[c]) S.class_maxlen[c] = std::max(S.class_maxlen[c], h_len[q] / 32);
+        ids.insert(ids.end(), cls[c].begin(), cls[c].end());
+    }
+    S.class_begin[5] = static_cast<i64>(ids.size());
+    S.class_ids.upload(ids.data(), ids.size(), s);
+    // keep row lengths in the len buffer's companion: store rlen in 'len' slot
+    S.len = std::move(rlen);
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    S.built = true;
+}
+
+SellArgs sell_args(const Matrix &m, const Sell &S, int cls) {
+    SellArgs a;
+    a.ids = S.class_ids.p + S.class_begin[cls];
+    a.n_ids = S.class_begin[cls + 1] - S.class_begin[cls];
+    a.base = S.base.p;
+    a.len = nullptr;
+    a.rlen = S.len.p;
+    a.col = S.col.p;
+    a.hi = S.hi.p;
+    a.lo = S.lo.p;
+    a.w64 = S.w64.p;
+    a.n_rows = m.n_dst;
+    return a;
+}
+
+template <int L>
+void launch_split(const SellArgs &a, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, i64 tile, int U,
+                  cudaStream_t s) {
+    i64 items = ((nrhs + tile - 1) / tile) * a.n_ids;
+    if (items == 0) return;
+    unsigned blocks = nblk(items * 32, 256);
+    if (U >= 4)
+        k_split<L, 4><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
+    else if (U >= 2)
+        k_split<L, 2><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
+    else
+        k_split<L, 1><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
+}
+
+template <int L>
+void launch_f64(const SellArgs &a, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, i64 tile, cudaStream_t s) {
+    i64 items = ((nrhs + tile - 1) / tile) * a.n_ids;
+    if (items == 0) return;
+    unsigned blocks = nblk(items * 32, 256);
+    if (nrhs >= 2)
+        k_f64<L, 2><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
+    else
+        k_f64<L, 1><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
+}
+
+// ─── conservation ──────────────────────────────────────────────────────────
+
+template <class T>
+__global__ void k_integral(const T *f, const double *area, const double *frac, i64 n, int mode, double *partial) {
+    // mode 0: sum f*area*frac; 1: sum over frac != 0 of f*area (DstArea)
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<i64>(gridDim.x) * blockDim.x) {
+        double v = static_cast<double>(f[i]);
+        if (mode == 0)
+            acc += v * area[i] * frac[i];
+        else if (frac[i] != 0.0)
+            acc += v * area[i];
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+template <class T>
+double integral(const T *f, const double *area, const double *frac, i64 n, int mode, cudaStream_t s) {
+    const int blocks = 1024;
+    DBuf<double> part(blocks);
+    k_integral<T><<<blocks, 256, 0, s>>>(f, area, frac, n, mode, part.p);
+    AXGB_CUDA(cudaGetLastError());
+    std::vector<double> h(blocks);
+    AXGB_CUDA(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * blocks, cudaMemcpyDeviceToHost, s));
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    double acc = 0.0;
+    for (double v : h) acc += v;
+    return acc;
+}
+
+// ─── persistent batch kernel ───────────────────────────────────────────────
+// Items of all matrices are handed out by one atomic counter (no waiting):
+// item -> (matrix, tile, slice). Entries of up to 32 per row are cached in
+// registers; longer rows are read from global memory.
+__global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ desc, int n_desc, i64 total,
+                                               unsigned long long *counter) {
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        unsigned long long it = 0;
+        if (lane == 0) it = atomicAdd(counter, 1ull);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (static_cast<i64>(it) >= total) return;
+        int m = 0;
+        while (m + 1 < n_desc && desc[m + 1].item_begin <= static_cast<i64>(it)) ++m;
+        const Batch::Desc &d = desc[m];
+        i64 local = static_cast<i64>(it) - d.item_begin;
+        i64 t = local / d.n_slices;
+        i64 sid = local - t * d.n_slices;
+        i64 row = sid * 32 + lane;
+        int base = d.base[sid];
+        int rl = d.rlen[sid * 32 + lane];
+        i64 f0 = t * d.tile, f1 = min(f0 + d.tile, d.nrhs);
+        bool store = row < d.n_rows;
+        constexpr int L = 32;
+        int c[L];
+        float h[L], lw[L];
+#pragma unroll
+        for (int k = 0; k < L; ++k) {
+            if (k < rl) {
+                int e = base + k * 32 + lane;
+                c[k] = d.col[e];
+                h[k] = d.hi[e];
+                lw[k] = d.lo[e];
+            } else {
+                c[k] = 0;
+                h[k] = 0.f;
+                lw[k] = 0.f;
+            }
+        }
+        for (i64 f = f0; f < f1; ++f) {
+            float s = 0.f, cc = 0.f;
+            const float *xf = d.x + f * d.ldx;
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (k < rl) csum1(s, cc, h[k], lw[k], __ldg(xf + c[k]));
+            for (int k = L; k < rl; ++k) {
+                int e = base + k * 32 + lane;
+                csum1(s, cc, d.hi[e], d.lo[e], __ldg(xf + d.col[e]));
+            }
+            if (store) d.y[f * d.ldy + row] = __fadd_rn(s, cc);
+        }
+    }
+}
+
+}  // namespace
+
+void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
+    std::lock_guard<std::mutex> lk(m.mu);
+    build_sell(m, format == 0 ? 0 : 1, s);
+    const Sell &S = format == 0 ? m.sell64 : m.sell32;
+    int launches = 0;
+    for (int c = 0; c < 5; ++c)
+        if (S.class_begin[c + 1] > S.class_begin[c]) ++launches;
+    m.stats[format == 0 ? 6 : 5] = launches;
+}
+
+void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, int fields_per_pass, int unroll,
+                 cudaStream_t s) {
+    if (!m.sell32.built) matrix_prepare(m, 1, s);
+    const Sell &S = m.sell32;
+    i64 tile = (fields_per_pass <= 0 || fields_per_pass > nrhs) ? nrhs : fields_per_pass;
+    if (tile <= 0) return;
+    launch_split<8>(sell_args(m, S, 0), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    launch_split<16>(sell_args(m, S, 1), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    launch_split<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    launch_split<64>(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    launch_split<0>(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    AXGB_CUDA(cudaGetLastError());
+}
+
+void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    if (!m.sell64.built) matrix_prepare(m, 0, s);
+    const Sell &S = m.sell64;
+    i64 tile = nrhs;
+    if (tile <= 0) return;
+    launch_f64<8>(sell_args(m, S, 0), x, ldx, y, ldy, nrhs, tile, s);
+    launch_f64<16>(sell_args(m, S, 1), x, ldx, y, ldy, nrhs, tile, s);
+    launch_f64<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, s);
+    launch_f64<64>(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, tile, s);
+    launch_f64<0>(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, tile, s);
+    AXGB_CUDA(cudaGetLastError());
+}
+
+void conservation(Matrix &m, const void *src, const void *dst, bool f32, int norm_type, double *out, cudaStream_t s) {
+    double si, di;
+    if (f32) {
+        si = integral(static_cast<const float *>(src), m.area_a.p, m.frac_a.p, m.n_src, 0, s);
+        di = integral(static_cast<const float *>(dst), m.area_b.p, m.frac_b.p, m.n_dst, norm_type == 0 ? 1 : 0, s);
+    } else {
+        si = integral(static_cast<const double *>(src), m.area_a.p, m.frac_a.p, m.n_src, 0, s);
+        di = integral(static_cast<const double *>(dst), m.area_b.p, m.frac_b.p, m.n_dst, norm_type == 0 ? 1 : 0, s);
+    }
+    double ae = std::abs(si - di);
+    double den = std::max({std::abs(si), std::abs(di), 2.220446049250313e-16});
+    out[0] = si;
+    out[1] = di;
+    out[2] = ae;
+    out[3] = ae / den;
+}
+
+std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &mats, const std::vector<i64> &nrhs) {
+    auto b = std::make_shared<Batch>();
+    b->mats = mats;
+    b->nrhs = nrhs;
+    i64 items = 0;
+    for (size_t q = 0; q < mats.size(); ++q) {
+        Matrix &m = *mats[q];
+        matrix_prepare(m, 1, 0);
+        Batch::Desc d{};
+        d.base = m.sell32.base.p;
+        d.len = nullptr;
+        d.rlen = m.sell32.len.p;
+        d.col = m.sell32.col.p;
+        d.hi = m.sell32.hi.p;
+        d.lo = m.sell32.lo.p;
+        d.n_rows = m.n_dst;
+        d.n_slices = m.sell32.n_slices;
+        d.nrhs = nrhs[q];
+        d.tile = std::max<i64>(1, std::min<i64>(nrhs[q], 8));
+        d.n_tiles = (nrhs[q] + d.tile - 1) / d.tile;
+        d.item_begin = items;
+        items += d.n_tiles * d.n_slices;
+        b->desc.push_back(d);
+    }
+    b->total_items = items;
+    b->d_desc.alloc(std::max<size_t>(1, b->desc.size()));
+    b->counter.alloc(1);
+    int dev = 0, sms = 0;
+    AXGB_CUDA(cudaGetDevice(&dev));
+    AXGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int per_sm = 0;
+    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0));
+    b->blocks = std::max(1, sms * std::max(1, per_sm));
+    return b;
+}
+
+void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *y, const i64 *ldy, cudaStream_t s) {
+    std::lock_guard<std::mutex> lk(b.mu);
+    const size_t k = b.desc.size();
+    std::vector<const void *> ptrs;
+    for (size_t q = 0; q < k; ++q) {
+        AXGB_REQUIRE(ldx[q] >= b.mats[q]->n_src && ldy[q] >= b.mats[q]->n_dst, "batch_apply: leading dimension");
+        ptrs.push_back(x[q]);
+        ptrs.push_back(y[q]);
+        ptrs.push_back(reinterpret_cast<const void *>(ldx[q]));
+        ptrs.push_back(reinterpret_cast<const void *>(ldy[q]));
+    }
+    if (ptrs != b.last_ptrs) {
+        for (size_t q = 0; q < k; ++q) {
+            b.desc[q].x = x[q];
+            b.desc[q].ldx = ldx[q];
+            b.desc[q].y = y[q];
+            b.desc[q].ldy = ldy[q];
+        }
+        // stream-ordered update of the descriptors the graph reads
+        AXGB_CUDA(cudaMemcpyAsync(b.d_desc.p, b.desc.data(), sizeof(Batch::Desc) * k, cudaMemcpyHostToDevice, s));
+        AXGB_CUDA(cudaStreamSynchronize(s));
+        b.last_ptrs = ptrs;
+    }
+    if (b.total_items == 0) return;
+    auto it = b.graphs.find(s);
+    if (it == b.graphs.end()) {
+        cudaStream_t cap = s;
+        bool own = false;
+        if (cap == 0) {  // legacy stream cannot be captured: capture on a private stream
+            AXGB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            own = true;
+        }
+        cudaGraph_t g;
+        cudaGraphExec_t ge;
+        AXGB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        cudaMemsetAsync(b.counter.p, 0, sizeof(unsigned long long), cap);
+        k_batch<<<b.blocks, 256, 0, cap>>>(b.d_desc.p, static_cast<int>(k), b.total_items, b.counter.p);
+        AXGB_CUDA(cudaStreamEndCapture(cap, &g));
+        AXGB_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        if (own) AXGB_CUDA(cudaStreamDestroy(cap));
+        it = b.graphs.emplace(s, std::make_pair(g, ge)).first;
+    }
+    AXGB_CUDA(cudaGraphLaunch(it->second.second, s));
+}
+
+}  // namespace axgb

@@ -1,0 +1,647 @@
+// Weight generation on the device.
+//
+// Conservative (Conservative1stOrder, GreatCircle) replaces
+// generate_conservative_impl<3> (libs/axis/src/solver/weight_generator.cpp:
+// 3304-3770):
+//   1. cell prep per mesh (prep.cu);
+//   2. an LBVH over the source cells' bounding caps: 30-bit Morton codes of
+//      the cap centroids, radix-sorted leaves, Karras hierarchy, bottom-up
+//      refit of FP32 boxes padded outward, and per-node ropes (escape
+//      links) for stackless traversal;
+//   3. one thread per destination cell walks the ropes; every leaf hit goes
+//      through the reference's exact gates (source mask / degenerate /
+//      area > 0, the reference's float AABB test, the FP64 cap test) and is
+//      counted (pass 1) or written (pass 2) row-grouped, so the candidate
+//      list is deterministic;
+//   4. one thread per candidate runs the FP64 great-circle clip and the
+//      spherical area (geom.cuh, --fmad=false); pairs whose polygons
+//      exceed 16 vertices are redone with the reference's 32-vertex cap;
+//   5. kept pairs (overlap > 0, the reference threshold at :3682) are
+//      compacted, radix-sorted by (row, col) into CSR, and the weights,
+//      frac_b (row order) and frac_a (column order, rows ascending) sums are
+//      formed per row / per column by one thread each.
+// Bilinear with a rectilinear source replaces
+// generate_bilinear_rect_nonuniform
+// (src/solver/weight_generator_bilinear_rect_nonuniform.cpp:22-149).
+#include <chrono>
+
+#include "geom.cuh"
+#include "internal.hpp"
+
+namespace axgb {
+namespace {
+
+constexpr unsigned char kExcluded = 1 | 2 | 4;  // degenerate | masked | area <= 0
+
+// ─── LBVH ──────────────────────────────────────────────────────────────────
+
+__device__ __forceinline__ unsigned spread10(unsigned v) {
+    v &= 1023u;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ unsigned morton30(double x, double y, double z) {
+    auto q = [](double t) {
+        double u = (t + 1.0) * 512.0;
+        u = fmin(fmax(u, 0.0), 1023.0);
+        return static_cast<unsigned>(u);
+    };
+    return (spread10(q(x)) << 2) | (spread10(q(y)) << 1) | spread10(q(z));
+}
+
+// Chord radius of a cap of angular radius r, rounded up into float with
+// slack for the float rounding of the centre (|dc| <= 2^-24 per axis).
+__device__ __forceinline__ float ball_radius(double r) {
+    double rho = 2.0 * sin(0.5 * fmin(r, 3.141592653589793));
+    return __double2float_ru(rho * (1.0 + 1e-6) + 1e-6);
+}
+
+__global__ void k_leaf_keys(MeshView S, unsigned *keys, int *vals) {
+    i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= S.n_cells) return;
+    DCap c = S.cap[i];
+    keys[i] = morton30(c.x, c.y, c.z);
+    vals[i] = static_cast<int>(i);
+}
+
+struct Bvh {
+    int n;          // leaves
+    int root;
+    float4 *lo;     // [2n-1] (lo.xyz, left child | cell)
+    float4 *hi;     // [2n-1] (hi.xyz, rope)
+    int *parent;    // [2n-1]
+    int *right;     // [n-1] right child of internal nodes
+    int *flag;      // [n-1] refit arrival counters
+    const unsigned *keys;  // sorted Morton keys [n]
+};
+
+__device__ __forceinline__ int delta(const unsigned *k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    unsigned a = k[i], b = k[j];
+    if (a == b) return 32 + __clz(static_cast<unsigned>(i ^ j));
+    return __clz(a ^ b);
+}
+
+// Internal node i of the Karras (2012) radix tree over sorted keys.
+__global__ void k_internal(Bvh t) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = t.n;
+    if (i >= n - 1) return;
+    const unsigned *k = t.keys;
+    int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(k, n, i, i - d);
+    int lmax = 2;
+    while (delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int s = lmax >> 1; s >= 1; s >>= 1)
+        if (delta(k, n, i, i + (l + s) * d) > dmin) l += s;
+    int j = i + l * d;
+    int dn = delta(k, n, i, j);
+    int s = 0;
+    int step = l;
+    do {
+        step = (step + 1) >> 1;
+        if (delta(k, n, i, i + (s + step) * d) > dn) s += step;
+    } while (step > 1);
+    int g = i + s * d + min(d, 0);
+    int lo_i = min(i, j), hi_i = max(i, j);
+    int left = (lo_i == g) ? (n - 1 + g) : g;
+    int right = (hi_i == g + 1) ? (n - 1 + g + 1) : (g + 1);
+    t.lo[i].w = __int_as_float(left);
+    t.right[i] = right;
+    t.parent[left] = i;
+    t.parent[right] = i;
+}
+
+__global__ void k_leaves(Bvh t, MeshView S, const int *vals) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= t.n) return;
+    int cell = vals[q];
+    DCap c = S.cap[cell];
+    float r = ball_radius(c.r);
+    float4 lo, hi;
+    lo.x = __fsub_rd(__double2float_rd(c.x), r);
+    lo.y = __fsub_rd(__double2float_rd(c.y), r);
+    lo.z = __fsub_rd(__double2float_rd(c.z), r);
+    hi.x = __fadd_ru(__double2float_ru(c.x), r);
+    hi.y = __fadd_ru(__double2float_ru(c.y), r);
+    hi.z = __fadd_ru(__double2float_ru(c.z), r);
+    lo.w = __int_as_float(cell);
+    hi.w = __int_as_float(-1);
+    t.lo[t.n - 1 + q] = lo;
+    t.hi[t.n - 1 + q] = hi;
+}
+
+__global__ void k_refit(Bvh t) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= t.n || t.n < 2) return;
+    int node = t.parent[t.n - 1 + q];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&t.flag[node], 1) == 0) return;  // first child to arrive stops
+        int l = __float_as_int(__ldcg(&t.lo[node].w));
+        int r = __ldcg(&t.right[node]);
+        float4 al = __ldcg(&t.lo[l]), ah = __ldcg(&t.hi[l]);
+        float4 bl = __ldcg(&t.lo[r]), bh = __ldcg(&t.hi[r]);
+        float4 nl = t.lo[node], nh;
+        nl.x = fminf(al.x, bl.x);
+        nl.y = fminf(al.y, bl.y);
+        nl.z = fminf(al.z, bl.z);
+        nh.x = fmaxf(ah.x, bh.x);
+        nh.y = fmaxf(ah.y, bh.y);
+        nh.z = fmaxf(ah.z, bh.z);
+        nh.w = __int_as_float(-1);
+        __stcg(&t.lo[node], nl);
+        __stcg(&t.hi[node], nh);
+        node = (node == t.root) ? -1 : t.parent[node];
+    }
+}
+
+// rope(x): the right sibling of the first left-child ancestor-or-self of x.
+__global__ void k_ropes(Bvh t) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int total = 2 * t.n - 1;
+    if (x >= total) return;
+    int node = x, rope = -1;
+    while (node != t.root) {
+        int p = t.parent[node];
+        int l = __float_as_int(t.lo[p].w);
+        if (l == node) {
+            rope = t.right[p];
+            break;
+        }
+        node = p;
+    }
+    t.hi[x].w = __int_as_float(rope);
+}
+
+// ─── candidate search (two passes) ─────────────────────────────────────────
+
+__device__ __forceinline__ bool fbox_meet(const float *a, const float *b) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        if (a[d] > b[3 + d] || a[3 + d] < b[d]) return false;
+    return true;
+}
+
+// Exact reference gates for a pair that the LBVH admitted.
+__device__ __forceinline__ bool gate(const MeshView &S, int i, const float *dbox, const DCap &dc) {
+    if (S.flags[i] & kExcluded) return false;
+    if (!fbox_meet(S.box + 6 * static_cast<i64>(i), dbox)) return false;
+    DCap sc = S.cap[i];
+    double cd = sc.x * dc.x + sc.y * dc.y + sc.z * dc.z;  // dot(centroid_s, centroid_d)
+    cd = fmin(1.0, fmax(-1.0, cd));
+    return !(acos(cd) > (sc.r + dc.r));
+}
+
+template <bool FILL>
+__global__ void k_search(MeshView S, MeshView D, const float4 *__restrict__ nlo, const float4 *__restrict__ nhi,
+                         int root, int n_leaf_base, int *counts, const i64 *offs, int *out_src,
+                         unsigned long long *raw_hits, int *err) {
+    i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    unsigned long long hits = 0;
+    if (j < D.n_cells) {
+        int cnt = 0;
+        if (!(D.flags[j] & kExcluded) && root >= 0) {
+            DCap dc = D.cap[j];
+            float dbox[6];
+#pragma unroll
+            for (int d = 0; d < 6; ++d) dbox[d] = D.box[6 * j + d];
+            float qx = static_cast<float>(dc.x), qy = static_cast<float>(dc.y), qz = static_cast<float>(dc.z);
+            float rq = ball_radius(dc.r);
+            float rq2 = __fmul_ru(rq, rq) * 1.000001f + 1e-12f;
+            i64 wbase = FILL ? offs[j] : 0;
+            int node = root;
+            // Ropes visit every node at most once; a longer walk means a
+            // malformed tree: flag it and stop instead of spinning.
+            const int max_steps = 2 * (2 * n_leaf_base + 1) + 8;
+            int steps = 0;
+            while (node >= 0) {
+                if (++steps > max_steps) {
+                    atomicOr(err, 1);
+                    break;
+                }
+                float4 lo = nlo[node], hi = nhi[node];
+                float dx = fmaxf(fmaxf(lo.x - qx, 0.f), qx - hi.x);
+                float dy = fmaxf(fmaxf(lo.y - qy, 0.f), qy - hi.y);
+                float dz = fmaxf(fmaxf(lo.z - qz, 0.f), qz - hi.z);
+                float d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 <= rq2) {
+                    if (node >= n_leaf_base) {
+                        int cell = __float_as_int(lo.w);
+                        ++hits;
+                        if (gate(S, cell, dbox, dc)) {
+                            if (FILL) out_src[wbase + cnt] = cell;
+                            ++cnt;
+                        }
+                        node = __float_as_int(hi.w);
+                    } else {
+                        node = __float_as_int(lo.w);
+                    }
+                } else {
+                    node = __float_as_int(hi.w);
+                }
+            }
+        }
+        if (!FILL) counts[j] = cnt;
+    }
+    if (!FILL) {
+        // warp-aggregated counter of raw leaf hits
+        for (int o = 16; o > 0; o >>= 1) hits += __shfl_down_sync(0xffffffffu, hits, o);
+        if ((threadIdx.x & 31) == 0 && hits) atomicAdd(raw_hits, hits);
+    }
+}
+
+__global__ void k_fill_rows(const i64 *offs, i64 n_dst, int *out_dst) {
+    i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n_dst) return;
+    for (i64 k = offs[j]; k < offs[j + 1]; ++k) out_dst[k] = static_cast<int>(j);
+}
+
+// ─── clipping ──────────────────────────────────────────────────────────────
+
+template <int CAP>
+__device__ __forceinline__ void load_poly(const MeshView &m, i64 c, DPoly<CAP> &p) {
+    p.clear();
+    if (m.regular) {
+        // node trig cache (trig_cache.hpp:284-289, weight_generator.cpp:492-520)
+        const int ni = m.ni, nj = m.nj;
+        const double *slon = m.trig, *clon = m.trig + (ni + 1), *slat = m.trig + 2 * (ni + 1),
+                     *clat = m.trig + 2 * (ni + 1) + (nj + 1);
+        i64 ci = c % ni, cj = c / ni;
+        auto at = [&](i64 i, i64 j) {
+            double cl = clat[j];
+            p.push({cl * clon[i], cl * slon[i], slat[j]});
+        };
+        at(ci, cj);
+        at(ci + 1, cj);
+        at(ci + 1, cj + 1);
+        at(ci, cj + 1);
+    } else {
+        const int b = m.off[c], e = m.off[c + 1];
+        for (int k = b; k < e && k < b + 32; ++k) {
+            const double *q = m.xyz + 3 * static_cast<i64>(m.idx[k]);
+            p.push({q[0], q[1], q[2]});
+        }
+    }
+}
+
+template <int CAP>
+__global__ void __launch_bounds__(128) k_clip(MeshView S, MeshView D, const int *__restrict__ cs,
+                                              const int *__restrict__ cd, i64 n, const int *list, double *ov,
+                                              int *over_list, int *n_over) {
+    i64 t = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    i64 k = list ? list[t] : t;
+    DPoly<CAP> sp, dp, ba, bb;
+    load_poly(S, cs[k], sp);
+    load_poly(D, cd[k], dp);
+    bool over = false;
+    double a = d_overlap_area(sp, dp, ba, bb, &over);
+    if (over && CAP < 32) {
+        int q = atomicAdd(n_over, 1);
+        over_list[q] = static_cast<int>(k);
+        ov[k] = 0.0;
+    } else {
+        ov[k] = a;
+    }
+}
+
+// ─── assembly ──────────────────────────────────────────────────────────────
+
+__global__ void k_keep_flags(const double *ov, i64 n, int *keep) {
+    i64 k = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n) keep[k] = ov[k] > 0.0 ? 1 : 0;
+}
+
+__global__ void k_compact(const double *ov, const int *cs, const int *cd, const i64 *pos, i64 n,
+                          std::uint64_t *key, int *vals, double *kov) {
+    i64 k = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (ov[k] > 0.0) {
+        i64 p = pos[k];
+        key[p] = (static_cast<unsigned long long>(cd[k]) << 32) | static_cast<unsigned>(cs[k]);
+        vals[p] = static_cast<int>(p);
+        kov[p] = ov[k];
+    }
+}
+
+__global__ void k_count_keys(const std::uint64_t *key, i64 n, int *cnt) {
+    i64 k = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n) atomicAdd(&cnt[key[k] >> 32], 1);
+}
+
+__global__ void k_csr_cols(const std::uint64_t *key, const int *perm, const double *kov, i64 n, int *col,
+                           double *ov_sorted, std::uint64_t *key2, int *vals2) {
+    i64 k = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    unsigned long long kk = key[k];
+    unsigned i = static_cast<unsigned>(kk & 0xffffffffu);
+    unsigned j = static_cast<unsigned>(kk >> 32);
+    col[k] = static_cast<int>(i);
+    ov_sorted[k] = kov[perm[k]];
+    key2[k] = (static_cast<unsigned long long>(i) << 32) | j;
+    vals2[k] = static_cast<int>(k);
+}
+
+// Weights and frac_b per row (weight_generator.cpp:3684-3716).
+__global__ void k_rows(const int *row_ptr, const double *ov, const double *area_dst, i64 n_dst, int fracarea,
+                       double *w, double *frac_b) {
+    i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n_dst) return;
+    double ad = area_dst[j];
+    double fb = 0.0;
+    for (int k = row_ptr[j]; k < row_ptr[j + 1]; ++k) {
+        double o = ov[k];
+        double wij = o / ad;
+        w[k] = fmax(wij, 0.0);
+        fb += o / ad;
+    }
+    if (fracarea && fb > 0.0)
+        for (int k = row_ptr[j]; k < row_ptr[j + 1]; ++k) w[k] /= fb;
+    frac_b[j] = fmin(fb, 1.0);
+}
+
+// frac_a per source cell, contributions in ascending row order.
+__global__ void k_cols(const int *col_ptr, const int *perm2, const double *ov, const double *area_src, i64 n_src,
+                       double *frac_a) {
+    i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n_src) return;
+    double as = area_src[i];
+    double fa = 0.0;
+    for (int k = col_ptr[i]; k < col_ptr[i + 1]; ++k) fa += ov[perm2[k]] / as;
+    frac_a[i] = fmin(fa, 1.0);
+}
+
+__global__ void k_unmapped(MeshView D, const int *row_ptr, int *bad) {
+    i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= D.n_cells) return;
+    unsigned char f = D.flags[j];
+    if (f & (1 | 2)) return;  // degenerate or masked
+    if ((f & 4) || row_ptr[j + 1] == row_ptr[j]) atomicAdd(bad, 1);
+}
+
+// ─── bilinear (rectilinear source) ─────────────────────────────────────────
+
+__device__ int upper_bound_d(const double *a, int n, double v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (!(v < a[mid])) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_bilinear(MeshView D, const double *clon, int ni, const double *clat, int nj, int *row_ptr, int *col,
+                           double *w) {
+    i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c > D.n_cells) return;
+    row_ptr[c] = static_cast<int>(4 * c);
+    if (c == D.n_cells) return;
+    int b = D.off[c], e = D.off[c + 1];
+    double ls = 0.0, ts = 0.0;
+    for (int k = b; k < e; ++k) {
+        i64 n = D.idx[k];
+        ls += D.lonlat[n];
+        ts += D.lonlat[n + D.n_nodes];
+    }
+    double ld = ls / static_cast<double>(e - b);
+    double td = ts / static_cast<double>(e - b);
+    int i = upper_bound_d(clon, ni, ld) - 1;
+    int j = upper_bound_d(clat, nj, td) - 1;
+    if (i < 0) i = 0;
+    if (i >= ni - 1) i = ni - 2;
+    if (i < 0) i = 0;
+    if (j < 0) j = 0;
+    if (j >= nj - 1) j = nj - 2;
+    if (j < 0) j = 0;
+    double x0 = clon[i], x1 = clon[i + 1], y0 = clat[j], y1 = clat[j + 1];
+    double tx = (ld - x0) / (x1 - x0);
+    double ty = (td - y0) / (y1 - y0);
+    tx = fmax(0.0, fmin(1.0, tx));
+    ty = fmax(0.0, fmin(1.0, ty));
+    i64 o = 4 * c;
+    col[o] = j * ni + i;
+    col[o + 1] = j * ni + i + 1;
+    col[o + 2] = (j + 1) * ni + i;
+    col[o + 3] = (j + 1) * ni + i + 1;
+    w[o] = (1.0 - tx) * (1.0 - ty);
+    w[o + 1] = tx * (1.0 - ty);
+    w[o + 2] = (1.0 - tx) * ty;
+    w[o + 3] = tx * ty;
+}
+
+__global__ void k_fill(double *a, i64 n, double v) {
+    i64 k = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n) a[k] = v;
+}
+
+inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
+
+using Clock = std::chrono::steady_clock;
+inline double ms_since(Clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+}  // namespace
+
+void generate_conservative(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {
+    cudaStream_t s = 0;
+    auto t_all = Clock::now();
+    auto t0 = Clock::now();
+    mesh_prepare(src, s);
+    mesh_prepare(dst, s);
+    out.times_ms[0] = ms_since(t0);
+    MeshView S = src.view(), D = dst.view();
+    const i64 n_src = src.n_cells, n_dst = dst.n_cells;
+    AXGB_REQUIRE(n_src < (i64(1) << 31) - 1 && n_dst < (i64(1) << 31) - 1, "meshes above 2^31 cells");
+    out.n_src = n_src;
+    out.n_dst = n_dst;
+
+    // 2. LBVH
+    t0 = Clock::now();
+    const int n = static_cast<int>(n_src);
+    DBuf<float4> nlo(n > 0 ? 2 * n - 1 : 1), nhi(n > 0 ? 2 * n - 1 : 1);
+    DBuf<int> parent(n > 0 ? 2 * n - 1 : 1), right(n > 1 ? n - 1 : 1), flag(n > 1 ? n - 1 : 1);
+    int root = -1;
+    if (n > 0) {
+        DBuf<unsigned> keys(n);
+        DBuf<int> vals(n);
+        k_leaf_keys<<<nblk(n, 256), 256, 0, s>>>(S, keys.p, vals.p);
+        AXGB_CUDA(cudaGetLastError());
+        radix_sort_pairs_u32(keys.p, vals.p, n, 30, s);
+        Bvh t{n, n > 1 ? 0 : 0, nlo.p, nhi.p, parent.p, right.p, flag.p, keys.p};
+        root = 0;  // internal node 0, or the single leaf (index n-1 = 0)
+        AXGB_CUDA(cudaMemsetAsync(parent.p, 0xff, sizeof(int) * (2 * n - 1), s));
+        flag.zero(s);
+        k_leaves<<<nblk(n, 256), 256, 0, s>>>(t, S, vals.p);
+        if (n > 1) {
+            k_internal<<<nblk(n - 1, 256), 256, 0, s>>>(t);
+            k_refit<<<nblk(n, 256), 256, 0, s>>>(t);
+        }
+        k_ropes<<<nblk(2 * n - 1, 256), 256, 0, s>>>(t);
+        AXGB_CUDA(cudaGetLastError());
+        AXGB_CUDA(cudaStreamSynchronize(s));
+    }
+    out.stats[4] = n > 0 ? 2 * n - 1 : 0;
+    out.times_ms[1] = ms_since(t0);
+
+    // 3. candidates
+    t0 = Clock::now();
+    DBuf<int> counts(n_dst);
+    DBuf<i64> offs(n_dst + 1);
+    DBuf<unsigned long long> raw(1);
+    raw.zero(s);
+    const int n_leaf_base = n > 0 ? n - 1 : 0;
+    DBuf<int> err(1);
+    err.zero(s);
+    k_search<false><<<nblk(n_dst, 128), 128, 0, s>>>(S, D, nlo.p, nhi.p, root, n_leaf_base, counts.p, nullptr,
+                                                    nullptr, raw.p, err.p);
+    AXGB_CUDA(cudaGetLastError());
+    scan_exclusive_i32_to_i64(counts.p, offs.p, n_dst, s);
+    i64 n_cand = 0;
+    unsigned long long n_raw = 0;
+    AXGB_CUDA(cudaMemcpy(&n_cand, offs.p + n_dst, sizeof(i64), cudaMemcpyDeviceToHost));
+    AXGB_CUDA(cudaMemcpy(&n_raw, raw.p, sizeof(n_raw), cudaMemcpyDeviceToHost));
+    AXGB_REQUIRE(n_cand < (i64(1) << 31), "more than 2^31 candidate pairs");
+    DBuf<int> cs(n_cand), cd(n_cand);
+    if (n_cand > 0) {
+        k_search<true><<<nblk(n_dst, 128), 128, 0, s>>>(S, D, nlo.p, nhi.p, root, n_leaf_base, nullptr, offs.p, cs.p,
+                                                       nullptr, err.p);
+        k_fill_rows<<<nblk(n_dst, 256), 256, 0, s>>>(offs.p, n_dst, cd.p);
+        AXGB_CUDA(cudaGetLastError());
+    }
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    int h_err = 0;
+    AXGB_CUDA(cudaMemcpy(&h_err, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h_err) throw Error(AXGB_ERROR, "LBVH traversal exceeded its step bound (malformed tree)");
+    out.stats[0] = static_cast<i64>(n_raw);
+    out.stats[1] = n_cand;
+    out.times_ms[2] = ms_since(t0);
+
+    // 4. clip
+    t0 = Clock::now();
+    DBuf<double> ov(n_cand);
+    DBuf<int> over_list(n_cand), n_over(1);
+    n_over.zero(s);
+    int h_over = 0;
+    if (n_cand > 0) {
+        k_clip<16><<<nblk(n_cand, 128), 128, 0, s>>>(S, D, cs.p, cd.p, n_cand, nullptr, ov.p, over_list.p, n_over.p);
+        AXGB_CUDA(cudaGetLastError());
+        AXGB_CUDA(cudaMemcpy(&h_over, n_over.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h_over > 0) {
+            k_clip<32><<<nblk(h_over, 64), 64, 0, s>>>(S, D, cs.p, cd.p, h_over, over_list.p, ov.p, nullptr, nullptr);
+            AXGB_CUDA(cudaGetLastError());
+        }
+    }
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    out.stats[2] = h_over;
+    out.times_ms[3] = ms_since(t0);
+
+    // 5. assembly
+    t0 = Clock::now();
+    DBuf<int> keep(n_cand);
+    DBuf<i64> pos(n_cand + 1);
+    i64 nnz = 0;
+    if (n_cand > 0) {
+        k_keep_flags<<<nblk(n_cand, 256), 256, 0, s>>>(ov.p, n_cand, keep.p);
+        scan_exclusive_i32_to_i64(keep.p, pos.p, n_cand, s);
+        AXGB_CUDA(cudaMemcpy(&nnz, pos.p + n_cand, sizeof(i64), cudaMemcpyDeviceToHost));
+    }
+    DBuf<std::uint64_t> key(nnz), key2(nnz);
+    DBuf<int> vals(nnz), vals2(nnz);
+    DBuf<double> kov(nnz);
+    out.row_ptr.alloc(n_dst + 1);
+    out.col.alloc(nnz);
+    out.val.alloc(nnz);
+    out.frac_a.alloc(n_src);
+    out.frac_b.alloc(n_dst);
+    out.area_a.alloc(n_src);
+    out.area_b.alloc(n_dst);
+    DBuf<double> ovs(nnz);
+    DBuf<int> rcnt(n_dst), ccnt(n_src), col_ptr(n_src + 1);
+    rcnt.zero(s);
+    ccnt.zero(s);
+    if (nnz > 0) {
+        k_compact<<<nblk(n_cand, 256), 256, 0, s>>>(ov.p, cs.p, cd.p, pos.p, n_cand, key.p, vals.p, kov.p);
+        int rbits = 32;
+        while (rbits < 64 && (static_cast<unsigned long long>(n_dst) >> (rbits - 32)) > 0) ++rbits;
+        radix_sort_pairs_u64(key.p, vals.p, nnz, rbits, s);
+        k_count_keys<<<nblk(nnz, 256), 256, 0, s>>>(key.p, nnz, rcnt.p);
+        k_csr_cols<<<nblk(nnz, 256), 256, 0, s>>>(key.p, vals.p, kov.p, nnz, out.col.p, ovs.p, key2.p, vals2.p);
+        AXGB_CUDA(cudaGetLastError());
+        int cbits = 32;
+        while (cbits < 64 && (static_cast<unsigned long long>(n_src) >> (cbits - 32)) > 0) ++cbits;
+        radix_sort_pairs_u64(key2.p, vals2.p, nnz, cbits, s);
+        k_count_keys<<<nblk(nnz, 256), 256, 0, s>>>(key2.p, nnz, ccnt.p);
+        AXGB_CUDA(cudaGetLastError());
+    }
+    scan_exclusive_i32(rcnt.p, out.row_ptr.p, n_dst, s);
+    scan_exclusive_i32(ccnt.p, col_ptr.p, n_src, s);
+    AXGB_CUDA(cudaMemcpyAsync(out.area_a.p, S.area, sizeof(double) * n_src, cudaMemcpyDeviceToDevice, s));
+    AXGB_CUDA(cudaMemcpyAsync(out.area_b.p, D.area, sizeof(double) * n_dst, cudaMemcpyDeviceToDevice, s));
+    if (n_dst > 0)
+        k_rows<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, ovs.p, D.area, n_dst,
+                                               cfg.norm_type == AXGB_FRACAREA ? 1 : 0, out.val.p, out.frac_b.p);
+    if (n_src > 0)
+        k_cols<<<nblk(n_src, 256), 256, 0, s>>>(col_ptr.p, vals2.p, ovs.p, S.area, n_src, out.frac_a.p);
+    AXGB_CUDA(cudaGetLastError());
+    if (cfg.unmapped == AXGB_UNMAPPED_ERROR && n_dst > 0) {
+        DBuf<int> bad(1);
+        bad.zero(s);
+        k_unmapped<<<nblk(n_dst, 256), 256, 0, s>>>(D, out.row_ptr.p, bad.p);
+        int h_bad = 0;
+        AXGB_CUDA(cudaMemcpy(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h_bad > 0)
+            throw Error(AXGB_ERR_UNMAPPED,
+                        "generate_conservative: " + std::to_string(h_bad) + " unmapped destination cell(s)");
+    }
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    out.nnz = nnz;
+    out.stats[3] = nnz;
+    out.times_ms[4] = ms_since(t0);
+    out.times_ms[5] = ms_since(t_all);
+}
+
+void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {
+    (void)cfg;
+    cudaStream_t s = 0;
+    auto t_all = Clock::now();
+    const GridInfo &g = src.grid;
+    const i64 ni = g.ni, nj = g.nj, n_dst = dst.n_cells, n_src = src.n_cells;
+    AXGB_REQUIRE(ni >= 2 && nj >= 2, "bilinear: rectilinear source needs at least 2x2 cells");
+    std::vector<double> cl(ni), ct(nj);
+    for (i64 i = 0; i < ni; ++i) cl[i] = 0.5 * (g.ulon[i] + g.ulon[i + 1]);
+    for (i64 j = 0; j < nj; ++j) ct[j] = 0.5 * (g.ulat[j] + g.ulat[j + 1]);
+    DBuf<double> dcl, dct;
+    dcl.upload(cl.data(), cl.size(), s);
+    dct.upload(ct.data(), ct.size(), s);
+    AXGB_REQUIRE(4 * n_dst < (i64(1) << 31), "bilinear: too many destination cells");
+    out.n_src = n_src;
+    out.n_dst = n_dst;
+    out.nnz = 4 * n_dst;
+    out.row_ptr.alloc(n_dst + 1);
+    out.col.alloc(4 * n_dst);
+    out.val.alloc(4 * n_dst);
+    out.frac_a.alloc(n_src);
+    out.frac_b.alloc(n_dst);
+    out.area_a.alloc(n_src);
+    out.area_b.alloc(n_dst);
+    k_bilinear<<<nblk(n_dst + 1, 128), 128, 0, s>>>(dst.view(), dcl.p, static_cast<int>(ni), dct.p,
+                                                   static_cast<int>(nj), out.row_ptr.p, out.col.p, out.val.p);
+    k_fill<<<nblk(n_src, 256), 256, 0, s>>>(out.frac_a.p, n_src, 1.0);
+    k_fill<<<nblk(n_dst, 256), 256, 0, s>>>(out.frac_b.p, n_dst, 1.0);
+    out.area_a.zero(s);
+    out.area_b.zero(s);
+    AXGB_CUDA(cudaGetLastError());
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    out.stats[3] = out.nnz;
+    out.times_ms[5] = ms_since(t_all);
+}
+
+}  // namespace axgb

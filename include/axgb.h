@@ -1,0 +1,235 @@
+/*
+ * axgb.h — C ABI of the GB300 (sm_103a) implementation of the AXIS
+ * regridding hot path: first-order conservative and rectilinear bilinear
+ * weight generation, and the sparse weight apply.
+ *
+ * Conventions (those of the AXIS Fortran/C interop layer,
+ * libs/axis/src/fortran/axis_c_interop.cpp:36-62):
+ *   - every entry point returns 0 (AXGB_SUCCESS) or a negative code; the
+ *     message of the last failure on the calling thread is available from
+ *     axgb_last_error();
+ *   - objects are opaque int handles >= 1 (0 is never a valid handle),
+ *     kept in a mutex-guarded registry (handle_registry.hpp:32-60);
+ *   - extents are validated before any output is written
+ *     (libs/axis/include/axis/solver/apply.hpp:63-71).
+ * Device-pointer entry points are stream-ordered on the given CUDA stream
+ * (0 = the legacy default stream) and return once the work is enqueued;
+ * host-pointer entry points are synchronous.
+ * Nothing here allocates on the calling thread's behalf in the apply path
+ * except the first use of a matrix in a given format (see axgb_matrix_prepare).
+ */
+#ifndef AXGB_H
+#define AXGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void *axgb_stream_t; /* a cudaStream_t */
+
+/* Return codes. AXGB_ERROR matches AXIS_ERROR (-1). */
+#define AXGB_SUCCESS 0
+#define AXGB_ERROR (-1)
+#define AXGB_ERR_INVALID (-2)     /* bad argument / extent mismatch (std::invalid_argument) */
+#define AXGB_ERR_CUDA (-3)        /* CUDA runtime failure */
+#define AXGB_ERR_UNSUPPORTED (-4) /* method/dispatch branch not provided by this library */
+#define AXGB_ERR_NOMEM (-5)       /* device allocation failed */
+#define AXGB_ERR_TIMEOUT (-6)     /* a bounded device wait gave up */
+#define AXGB_ERR_UNMAPPED (-7)    /* UnmappedAction::Error hit an uncovered destination cell */
+#define AXGB_ERR_HANDLE (-8)      /* unknown or destroyed handle */
+
+/* Enumerations with the values of libs/axis/include/axis/solver/regrid_config.hpp:24-72
+ * and libs/axis/include/axis/topology/enums.hpp:73-80. */
+enum axgb_method {
+    AXGB_BILINEAR = 0,
+    AXGB_NEAREST_NEIGHBOR = 1,
+    AXGB_BICUBIC = 2,
+    AXGB_PATCH = 3,
+    AXGB_CONSERVATIVE = 4,
+    AXGB_CONSERVATIVE_2ND = 5
+};
+enum axgb_norm_type { AXGB_DSTAREA = 0, AXGB_FRACAREA = 1 };
+enum axgb_line_type { AXGB_CARTESIAN = 0, AXGB_GREAT_CIRCLE = 1 };
+enum axgb_unmapped { AXGB_UNMAPPED_ERROR = 0, AXGB_UNMAPPED_IGNORE = 1 };
+enum axgb_extrap { AXGB_EXTRAP_NONE = 0, AXGB_EXTRAP_NEAREST_WET = 1 };
+enum axgb_coord_sys { AXGB_SPHERICAL_DEG = 0, AXGB_SPHERICAL_RAD = 1, AXGB_CARTESIAN3D = 2 };
+
+/* RegridConfig (regrid_config.hpp:80-89), one int per field. */
+typedef struct axgb_regrid_config {
+    int32_t method;
+    int32_t norm_type;
+    int32_t line_type;
+    int32_t unmapped;
+    int32_t use_limiter;
+    int32_t extrap_method;
+} axgb_regrid_config;
+
+/* Fills the RegridConfig defaults: Bilinear, DstArea, GreatCircle, Ignore,
+ * no limiter, NearestWet (regrid_config.hpp:80-89). */
+void axgb_default_config(axgb_regrid_config *cfg);
+
+/* Replaces axis_init_c (axis_c_interop.cpp:88-90): selects the CUDA device
+ * for this process and creates the library context. Safe to call again. */
+int axgb_init(int device);
+
+/* Copies the message of the last failure on this thread (NUL-terminated,
+ * truncated to len). Returns the full message length. */
+int axgb_last_error(char *buf, size_t len);
+
+/* Library build/identity string (arch, version). */
+const char *axgb_version(void);
+
+/* ─── Meshes ─────────────────────────────────────────────────────────────
+ * Replaces UnstructuredMesh construction (unstructured_mesh.hpp:68-76) /
+ * make_ugrid_mesh (python/axis_py.cpp:126-140) / axis_mesh_from_descriptor_c
+ * (axis_c_interop.cpp:105-109). Host pointers:
+ *   node_coords  [n_nodes, 2] LayoutLeft (all lon, then all lat), degrees
+ *                for AXGB_SPHERICAL_DEG;
+ *   conn_offsets [n_cells + 1], conn_indices [conn_offsets[n_cells]] (CSR);
+ *   areas        optional precomputed cell areas [n_cells] or NULL;
+ *   mask         optional cell mask [n_cells] (0 = masked) or NULL.
+ * The arrays are copied; the caller keeps ownership. */
+int axgb_mesh_create(const double *node_coords, int64_t n_nodes, const int64_t *conn_offsets,
+                     const int64_t *conn_indices, int64_t n_cells, int coord_sys, const double *areas,
+                     const int32_t *mask, int *mesh_handle);
+
+/* Replaces make_regular_mesh (python/axis_py.cpp:75-103). */
+int axgb_mesh_create_regular(int64_t ni, int64_t nj, double lon_start, double lat_start, double dlon, double dlat,
+                             int *mesh_handle);
+
+/* Mesh facts: n_nodes, n_cells, and the regular/rectilinear detection of
+ * detail/regular_grid_detector.hpp:64-299 (flags[0] regular, flags[1]
+ * rectilinear; dims = ni, nj; vals = lon_min, delta_lon, lat_min, delta_lat).
+ * Any output pointer may be NULL. */
+int axgb_mesh_info(int mesh_handle, int64_t *n_nodes, int64_t *n_cells, int32_t *flags, int64_t *dims,
+                   double *vals);
+
+/* Per-cell geometry computed on the device for this mesh (host outputs,
+ * each may be NULL): spherical area (spherical_clipper.hpp:112-137),
+ * bounding-cap centroid [n,3] and angular radius
+ * (spherical_cap_filter.hpp:85-173), the dilated float AABB [n,6]
+ * (weight_generator.cpp:198-262) and the degenerate class
+ * (degenerate_cell_handler.hpp:115-142: 0 none, 1 zero area, 2 collapsed,
+ * 3 self-intersecting). */
+int axgb_mesh_cell_geometry(int mesh_handle, double *area, double *cap_centroid, double *cap_radius, float *box,
+                            int32_t *degenerate);
+
+/* Replaces axis_destroy_mesh_c (axis_c_interop.cpp:240-242). */
+int axgb_destroy_mesh(int mesh_handle);
+
+/* ─── Weight generation ──────────────────────────────────────────────────
+ * Replaces WeightGenerator::generate (solver/weight_generator.hpp:60-62,
+ * weight_generator.cpp:1887-2019) and python generate_weights
+ * (axis_py.cpp:633-652). Supported: Conservative1stOrder with GreatCircle
+ * lines through the general (BVH + spherical clipper) path, and Bilinear
+ * with a rectilinear source. Other dispatch branches return
+ * AXGB_ERR_UNSUPPORTED. The matrix lives on the device in CSR form with its
+ * frac_a/frac_b/area_a/area_b arrays. Synchronous. */
+int axgb_generate_weights(int src_mesh, int dst_mesh, const axgb_regrid_config *cfg, int *matrix_handle);
+
+/* Replaces axis_generate_weights_c (axis_c_interop.cpp:117-145): method code
+ * 0 Bilinear, 1 NearestNeighbor, 2 Conservative1stOrder, other fields default. */
+int axgb_generate_weights_c(int src_mesh, int dst_mesh, int method, int *matrix_handle);
+
+/* Statistics of the last generation into this matrix. stats (int64[8]):
+ * BVH candidate pairs, pairs passing the reference gates (float AABB, cap,
+ * degenerate, area, mask), pairs clipped with the 32-vertex fallback,
+ * kept pairs (nnz), LBVH nodes, kernel launches per split-FP32 apply and per
+ * FP64 apply (after axgb_matrix_prepare), 0. times_ms (double[8]): cell prep,
+ * LBVH build, candidate search, clip, CSR assembly, total, 0, 0. */
+int axgb_matrix_stats(int matrix_handle, int64_t *stats, double *times_ms);
+
+/* n_src, n_dst, nnz of a matrix (InterpolationMatrix accessors,
+ * interpolation_matrix.hpp:97-111). Any pointer may be NULL. */
+int axgb_matrix_info(int matrix_handle, int64_t *n_src, int64_t *n_dst, int64_t *nnz);
+
+/* Copies the CSR arrays to HOST buffers (to_csr order: rows ascending,
+ * columns ascending within a row; interpolation_matrix.hpp:180-255) and the
+ * frac/area arrays. Any pointer may be NULL. */
+int axgb_matrix_export_csr(int matrix_handle, int64_t *row_ptr, int64_t *col_idx, double *values, double *frac_a,
+                           double *frac_b, double *area_a, double *area_b);
+
+/* Builds a device matrix from HOST CSR arrays (columns must lie in
+ * [0, n_src); rows need not be column-sorted). frac/area may be NULL
+ * (filled with 1 and 0). Mirrors the InterpolationMatrix adopting
+ * constructor (interpolation_matrix.hpp:80-92) followed by to_csr(). */
+int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int64_t *row_ptr, const int64_t *col_idx,
+                           const double *values, const double *frac_a, const double *frac_b, const double *area_a,
+                           const double *area_b, int *matrix_handle);
+
+/* Builds the apply layouts of a matrix ahead of time (format 0: FP64
+ * sliced-ELL, 1: split-FP32 hi+lo sliced-ELL) so that later apply calls
+ * allocate nothing. Synchronous. */
+int axgb_matrix_prepare(int matrix_handle, int format);
+
+/* Replaces axis_destroy_matrix_c (axis_c_interop.cpp:247-249). */
+int axgb_destroy_matrix(int matrix_handle);
+
+/* ─── Apply (device pointers) ────────────────────────────────────────────
+ * y[:, v] = S x[:, v] for v < nrhs; x is [nrhs][ld_x] (field v starts at
+ * x + v*ld_x, ld_x >= n_src), y is [nrhs][ld_y]. This is the LayoutLeft
+ * (n_cells, n_vars) layout of batch_apply (apply.hpp:275-343); nrhs = 1 is
+ * the single-field apply (apply.hpp:61-119). y is overwritten. */
+int axgb_apply_f64(int matrix_handle, const double *x, int64_t ld_x, double *y, int64_t ld_y, int64_t nrhs,
+                   axgb_stream_t stream);
+
+/* FP32 fields, FP64 weights stored as an FP32 hi+lo pair, products and sums
+ * carried with error-free transforms and compensated per row. New in this
+ * library (the reference applies in FP64 only). */
+int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
+                        axgb_stream_t stream);
+
+/* Same, tuning explicit: fields_per_pass = RHS tile width (0 = all),
+ * unroll = fields accumulated together per thread (1, 2 or 4). */
+int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
+                              int fields_per_pass, int unroll, axgb_stream_t stream);
+
+/* Autotuner: times the split apply over (fields_per_pass, unroll) choices on
+ * the given device buffers, caches the best per (matrix, nrhs) and returns
+ * it in best[2]. Used automatically by axgb_apply_f32split when enabled
+ * with axgb_set_autotune(1). */
+int axgb_autotune_f32split(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
+                           axgb_stream_t stream, int32_t *best);
+int axgb_set_autotune(int enable);
+
+/* ─── Apply (host pointers, synchronous) ─────────────────────────────────
+ * Replaces axis_apply_c (axis_c_interop.cpp:217-236): FP64, one field,
+ * host arrays; returns AXGB_ERR_INVALID before touching dst on extent
+ * mismatch. */
+int axgb_apply_c(int matrix_handle, const double *src, double *dst, int n_src, int n_dst);
+
+/* Replaces python batch_apply (axis_py.cpp:690-759) for host arrays laid
+ * out LayoutLeft [n_src, n_vars] / [n_dst, n_vars]. */
+int axgb_batch_apply_host_f64(int matrix_handle, const double *src, int64_t n_src, double *dst, int64_t n_dst,
+                              int64_t n_vars);
+int axgb_batch_apply_host_f32split(int matrix_handle, const float *src, int64_t n_src, float *dst, int64_t n_dst,
+                                   int64_t n_vars);
+
+/* ─── Many grid pairs in one persistent launch ───────────────────────────
+ * A batch groups k matrices, each with its own field count. axgb_batch_apply
+ * runs all of them (split-FP32) in one persistent kernel fed by a work queue
+ * over (matrix, row slice, field tile) items, replayed from a CUDA graph
+ * captured on first use per stream and per pointer set. No reference
+ * counterpart: the reference applies one matrix per call. */
+int axgb_batch_create(const int *matrix_handles, const int64_t *nrhs, int count, int *batch_handle);
+int axgb_batch_apply(int batch_handle, const float *const *x, const int64_t *ld_x, float *const *y,
+                     const int64_t *ld_y, axgb_stream_t stream);
+int axgb_destroy_batch(int batch_handle);
+
+/* ─── Conservation (device pointers to FP64 fields) ──────────────────────
+ * check_conservation (solver/conservation.hpp:96, conservation.cpp:83-96):
+ * out[0] source integral sum(src*area_a*frac_a), out[1] destination integral
+ * (DstArea: sum over frac_b != 0 of dst*area_b; FracArea: * frac_b),
+ * out[2] |difference|, out[3] relative error. Synchronous. */
+int axgb_conservation_f64(int matrix_handle, const double *src, const double *dst, int norm_type, double *out,
+                          axgb_stream_t stream);
+int axgb_conservation_f32(int matrix_handle, const float *src, const float *dst, int norm_type, double *out,
+                          axgb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AXGB_H */

@@ -1,0 +1,144 @@
+"""CPU tests of the oracle: pinned against the reference's own geometry
+headers (oracle/_ref, built from the reference checkout where it exists) and
+against the known answers of the reference's unit tests."""
+import numpy as np
+import pytest
+
+from axgb import grids
+
+
+def test_spmv_known_answers(oracle):
+    # tests/test_spmv_apply.cpp:33-105 of the reference: 3 src, 2 dst
+    from oracle import Weights
+    w = Weights(3, 2, np.array([0, 0, 1, 1]), np.array([0, 1, 1, 2]), np.array([0.5, 0.3, 0.2, 1.0]),
+                np.ones(3), np.ones(2), np.ones(3), np.ones(2))
+    y = oracle.apply_csr(w, np.array([2.0, 4.0, 6.0]))[0]
+    assert abs(y[0] - 2.2) < 1e-14 and abs(y[1] - 6.8) < 1e-14
+    y = oracle.apply_csr(w, np.array([1.0, 1.0, 1.0]))[0]
+    assert abs(y[0] - 0.8) < 1e-14 and abs(y[1] - 1.2) < 1e-14
+    y2 = oracle.apply_coo_atomic(w, np.array([2.0, 4.0, 6.0]))[0]
+    assert abs(y2[0] - 2.2) < 1e-14 and abs(y2[1] - 6.8) < 1e-14
+
+
+def test_morton_known_answers(oracle):
+    # tests/test_morton_sort.cpp:19-118 of the reference
+    e = oracle.morton_encode
+    assert e(0, 0) == 0 and e(1, 0) == 1 and e(0, 1) == 2 and e(1, 1) == 3 and e(2, 2) == 12
+    assert e(65535, 65535) == 0xFFFFFFFF
+    assert e(3, 5) != e(5, 3)
+    n = oracle.normalize_coord
+    assert n(0.0, 0.0, 100.0) == 0 and n(100.0, 0.0, 100.0) == 65535
+    assert abs(n(50.0, 0.0, 100.0) - 32767.5) <= 1.0
+    assert n(-10.0, 0.0, 100.0) == 0 and n(200.0, 0.0, 100.0) == 65535
+    assert n(5.0, 10.0, 10.0) == 0 and n(5.0, 10.0, 5.0) == 0
+    assert abs(n(0.0, -180.0, 180.0) - 32767.5) <= 1.0
+
+
+def _cap_poly(center, radius, nv):
+    c = np.asarray(center, float)
+    c /= np.linalg.norm(c)
+    arb = np.array([0, 0, 1.0]) if abs(c[2]) < 0.9 else np.array([1.0, 0, 0])
+    u = np.cross(c, arb)
+    u /= np.linalg.norm(u)
+    v = np.cross(c, u)
+    a = 2 * np.pi * np.arange(nv) / nv
+    p = c[None] * np.cos(radius) + np.sin(radius) * (np.cos(a)[:, None] * u + np.sin(a)[:, None] * v)
+    return p / np.linalg.norm(p, axis=1, keepdims=True)
+
+
+def _ll(lon, lat):
+    return np.array([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)])
+
+
+def test_clipper_properties(oracle):
+    # tests/prop_spherical_clipper.cpp:84-228 of the reference
+    rng = np.random.default_rng(7)
+    for _ in range(200):
+        ca = _ll(rng.uniform(-0.3, 0.3), rng.uniform(-0.3, 0.3))
+        cb = _ll(np.pi + rng.uniform(-0.3, 0.3), rng.uniform(-0.3, 0.3))
+        a = _cap_poly(ca, rng.uniform(0.05, 0.5), rng.integers(4, 9))
+        b = _cap_poly(cb, rng.uniform(0.05, 0.5), rng.integers(4, 9))
+        area, _ = oracle.clip(a, b)
+        assert area == 0.0
+    for _ in range(200):
+        c = _ll(rng.uniform(-3, 3), rng.uniform(-1.2, 1.2))
+        big = _cap_poly(c, rng.uniform(0.3, 0.6), rng.integers(6, 12))
+        small = _cap_poly(c, rng.uniform(0.05, 0.1), rng.integers(4, 9))
+        a0 = oracle.poly_area(small)
+        a1, _ = oracle.clip(small, big)
+        assert abs(a1 - a0) / a0 < 1e-14
+    for _ in range(300):
+        a = _cap_poly(_ll(rng.uniform(-3, 3), rng.uniform(-1.5, 1.5)), rng.uniform(0.001, 1.0), rng.integers(3, 12))
+        b = _cap_poly(_ll(rng.uniform(-3, 3), rng.uniform(-1.5, 1.5)), rng.uniform(0.001, 1.0), rng.integers(3, 12))
+        area, poly = oracle.clip(a, b)
+        assert poly.shape[0] == 0 or poly.shape[0] >= 3
+        assert np.isfinite(poly).all() and area >= 0.0
+
+
+def test_clip_matches_reference(oracle, reflib):
+    rng = np.random.default_rng(11)
+    for _ in range(500):
+        a = _cap_poly(_ll(rng.uniform(-3, 3), rng.uniform(-1.5, 1.5)), rng.uniform(0.001, 0.5), rng.integers(3, 12))
+        b = _cap_poly(_ll(rng.uniform(-3, 3), rng.uniform(-1.5, 1.5)), rng.uniform(0.001, 0.5), rng.integers(3, 12))
+        x1, p1 = oracle.clip(a, b)
+        x2, p2 = reflib.clip(a, b)
+        assert x1 == x2 and np.array_equal(p1, p2)
+
+
+GRID_CASES = [
+    ("latlon5", lambda: grids.latlon_deg(5.0)),
+    ("C8", lambda: grids.cubed_sphere(8)),
+    ("latlon1", lambda: grids.latlon_deg(1.0)),
+    ("C48", lambda: grids.cubed_sphere(48)),
+]
+
+
+@pytest.mark.parametrize("name,make", GRID_CASES)
+def test_cell_prep_matches_reference(oracle, reflib, name, make):
+    m = make()
+    a = oracle.cell_prep(m)
+    b = reflib.cell_prep(m)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert oracle.detect(m) == reflib.detect(m)
+    assert np.array_equal(oracle.morton_order(m), reflib.morton_order(m))
+
+
+PAIRS = [
+    ("1deg->C48", lambda: (grids.latlon_deg(1.0), grids.cubed_sphere(48))),
+    ("C48->1deg", lambda: (grids.cubed_sphere(48), grids.latlon_deg(1.0))),
+    ("5deg->C8", lambda: (grids.latlon_deg(5.0), grids.cubed_sphere(8))),
+    ("C12->C8", lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8))),
+]
+
+
+@pytest.mark.parametrize("name,make", PAIRS)
+def test_conservative_matches_reference(oracle, reflib, name, make):
+    src, dst = make()
+    wo = oracle.conservative(src, dst)
+    wf = oracle.conservative(src, dst, faithful=True)
+    wr = reflib.conservative(src, dst)
+    for k in ("row", "col", "w", "frac_a", "frac_b", "area_a", "area_b"):
+        assert np.array_equal(getattr(wo, k), getattr(wr, k)), k
+        assert np.array_equal(getattr(wo, k), getattr(wf, k)), k
+    # row sums of a global-to-global conservative map are 1 (DstArea)
+    rs = np.bincount(wo.row, weights=wo.w, minlength=wo.n_dst)
+    assert np.all(np.abs(rs - 1.0) < 1e-11)
+
+
+def test_conservation_report(oracle):
+    src, dst = grids.latlon_deg(5.0), grids.cubed_sphere(8)
+    w = oracle.conservative(src, dst)
+    x = np.cos(np.radians(np.repeat(np.arange(-87.5, 90, 5.0), 72))) + 280.0
+    y = oracle.apply_csr(w, x)[0]
+    rep = oracle.conservation(w, x, y)
+    assert rep["relative_error"] < 1e-12
+
+
+def test_bilinear_rect_source(oracle):
+    src, dst = grids.latlon_deg(5.0), grids.cubed_sphere(8)
+    w = oracle.bilinear(src, dst)
+    assert w.nnz == 4 * dst.n_cells
+    rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
+    assert np.allclose(rs, 1.0, atol=1e-14)
+    assert np.all(w.w >= 0) and np.all(w.col < src.n_cells)

@@ -1,0 +1,242 @@
+"""GPU parity: libaxgb (through its C ABI) against the CPU oracle on the same
+seeded inputs. Index sets bit-exact after the reference's area threshold,
+weights within 1e-12 relative, the FP64 apply within 1e-13 relative of a
+compensated FP64 oracle, the split-FP32 apply within 1e-6 relative."""
+import numpy as np
+import pytest
+
+from axgb import fields, grids
+
+pytestmark = pytest.mark.gpu
+
+W_RTOL = 1e-12  # weights / fractions vs the oracle
+F64_RTOL = 1e-13  # FP64 apply vs compensated FP64 oracle
+SPLIT_RTOL = 1e-6  # split-FP32 apply vs FP64 oracle on the same FP32 inputs
+
+
+def _rows(csr, n_dst):
+    return np.repeat(np.arange(n_dst), np.diff(csr["row_ptr"]))
+
+
+def _mismatch_report(rows_g, cols_g, wo):
+    g = set(zip(rows_g.tolist(), cols_g.tolist()))
+    o = set(zip(wo.row.tolist(), wo.col.tolist()))
+    only_g = sorted(g - o)[:10]
+    only_o = sorted(o - g)[:10]
+    return f"only GPU: {len(g - o)} {only_g}; only oracle: {len(o - g)} {only_o}"
+
+
+def _check_weights(M, wo):
+    csr = M.to_csr()
+    rows = _rows(csr, M.n_dst)
+    same = M.nnz == wo.nnz and np.array_equal(rows, wo.row) and np.array_equal(csr["col"], wo.col)
+    assert same, _mismatch_report(rows, csr["col"], wo)
+    rel = np.abs(csr["val"] - wo.w) / np.maximum(np.abs(wo.w), 1e-300)
+    assert rel.max() < W_RTOL, rel.max()
+    for k, ref in (("frac_a", wo.frac_a), ("frac_b", wo.frac_b), ("area_a", wo.area_a), ("area_b", wo.area_b)):
+        d = np.abs(csr[k] - ref) / np.maximum(np.abs(ref), 1e-300)
+        assert d.max() < W_RTOL, (k, d.max())
+    return csr
+
+
+PAIRS = [
+    ("1deg->C48", lambda: (grids.latlon_deg(1.0), grids.cubed_sphere(48))),
+    ("C48->1deg", lambda: (grids.cubed_sphere(48), grids.latlon_deg(1.0))),
+    ("5deg->C8", lambda: (grids.latlon_deg(5.0), grids.cubed_sphere(8))),
+    ("C12->C8", lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8))),
+    ("2deg->C96", lambda: (grids.latlon_deg(2.0), grids.cubed_sphere(96))),
+]
+
+
+@pytest.mark.parametrize("name,make", PAIRS)
+def test_conservative_parity(gpu, oracle, name, make):
+    src, dst = make()
+    ms, md = gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst)
+    M = gpu.generate_weights(ms, md, {"method": "conservative"})
+    wo = oracle.conservative(src, dst)
+    _check_weights(M, wo)
+    st = M.stats()
+    assert st["gated_pairs"] == wo.stats["cap_pass"], (st, wo.stats)
+
+
+def test_conservative_fracarea_parity(gpu, oracle):
+    src, dst = grids.latlon_deg(5.0), grids.cubed_sphere(8)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst),
+                             {"method": "conservative", "norm_type": "FracArea"})
+    _check_weights(M, oracle.conservative(src, dst, norm_type=1))
+
+
+def test_deterministic(gpu):
+    src, dst = grids.latlon_deg(2.0), grids.cubed_sphere(24)
+    ms, md = gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst)
+    a = gpu.generate_weights(ms, md, {"method": "conservative"}).to_csr()
+    b = gpu.generate_weights(ms, md, {"method": "conservative"}).to_csr()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_cell_geometry_parity(gpu, oracle):
+    for g in (grids.latlon_deg(1.0), grids.cubed_sphere(48)):
+        m = gpu.Mesh.from_grid(g)
+        a = m.cell_geometry()
+        b = oracle.cell_prep(g)
+        assert np.array_equal(a["degen"], b["degen"])
+        assert np.array_equal(a["cap_c"], b["cap_c"])
+        assert np.max(np.abs(a["area"] - b["area"]) / b["area"]) < 1e-14
+        assert np.max(np.abs(a["cap_r"] - b["cap_r"])) < 1e-15
+        # float boxes: equal up to one float ulp where CUDA and libm trig differ
+        assert np.max(np.abs(a["box"] - b["box"])) <= 1.2e-7
+        assert np.mean(a["box"] == b["box"]) > 0.999
+
+
+def test_bilinear_parity(gpu, oracle):
+    src, dst = grids.latlon_deg(1.0), grids.cubed_sphere(48)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "bilinear"})
+    wo = oracle.bilinear(src, dst)
+    csr = M.to_csr()
+    assert np.array_equal(_rows(csr, M.n_dst), wo.row)
+    assert np.array_equal(csr["col"], wo.col)
+    assert np.array_equal(csr["val"], wo.w)
+
+
+def test_unsupported_and_unmapped(gpu, oracle):
+    a = gpu.make_regular_mesh(36, 18, 0.0, -90.0, 10.0, 10.0)
+    b = gpu.make_regular_mesh(18, 9, 0.0, -90.0, 20.0, 20.0)
+    with pytest.raises(gpu.Unsupported):
+        gpu.generate_weights(a, b, {"method": "conservative"})
+    with pytest.raises(gpu.Unsupported):
+        gpu.generate_weights(a, b, {"method": "patch"})
+    # a regional source leaves most of a global destination unmapped
+    reg = grids.regular_latlon(20, 10, 0.0, 0.0, 2.0, 2.0)
+    dst = grids.cubed_sphere(8)
+    with pytest.raises(gpu.AxgbError) as e:
+        gpu.generate_weights(gpu.Mesh.from_grid(reg), gpu.Mesh.from_grid(dst),
+                             {"method": "conservative", "unmapped": "error"})
+    assert e.value.code == gpu.ERR_UNMAPPED
+    with pytest.raises(RuntimeError):
+        oracle.conservative(reg, dst, unmapped=0)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(reg), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    _check_weights(M, oracle.conservative(reg, dst))
+
+
+def test_invalid_mesh_rejected(gpu):
+    g = grids.latlon_deg(10.0)
+    bad = g.node_lonlat.copy()
+    bad[3, 1] = np.nan
+    with pytest.raises(gpu.InvalidArgument):
+        gpu.Mesh.from_arrays(bad, g.conn_offsets, g.conn_indices)
+    idx = g.conn_indices.copy()
+    idx[5] = g.n_nodes + 3
+    with pytest.raises(gpu.InvalidArgument):
+        gpu.Mesh.from_arrays(g.node_lonlat, g.conn_offsets, idx)
+
+
+# ─── apply ─────────────────────────────────────────────────────────────────
+
+
+def test_spmv_golden_matrix(gpu):
+    # tests/test_spmv_apply.cpp:33-142 of the reference
+    M = gpu.Matrix.from_csr(3, 2, [0, 2, 4], [0, 1, 1, 2], [0.5, 0.3, 0.2, 1.0])
+    y = gpu.apply_weights(M, np.array([2.0, 4.0, 6.0]))
+    assert abs(y[0] - 2.2) < 1e-14 and abs(y[1] - 6.8) < 1e-14
+    y = gpu.apply_weights(M, np.array([1.0, 1.0, 1.0]))
+    assert abs(y[0] - 0.8) < 1e-14 and abs(y[1] - 1.2) < 1e-14
+    with pytest.raises(gpu.InvalidArgument):
+        gpu.apply_weights(M, np.ones(5))
+    import ctypes
+    dst = np.zeros(5)
+    rc = gpu.lib().axgb_apply_c(M.handle, np.ones(3).ctypes.data_as(ctypes.c_void_p),
+                                dst.ctypes.data_as(ctypes.c_void_p), 3, 5)
+    assert rc == gpu.ERR_INVALID and np.all(dst == 0.0)
+    out = gpu.batch_apply(M, np.array([[2.0, 1.0], [4.0, 1.0], [6.0, 1.0]]))
+    assert np.allclose(out, [[2.2, 0.8], [6.8, 1.2]], atol=1e-14)
+
+
+@pytest.fixture(scope="module")
+def cfg1(gpu, oracle):
+    src, dst = grids.latlon_deg(1.0), grids.cubed_sphere(48)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    wo = oracle.conservative(src, dst)
+    xyz = grids.cell_centroids_xyz(src)
+    f = fields.sh_field(xyz, 16, seed=1, offset=280.0).numpy()
+    return src, dst, M, wo, f
+
+
+def test_apply_f64_parity(gpu, oracle, cfg1):
+    import torch
+    src, dst, M, wo, f = cfg1
+    x = torch.tensor(f, device="cuda")
+    y = gpu.apply_weights(M, x).cpu().numpy()
+    ref = oracle.apply_csr(wo, f, compensated=True)[0]
+    assert np.max(np.abs(y - ref) / np.abs(ref)) < F64_RTOL
+    yh = gpu.apply_weights(M, f)  # host path
+    assert np.max(np.abs(yh - ref) / np.abs(ref)) < F64_RTOL
+
+
+def test_apply_split_parity(gpu, oracle, cfg1):
+    import torch
+    src, dst, M, wo, f = cfg1
+    rng = np.random.default_rng(3)
+    X = np.stack([f * s for s in rng.lognormal(0, 1, 7)]).astype(np.float32)
+    ref = oracle.apply_csr(wo, X.astype(np.float64), compensated=True)
+    xs = torch.tensor(X, device="cuda")
+    outs = []
+    for fpp, u in ((0, 1), (0, 2), (0, 4), (3, 2), (1, 1)):
+        y = gpu.apply_f32split(M, xs, fields_per_pass=fpp, unroll=u).cpu().numpy()
+        err = np.max(np.abs(y - ref) / np.abs(ref))
+        assert err < SPLIT_RTOL, (fpp, u, err)
+        outs.append(y)
+    for y in outs[1:]:
+        assert np.array_equal(y, outs[0])
+    # strided fields (ld > n)
+    xp = torch.zeros((7, M.n_src + 37), dtype=torch.float32, device="cuda")
+    xp[:, : M.n_src] = xs
+    yp = torch.full((7, M.n_dst + 5), -1.0, dtype=torch.float32, device="cuda")
+    gpu.apply_f32split(M, xp[:, : M.n_src], yp[:, : M.n_dst])
+    assert np.array_equal(yp[:, : M.n_dst].cpu().numpy(), outs[0])
+    assert np.all(yp[:, M.n_dst:].cpu().numpy() == -1.0)
+
+
+def test_apply_split_host_path(gpu, oracle, cfg1):
+    import torch
+    src, dst, M, wo, f = cfg1
+    X = np.stack([f, 2 * f, -f]).astype(np.float32)
+    Y = np.zeros((3, M.n_dst), np.float32)
+    gpu.batch_apply_host_f32split(M, X, Y)
+    dev = gpu.apply_f32split(M, torch.tensor(X, device="cuda")).cpu().numpy()
+    assert np.array_equal(Y, dev)
+
+
+def test_autotune_and_batch(gpu, oracle, cfg1):
+    import torch
+    src, dst, M, wo, f = cfg1
+    X = torch.tensor(np.stack([f] * 5).astype(np.float32), device="cuda")
+    Y = torch.empty((5, M.n_dst), dtype=torch.float32, device="cuda")
+    best = gpu.autotune_f32split(M, X, Y)
+    assert best[1] in (1, 2, 4)
+    ref = gpu.apply_f32split(M, X, fields_per_pass=0, unroll=1).cpu().numpy()
+    # persistent multi-matrix batch: same matrix twice plus a reversed pair
+    M2 = gpu.generate_weights(gpu.Mesh.from_grid(dst), gpu.Mesh.from_grid(src), {"method": "conservative"})
+    x2 = torch.rand((3, M2.n_src), dtype=torch.float32, device="cuda")
+    y2ref = gpu.apply_f32split(M2, x2, fields_per_pass=0, unroll=1).cpu().numpy()
+    B = gpu.Batch([M, M2, M], [5, 3, 2])
+    ya = torch.empty((5, M.n_dst), dtype=torch.float32, device="cuda")
+    yb = torch.empty((3, M2.n_dst), dtype=torch.float32, device="cuda")
+    yc = torch.empty((2, M.n_dst), dtype=torch.float32, device="cuda")
+    for _ in range(2):  # second call replays the captured graph
+        B.apply([X, x2, X[:2]], [ya, yb, yc])
+        torch.cuda.synchronize()
+        assert np.array_equal(ya.cpu().numpy(), ref)
+        assert np.array_equal(yb.cpu().numpy(), y2ref)
+        assert np.array_equal(yc.cpu().numpy(), ref[:2])
+
+
+def test_conservation_parity(gpu, oracle, cfg1):
+    import torch
+    src, dst, M, wo, f = cfg1
+    x = torch.tensor(f, device="cuda")
+    y = gpu.apply_weights(M, x)
+    rep = gpu.check_conservation(M, x, y)
+    ro = oracle.conservation(wo, f, oracle.apply_csr(wo, f)[0])
+    assert abs(rep["src_integral"] - ro["src_integral"]) / abs(ro["src_integral"]) < 1e-13
+    assert rep["relative_error"] < 1e-12
