@@ -241,14 +241,15 @@ def main():
     log(f"fields {time.perf_counter() - t0:.1f}s")
     Y = torch.empty((NRHS, M.n_dst), dtype=torch.float32, device=dev)
     M.prepare(1)
-    tile, unroll = axgb.autotune_f32split(M, X, Y)
-    launches_per_step = axgb_launches(M)
-    log(f"autotune: fields_per_pass={tile} unroll={unroll} launches/step={launches_per_step}")
+    M.prepare(2)
+    tuned = axgb.autotune_f32split(M, X, Y)
+    launches_per_step = axgb_launches(M, tuned["variant"])
+    log(f"autotune: {tuned} launches/step={launches_per_step}")
 
     stream = torch.cuda.current_stream()
 
     def run_split():
-        axgb.apply_f32split(M, X, Y, stream=stream, fields_per_pass=tile, unroll=unroll)
+        axgb.apply_f32split(M, X, Y, stream=stream)  # the tuned kernel
 
     for _ in range(args.warmup):
         run_split()
@@ -299,7 +300,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n_src": M.n_src, "n_dst": M.n_dst, "nnz": M.nnz, "nrhs": NRHS,
-                   "fields_per_pass": tile, "unroll": unroll, "l2": "inputs 14.4 GB per step > L2",
+                   "kernel": tuned, "l2": "inputs 14.4 GB per step > L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(), "peak_kind": peak_kind,
@@ -363,14 +364,15 @@ def main():
     return 0
 
 
-def axgb_launches(M):
-    # one launch per non-empty slice length class of the split layout
+def axgb_launches(M, variant):
+    # one launch per non-empty length class of the chosen layout
     st = np.zeros(8, np.int64)
     import ctypes
 
     import axgb
     axgb._check(axgb.lib().axgb_matrix_stats(M.handle, st.ctypes.data_as(ctypes.c_void_p), None))
-    return int(st[5]) if st[5] > 0 else 1
+    n = int(st[7] if variant == 1 else st[5])
+    return n if n > 0 else 1
 
 
 def profiled_traffic():

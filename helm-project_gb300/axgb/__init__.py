@@ -99,7 +99,7 @@ def lib():
     L.axgb_destroy_matrix.argtypes = [C.c_int]
     L.axgb_apply_f64.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp]
     L.axgb_apply_f32split.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp]
-    L.axgb_apply_f32split_tuned.argtypes = [C.c_int, vp, i64, vp, i64, i64, C.c_int, C.c_int, vp]
+    L.axgb_apply_f32split_tuned.argtypes = [C.c_int, vp, i64, vp, i64, i64, C.c_int, C.c_int, C.c_int, vp]
     L.axgb_autotune_f32split.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp, vp]
     L.axgb_set_autotune.argtypes = [C.c_int]
     L.axgb_apply_c.argtypes = [C.c_int, vp, vp, C.c_int, C.c_int]
@@ -368,29 +368,33 @@ def apply_f64(matrix: Matrix, x, y=None, stream=None):
     return y
 
 
-def apply_f32split(matrix: Matrix, x, y=None, stream=None, fields_per_pass=None, unroll=None):
-    """Device split-FP32 apply: x, y CUDA float32 tensors [nrhs, n]."""
+def apply_f32split(matrix: Matrix, x, y=None, stream=None, fields_per_pass=None, unroll=None, variant=None):
+    """Device split-FP32 apply: x, y CUDA float32 tensors [nrhs, n].
+    With no tuning arguments the matrix's tuned (or default) kernel is used;
+    variant 0 = direct gathers, 1 = shared-memory staged."""
     import torch
     if x.dim() == 1:
         x = x.view(1, -1)
     if y is None:
         y = torch.empty((x.shape[0], matrix.n_dst), dtype=torch.float32, device=x.device)
     s = _stream(stream if stream is not None else torch.cuda.current_stream())
-    if fields_per_pass is None and unroll is None:
+    if fields_per_pass is None and unroll is None and variant is None:
         _check(lib().axgb_apply_f32split(matrix.handle, _ptr(x), x.stride(0), _ptr(y), y.stride(0), x.shape[0], s))
     else:
+        v = 0 if variant is None else int(variant)
+        u = int(unroll) if unroll is not None else (2 if v == 0 else 4)
         _check(lib().axgb_apply_f32split_tuned(matrix.handle, _ptr(x), x.stride(0), _ptr(y), y.stride(0), x.shape[0],
-                                               int(fields_per_pass or 0), int(unroll or 2), s))
+                                               v, int(fields_per_pass or 0), u, s))
     return y
 
 
 def autotune_f32split(matrix: Matrix, x, y, stream=None):
     import torch
-    best = np.zeros(2, np.int32)
+    best = np.zeros(3, np.int32)
     _check(lib().axgb_autotune_f32split(matrix.handle, _ptr(x), x.stride(0), _ptr(y), y.stride(0), x.shape[0],
                                         _stream(stream if stream is not None else torch.cuda.current_stream()),
                                         _ptr(best)))
-    return int(best[0]), int(best[1])
+    return dict(variant=int(best[0]), fields_per_pass=int(best[1]), unroll=int(best[2]))
 
 
 def set_autotune(enable: bool):

@@ -223,40 +223,43 @@ void check_apply(const Matrix &m, const void *x, i64 ldx, const void *y, i64 ldy
     AXGB_REQUIRE(m.n_dst == 0 || y != nullptr, "apply: y is NULL");
 }
 
-std::pair<int, int> tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    std::vector<SplitParams> cands;
+    for (int t : {2, 4, 8})
+        if (t <= std::max<i64>(2, nrhs)) cands.push_back({1, 0, t});
     std::vector<i64> tiles = {nrhs};
-    for (i64 t : {512, 128, 32, 8})
+    for (i64 t : {32, 8})
         if (t < nrhs) tiles.push_back(t);
-    std::vector<int> unrolls = {1};
-    if (nrhs >= 2) unrolls.push_back(2);
-    if (nrhs >= 4) unrolls.push_back(4);
+    for (i64 t : tiles)
+        for (int u : {2, 4})
+            if (u <= std::max<i64>(1, nrhs)) cands.push_back({0, static_cast<int>(t), u});
+    if (nrhs == 1) cands.push_back({0, 1, 1});
     cudaEvent_t e0, e1;
     AXGB_CUDA(cudaEventCreate(&e0));
     AXGB_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
-    std::pair<int, int> arg{static_cast<int>(nrhs), unrolls.back()};
-    for (i64 t : tiles)
-        for (int u : unrolls) {
-            apply_split(m, x, ldx, y, ldy, nrhs, static_cast<int>(t), u, s);  // warm-up
-            AXGB_CUDA(cudaEventRecord(e0, s));
-            for (int r = 0; r < 2; ++r) apply_split(m, x, ldx, y, ldy, nrhs, static_cast<int>(t), u, s);
-            AXGB_CUDA(cudaEventRecord(e1, s));
-            AXGB_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            AXGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best) {
-                best = ms;
-                arg = {static_cast<int>(t), u};
-            }
+    SplitParams arg = cands.front();
+    for (const SplitParams &c : cands) {
+        apply_split(m, x, ldx, y, ldy, nrhs, c, s);  // warm-up (and layout build)
+        AXGB_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < 2; ++r) apply_split(m, x, ldx, y, ldy, nrhs, c, s);
+        AXGB_CUDA(cudaEventRecord(e1, s));
+        AXGB_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        AXGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            arg = c;
         }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return arg;
 }
 
 // Host-buffer batch apply, LayoutLeft [n, n_vars]. Fields are streamed in
-// chunks through two device staging halves so that the copy of chunk q+1
-// overlaps the apply of chunk q (copy and compute on separate streams).
+// chunks through two device staging halves on two streams, so the copies of
+// one chunk overlap the apply of the other.
 template <class T, class F>
 void host_batch(Matrix &m, const T *src, T *dst, int64_t n_vars, F apply_fn) {
     auto &st = Staging::get();
@@ -266,13 +269,8 @@ void host_batch(Matrix &m, const T *src, T *dst, int64_t n_vars, F apply_fn) {
     T *dx = static_cast<T *>(st.get_a(sizeof(T) * ns * per * 2));
     T *dy = static_cast<T *>(st.get_b(sizeof(T) * nd * per * 2));
     cudaStream_t cs[2];
-    cudaEvent_t in_done[2], out_done[2];
     AXGB_CUDA(cudaStreamCreateWithFlags(&cs[0], cudaStreamNonBlocking));
     AXGB_CUDA(cudaStreamCreateWithFlags(&cs[1], cudaStreamNonBlocking));
-    for (int q = 0; q < 2; ++q) {
-        AXGB_CUDA(cudaEventCreateWithFlags(&in_done[q], cudaEventDisableTiming));
-        AXGB_CUDA(cudaEventCreateWithFlags(&out_done[q], cudaEventDisableTiming));
-    }
     int64_t chunk = 0;
     for (int64_t v0 = 0; v0 < n_vars; v0 += per, ++chunk) {
         int64_t nv = std::min(per, n_vars - v0);
@@ -288,16 +286,24 @@ void host_batch(Matrix &m, const T *src, T *dst, int64_t n_vars, F apply_fn) {
     }
     AXGB_CUDA(cudaStreamSynchronize(cs[0]));
     AXGB_CUDA(cudaStreamSynchronize(cs[1]));
-    for (int q = 0; q < 2; ++q) {
-        cudaEventDestroy(in_done[q]);
-        cudaEventDestroy(out_done[q]);
-        cudaStreamDestroy(cs[q]);
-    }
+    cudaStreamDestroy(cs[0]);
+    cudaStreamDestroy(cs[1]);
 }
 
-std::pair<int, int> default_split_params(i64 nrhs) {
-    int u = nrhs >= 4 ? 4 : (nrhs >= 2 ? 2 : 1);
-    return {static_cast<int>(nrhs), u};
+SplitParams default_split_params(i64 nrhs);
+SplitParams pick_params(Matrix &m, i64 nrhs) {
+    std::lock_guard<std::mutex> lk(m.mu);
+    auto it = m.tuned.find(nrhs);
+    if (it != m.tuned.end()) return it->second;
+    return default_split_params(nrhs);
+}
+
+SplitParams default_split_params(i64 nrhs) {
+    SplitParams p;
+    p.variant = 1;
+    p.fields_per_pass = 0;
+    p.unroll = nrhs >= 8 ? 8 : 4;
+    return p;
 }
 
 }  // namespace
@@ -616,7 +622,7 @@ int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int6
 
 int axgb_matrix_prepare(int h, int format) {
     AXGB_TRY({
-        AXGB_REQUIRE(format == 0 || format == 1, "matrix_prepare: format must be 0 or 1");
+        AXGB_REQUIRE(format >= 0 && format <= 2, "matrix_prepare: format must be 0, 1 or 2");
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         matrix_prepare(*m, format, 0);
     });
@@ -637,13 +643,18 @@ int axgb_apply_f64(int h, const double *x, int64_t ldx, double *y, int64_t ldy, 
     });
 }
 
-int axgb_apply_f32split_tuned(int h, const float *x, int64_t ldx, float *y, int64_t ldy, int64_t nrhs,
+int axgb_apply_f32split_tuned(int h, const float *x, int64_t ldx, float *y, int64_t ldy, int64_t nrhs, int variant,
                               int fields_per_pass, int unroll, axgb_stream_t stream) {
     AXGB_TRY({
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         check_apply(*m, x, ldx, y, ldy, nrhs);
-        AXGB_REQUIRE(unroll == 1 || unroll == 2 || unroll == 4, "apply: unroll must be 1, 2 or 4");
-        if (nrhs > 0) apply_split(*m, x, ldx, y, ldy, nrhs, fields_per_pass, unroll, static_cast<cudaStream_t>(stream));
+        AXGB_REQUIRE(variant == 0 || variant == 1, "apply: variant must be 0 (direct) or 1 (staged)");
+        if (variant == 0)
+            AXGB_REQUIRE(unroll == 1 || unroll == 2 || unroll == 4, "apply: direct unroll must be 1, 2 or 4");
+        else
+            AXGB_REQUIRE(unroll == 2 || unroll == 4 || unroll == 8, "apply: staged fields per stage must be 2, 4 or 8");
+        SplitParams p{variant, fields_per_pass, unroll};
+        if (nrhs > 0) apply_split(*m, x, ldx, y, ldy, nrhs, p, static_cast<cudaStream_t>(stream));
     });
 }
 
@@ -659,8 +670,9 @@ int axgb_autotune_f32split(int h, const float *x, int64_t ldx, float *y, int64_t
             m->tuned[nrhs] = p;
         }
         if (best) {
-            best[0] = p.first;
-            best[1] = p.second;
+            best[0] = p.variant;
+            best[1] = p.fields_per_pass;
+            best[2] = p.unroll;
         }
     });
 }
@@ -677,7 +689,7 @@ int axgb_apply_f32split(int h, const float *x, int64_t ldx, float *y, int64_t ld
         check_apply(*m, x, ldx, y, ldy, nrhs);
         if (nrhs > 0) {
             cudaStream_t s = static_cast<cudaStream_t>(stream);
-            std::pair<int, int> p;
+            SplitParams p;
             bool have = false;
             {
                 std::lock_guard<std::mutex> lk(m->mu);
@@ -694,7 +706,7 @@ int axgb_apply_f32split(int h, const float *x, int64_t ldx, float *y, int64_t ld
                 have = true;
             }
             if (!have) p = default_split_params(nrhs);
-            apply_split(*m, x, ldx, y, ldy, nrhs, p.first, p.second, s);
+            apply_split(*m, x, ldx, y, ldy, nrhs, p, s);
         }
     });
 }
@@ -737,8 +749,7 @@ int axgb_batch_apply_host_f32split(int h, const float *src, int64_t n_src, float
         if (n_vars > 0)
             host_batch<float>(*m, src, dst, n_vars,
                               [&](const float *x, int64_t lx, float *y, int64_t ly, int64_t nv, cudaStream_t s) {
-                                  auto p = default_split_params(nv);
-                                  apply_split(*m, x, lx, y, ly, nv, p.first, p.second, s);
+                                  apply_split(*m, x, lx, y, ly, nv, pick_params(*m, nv), s);
                               });
     });
 }

@@ -398,6 +398,8 @@ void build_sell(Matrix &m, int fmt, cudaStream_t s) {
     }
     S.class_begin[5] = static_cast<i64>(ids.size());
     S.class_ids.upload(ids.data(), ids.size(), s);
+    S.h_slice_len.resize(n_slices);
+    for (i64 q = 0; q < n_slices; ++q) S.h_slice_len[q] = h_len[q] / 32;
     // keep row lengths in the len buffer's companion: store rlen in 'len' slot
     S.len = std::move(rlen);
     AXGB_CUDA(cudaStreamSynchronize(s));
@@ -482,6 +484,275 @@ double integral(const T *f, const double *area, const double *frac, i64 n, int m
     return acc;
 }
 
+// ─── staged split-FP32 kernel ──────────────────────────────────────────────
+// One CTA owns a block of 128 rows (4 slices). The block's unique source
+// columns are staged per field into shared memory with cp.async (coalesced:
+// the column list is sorted), double-buffered over tiles of T fields, and
+// each thread reduces its row from shared memory with its entries (16-bit
+// local column, hi, lo) held in registers.
+
+constexpr int kSR = 128;            // rows per staged block
+constexpr int kStagedMaxU = 2048;   // unique columns a block may stage (139 KB of smem at T = 8)
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+struct StagedArgs {
+    const int *blocks;
+    i64 n_blocks;
+    const int *base, *rlen;
+    const unsigned short *lidx;
+    const float *hi, *lo;
+    const int *ucol, *ustart, *ucount;
+    i64 n_rows, n_slices;
+    int ustride;
+};
+
+template <int L, int T>
+__global__ void __launch_bounds__(kSR) k_staged(StagedArgs a, const float *__restrict__ x, i64 ldx,
+                                               float *__restrict__ y, i64 ldy, i64 nrhs) {
+    extern __shared__ __align__(16) float smem[];
+    const int US = a.ustride;
+    int *ucs = reinterpret_cast<int *>(smem);
+    float *xs = smem + US;  // [2][T][US]
+    const int b = a.blocks[blockIdx.x];
+    const int U = a.ucount[b];
+    const int *ug = a.ucol + a.ustart[b];
+    for (int u = threadIdx.x; u < U; u += kSR) ucs[u] = ug[u];
+    const i64 row = static_cast<i64>(b) * kSR + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const i64 sid = row >> 5;
+    int rl = 0, base = 0;
+    if (sid < a.n_slices) {
+        base = a.base[sid];
+        rl = a.rlen[row];
+    }
+    int li[L];
+    float h[L], lw[L];
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        if (k < rl) {
+            int e = base + k * 32 + lane;
+            li[k] = a.lidx[e];
+            h[k] = a.hi[e];
+            lw[k] = a.lo[e];
+        } else {
+            li[k] = 0;
+            h[k] = 0.f;
+            lw[k] = 0.f;
+        }
+    }
+    const bool store = row < a.n_rows;
+    __syncthreads();
+    const i64 ntile = (nrhs + T - 1) / T;
+    auto stage = [&](i64 t, float *dst) {
+#pragma unroll
+        for (int f = 0; f < T; ++f) {
+            i64 fg = t * T + f;
+            if (fg < nrhs) {
+                const float *xf = x + fg * ldx;
+                for (int u = threadIdx.x; u < U; u += kSR) cp_async4(dst + f * US + u, xf + ucs[u]);
+            }
+        }
+        cp_async_commit();
+    };
+    stage(0, xs);
+    for (i64 t = 0; t < ntile; ++t) {
+        const float *cur = xs + (t & 1) * T * US;
+        if (t + 1 < ntile) {
+            stage(t + 1, xs + ((t + 1) & 1) * T * US);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const i64 f0 = t * T;
+#pragma unroll
+        for (int f = 0; f < T; f += 2) {
+            if (f0 + f + 1 < nrhs) {
+                F2 sa = pk(0.f, 0.f), ca = pk(0.f, 0.f);
+                const float *c0 = cur + f * US, *c1 = cur + (f + 1) * US;
+#pragma unroll
+                for (int k = 0; k < L; ++k)
+                    if (k < rl) csum2(sa, ca, pk(h[k], h[k]), pk(-h[k], -h[k]), pk(lw[k], lw[k]), pk(c0[li[k]], c1[li[k]]));
+                if (store) {
+                    float ra, rb;
+                    upk(add2(sa, ca), ra, rb);
+                    y[(f0 + f) * ldy + row] = ra;
+                    y[(f0 + f + 1) * ldy + row] = rb;
+                }
+            } else if (f0 + f < nrhs) {
+                float s1 = 0.f, c1 = 0.f;
+                const float *c0 = cur + f * US;
+#pragma unroll
+                for (int k = 0; k < L; ++k)
+                    if (k < rl) csum1(s1, c1, h[k], lw[k], c0[li[k]]);
+                if (store) y[(f0 + f) * ldy + row] = __fadd_rn(s1, c1);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_entry_rows(const int *rp, i64 n_rows, int *erow) {
+    i64 r = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    for (int k = rp[r]; k < rp[r + 1]; ++k) erow[k] = static_cast<int>(r);
+}
+
+__global__ void k_block_keys(const int *erow, const int *col, i64 nnz, std::uint64_t *key, int *val) {
+    i64 e = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= nnz) return;
+    key[e] = (static_cast<std::uint64_t>(erow[e] / kSR) << 32) | static_cast<unsigned>(col[e]);
+    val[e] = static_cast<int>(e);
+}
+
+__global__ void k_unique_flags(const std::uint64_t *key, i64 n, int *flag) {
+    i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = (i == 0 || key[i] != key[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_unique_emit(const std::uint64_t *key, const int *flag, const i64 *pos, i64 n, int *ucol, int *ucount) {
+    i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n || !flag[i]) return;
+    ucol[pos[i]] = static_cast<int>(key[i] & 0xffffffffu);
+    atomicAdd(&ucount[key[i] >> 32], 1);
+}
+
+__global__ void k_entry_lidx(const std::uint64_t *key, const int *val, const int *flag, const i64 *pos,
+                             const int *ustart, i64 n, unsigned short *lidx_csr) {
+    i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    i64 uid = pos[i] + flag[i] - 1;
+    lidx_csr[val[i]] = static_cast<unsigned short>(uid - ustart[key[i] >> 32]);
+}
+
+__global__ void k_sell_lidx(const int *rp, i64 n_rows, i64 n_slices, const int *base, const int *rlen,
+                            const unsigned short *lidx_csr, unsigned short *slidx) {
+    i64 r = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= n_slices * 32) return;
+    i64 s = r >> 5;
+    int lane = static_cast<int>(r & 31);
+    int L = (base[s + 1] - base[s]) / 32;
+    int n = rlen[r];
+    int r0 = r < n_rows ? rp[r] : 0;
+    for (int k = 0; k < L; ++k) slidx[base[s] + k * 32 + lane] = k < n ? lidx_csr[r0 + k] : 0;
+}
+
+void build_staged(Matrix &m, cudaStream_t s) {
+    Staged &G = m.staged;
+    if (G.built) return;
+    build_sell(m, 1, s);
+    const Sell &S = m.sell32;
+    const i64 n_rows = m.n_dst, nnz = m.nnz;
+    const i64 nb = (n_rows + kSR - 1) / kSR;
+    G.n_blocks = nb;
+    G.ucount.alloc(nb);
+    G.ucount.zero(s);
+    G.ustart.alloc(nb + 1);
+    G.lidx.alloc(S.n_entries);
+    DBuf<unsigned short> lidx_csr(nnz);
+    i64 n_unique = 0;
+    if (nnz > 0) {
+        DBuf<int> erow(nnz), val(nnz), flag(nnz);
+        DBuf<std::uint64_t> key(nnz);
+        DBuf<i64> pos(nnz + 1);
+        k_entry_rows<<<nblk(n_rows, 256), 256, 0, s>>>(m.row_ptr.p, n_rows, erow.p);
+        k_block_keys<<<nblk(nnz, 256), 256, 0, s>>>(erow.p, m.col.p, nnz, key.p, val.p);
+        AXGB_CUDA(cudaGetLastError());
+        int bits = 32;
+        while (bits < 64 && (static_cast<unsigned long long>(nb) >> (bits - 32)) > 0) ++bits;
+        radix_sort_pairs_u64(key.p, val.p, nnz, bits, s);
+        k_unique_flags<<<nblk(nnz, 256), 256, 0, s>>>(key.p, nnz, flag.p);
+        scan_exclusive_i32_to_i64(flag.p, pos.p, nnz, s);
+        AXGB_CUDA(cudaMemcpy(&n_unique, pos.p + nnz, sizeof(i64), cudaMemcpyDeviceToHost));
+        G.ucol.alloc(n_unique);
+        k_unique_emit<<<nblk(nnz, 256), 256, 0, s>>>(key.p, flag.p, pos.p, nnz, G.ucol.p, G.ucount.p);
+        scan_exclusive_i32(G.ucount.p, G.ustart.p, nb, s);
+        k_entry_lidx<<<nblk(nnz, 256), 256, 0, s>>>(key.p, val.p, flag.p, pos.p, G.ustart.p, nnz, lidx_csr.p);
+        AXGB_CUDA(cudaGetLastError());
+    } else {
+        G.ucol.alloc(1);
+        scan_exclusive_i32(G.ucount.p, G.ustart.p, nb, s);
+    }
+    if (S.n_slices > 0) {
+        k_sell_lidx<<<nblk(S.n_slices * 32, 256), 256, 0, s>>>(m.row_ptr.p, n_rows, S.n_slices, S.base.p, S.len.p,
+                                                              lidx_csr.p, G.lidx.p);
+        AXGB_CUDA(cudaGetLastError());
+    }
+    // classes on the host
+    std::vector<int> hc(nb);
+    if (nb) AXGB_CUDA(cudaMemcpy(hc.data(), G.ucount.p, sizeof(int) * nb, cudaMemcpyDeviceToHost));
+    std::vector<std::vector<int>> cls(3);
+    std::vector<int> fb;
+    G.class_umax.assign(3, 0);
+    for (i64 b = 0; b < nb; ++b) {
+        int L = 0;
+        for (i64 q = b * (kSR / 32); q < std::min<i64>((b + 1) * (kSR / 32), S.n_slices); ++q)
+            L = std::max(L, S.h_slice_len[q]);
+        int c = L <= 8 ? 0 : (L <= 16 ? 1 : (L <= 32 ? 2 : 3));
+        if (c < 3 && hc[b] <= kStagedMaxU) {
+            cls[c].push_back(static_cast<int>(b));
+            G.class_umax[c] = std::max(G.class_umax[c], hc[b]);
+        } else {
+            for (i64 q = b * (kSR / 32); q < std::min<i64>((b + 1) * (kSR / 32), S.n_slices); ++q)
+                fb.push_back(static_cast<int>(q));
+        }
+    }
+    std::vector<int> ids;
+    G.class_begin.assign(4, 0);
+    for (int c = 0; c < 3; ++c) {
+        G.class_begin[c] = static_cast<i64>(ids.size());
+        ids.insert(ids.end(), cls[c].begin(), cls[c].end());
+    }
+    G.class_begin[3] = static_cast<i64>(ids.size());
+    G.block_ids.upload(ids.data(), ids.size(), s);
+    G.fallback_slices.upload(fb.data(), fb.size(), s);
+    G.n_fallback = static_cast<i64>(fb.size());
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    G.built = true;
+}
+
+template <int L, int T>
+void launch_staged(const Matrix &m, int cls, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    const Staged &G = m.staged;
+    const Sell &S = m.sell32;
+    i64 nb = G.class_begin[cls + 1] - G.class_begin[cls];
+    if (nb == 0) return;
+    StagedArgs a;
+    a.blocks = G.block_ids.p + G.class_begin[cls];
+    a.n_blocks = nb;
+    a.base = S.base.p;
+    a.rlen = S.len.p;
+    a.lidx = G.lidx.p;
+    a.hi = S.hi.p;
+    a.lo = S.lo.p;
+    a.ucol = G.ucol.p;
+    a.ustart = G.ustart.p;
+    a.ucount = G.ucount.p;
+    a.n_rows = m.n_dst;
+    a.n_slices = S.n_slices;
+    a.ustride = (std::max(G.class_umax[cls], 1) + 31) / 32 * 32;
+    size_t bytes = sizeof(float) * static_cast<size_t>(a.ustride) * (1 + 2 * T);
+    AXGB_CUDA(cudaFuncSetAttribute(k_staged<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+    k_staged<L, T><<<static_cast<unsigned>(nb), kSR, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+
+template <int T>
+void apply_staged_T(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    launch_staged<8, T>(m, 0, x, ldx, y, ldy, nrhs, s);
+    launch_staged<16, T>(m, 1, x, ldx, y, ldy, nrhs, s);
+    launch_staged<32, T>(m, 2, x, ldx, y, ldy, nrhs, s);
+}
+
 // ─── persistent batch kernel ───────────────────────────────────────────────
 // Items of all matrices are handed out by one atomic counter (no waiting):
 // item -> (matrix, tile, slice). Entries of up to 32 per row are cached in
@@ -540,6 +811,15 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
 
 void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(m.mu);
+    if (format == 2) {
+        build_staged(m, s);
+        const Staged &G = m.staged;
+        int launches = G.n_fallback > 0 ? 1 : 0;
+        for (int c = 0; c < 3; ++c)
+            if (G.class_begin[c + 1] > G.class_begin[c]) ++launches;
+        m.stats[7] = launches;
+        return;
+    }
     build_sell(m, format == 0 ? 0 : 1, s);
     const Sell &S = format == 0 ? m.sell64 : m.sell32;
     int launches = 0;
@@ -548,12 +828,31 @@ void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
     m.stats[format == 0 ? 6 : 5] = launches;
 }
 
-void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, int fields_per_pass, int unroll,
+void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
                  cudaStream_t s) {
+    if (nrhs <= 0) return;
+    if (p.variant == 1) {
+        if (!m.staged.built) matrix_prepare(m, 2, s);
+        if (p.unroll >= 8)
+            apply_staged_T<8>(m, x, ldx, y, ldy, nrhs, s);
+        else if (p.unroll >= 4)
+            apply_staged_T<4>(m, x, ldx, y, ldy, nrhs, s);
+        else
+            apply_staged_T<2>(m, x, ldx, y, ldy, nrhs, s);
+        const Staged &G = m.staged;
+        if (G.n_fallback > 0) {
+            SellArgs a = sell_args(m, m.sell32, 4);
+            a.ids = G.fallback_slices.p;
+            a.n_ids = G.n_fallback;
+            launch_split<0>(a, x, ldx, y, ldy, nrhs, nrhs, 1, s);
+        }
+        AXGB_CUDA(cudaGetLastError());
+        return;
+    }
     if (!m.sell32.built) matrix_prepare(m, 1, s);
     const Sell &S = m.sell32;
-    i64 tile = (fields_per_pass <= 0 || fields_per_pass > nrhs) ? nrhs : fields_per_pass;
-    if (tile <= 0) return;
+    i64 tile = (p.fields_per_pass <= 0 || p.fields_per_pass > nrhs) ? nrhs : p.fields_per_pass;
+    const int unroll = p.unroll;
     launch_split<8>(sell_args(m, S, 0), x, ldx, y, ldy, nrhs, tile, unroll, s);
     launch_split<16>(sell_args(m, S, 1), x, ldx, y, ldy, nrhs, tile, unroll, s);
     launch_split<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, unroll, s);

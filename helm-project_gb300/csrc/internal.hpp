@@ -147,6 +147,30 @@ struct Sell {
     std::vector<i64> class_begin;  // 6 entries into class_ids
     DBuf<int> class_ids;
     std::vector<int> class_maxlen;
+    std::vector<int> h_slice_len;  // entries per row slot of each slice
+};
+
+// Staged split-FP32 layout: rows in blocks of 128; per block the sorted
+// unique source columns (ucol[ustart[b] .. +ucount[b]]) and, per entry in the
+// sliced-ELL positions of Sell, the 16-bit index of its column in that list.
+struct Staged {
+    bool built = false;
+    i64 n_blocks = 0;
+    DBuf<unsigned short> lidx;
+    DBuf<int> ucol, ustart, ucount;
+    // block ids by class (max slice length <= 8, <= 16, <= 32 and unique
+    // columns <= kStagedMaxU = 2048); slices of all other blocks use the direct kernel
+    std::vector<i64> class_begin;  // 4 entries into block_ids
+    std::vector<int> class_umax;
+    DBuf<int> block_ids, fallback_slices;
+    i64 n_fallback = 0;
+};
+
+// Kernel choice for the split-FP32 apply.
+struct SplitParams {
+    int variant = 1;          // 0 direct gathers, 1 shared-memory staged
+    int fields_per_pass = 0;  // direct: RHS tile width (0 = all)
+    int unroll = 4;           // direct: fields per thread iteration; staged: fields per stage
 };
 
 struct Matrix {
@@ -156,7 +180,8 @@ struct Matrix {
     i64 stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     double times_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     Sell sell64, sell32;
-    std::map<i64, std::pair<int, int>> tuned;  // nrhs -> (fields_per_pass, unroll)
+    Staged staged;
+    std::map<i64, SplitParams> tuned;  // nrhs -> best kernel choice
     std::mutex mu;
 };
 
@@ -172,7 +197,7 @@ void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matr
 // apply.cu
 void matrix_prepare(Matrix &m, int format, cudaStream_t s);
 void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s);
-void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, int fields_per_pass, int unroll,
+void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
                  cudaStream_t s);
 void conservation(Matrix &m, const void *src, const void *dst, bool f32, int norm_type, double *out, cudaStream_t s);
 std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &mats, const std::vector<i64> &nrhs);

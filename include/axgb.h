@@ -137,8 +137,9 @@ int axgb_generate_weights_c(int src_mesh, int dst_mesh, int method, int *matrix_
 /* Statistics of the last generation into this matrix. stats (int64[8]):
  * BVH candidate pairs, pairs passing the reference gates (float AABB, cap,
  * degenerate, area, mask), pairs clipped with the 32-vertex fallback,
- * kept pairs (nnz), LBVH nodes, kernel launches per split-FP32 apply and per
- * FP64 apply (after axgb_matrix_prepare), 0. times_ms (double[8]): cell prep,
+ * kept pairs (nnz), LBVH nodes, kernel launches per direct split-FP32 apply,
+ * per FP64 apply and per staged split-FP32 apply (each known after
+ * axgb_matrix_prepare of its format). times_ms (double[8]): cell prep,
  * LBVH build, candidate search, clip, CSR assembly, total, 0, 0. */
 int axgb_matrix_stats(int matrix_handle, int64_t *stats, double *times_ms);
 
@@ -161,8 +162,9 @@ int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int6
                            const double *area_b, int *matrix_handle);
 
 /* Builds the apply layouts of a matrix ahead of time (format 0: FP64
- * sliced-ELL, 1: split-FP32 hi+lo sliced-ELL) so that later apply calls
- * allocate nothing. Synchronous. */
+ * sliced-ELL, 1: split-FP32 hi+lo sliced-ELL, 2: the staged split-FP32
+ * layout on top of 1) so that later apply calls allocate nothing.
+ * Synchronous. */
 int axgb_matrix_prepare(int matrix_handle, int format);
 
 /* Replaces axis_destroy_matrix_c (axis_c_interop.cpp:247-249). */
@@ -182,15 +184,18 @@ int axgb_apply_f64(int matrix_handle, const double *x, int64_t ld_x, double *y, 
 int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                         axgb_stream_t stream);
 
-/* Same, tuning explicit: fields_per_pass = RHS tile width (0 = all),
- * unroll = fields accumulated together per thread (1, 2 or 4). */
+/* Same, kernel choice explicit. variant 0: direct gathers from global
+ * memory, fields_per_pass = RHS tile width (0 = all), unroll = fields per
+ * thread iteration (1, 2 or 4). variant 1: per 128-row block the unique
+ * source values are staged in shared memory with cp.async, unroll = fields
+ * per stage (2, 4 or 8), fields_per_pass ignored. */
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
-                              int fields_per_pass, int unroll, axgb_stream_t stream);
+                              int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 
-/* Autotuner: times the split apply over (fields_per_pass, unroll) choices on
- * the given device buffers, caches the best per (matrix, nrhs) and returns
- * it in best[2]. Used automatically by axgb_apply_f32split when enabled
- * with axgb_set_autotune(1). */
+/* Autotuner: times the split apply over (variant, fields_per_pass, unroll)
+ * choices on the given device buffers, caches the best per (matrix, nrhs)
+ * and returns it in best[3]. Used automatically by axgb_apply_f32split when
+ * enabled with axgb_set_autotune(1). */
 int axgb_autotune_f32split(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                            axgb_stream_t stream, int32_t *best);
 int axgb_set_autotune(int enable);

@@ -181,10 +181,10 @@ def test_apply_split_parity(gpu, oracle, cfg1):
     ref = oracle.apply_csr(wo, X.astype(np.float64), compensated=True)
     xs = torch.tensor(X, device="cuda")
     outs = []
-    for fpp, u in ((0, 1), (0, 2), (0, 4), (3, 2), (1, 1)):
-        y = gpu.apply_f32split(M, xs, fields_per_pass=fpp, unroll=u).cpu().numpy()
+    for v, fpp, u in ((0, 0, 1), (0, 0, 2), (0, 0, 4), (0, 3, 2), (0, 1, 1), (1, 0, 2), (1, 0, 4), (1, 0, 8)):
+        y = gpu.apply_f32split(M, xs, fields_per_pass=fpp, unroll=u, variant=v).cpu().numpy()
         err = np.max(np.abs(y - ref) / np.abs(ref))
-        assert err < SPLIT_RTOL, (fpp, u, err)
+        assert err < SPLIT_RTOL, (v, fpp, u, err)
         outs.append(y)
     for y in outs[1:]:
         assert np.array_equal(y, outs[0])
@@ -213,8 +213,9 @@ def test_autotune_and_batch(gpu, oracle, cfg1):
     X = torch.tensor(np.stack([f] * 5).astype(np.float32), device="cuda")
     Y = torch.empty((5, M.n_dst), dtype=torch.float32, device="cuda")
     best = gpu.autotune_f32split(M, X, Y)
-    assert best[1] in (1, 2, 4)
+    assert best["variant"] in (0, 1) and best["unroll"] in (1, 2, 4, 8)
     ref = gpu.apply_f32split(M, X, fields_per_pass=0, unroll=1).cpu().numpy()
+    assert np.array_equal(gpu.apply_f32split(M, X).cpu().numpy(), ref)  # tuned choice, same bits
     # persistent multi-matrix batch: same matrix twice plus a reversed pair
     M2 = gpu.generate_weights(gpu.Mesh.from_grid(dst), gpu.Mesh.from_grid(src), {"method": "conservative"})
     x2 = torch.rand((3, M2.n_src), dtype=torch.float32, device="cuda")
