@@ -43,7 +43,7 @@ _SYMBOLS = [
     "axgb_apply_f64", "axgb_apply_f32split", "axgb_apply_f32split_tuned", "axgb_autotune_f32split",
     "axgb_set_autotune", "axgb_apply_c", "axgb_batch_apply_host_f64", "axgb_batch_apply_host_f32split",
     "axgb_batch_create", "axgb_batch_apply", "axgb_destroy_batch", "axgb_conservation_f64",
-    "axgb_conservation_f32",
+    "axgb_conservation_f32", "axgb_matrix_device_status",
 ]
 
 
@@ -97,6 +97,7 @@ def lib():
     L.axgb_matrix_import_csr.argtypes = [i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, ip]
     L.axgb_matrix_prepare.argtypes = [C.c_int, C.c_int]
     L.axgb_destroy_matrix.argtypes = [C.c_int]
+    L.axgb_matrix_device_status.argtypes = [C.c_int, vp]
     L.axgb_apply_f64.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp]
     L.axgb_apply_f32split.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp]
     L.axgb_apply_f32split_tuned.argtypes = [C.c_int, vp, i64, vp, i64, i64, C.c_int, C.c_int, C.c_int, vp]
@@ -295,6 +296,11 @@ class Matrix:
 
     def prepare(self, fmt: int):
         _check(lib().axgb_matrix_prepare(self.handle, fmt))
+
+    def device_status(self) -> int:
+        st = np.zeros(1, np.int32)
+        _check(lib().axgb_matrix_device_status(self.handle, _ptr(st)))
+        return int(st[0])
 
     @classmethod
     def from_csr(cls, n_src, n_dst, row_ptr, col, val, frac_a=None, frac_b=None, area_a=None, area_b=None):

@@ -753,6 +753,337 @@ void apply_staged_T(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 n
     launch_staged<32, T>(m, 2, x, ldx, y, ldy, nrhs, s);
 }
 
+// ─── bulk-staged split-FP32 kernel ─────────────────────────────────────────
+// Same blocking as k_staged, but the block's source values are fetched as
+// contiguous runs (rounded out to 16-byte chunks) with cp.async.bulk on the
+// TMA engine, one copy per (run, field), completion counted on an mbarrier
+// per buffer. Padding entries of a row point at a zero slot at the end of
+// each field's staging area, so the row loop is branch-free; rows are
+// grouped in length classes of 4. Requires x 16-byte aligned, ld_x and
+// n_src multiples of 4 (so no rounded copy leaves a field's row).
+
+constexpr int kBulkMaxUS = 3072;  // staged floats per field per block (196 KB of smem at T = 8)
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(std::uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(std::uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(std::uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, std::uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+struct BulkArgs {
+    const int *blocks;
+    i64 n_blocks;
+    const int *base, *rlen;
+    const unsigned short *lidx;  // staging-area index per sliced-ELL entry (zero slot for padding)
+    const float *hi, *lo;
+    const int *rstart;  // runs of block b: [rstart[b], rstart[b+1])
+    const int4 *runs;   // (global col of the first chunk, chunks, staging offset, 0)
+    const int *bus;     // staging floats per field of block b (incl. the 4-float zero slot)
+    i64 n_rows, n_slices;
+    int us_max;          // stride of a field's staging area in this launch
+    int *status;         // device status word (1 = a bounded wait timed out)
+};
+
+template <int L, int T>
+__global__ void __launch_bounds__(kSR) k_bulk(BulkArgs a, const float *__restrict__ x, i64 ldx,
+                                             float *__restrict__ y, i64 ldy, i64 nrhs) {
+    extern __shared__ __align__(128) float smem[];
+    __shared__ __align__(8) std::uint64_t bar[2];
+    __shared__ int abort_flag;
+    const int US = a.us_max;
+    float *xs = smem;  // [2][T][US]
+    const int b = a.blocks[blockIdx.x];
+    const int r0 = a.rstart[b], nr = a.rstart[b + 1] - r0;
+    const int zero = a.bus[b] - 4;
+    const i64 row = static_cast<i64>(b) * kSR + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const i64 sid = row >> 5;
+    int rl = 0, base = 0;
+    if (sid < a.n_slices) {
+        base = a.base[sid];
+        rl = a.rlen[row];
+    }
+    int li[L];
+    F2 hp[L], hn[L], lp[L];
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        float h = 0.f, l = 0.f;
+        int q = zero;
+        if (k < rl) {
+            int e = base + k * 32 + lane;
+            q = a.lidx[e];
+            h = a.hi[e];
+            l = a.lo[e];
+        }
+        li[k] = q;
+        hp[k] = pk(h, h);
+        hn[k] = pk(-h, -h);
+        lp[k] = pk(l, l);
+    }
+    const bool store = row < a.n_rows;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // zero slots of both buffers (never written by the bulk copies)
+    for (int q = threadIdx.x; q < 2 * T; q += kSR) {
+        float4 *zp = reinterpret_cast<float4 *>(xs + q * US + zero);
+        *zp = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const i64 ntile = (nrhs + T - 1) / T;
+    auto issue = [&](i64 t, int buf) {
+        if (warp != 0) return;
+        const i64 fa = t * T;
+        const int nf = static_cast<int>((nrhs - fa < static_cast<i64>(T) ? nrhs - fa : static_cast<i64>(T)));
+        if (lane == 0) {
+            unsigned bytes = nr > 0 ? 16u * static_cast<unsigned>(a.runs[r0].w) : 0u;
+            mbar_expect_tx(&bar[buf], bytes * static_cast<unsigned>(nf));
+        }
+        __syncwarp();
+        float *dst0 = xs + buf * T * US;
+        for (int q = lane; q < nr; q += 32) {
+            int4 r = a.runs[r0 + q];
+            for (int f = 0; f < nf; ++f)
+                bulk_g2s(dst0 + f * US + r.z, x + (fa + f) * ldx + r.x, 16u * static_cast<unsigned>(r.y), &bar[buf]);
+        }
+    };
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    issue(0, 0);
+    for (i64 t = 0; t < ntile; ++t) {
+        const int buf = static_cast<int>(t & 1);
+        if (t + 1 < ntile) issue(t + 1, buf ^ 1);
+        // bounded wait for this tile's copies
+        const unsigned parity = static_cast<unsigned>((t >> 1) & 1);
+        const unsigned long long t0 = globaltimer_ns();
+        while (!mbar_try_wait(&bar[buf], parity)) {
+            if (globaltimer_ns() - t0 > 1000000000ull) {
+                abort_flag = 1;
+                atomicExch(a.status, 1);
+                break;
+            }
+        }
+        __syncthreads();
+        if (abort_flag) break;
+        const float *cur = xs + buf * T * US;
+        const i64 f0 = t * T;
+#pragma unroll
+        for (int f = 0; f < T; f += 2) {
+            if (f0 + f + 1 < nrhs) {
+                F2 sa = pk(0.f, 0.f), ca = pk(0.f, 0.f);
+                const float *c0 = cur + f * US, *c1 = cur + (f + 1) * US;
+#pragma unroll
+                for (int k = 0; k < L; ++k) csum2(sa, ca, hp[k], hn[k], lp[k], pk(c0[li[k]], c1[li[k]]));
+                if (store) {
+                    float ra, rb;
+                    upk(add2(sa, ca), ra, rb);
+                    y[(f0 + f) * ldy + row] = ra;
+                    y[(f0 + f + 1) * ldy + row] = rb;
+                }
+            } else if (f0 + f < nrhs) {
+                float s1 = 0.f, c1 = 0.f;
+                const float *c0 = cur + f * US;
+#pragma unroll
+                for (int k = 0; k < L; ++k) {
+                    float hh, dummy, ll;
+                    upk(hp[k], hh, dummy);
+                    upk(lp[k], ll, dummy);
+                    csum1(s1, c1, hh, ll, c0[li[k]]);
+                }
+                if (store) y[(f0 + f) * ldy + row] = __fadd_rn(s1, c1);
+            }
+        }
+        __syncthreads();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+}
+
+__global__ void k_bulk_lidx(const int *rp, i64 n_rows, i64 n_slices, const int *base, const int *rlen,
+                            const unsigned short *lidx_sell, const int *ustart, const int *remap, const int *bus,
+                            const unsigned char *staged_ok, unsigned short *out) {
+    i64 r = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= n_slices * 32) return;
+    i64 s = r >> 5;
+    int lane = static_cast<int>(r & 31);
+    i64 b = r / kSR;
+    int L = (base[s + 1] - base[s]) / 32;
+    int n = rlen[r];
+    bool ok = staged_ok[b] != 0;
+    for (int k = 0; k < L; ++k) {
+        int e = base[s] + k * 32 + lane;
+        int v = 0;
+        if (ok) v = k < n ? remap[ustart[b] + lidx_sell[e]] : bus[b] - 4;
+        out[e] = static_cast<unsigned short>(v);
+    }
+}
+
+void build_bulk(Matrix &m, cudaStream_t s) {
+    Bulk &B = m.bulk;
+    if (B.built) return;
+    build_staged(m, s);
+    const Staged &G = m.staged;
+    const Sell &S = m.sell32;
+    const i64 nb = G.n_blocks;
+    std::vector<int> ustart(nb + 1), ucount(nb);
+    std::vector<int> ucol(std::max<size_t>(1, G.ucol.n));
+    if (nb) {
+        AXGB_CUDA(cudaMemcpy(ustart.data(), G.ustart.p, sizeof(int) * (nb + 1), cudaMemcpyDeviceToHost));
+        AXGB_CUDA(cudaMemcpy(ucount.data(), G.ucount.p, sizeof(int) * nb, cudaMemcpyDeviceToHost));
+        AXGB_CUDA(cudaMemcpy(ucol.data(), G.ucol.p, sizeof(int) * G.ucol.n, cudaMemcpyDeviceToHost));
+    }
+    const i64 n_unique = nb ? ustart[nb] : 0;
+    std::vector<int> remap(std::max<i64>(1, n_unique));
+    std::vector<std::vector<int4>> runs(nb);
+    std::vector<int> bus(nb, 4);
+    // runs of consecutive columns, rounded out to 16-byte chunks; runs whose
+    // chunks touch or are one chunk apart are merged
+    for (i64 b = 0; b < nb; ++b) {
+        const int *c = ucol.data() + ustart[b];
+        const int n = ucount[b];
+        int off = 0;
+        int q = 0;
+        while (q < n) {
+            int g4 = c[q] & ~3;
+            int end4 = (c[q] | 3) + 1;
+            int q1 = q + 1;
+            while (q1 < n && (c[q1] & ~3) <= end4 + 4) {
+                end4 = std::max(end4, (c[q1] | 3) + 1);
+                ++q1;
+            }
+            int chunks = (end4 - g4) / 4;
+            runs[b].push_back(make_int4(g4, chunks, off, 0));
+            for (int t = q; t < q1; ++t) remap[ustart[b] + t] = off + (c[t] - g4);
+            off += 4 * chunks;
+            q = q1;
+        }
+        bus[b] = off + 4;  // + zero slot
+        if (!runs[b].empty()) runs[b][0].w = off / 4;  // total chunks of the block
+    }
+    // classes: (row length class in steps of 4) x fits-in-smem
+    std::vector<unsigned char> ok(nb, 0);
+    const int nclass = 8;
+    std::vector<std::vector<int>> cls(nclass);
+    B.class_usmax.assign(nclass, 0);
+    std::vector<int> rstart(nb + 1, 0);
+    std::vector<int4> allruns;
+    for (i64 b = 0; b < nb; ++b) {
+        int L = 0;
+        for (i64 q = b * (kSR / 32); q < std::min<i64>((b + 1) * (kSR / 32), S.n_slices); ++q)
+            L = std::max(L, S.h_slice_len[q]);
+        int c = L <= 4 ? 0 : (L + 3) / 4 - 1;
+        rstart[b] = static_cast<int>(allruns.size());
+        allruns.insert(allruns.end(), runs[b].begin(), runs[b].end());
+        if (c < nclass && bus[b] <= kBulkMaxUS) {
+            ok[b] = 1;
+            cls[c].push_back(static_cast<int>(b));
+            B.class_usmax[c] = std::max(B.class_usmax[c], bus[b]);
+        }
+    }
+    rstart[nb] = static_cast<int>(allruns.size());
+    std::vector<int> ids, fb;
+    B.class_begin.assign(nclass + 1, 0);
+    for (int c = 0; c < nclass; ++c) {
+        B.class_begin[c] = static_cast<i64>(ids.size());
+        ids.insert(ids.end(), cls[c].begin(), cls[c].end());
+    }
+    B.class_begin[nclass] = static_cast<i64>(ids.size());
+    for (i64 b = 0; b < nb; ++b)
+        if (!ok[b])
+            for (i64 q = b * (kSR / 32); q < std::min<i64>((b + 1) * (kSR / 32), S.n_slices); ++q)
+                fb.push_back(static_cast<int>(q));
+    B.block_ids.upload(ids.data(), ids.size(), s);
+    B.fallback_slices.upload(fb.data(), fb.size(), s);
+    B.n_fallback = static_cast<i64>(fb.size());
+    B.rstart.upload(rstart.data(), rstart.size(), s);
+    B.runs.upload(allruns.data(), std::max<size_t>(1, allruns.size()), s);
+    B.bus.upload(bus.data(), std::max<size_t>(1, bus.size()), s);
+    DBuf<int> d_remap;
+    d_remap.upload(remap.data(), remap.size(), s);
+    DBuf<unsigned char> d_ok;
+    d_ok.upload(ok.data(), std::max<size_t>(1, ok.size()), s);
+    B.lidx.alloc(S.n_entries);
+    if (S.n_slices > 0) {
+        k_bulk_lidx<<<nblk(S.n_slices * 32, 256), 256, 0, s>>>(m.row_ptr.p, m.n_dst, S.n_slices, S.base.p, S.len.p,
+                                                              G.lidx.p, G.ustart.p, d_remap.p, B.bus.p, d_ok.p,
+                                                              B.lidx.p);
+        AXGB_CUDA(cudaGetLastError());
+    }
+    if (!B.status.p) {
+        B.status.alloc(1);
+        B.status.zero(s);
+    }
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    B.built = true;
+}
+
+template <int L, int T>
+void launch_bulk(Matrix &m, int cls, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    const Bulk &B = m.bulk;
+    const Sell &S = m.sell32;
+    i64 nb = B.class_begin[cls + 1] - B.class_begin[cls];
+    if (nb == 0) return;
+    BulkArgs a;
+    a.blocks = B.block_ids.p + B.class_begin[cls];
+    a.n_blocks = nb;
+    a.base = S.base.p;
+    a.rlen = S.len.p;
+    a.lidx = B.lidx.p;
+    a.hi = S.hi.p;
+    a.lo = S.lo.p;
+    a.rstart = B.rstart.p;
+    a.runs = B.runs.p;
+    a.bus = B.bus.p;
+    a.n_rows = m.n_dst;
+    a.n_slices = S.n_slices;
+    a.us_max = (B.class_usmax[cls] + 31) / 32 * 32;
+    a.status = B.status.p;
+    size_t bytes = sizeof(float) * static_cast<size_t>(a.us_max) * 2 * T;
+    AXGB_CUDA(cudaFuncSetAttribute(k_bulk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+    k_bulk<L, T><<<static_cast<unsigned>(nb), kSR, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+
+template <int T>
+void apply_bulk_T(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    launch_bulk<4, T>(m, 0, x, ldx, y, ldy, nrhs, s);
+    launch_bulk<8, T>(m, 1, x, ldx, y, ldy, nrhs, s);
+    launch_bulk<12, T>(m, 2, x, ldx, y, ldy, nrhs, s);
+    launch_bulk<16, T>(m, 3, x, ldx, y, ldy, nrhs, s);
+    launch_bulk<20, T>(m, 4, x, ldx, y, ldy, nrhs, s);
+    launch_bulk<24, T>(m, 5, x, ldx, y, ldy, nrhs, s);
+    launch_bulk<28, T>(m, 6, x, ldx, y, ldy, nrhs, s);
+    launch_bulk<32, T>(m, 7, x, ldx, y, ldy, nrhs, s);
+}
+
+bool bulk_eligible(const Matrix &m, const float *x, i64 ldx) {
+    return (reinterpret_cast<std::uintptr_t>(x) % 16 == 0) && (ldx % 4 == 0) && (m.n_src % 4 == 0);
+}
+
 // ─── persistent batch kernel ───────────────────────────────────────────────
 // Items of all matrices are handed out by one atomic counter (no waiting):
 // item -> (matrix, tile, slice). Entries of up to 32 per row are cached in
@@ -811,6 +1142,15 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
 
 void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(m.mu);
+    if (format == 3) {
+        build_bulk(m, s);
+        const Bulk &B = m.bulk;
+        int launches = B.n_fallback > 0 ? 1 : 0;
+        for (size_t c = 0; c + 1 < B.class_begin.size(); ++c)
+            if (B.class_begin[c + 1] > B.class_begin[c]) ++launches;
+        m.stats[6] = launches;
+        return;
+    }
     if (format == 2) {
         build_staged(m, s);
         const Staged &G = m.staged;
@@ -821,17 +1161,37 @@ void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
         return;
     }
     build_sell(m, format == 0 ? 0 : 1, s);
-    const Sell &S = format == 0 ? m.sell64 : m.sell32;
-    int launches = 0;
-    for (int c = 0; c < 5; ++c)
-        if (S.class_begin[c + 1] > S.class_begin[c]) ++launches;
-    m.stats[format == 0 ? 6 : 5] = launches;
+    if (format == 1) {
+        const Sell &S = m.sell32;
+        int launches = 0;
+        for (int c = 0; c < 5; ++c)
+            if (S.class_begin[c + 1] > S.class_begin[c]) ++launches;
+        m.stats[5] = launches;
+    }
 }
 
 void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
                  cudaStream_t s) {
     if (nrhs <= 0) return;
-    if (p.variant == 1) {
+    if (p.variant == 2 && bulk_eligible(m, x, ldx)) {
+        if (!m.bulk.built) matrix_prepare(m, 3, s);
+        if (p.unroll >= 8)
+            apply_bulk_T<8>(m, x, ldx, y, ldy, nrhs, s);
+        else if (p.unroll >= 4)
+            apply_bulk_T<4>(m, x, ldx, y, ldy, nrhs, s);
+        else
+            apply_bulk_T<2>(m, x, ldx, y, ldy, nrhs, s);
+        const Bulk &B = m.bulk;
+        if (B.n_fallback > 0) {
+            SellArgs a = sell_args(m, m.sell32, 4);
+            a.ids = B.fallback_slices.p;
+            a.n_ids = B.n_fallback;
+            launch_split<0>(a, x, ldx, y, ldy, nrhs, nrhs, 1, s);
+        }
+        AXGB_CUDA(cudaGetLastError());
+        return;
+    }
+    if (p.variant >= 1) {
         if (!m.staged.built) matrix_prepare(m, 2, s);
         if (p.unroll >= 8)
             apply_staged_T<8>(m, x, ldx, y, ldy, nrhs, s);

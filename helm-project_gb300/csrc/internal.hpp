@@ -166,9 +166,23 @@ struct Staged {
     i64 n_fallback = 0;
 };
 
+// Bulk-staged layout on top of Staged: per block the unique columns as runs
+// of 16-byte chunks copied with cp.async.bulk, and per sliced-ELL entry the
+// index into the block's staging area (padding -> the zero slot).
+struct Bulk {
+    bool built = false;
+    DBuf<unsigned short> lidx;
+    DBuf<int> rstart, bus, block_ids, fallback_slices;
+    DBuf<int4> runs;
+    std::vector<i64> class_begin;  // 9 entries: row-length classes 4, 8, ..., 32
+    std::vector<int> class_usmax;
+    i64 n_fallback = 0;
+    DBuf<int> status;  // device status word: 1 = a bounded wait timed out
+};
+
 // Kernel choice for the split-FP32 apply.
 struct SplitParams {
-    int variant = 1;          // 0 direct gathers, 1 shared-memory staged
+    int variant = 2;          // 0 direct gathers, 1 cp.async staged, 2 bulk (TMA) staged
     int fields_per_pass = 0;  // direct: RHS tile width (0 = all)
     int unroll = 4;           // direct: fields per thread iteration; staged: fields per stage
 };
@@ -181,6 +195,7 @@ struct Matrix {
     double times_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     Sell sell64, sell32;
     Staged staged;
+    Bulk bulk;
     std::map<i64, SplitParams> tuned;  // nrhs -> best kernel choice
     std::mutex mu;
 };

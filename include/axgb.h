@@ -137,9 +137,9 @@ int axgb_generate_weights_c(int src_mesh, int dst_mesh, int method, int *matrix_
 /* Statistics of the last generation into this matrix. stats (int64[8]):
  * BVH candidate pairs, pairs passing the reference gates (float AABB, cap,
  * degenerate, area, mask), pairs clipped with the 32-vertex fallback,
- * kept pairs (nnz), LBVH nodes, kernel launches per direct split-FP32 apply,
- * per FP64 apply and per staged split-FP32 apply (each known after
- * axgb_matrix_prepare of its format). times_ms (double[8]): cell prep,
+ * kept pairs (nnz), LBVH nodes, and the kernel launches per split-FP32
+ * apply of the direct, bulk-staged and cp.async-staged variants (each known
+ * after axgb_matrix_prepare of its format). times_ms (double[8]): cell prep,
  * LBVH build, candidate search, clip, CSR assembly, total, 0, 0. */
 int axgb_matrix_stats(int matrix_handle, int64_t *stats, double *times_ms);
 
@@ -162,10 +162,15 @@ int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int6
                            const double *area_b, int *matrix_handle);
 
 /* Builds the apply layouts of a matrix ahead of time (format 0: FP64
- * sliced-ELL, 1: split-FP32 hi+lo sliced-ELL, 2: the staged split-FP32
- * layout on top of 1) so that later apply calls allocate nothing.
- * Synchronous. */
+ * sliced-ELL, 1: split-FP32 hi+lo sliced-ELL, 2: the cp.async-staged
+ * split-FP32 layout on top of 1, 3: the bulk-copy staged layout on top of 2)
+ * so that later apply calls allocate nothing. Synchronous. */
 int axgb_matrix_prepare(int matrix_handle, int format);
+
+/* Reads (and clears) the device status word of a matrix's bulk-staged apply:
+ * 0 = fine, 1 = a bounded wait for staged copies gave up (the affected
+ * block rows were not written). Synchronizes the device. */
+int axgb_matrix_device_status(int matrix_handle, int32_t *status);
 
 /* Replaces axis_destroy_matrix_c (axis_c_interop.cpp:247-249). */
 int axgb_destroy_matrix(int matrix_handle);
@@ -188,7 +193,10 @@ int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *
  * memory, fields_per_pass = RHS tile width (0 = all), unroll = fields per
  * thread iteration (1, 2 or 4). variant 1: per 128-row block the unique
  * source values are staged in shared memory with cp.async, unroll = fields
- * per stage (2, 4 or 8), fields_per_pass ignored. */
+ * per stage (2, 4 or 8), fields_per_pass ignored. variant 2: as 1 but the
+ * block's source runs are fetched with bulk (TMA) copies completing on an
+ * mbarrier; used when x is 16-byte aligned and ld_x, n_src are multiples of
+ * 4, otherwise variant 1 runs. */
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                               int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 
