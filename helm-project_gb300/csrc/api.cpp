@@ -663,14 +663,14 @@ int axgb_apply_f32split_tuned(int h, const float *x, int64_t ldx, float *y, int6
     AXGB_TRY({
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         check_apply(*m, x, ldx, y, ldy, nrhs);
-        AXGB_REQUIRE(variant >= 0 && variant <= 2, "apply: variant must be 0 (direct), 1 or 2 (staged)");
+        AXGB_REQUIRE(variant >= 0 && variant <= 3, "apply: variant must be 0 (direct) or 1..3 (staged)");
         if (variant == 0) {
             AXGB_REQUIRE(unroll == 1 || unroll == 2 || unroll == 4, "apply: direct unroll must be 1, 2 or 4");
         } else {
             AXGB_REQUIRE(unroll == 2 || unroll == 4 || unroll == 8, "apply: staged fields per stage must be 2, 4 or 8");
         }
         // the bulk path needs 16-byte aligned field rows; otherwise run the cp.async staging
-        if (variant == 2 && !(reinterpret_cast<std::uintptr_t>(x) % 16 == 0 && ldx % 4 == 0 && m->n_src % 4 == 0))
+        if (variant >= 2 && !(reinterpret_cast<std::uintptr_t>(x) % 16 == 0 && ldx % 4 == 0 && m->n_src % 4 == 0))
             variant = 1;
         SplitParams p{variant, fields_per_pass, unroll};
         if (nrhs > 0) apply_split(*m, x, ldx, y, ldy, nrhs, p, static_cast<cudaStream_t>(stream));

@@ -924,6 +924,153 @@ __global__ void __launch_bounds__(kSR) k_bulk(BulkArgs a, const float *__restric
     }
 }
 
+// Chunked variant: the same staging layout and branch-free row loop as
+// k_bulk, but the 16-byte chunks are copied by all threads with
+// cp.async.cg (one instruction per chunk and field), double-buffered with
+// cp.async groups.
+struct ChunkArgs {
+    const int *blocks;
+    i64 n_blocks;
+    const int *base, *rlen;
+    const unsigned short *lidx;
+    const float *hi, *lo;
+    const int *cstart;  // chunks of block b: [cstart[b], cstart[b+1])
+    const int *ccol;    // global column of each chunk (multiple of 4)
+    i64 n_rows, n_slices;
+    int us_max;
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+
+template <int L, int T>
+__global__ void __launch_bounds__(kSR) k_chunk(ChunkArgs a, const float *__restrict__ x, i64 ldx,
+                                              float *__restrict__ y, i64 ldy, i64 nrhs) {
+    extern __shared__ __align__(128) float smem[];
+    const int US = a.us_max;
+    float *xs = smem;  // [2][T][US]
+    const int b = a.blocks[blockIdx.x];
+    const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
+    const int zero = 4 * nch;
+    const i64 row = static_cast<i64>(b) * kSR + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const i64 sid = row >> 5;
+    int rl = 0, base = 0;
+    if (sid < a.n_slices) {
+        base = a.base[sid];
+        rl = a.rlen[row];
+    }
+    int li[L];
+    F2 hp[L], hn[L], lp[L];
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        float h = 0.f, l = 0.f;
+        int q = zero;
+        if (k < rl) {
+            int e = base + k * 32 + lane;
+            q = a.lidx[e];
+            h = a.hi[e];
+            l = a.lo[e];
+        }
+        li[k] = q;
+        hp[k] = pk(h, h);
+        hn[k] = pk(-h, -h);
+        lp[k] = pk(l, l);
+    }
+    const bool store = row < a.n_rows;
+    for (int q = threadIdx.x; q < 2 * T; q += kSR)
+        *reinterpret_cast<float4 *>(xs + q * US + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
+    const i64 ntile = (nrhs + T - 1) / T;
+    auto stage = [&](i64 t, float *dst) {
+        const i64 fa = t * T;
+        const int nf = static_cast<int>((nrhs - fa < static_cast<i64>(T)) ? nrhs - fa : static_cast<i64>(T));
+        for (int j = threadIdx.x; j < nch; j += kSR) {
+            const int g = a.ccol[c0 + j];
+            const float *src = x + fa * ldx + g;
+#pragma unroll
+            for (int f = 0; f < T; ++f)
+                if (f < nf) cp_async16(dst + f * US + 4 * j, src + f * ldx);
+        }
+        cp_async_commit();
+    };
+    stage(0, xs);
+    for (i64 t = 0; t < ntile; ++t) {
+        const float *cur = xs + (t & 1) * T * US;
+        if (t + 1 < ntile) {
+            stage(t + 1, xs + ((t + 1) & 1) * T * US);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const i64 f0 = t * T;
+#pragma unroll
+        for (int f = 0; f < T; f += 2) {
+            if (f0 + f + 1 < nrhs) {
+                F2 sa = pk(0.f, 0.f), ca = pk(0.f, 0.f);
+                const float *p0 = cur + f * US, *p1 = cur + (f + 1) * US;
+#pragma unroll
+                for (int k = 0; k < L; ++k) csum2(sa, ca, hp[k], hn[k], lp[k], pk(p0[li[k]], p1[li[k]]));
+                if (store) {
+                    float ra, rb;
+                    upk(add2(sa, ca), ra, rb);
+                    y[(f0 + f) * ldy + row] = ra;
+                    y[(f0 + f + 1) * ldy + row] = rb;
+                }
+            } else if (f0 + f < nrhs) {
+                float s1 = 0.f, c1 = 0.f;
+                const float *p0 = cur + f * US;
+#pragma unroll
+                for (int k = 0; k < L; ++k) {
+                    float hh, dummy, ll;
+                    upk(hp[k], hh, dummy);
+                    upk(lp[k], ll, dummy);
+                    csum1(s1, c1, hh, ll, p0[li[k]]);
+                }
+                if (store) y[(f0 + f) * ldy + row] = __fadd_rn(s1, c1);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int L, int T>
+void launch_chunk(Matrix &m, int cls, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    const Bulk &B = m.bulk;
+    const Sell &S = m.sell32;
+    i64 nb = B.class_begin[cls + 1] - B.class_begin[cls];
+    if (nb == 0) return;
+    ChunkArgs a;
+    a.blocks = B.block_ids.p + B.class_begin[cls];
+    a.n_blocks = nb;
+    a.base = S.base.p;
+    a.rlen = S.len.p;
+    a.lidx = B.lidx.p;
+    a.hi = S.hi.p;
+    a.lo = S.lo.p;
+    a.cstart = B.cstart.p;
+    a.ccol = B.ccol.p;
+    a.n_rows = m.n_dst;
+    a.n_slices = S.n_slices;
+    a.us_max = (B.class_usmax[cls] + 31) / 32 * 32;
+    size_t bytes = sizeof(float) * static_cast<size_t>(a.us_max) * 2 * T;
+    AXGB_CUDA(cudaFuncSetAttribute(k_chunk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+    k_chunk<L, T><<<static_cast<unsigned>(nb), kSR, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+
+template <int T>
+void apply_chunk_T(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    launch_chunk<4, T>(m, 0, x, ldx, y, ldy, nrhs, s);
+    launch_chunk<8, T>(m, 1, x, ldx, y, ldy, nrhs, s);
+    launch_chunk<12, T>(m, 2, x, ldx, y, ldy, nrhs, s);
+    launch_chunk<16, T>(m, 3, x, ldx, y, ldy, nrhs, s);
+    launch_chunk<20, T>(m, 4, x, ldx, y, ldy, nrhs, s);
+    launch_chunk<24, T>(m, 5, x, ldx, y, ldy, nrhs, s);
+    launch_chunk<28, T>(m, 6, x, ldx, y, ldy, nrhs, s);
+    launch_chunk<32, T>(m, 7, x, ldx, y, ldy, nrhs, s);
+}
+
 __global__ void k_bulk_lidx(const int *rp, i64 n_rows, i64 n_slices, const int *base, const int *rlen,
                             const unsigned short *lidx_sell, const int *ustart, const int *remap, const int *bus,
                             const unsigned char *staged_ok, unsigned short *out) {
@@ -1021,6 +1168,16 @@ void build_bulk(Matrix &m, cudaStream_t s) {
     B.fallback_slices.upload(fb.data(), fb.size(), s);
     B.n_fallback = static_cast<i64>(fb.size());
     B.rstart.upload(rstart.data(), rstart.size(), s);
+    // flattened 16-byte chunk list (chunk j of a block stages at offset 4*j)
+    std::vector<int> cstart(nb + 1, 0), ccol;
+    for (i64 b = 0; b < nb; ++b) {
+        cstart[b] = static_cast<int>(ccol.size());
+        for (const int4 &r : runs[b])
+            for (int j = 0; j < r.y; ++j) ccol.push_back(r.x + 4 * j);
+    }
+    cstart[nb] = static_cast<int>(ccol.size());
+    B.cstart.upload(cstart.data(), cstart.size(), s);
+    B.ccol.upload(ccol.data(), std::max<size_t>(1, ccol.size()), s);
     B.runs.upload(allruns.data(), std::max<size_t>(1, allruns.size()), s);
     B.bus.upload(bus.data(), std::max<size_t>(1, bus.size()), s);
     DBuf<int> d_remap;
@@ -1173,14 +1330,23 @@ void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
 void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
                  cudaStream_t s) {
     if (nrhs <= 0) return;
-    if (p.variant == 2 && bulk_eligible(m, x, ldx)) {
+    if ((p.variant == 2 || p.variant == 3) && bulk_eligible(m, x, ldx)) {
         if (!m.bulk.built) matrix_prepare(m, 3, s);
-        if (p.unroll >= 8)
-            apply_bulk_T<8>(m, x, ldx, y, ldy, nrhs, s);
-        else if (p.unroll >= 4)
-            apply_bulk_T<4>(m, x, ldx, y, ldy, nrhs, s);
-        else
-            apply_bulk_T<2>(m, x, ldx, y, ldy, nrhs, s);
+        if (p.variant == 3) {
+            if (p.unroll >= 8)
+                apply_bulk_T<8>(m, x, ldx, y, ldy, nrhs, s);
+            else if (p.unroll >= 4)
+                apply_bulk_T<4>(m, x, ldx, y, ldy, nrhs, s);
+            else
+                apply_bulk_T<2>(m, x, ldx, y, ldy, nrhs, s);
+        } else {
+            if (p.unroll >= 8)
+                apply_chunk_T<8>(m, x, ldx, y, ldy, nrhs, s);
+            else if (p.unroll >= 4)
+                apply_chunk_T<4>(m, x, ldx, y, ldy, nrhs, s);
+            else
+                apply_chunk_T<2>(m, x, ldx, y, ldy, nrhs, s);
+        }
         const Bulk &B = m.bulk;
         if (B.n_fallback > 0) {
             SellArgs a = sell_args(m, m.sell32, 4);

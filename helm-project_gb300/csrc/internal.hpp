@@ -172,7 +172,7 @@ struct Staged {
 struct Bulk {
     bool built = false;
     DBuf<unsigned short> lidx;
-    DBuf<int> rstart, bus, block_ids, fallback_slices;
+    DBuf<int> rstart, bus, block_ids, fallback_slices, cstart, ccol;
     DBuf<int4> runs;
     std::vector<i64> class_begin;  // 9 entries: row-length classes 4, 8, ..., 32
     std::vector<int> class_usmax;
@@ -182,7 +182,8 @@ struct Bulk {
 
 // Kernel choice for the split-FP32 apply.
 struct SplitParams {
-    int variant = 2;          // 0 direct gathers, 1 cp.async staged, 2 bulk (TMA) staged
+    int variant = 2;          // 0 direct, 1 cp.async 4-byte staged, 2 cp.async 16-byte chunk staged,
+                              // 3 bulk-copy (TMA) staged
     int fields_per_pass = 0;  // direct: RHS tile width (0 = all)
     int unroll = 4;           // direct: fields per thread iteration; staged: fields per stage
 };

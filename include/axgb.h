@@ -194,9 +194,10 @@ int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *
  * thread iteration (1, 2 or 4). variant 1: per 128-row block the unique
  * source values are staged in shared memory with cp.async, unroll = fields
  * per stage (2, 4 or 8), fields_per_pass ignored. variant 2: as 1 but the
- * block's source runs are fetched with bulk (TMA) copies completing on an
- * mbarrier; used when x is 16-byte aligned and ld_x, n_src are multiples of
- * 4, otherwise variant 1 runs. */
+ * block's source runs are staged as 16-byte chunks (cp.async.cg) and the row
+ * loop is branch-free; variant 3: the runs are fetched with bulk (TMA) copies
+ * completing on an mbarrier. Variants 2 and 3 need x 16-byte aligned and
+ * ld_x, n_src multiples of 4; otherwise variant 1 runs. */
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                               int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 
