@@ -122,6 +122,23 @@ __device__ __forceinline__ void csum2(F2 &s, F2 &c, F2 h, F2 hn, F2 l, F2 x) {
     c = add2(c, add2(e, q));
 }
 
+// Same arithmetic as csum2 (bitwise identical results) but without a
+// negated-weight register pair: the product error is formed with -x and
+// the compensation is carried negated (cn = -c); the row value is s - cn.
+__device__ __forceinline__ void cstep2(F2 &s, F2 &cn, F2 h, F2 l, F2 x, F2 mone) {
+    F2 nx = mul2(x, mone);
+    F2 p = mul2(h, x);
+    F2 pen = fma2(h, nx, p);  // p - h*x = -(product error), exact
+    F2 t = add2(s, p);
+    F2 bp = sub2(t, s);
+    F2 a2 = sub2(s, sub2(t, bp));
+    F2 a3 = sub2(p, bp);
+    F2 e = add2(a2, a3);      // TwoSum error
+    F2 u1 = fma2(l, nx, pen); // -(lo*x + product error)
+    cn = add2(cn, sub2(u1, e));
+    s = t;
+}
+
 struct SellArgs {
     const int *ids;
     i64 n_ids;
@@ -504,7 +521,14 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Slice of warp w in staged block b (-1 = none).
+__device__ __forceinline__ int block_slice(const int4 *bs, int b, int w) {
+    int4 v = bs[b];
+    return w == 0 ? v.x : (w == 1 ? v.y : (w == 2 ? v.z : v.w));
+}
+
 struct StagedArgs {
+    const int4 *bslices;
     const int *blocks;
     i64 n_blocks;
     const int *base, *rlen;
@@ -526,11 +550,11 @@ __global__ void __launch_bounds__(kSR) k_staged(StagedArgs a, const float *__res
     const int U = a.ucount[b];
     const int *ug = a.ucol + a.ustart[b];
     for (int u = threadIdx.x; u < U; u += kSR) ucs[u] = ug[u];
-    const i64 row = static_cast<i64>(b) * kSR + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    const i64 sid = row >> 5;
+    const i64 sid = block_slice(a.bslices, b, threadIdx.x >> 5);
+    const i64 row = sid * 32 + lane;
     int rl = 0, base = 0;
-    if (sid < a.n_slices) {
+    if (sid >= 0) {
         base = a.base[sid];
         rl = a.rlen[row];
     }
@@ -549,7 +573,7 @@ __global__ void __launch_bounds__(kSR) k_staged(StagedArgs a, const float *__res
             lw[k] = 0.f;
         }
     }
-    const bool store = row < a.n_rows;
+    const bool store = sid >= 0 && row < a.n_rows;
     __syncthreads();
     const i64 ntile = (nrhs + T - 1) / T;
     auto stage = [&](i64 t, float *dst) {
@@ -607,10 +631,11 @@ __global__ void k_entry_rows(const int *rp, i64 n_rows, int *erow) {
     for (int k = rp[r]; k < rp[r + 1]; ++k) erow[k] = static_cast<int>(r);
 }
 
-__global__ void k_block_keys(const int *erow, const int *col, i64 nnz, std::uint64_t *key, int *val) {
+__global__ void k_block_keys(const int *erow, const int *col, const int *blk_of_slice, i64 nnz, std::uint64_t *key,
+                             int *val) {
     i64 e = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (e >= nnz) return;
-    key[e] = (static_cast<std::uint64_t>(erow[e] / kSR) << 32) | static_cast<unsigned>(col[e]);
+    key[e] = (static_cast<std::uint64_t>(blk_of_slice[erow[e] >> 5]) << 32) | static_cast<unsigned>(col[e]);
     val[e] = static_cast<int>(e);
 }
 
@@ -653,8 +678,40 @@ void build_staged(Matrix &m, cudaStream_t s) {
     build_sell(m, 1, s);
     const Sell &S = m.sell32;
     const i64 n_rows = m.n_dst, nnz = m.nnz;
-    const i64 nb = (n_rows + kSR - 1) / kSR;
+    // Blocks of 4 slices grouped by source locality: slices sorted by the
+    // median source column of their entries, then taken 4 at a time, so a
+    // block's rows share source cells and consecutive blocks are neighbours.
+    const i64 nsl = S.n_slices;
+    std::vector<int> hrp(n_rows + 1), hcol(std::max<i64>(1, nnz));
+    AXGB_CUDA(cudaMemcpy(hrp.data(), m.row_ptr.p, sizeof(int) * (n_rows + 1), cudaMemcpyDeviceToHost));
+    if (nnz) AXGB_CUDA(cudaMemcpy(hcol.data(), m.col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+    std::vector<long long> skey(nsl);
+    for (i64 q = 0; q < nsl; ++q) {
+        int a0 = hrp[q * 32], a1 = hrp[std::min<i64>((q + 1) * 32, n_rows)];
+        if (a1 == a0) {
+            skey[q] = (1ll << 40) + q;  // empty slices last
+            continue;
+        }
+        std::vector<int> c(hcol.begin() + a0, hcol.begin() + a1);
+        std::nth_element(c.begin(), c.begin() + c.size() / 2, c.end());
+        skey[q] = (static_cast<long long>(c[c.size() / 2]) << 20) + (q & 0xfffff);
+    }
+    std::vector<int> order(nsl);
+    for (i64 q = 0; q < nsl; ++q) order[q] = static_cast<int>(q);
+    std::stable_sort(order.begin(), order.end(), [&](int x1, int x2) { return skey[x1] < skey[x2]; });
+    const i64 nb = (nsl + 3) / 4;
     G.n_blocks = nb;
+    G.h_bslices.assign(nb, make_int4(-1, -1, -1, -1));
+    std::vector<int> blk_of_slice(std::max<i64>(1, nsl));
+    for (i64 q = 0; q < nsl; ++q) {
+        i64 b = q / 4;
+        int *slot = &G.h_bslices[b].x;
+        slot[q % 4] = order[q];
+        blk_of_slice[order[q]] = static_cast<int>(b);
+    }
+    G.bslices.upload(G.h_bslices.data(), std::max<size_t>(1, G.h_bslices.size()), s);
+    G.blk_of_slice.upload(blk_of_slice.data(), blk_of_slice.size(), s);
+    const int *d_blk_p = G.blk_of_slice.p;
     G.ucount.alloc(nb);
     G.ucount.zero(s);
     G.ustart.alloc(nb + 1);
@@ -666,7 +723,7 @@ void build_staged(Matrix &m, cudaStream_t s) {
         DBuf<std::uint64_t> key(nnz);
         DBuf<i64> pos(nnz + 1);
         k_entry_rows<<<nblk(n_rows, 256), 256, 0, s>>>(m.row_ptr.p, n_rows, erow.p);
-        k_block_keys<<<nblk(nnz, 256), 256, 0, s>>>(erow.p, m.col.p, nnz, key.p, val.p);
+        k_block_keys<<<nblk(nnz, 256), 256, 0, s>>>(erow.p, m.col.p, d_blk_p, nnz, key.p, val.p);
         AXGB_CUDA(cudaGetLastError());
         int bits = 32;
         while (bits < 64 && (static_cast<unsigned long long>(nb) >> (bits - 32)) > 0) ++bits;
@@ -696,15 +753,16 @@ void build_staged(Matrix &m, cudaStream_t s) {
     G.class_umax.assign(3, 0);
     for (i64 b = 0; b < nb; ++b) {
         int L = 0;
-        for (i64 q = b * (kSR / 32); q < std::min<i64>((b + 1) * (kSR / 32), S.n_slices); ++q)
-            L = std::max(L, S.h_slice_len[q]);
+        const int *bsl = &G.h_bslices[b].x;
+        for (int w = 0; w < 4; ++w)
+            if (bsl[w] >= 0) L = std::max(L, S.h_slice_len[bsl[w]]);
         int c = L <= 8 ? 0 : (L <= 16 ? 1 : (L <= 32 ? 2 : 3));
         if (c < 3 && hc[b] <= kStagedMaxU) {
             cls[c].push_back(static_cast<int>(b));
             G.class_umax[c] = std::max(G.class_umax[c], hc[b]);
         } else {
-            for (i64 q = b * (kSR / 32); q < std::min<i64>((b + 1) * (kSR / 32), S.n_slices); ++q)
-                fb.push_back(static_cast<int>(q));
+            for (int w = 0; w < 4; ++w)
+                if (bsl[w] >= 0) fb.push_back(bsl[w]);
         }
     }
     std::vector<int> ids;
@@ -728,6 +786,7 @@ void launch_staged(const Matrix &m, int cls, const float *x, i64 ldx, float *y, 
     i64 nb = G.class_begin[cls + 1] - G.class_begin[cls];
     if (nb == 0) return;
     StagedArgs a;
+    a.bslices = G.bslices.p;
     a.blocks = G.block_ids.p + G.class_begin[cls];
     a.n_blocks = nb;
     a.base = S.base.p;
@@ -795,6 +854,7 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 }
 
 struct BulkArgs {
+    const int4 *bslices;
     const int *blocks;
     i64 n_blocks;
     const int *base, *rlen;
@@ -819,11 +879,11 @@ __global__ void __launch_bounds__(kSR) k_bulk(BulkArgs a, const float *__restric
     const int b = a.blocks[blockIdx.x];
     const int r0 = a.rstart[b], nr = a.rstart[b + 1] - r0;
     const int zero = a.bus[b] - 4;
-    const i64 row = static_cast<i64>(b) * kSR + threadIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const i64 sid = row >> 5;
+    const i64 sid = block_slice(a.bslices, b, warp);
+    const i64 row = sid * 32 + lane;
     int rl = 0, base = 0;
-    if (sid < a.n_slices) {
+    if (sid >= 0) {
         base = a.base[sid];
         rl = a.rlen[row];
     }
@@ -844,7 +904,7 @@ __global__ void __launch_bounds__(kSR) k_bulk(BulkArgs a, const float *__restric
         hn[k] = pk(-h, -h);
         lp[k] = pk(l, l);
     }
-    const bool store = row < a.n_rows;
+    const bool store = sid >= 0 && row < a.n_rows;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -929,6 +989,7 @@ __global__ void __launch_bounds__(kSR) k_bulk(BulkArgs a, const float *__restric
 // cp.async.cg (one instruction per chunk and field), double-buffered with
 // cp.async groups.
 struct ChunkArgs {
+    const int4 *bslices;
     const int *blocks;
     i64 n_blocks;
     const int *base, *rlen;
@@ -947,38 +1008,38 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 template <int L, int T>
 __global__ void __launch_bounds__(kSR) k_chunk(ChunkArgs a, const float *__restrict__ x, i64 ldx,
                                               float *__restrict__ y, i64 ldy, i64 nrhs) {
+    static_assert(T % 2 == 0, "fields per stage must be even");
     extern __shared__ __align__(128) float smem[];
     const int US = a.us_max;
     float *xs = smem;  // [2][T][US]
     const int b = a.blocks[blockIdx.x];
     const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
     const int zero = 4 * nch;
-    const i64 row = static_cast<i64>(b) * kSR + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    const i64 sid = row >> 5;
+    const i64 sid = block_slice(a.bslices, b, threadIdx.x >> 5);
+    const i64 row = sid * 32 + lane;
     int rl = 0, base = 0;
-    if (sid < a.n_slices) {
+    if (sid >= 0) {
         base = a.base[sid];
         rl = a.rlen[row];
     }
     int li[L];
-    F2 hp[L], hn[L], lp[L];
+    float h[L], lw[L];
 #pragma unroll
     for (int k = 0; k < L; ++k) {
-        float h = 0.f, l = 0.f;
+        float hv = 0.f, lv = 0.f;
         int q = zero;
         if (k < rl) {
             int e = base + k * 32 + lane;
             q = a.lidx[e];
-            h = a.hi[e];
-            l = a.lo[e];
+            hv = a.hi[e];
+            lv = a.lo[e];
         }
         li[k] = q;
-        hp[k] = pk(h, h);
-        hn[k] = pk(-h, -h);
-        lp[k] = pk(l, l);
+        h[k] = hv;
+        lw[k] = lv;
     }
-    const bool store = row < a.n_rows;
+    const bool store = sid >= 0 && row < a.n_rows;
     for (int q = threadIdx.x; q < 2 * T; q += kSR)
         *reinterpret_cast<float4 *>(xs + q * US + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
     const i64 ntile = (nrhs + T - 1) / T;
@@ -994,6 +1055,7 @@ __global__ void __launch_bounds__(kSR) k_chunk(ChunkArgs a, const float *__restr
         }
         cp_async_commit();
     };
+    const F2 mone = pk(-1.f, -1.f);
     stage(0, xs);
     for (i64 t = 0; t < ntile; ++t) {
         const float *cur = xs + (t & 1) * T * US;
@@ -1005,29 +1067,37 @@ __global__ void __launch_bounds__(kSR) k_chunk(ChunkArgs a, const float *__restr
         }
         __syncthreads();
         const i64 f0 = t * T;
+        if (f0 + T <= nrhs) {
+            F2 sa[T / 2], cn[T / 2];
 #pragma unroll
-        for (int f = 0; f < T; f += 2) {
-            if (f0 + f + 1 < nrhs) {
-                F2 sa = pk(0.f, 0.f), ca = pk(0.f, 0.f);
-                const float *p0 = cur + f * US, *p1 = cur + (f + 1) * US;
+            for (int q = 0; q < T / 2; ++q) {
+                sa[q] = pk(0.f, 0.f);
+                cn[q] = pk(0.f, 0.f);
+            }
 #pragma unroll
-                for (int k = 0; k < L; ++k) csum2(sa, ca, hp[k], hn[k], lp[k], pk(p0[li[k]], p1[li[k]]));
-                if (store) {
+            for (int k = 0; k < L; ++k) {
+                const F2 h2 = pk(h[k], h[k]), l2 = pk(lw[k], lw[k]);
+                const float *pk0 = cur + li[k];
+#pragma unroll
+                for (int q = 0; q < T / 2; ++q)
+                    cstep2(sa[q], cn[q], h2, l2, pk(pk0[(2 * q) * US], pk0[(2 * q + 1) * US]), mone);
+            }
+            if (store) {
+#pragma unroll
+                for (int q = 0; q < T / 2; ++q) {
                     float ra, rb;
-                    upk(add2(sa, ca), ra, rb);
-                    y[(f0 + f) * ldy + row] = ra;
-                    y[(f0 + f + 1) * ldy + row] = rb;
+                    upk(sub2(sa[q], cn[q]), ra, rb);
+                    y[(f0 + 2 * q) * ldy + row] = ra;
+                    y[(f0 + 2 * q + 1) * ldy + row] = rb;
                 }
-            } else if (f0 + f < nrhs) {
+            }
+        } else {
+            for (int f = 0; f < T; ++f) {
+                if (f0 + f >= nrhs) break;
                 float s1 = 0.f, c1 = 0.f;
                 const float *p0 = cur + f * US;
 #pragma unroll
-                for (int k = 0; k < L; ++k) {
-                    float hh, dummy, ll;
-                    upk(hp[k], hh, dummy);
-                    upk(lp[k], ll, dummy);
-                    csum1(s1, c1, hh, ll, p0[li[k]]);
-                }
+                for (int k = 0; k < L; ++k) csum1(s1, c1, h[k], lw[k], p0[li[k]]);
                 if (store) y[(f0 + f) * ldy + row] = __fadd_rn(s1, c1);
             }
         }
@@ -1042,6 +1112,7 @@ void launch_chunk(Matrix &m, int cls, const float *x, i64 ldx, float *y, i64 ldy
     i64 nb = B.class_begin[cls + 1] - B.class_begin[cls];
     if (nb == 0) return;
     ChunkArgs a;
+    a.bslices = m.staged.bslices.p;
     a.blocks = B.block_ids.p + B.class_begin[cls];
     a.n_blocks = nb;
     a.base = S.base.p;
@@ -1073,12 +1144,12 @@ void apply_chunk_T(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nr
 
 __global__ void k_bulk_lidx(const int *rp, i64 n_rows, i64 n_slices, const int *base, const int *rlen,
                             const unsigned short *lidx_sell, const int *ustart, const int *remap, const int *bus,
-                            const unsigned char *staged_ok, unsigned short *out) {
+                            const unsigned char *staged_ok, const int *blk_of_slice, unsigned short *out) {
     i64 r = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (r >= n_slices * 32) return;
     i64 s = r >> 5;
     int lane = static_cast<int>(r & 31);
-    i64 b = r / kSR;
+    i64 b = blk_of_slice[s];
     int L = (base[s + 1] - base[s]) / 32;
     int n = rlen[r];
     bool ok = staged_ok[b] != 0;
@@ -1141,8 +1212,9 @@ void build_bulk(Matrix &m, cudaStream_t s) {
     std::vector<int4> allruns;
     for (i64 b = 0; b < nb; ++b) {
         int L = 0;
-        for (i64 q = b * (kSR / 32); q < std::min<i64>((b + 1) * (kSR / 32), S.n_slices); ++q)
-            L = std::max(L, S.h_slice_len[q]);
+        const int *bsl = &G.h_bslices[b].x;
+        for (int w = 0; w < 4; ++w)
+            if (bsl[w] >= 0) L = std::max(L, S.h_slice_len[bsl[w]]);
         int c = L <= 4 ? 0 : (L + 3) / 4 - 1;
         rstart[b] = static_cast<int>(allruns.size());
         allruns.insert(allruns.end(), runs[b].begin(), runs[b].end());
@@ -1161,9 +1233,11 @@ void build_bulk(Matrix &m, cudaStream_t s) {
     }
     B.class_begin[nclass] = static_cast<i64>(ids.size());
     for (i64 b = 0; b < nb; ++b)
-        if (!ok[b])
-            for (i64 q = b * (kSR / 32); q < std::min<i64>((b + 1) * (kSR / 32), S.n_slices); ++q)
-                fb.push_back(static_cast<int>(q));
+        if (!ok[b]) {
+            const int *bsl = &G.h_bslices[b].x;
+            for (int w = 0; w < 4; ++w)
+                if (bsl[w] >= 0) fb.push_back(bsl[w]);
+        }
     B.block_ids.upload(ids.data(), ids.size(), s);
     B.fallback_slices.upload(fb.data(), fb.size(), s);
     B.n_fallback = static_cast<i64>(fb.size());
@@ -1188,7 +1262,7 @@ void build_bulk(Matrix &m, cudaStream_t s) {
     if (S.n_slices > 0) {
         k_bulk_lidx<<<nblk(S.n_slices * 32, 256), 256, 0, s>>>(m.row_ptr.p, m.n_dst, S.n_slices, S.base.p, S.len.p,
                                                               G.lidx.p, G.ustart.p, d_remap.p, B.bus.p, d_ok.p,
-                                                              B.lidx.p);
+                                                              G.blk_of_slice.p, B.lidx.p);
         AXGB_CUDA(cudaGetLastError());
     }
     if (!B.status.p) {
@@ -1206,6 +1280,7 @@ void launch_bulk(Matrix &m, int cls, const float *x, i64 ldx, float *y, i64 ldy,
     i64 nb = B.class_begin[cls + 1] - B.class_begin[cls];
     if (nb == 0) return;
     BulkArgs a;
+    a.bslices = m.staged.bslices.p;
     a.blocks = B.block_ids.p + B.class_begin[cls];
     a.n_blocks = nb;
     a.base = S.base.p;

@@ -150,12 +150,16 @@ struct Sell {
     std::vector<int> h_slice_len;  // entries per row slot of each slice
 };
 
-// Staged split-FP32 layout: rows in blocks of 128; per block the sorted
+// Staged split-FP32 layout: rows in blocks of 4 slices (128 rows); per block the sorted
 // unique source columns (ucol[ustart[b] .. +ucount[b]]) and, per entry in the
 // sliced-ELL positions of Sell, the 16-bit index of its column in that list.
 struct Staged {
     bool built = false;
     i64 n_blocks = 0;
+    // block b = slices bslices[b].{x,y,z,w} (-1 = none), grouped by source locality
+    std::vector<int4> h_bslices;
+    DBuf<int4> bslices;
+    DBuf<int> blk_of_slice;
     DBuf<unsigned short> lidx;
     DBuf<int> ucol, ustart, ucount;
     // block ids by class (max slice length <= 8, <= 16, <= 32 and unique
