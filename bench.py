@@ -240,7 +240,6 @@ def main():
     torch.cuda.synchronize()
     log(f"fields {time.perf_counter() - t0:.1f}s")
     Y = torch.empty((NRHS, M.n_dst), dtype=torch.float32, device=dev)
-    M.prepare(1)
     M.prepare(2)
     tuned = axgb.autotune_f32split(M, X, Y)
     launches_per_step = axgb_launches(M, tuned["variant"])
@@ -371,7 +370,7 @@ def axgb_launches(M, variant):
 
     import axgb
     axgb._check(axgb.lib().axgb_matrix_stats(M.handle, st.ctypes.data_as(ctypes.c_void_p), None))
-    n = int(st[7] if variant == 1 else st[5])
+    n = int(st[6] if variant >= 1 else st[5])
     return n if n > 0 else 1
 
 

@@ -27,9 +27,10 @@ UNITS = [
     ("prep.cu", ["--fmad=false"]),
     ("weights.cu", ["--fmad=false"]),
     ("apply.cu", []),
+    ("staged.cu", []),
     ("scan_sort.cu", []),
 ]
-HEADERS = ["internal.hpp", "geom.cuh", os.path.join("..", "..", "include", "axgb.h")]
+HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", os.path.join("..", "..", "include", "axgb.h")]
 
 
 def _nvcc():

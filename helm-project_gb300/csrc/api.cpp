@@ -225,7 +225,7 @@ void check_apply(const Matrix &m, const void *x, i64 ldx, const void *y, i64 ldy
 
 SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
     std::vector<SplitParams> cands;
-    for (int v : {2, 1})
+    for (int v : {1, 2})
         for (int t : {2, 4, 8})
             if (t <= std::max<i64>(2, nrhs)) cands.push_back({v, 0, t});
     std::vector<i64> tiles = {nrhs};
@@ -301,7 +301,7 @@ SplitParams pick_params(Matrix &m, i64 nrhs) {
 
 SplitParams default_split_params(i64 nrhs) {
     SplitParams p;
-    p.variant = 2;
+    p.variant = 1;
     p.fields_per_pass = 0;
     p.unroll = nrhs >= 8 ? 8 : 4;
     return p;
@@ -623,7 +623,7 @@ int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int6
 
 int axgb_matrix_prepare(int h, int format) {
     AXGB_TRY({
-        AXGB_REQUIRE(format >= 0 && format <= 3, "matrix_prepare: format must be 0, 1, 2 or 3");
+        AXGB_REQUIRE(format >= 0 && format <= 2, "matrix_prepare: format must be 0, 1 or 2");
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         matrix_prepare(*m, format, 0);
     });
@@ -635,9 +635,9 @@ int axgb_matrix_device_status(int h, int32_t *status) {
         AXGB_REQUIRE(status, "matrix_device_status: NULL status");
         AXGB_CUDA(cudaDeviceSynchronize());
         int v = 0;
-        if (m->bulk.status.p) {
-            AXGB_CUDA(cudaMemcpy(&v, m->bulk.status.p, sizeof(int), cudaMemcpyDeviceToHost));
-            AXGB_CUDA(cudaMemset(m->bulk.status.p, 0, sizeof(int)));
+        if (m->blocked.status.p) {
+            AXGB_CUDA(cudaMemcpy(&v, m->blocked.status.p, sizeof(int), cudaMemcpyDeviceToHost));
+            AXGB_CUDA(cudaMemset(m->blocked.status.p, 0, sizeof(int)));
         }
         *status = v;
     });
@@ -663,15 +663,12 @@ int axgb_apply_f32split_tuned(int h, const float *x, int64_t ldx, float *y, int6
     AXGB_TRY({
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         check_apply(*m, x, ldx, y, ldy, nrhs);
-        AXGB_REQUIRE(variant >= 0 && variant <= 3, "apply: variant must be 0 (direct) or 1..3 (staged)");
+        AXGB_REQUIRE(variant >= 0 && variant <= 2, "apply: variant must be 0 (direct), 1 or 2 (blocked)");
         if (variant == 0) {
             AXGB_REQUIRE(unroll == 1 || unroll == 2 || unroll == 4, "apply: direct unroll must be 1, 2 or 4");
         } else {
             AXGB_REQUIRE(unroll == 2 || unroll == 4 || unroll == 8, "apply: staged fields per stage must be 2, 4 or 8");
         }
-        // the bulk path needs 16-byte aligned field rows; otherwise run the cp.async staging
-        if (variant >= 2 && !(reinterpret_cast<std::uintptr_t>(x) % 16 == 0 && ldx % 4 == 0 && m->n_src % 4 == 0))
-            variant = 1;
         SplitParams p{variant, fields_per_pass, unroll};
         if (nrhs > 0) apply_split(*m, x, ldx, y, ldy, nrhs, p, static_cast<cudaStream_t>(stream));
     });

@@ -150,44 +150,33 @@ struct Sell {
     std::vector<int> h_slice_len;  // entries per row slot of each slice
 };
 
-// Staged split-FP32 layout: rows in blocks of 4 slices (128 rows); per block the sorted
-// unique source columns (ucol[ustart[b] .. +ucount[b]]) and, per entry in the
-// sliced-ELL positions of Sell, the 16-bit index of its column in that list.
-struct Staged {
+// Blocked split-FP32 layout (staged.cu). Rows are grouped in blocks of up to
+// 4 slices (128 rows) chosen for source locality; inside a block rows are
+// sorted by length so each warp's trip count follows its own rows. Per block:
+// the 16-byte chunks of source columns to stage (ccol), runs of consecutive
+// chunks for bulk copies, and per entry the staging index (lidx; padding
+// entries point at a zero slot), hi and lo weights, laid out k-major per warp.
+struct Blocked {
+    struct Launch {
+        int L;        // row-length class (multiple of 4, <= 32)
+        int us;       // staging floats per field (allocation for the class)
+        i64 begin, n; // range in block_ids
+    };
     bool built = false;
     i64 n_blocks = 0;
-    // block b = slices bslices[b].{x,y,z,w} (-1 = none), grouped by source locality
-    std::vector<int4> h_bslices;
-    DBuf<int4> bslices;
-    DBuf<int> blk_of_slice;
+    DBuf<int> brow, wbase, wlen, cstart, ccol, rstart, block_ids, fallback_slices;
+    DBuf<int4> runs;  // (global col of first chunk, chunks, staging offset, 0)
     DBuf<unsigned short> lidx;
-    DBuf<int> ucol, ustart, ucount;
-    // block ids by class (max slice length <= 8, <= 16, <= 32 and unique
-    // columns <= kStagedMaxU = 2048); slices of all other blocks use the direct kernel
-    std::vector<i64> class_begin;  // 4 entries into block_ids
-    std::vector<int> class_umax;
-    DBuf<int> block_ids, fallback_slices;
-    i64 n_fallback = 0;
-};
-
-// Bulk-staged layout on top of Staged: per block the unique columns as runs
-// of 16-byte chunks copied with cp.async.bulk, and per sliced-ELL entry the
-// index into the block's staging area (padding -> the zero slot).
-struct Bulk {
-    bool built = false;
-    DBuf<unsigned short> lidx;
-    DBuf<int> rstart, bus, block_ids, fallback_slices, cstart, ccol;
-    DBuf<int4> runs;
-    std::vector<i64> class_begin;  // 9 entries: row-length classes 4, 8, ..., 32
-    std::vector<int> class_usmax;
+    DBuf<float> hi, lo;
+    std::vector<Launch> launches;
     i64 n_fallback = 0;
     DBuf<int> status;  // device status word: 1 = a bounded wait timed out
 };
 
 // Kernel choice for the split-FP32 apply.
 struct SplitParams {
-    int variant = 2;          // 0 direct, 1 cp.async 4-byte staged, 2 cp.async 16-byte chunk staged,
-                              // 3 bulk-copy (TMA) staged
+    int variant = 1;          // 0 direct gathers, 1 blocked + cp.async chunk staging,
+                              // 2 blocked + bulk-copy (TMA) staging
     int fields_per_pass = 0;  // direct: RHS tile width (0 = all)
     int unroll = 4;           // direct: fields per thread iteration; staged: fields per stage
 };
@@ -199,8 +188,8 @@ struct Matrix {
     i64 stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     double times_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     Sell sell64, sell32;
-    Staged staged;
-    Bulk bulk;
+    Blocked blocked;
+    std::vector<float> slice_xyz;  // mean unit vector of each 32-row slice (locality hint), may be empty
     std::map<i64, SplitParams> tuned;  // nrhs -> best kernel choice
     std::mutex mu;
 };
@@ -222,6 +211,14 @@ void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs
 void conservation(Matrix &m, const void *src, const void *dst, bool f32, int norm_type, double *out, cudaStream_t s);
 std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &mats, const std::vector<i64> &nrhs);
 void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *y, const i64 *ldy, cudaStream_t s);
+
+// staged.cu
+void build_blocked(Matrix &m, cudaStream_t s);
+bool blocked_eligible(const Matrix &m, const void *x, i64 ldx);
+void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T,
+                   cudaStream_t s);
+int blocked_launches(const Matrix &m);
+void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s);
 
 // scan_sort.cu: device primitives (own implementations)
 // out[0..n] = exclusive prefix sum of in[0..n-1], out[n] = total.

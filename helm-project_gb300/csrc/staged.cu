@@ -1,0 +1,621 @@
+// Blocked, shared-memory staged split-FP32 SpMM (the fast apply path).
+//
+// Layout (built once per matrix on the host from the CSR):
+//   * rows are taken in 32-row slices (consecutive rows, so output stores of
+//     a warp stay coalesced) and slices are grouped 4 at a time into blocks
+//     of source locality: with a centroid hint (matrices from
+//     generate_weights), slices are visited in 3-D Morton order and each
+//     block takes the 3 nearest unused slices among the next ones in that
+//     order; without a hint, 4 consecutive slices;
+//   * inside a block the rows are sorted by entry count (longest first), so
+//     warp w holds rows of similar length and loops only to its own maximum;
+//   * the block's distinct source columns are rounded out to 16-byte chunks;
+//     chunk j is staged at float offset 4*j of a field's staging area, and a
+//     zero slot follows the chunks (padding entries read it);
+//   * entries are stored k-major per warp: (staging index, hi, lo).
+// Kernel: one CTA (4 warps) per block. Tiles of T fields are staged into
+// shared memory double-buffered, either with cp.async.cg 16-byte copies by
+// all threads (chunk variant) or with one cp.async.bulk per run of
+// consecutive chunks and field, completing on an mbarrier (bulk variant).
+// Each thread then reduces its row for the T fields with packed f32x2
+// compensated arithmetic (fp32x2.cuh).
+#include <algorithm>
+#include <array>
+#include <cstdint>
+#include <thread>
+
+#include "fp32x2.cuh"
+#include "internal.hpp"
+
+namespace axgb {
+namespace {
+
+constexpr int kRows = 128;       // rows per block (4 warps)
+constexpr int kMaxUS = 3072;     // staging floats per field a block may use
+constexpr int kMaxL = 32;        // longest row handled by the blocked kernels
+const int kUsBuckets[] = {256, 512, 768, 1024, 1280, 1536, 2048, 3072};
+
+inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
+
+template <class F>
+void parallel_for_host(i64 n, F f) {
+    unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    if (n < 256 || nt == 1) {
+        f(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    i64 chunk = (n + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; ++t) {
+        i64 b = t * chunk, e = std::min(n, b + chunk);
+        if (b >= e) break;
+        th.emplace_back([=] { f(b, e); });
+    }
+    for (auto &t : th) t.join();
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void mbar_init(std::uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(std::uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(std::uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, std::uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+struct BlkArgs {
+    const int *blocks;  // block ids of this launch
+    const int *brow, *wbase, *wlen;
+    const unsigned short *lidx;
+    const float *hi, *lo;
+    const int *cstart, *ccol;  // chunk list per block
+    const int *rstart;         // runs per block (bulk variant)
+    const int4 *runs;
+    int us;                    // staging stride of a field (floats)
+    int *status;
+};
+
+// Row reduction of one staged tile of T fields. s/cn accumulators per pair.
+template <int L, int T>
+__device__ __forceinline__ void reduce_tile(const float *cur, int us, const int *li, const float *h, const float *lw,
+                                            int wl, i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy) {
+    if (f0 + T <= nrhs) {
+        F2 sa[T / 2], cn[T / 2];
+#pragma unroll
+        for (int q = 0; q < T / 2; ++q) {
+            sa[q] = pk(0.f, 0.f);
+            cn[q] = pk(0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < L; ++k) {
+            if (k < wl) {  // warp-uniform
+                const F2 h2 = pk(h[k], h[k]), l2 = pk(lw[k], lw[k]);
+                const float *p0 = cur + li[k];
+#pragma unroll
+                for (int q = 0; q < T / 2; ++q) cstep2i(sa[q], cn[q], h2, l2, pk(p0[(2 * q) * us], p0[(2 * q + 1) * us]));
+            }
+        }
+        if (row >= 0) {
+#pragma unroll
+            for (int q = 0; q < T / 2; ++q) {
+                float ra, rb;
+                upk(sub2(sa[q], cn[q]), ra, rb);
+                y[(f0 + 2 * q) * ldy + row] = ra;
+                y[(f0 + 2 * q + 1) * ldy + row] = rb;
+            }
+        }
+    } else {
+        for (int f = 0; f < T; ++f) {
+            if (f0 + f >= nrhs) break;
+            float s1 = 0.f, c1 = 0.f;
+            const float *p0 = cur + f * us;
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (k < wl) csum1(s1, c1, h[k], lw[k], p0[li[k]]);
+            if (row >= 0) y[(f0 + f) * ldy + row] = __fadd_rn(s1, c1);
+        }
+    }
+}
+
+template <int L>
+__device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, int *li, float *h, float *lw, int &wl,
+                                             i64 &row) {
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    row = a.brow[static_cast<i64>(b) * kRows + tid];
+    wl = a.wlen[b * 4 + w];
+    const int base = a.wbase[b * 4 + w];
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        if (k < wl) {
+            int e = base + k * 32 + lane;
+            li[k] = a.lidx[e];
+            h[k] = a.hi[e];
+            lw[k] = a.lo[e];
+        } else {
+            li[k] = zero;
+            h[k] = 0.f;
+            lw[k] = 0.f;
+        }
+    }
+}
+
+template <int L, int T>
+__global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__restrict__ x, i64 ldx,
+                                                    float *__restrict__ y, i64 ldy, i64 nrhs) {
+    static_assert(T % 2 == 0, "fields per stage must be even");
+    extern __shared__ __align__(128) float smem[];
+    const int us = a.us;
+    float *xs = smem;                                   // [2][T][us]
+    int *cc = reinterpret_cast<int *>(smem + 2 * T * us);  // chunk columns
+    const int b = a.blocks[blockIdx.x];
+    const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
+    const int zero = 4 * nch;
+    for (int j = threadIdx.x; j < nch; j += kRows) cc[j] = a.ccol[c0 + j];
+    int li[L];
+    float h[L], lw[L];
+    int wl;
+    i64 row;
+    load_entries<L>(a, b, zero, li, h, lw, wl, row);
+    for (int q = threadIdx.x; q < 2 * T; q += kRows)
+        *reinterpret_cast<float4 *>(xs + q * us + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const i64 ntile = (nrhs + T - 1) / T;
+    auto stage = [&](i64 t, float *dst) {
+        const i64 fa = t * T;
+        const int nf = static_cast<int>((nrhs - fa < static_cast<i64>(T)) ? nrhs - fa : static_cast<i64>(T));
+        const float *xt = x + fa * ldx;
+        for (int j = threadIdx.x; j < nch; j += kRows) {
+            const float *src = xt + cc[j];
+#pragma unroll
+            for (int f = 0; f < T; ++f)
+                if (f < nf) cp_async16(dst + f * us + 4 * j, src + f * ldx);
+        }
+        cp_async_commit();
+    };
+    stage(0, xs);
+    for (i64 t = 0; t < ntile; ++t) {
+        const float *cur = xs + (t & 1) * T * us;
+        if (t + 1 < ntile) {
+            stage(t + 1, xs + ((t + 1) & 1) * T * us);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        reduce_tile<L, T>(cur, us, li, h, lw, wl, t * T, nrhs, row, y, ldy);
+        __syncthreads();
+    }
+}
+
+template <int L, int T>
+__global__ void __launch_bounds__(kRows) k_blk_bulk(BlkArgs a, const float *__restrict__ x, i64 ldx,
+                                                   float *__restrict__ y, i64 ldy, i64 nrhs) {
+    static_assert(T % 2 == 0, "fields per stage must be even");
+    extern __shared__ __align__(128) float smem[];
+    __shared__ __align__(8) std::uint64_t bar[2];
+    __shared__ int abort_flag;
+    const int us = a.us;
+    float *xs = smem;  // [2][T][us]
+    const int b = a.blocks[blockIdx.x];
+    const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
+    const int zero = 4 * nch;
+    const int r0 = a.rstart[b], nr = a.rstart[b + 1] - r0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int li[L];
+    float h[L], lw[L];
+    int wl;
+    i64 row;
+    load_entries<L>(a, b, zero, li, h, lw, wl, row);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int q = threadIdx.x; q < 2 * T; q += kRows)
+        *reinterpret_cast<float4 *>(xs + q * us + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const i64 ntile = (nrhs + T - 1) / T;
+    auto issue = [&](i64 t, int buf) {
+        if (warp != 0) return;
+        const i64 fa = t * T;
+        const int nf = static_cast<int>((nrhs - fa < static_cast<i64>(T)) ? nrhs - fa : static_cast<i64>(T));
+        if (lane == 0) mbar_expect_tx(&bar[buf], 16u * static_cast<unsigned>(nch) * static_cast<unsigned>(nf));
+        __syncwarp();
+        float *dst0 = xs + buf * T * us;
+        for (int q = lane; q < nr; q += 32) {
+            int4 r = a.runs[r0 + q];
+            for (int f = 0; f < nf; ++f)
+                bulk_g2s(dst0 + f * us + r.z, x + (fa + f) * ldx + r.x, 16u * static_cast<unsigned>(r.y), &bar[buf]);
+        }
+    };
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    issue(0, 0);
+    for (i64 t = 0; t < ntile; ++t) {
+        const int buf = static_cast<int>(t & 1);
+        if (t + 1 < ntile) issue(t + 1, buf ^ 1);
+        const unsigned parity = static_cast<unsigned>((t >> 1) & 1);
+        const unsigned long long t0 = globaltimer_ns();
+        while (!mbar_try_wait(&bar[buf], parity)) {
+            if (globaltimer_ns() - t0 > 1000000000ull) {  // 1 s bound
+                abort_flag = 1;
+                atomicExch(a.status, 1);
+                break;
+            }
+        }
+        __syncthreads();
+        if (abort_flag) break;
+        reduce_tile<L, T>(xs + buf * T * us, us, li, h, lw, wl, t * T, nrhs, row, y, ldy);
+        __syncthreads();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+}
+
+__global__ void k_slice_centroid(const DCap *cap, i64 n_rows, i64 n_slices, float *out) {
+    i64 s = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= n_slices) return;
+    double sx = 0, sy = 0, sz = 0;
+    int n = 0;
+    const i64 r1 = (n_rows < s * 32 + 32) ? n_rows : s * 32 + 32;
+    for (i64 r = s * 32; r < r1; ++r) {
+        sx += cap[r].x;
+        sy += cap[r].y;
+        sz += cap[r].z;
+        ++n;
+    }
+    double inv = n ? 1.0 / n : 0.0;
+    out[3 * s] = static_cast<float>(sx * inv);
+    out[3 * s + 1] = static_cast<float>(sy * inv);
+    out[3 * s + 2] = static_cast<float>(sz * inv);
+}
+
+inline unsigned spread10h(unsigned v) {
+    v &= 1023u;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// Groups of up to 4 slices: Morton visit order, each group completed with
+// the nearest unused slices among the next kWindow candidates.
+std::vector<std::array<int, 4>> group_slices(i64 nsl, const std::vector<float> &xyz) {
+    std::vector<std::array<int, 4>> groups;
+    if (xyz.size() != static_cast<size_t>(3 * nsl)) {
+        for (i64 q = 0; q < nsl; q += 4) {
+            std::array<int, 4> g{-1, -1, -1, -1};
+            for (int w = 0; w < 4 && q + w < nsl; ++w) g[w] = static_cast<int>(q + w);
+            groups.push_back(g);
+        }
+        return groups;
+    }
+    std::vector<std::pair<unsigned, int>> code(nsl);
+    for (i64 q = 0; q < nsl; ++q) {
+        auto qz = [](float v) { return static_cast<unsigned>(std::min(1023.f, std::max(0.f, (v + 1.f) * 512.f))); };
+        code[q] = {(spread10h(qz(xyz[3 * q])) << 2) | (spread10h(qz(xyz[3 * q + 1])) << 1) | spread10h(qz(xyz[3 * q + 2])),
+                   static_cast<int>(q)};
+    }
+    std::stable_sort(code.begin(), code.end());
+    std::vector<int> order(nsl);
+    for (i64 q = 0; q < nsl; ++q) order[q] = code[q].second;
+    std::vector<char> used(nsl, 0);
+    constexpr int kWindow = 48;
+    i64 head = 0;
+    for (i64 q = 0; q < nsl; ++q) {
+        int s = order[q];
+        if (used[s]) continue;
+        used[s] = 1;
+        std::array<int, 4> g{s, -1, -1, -1};
+        // nearest 3 among the next kWindow unused slices in Morton order
+        std::vector<std::pair<float, int>> cand;
+        for (i64 r = q + 1; r < nsl && static_cast<int>(cand.size()) < kWindow; ++r) {
+            int c = order[r];
+            if (used[c]) continue;
+            float dx = xyz[3 * c] - xyz[3 * s], dy = xyz[3 * c + 1] - xyz[3 * s + 1], dz = xyz[3 * c + 2] - xyz[3 * s + 2];
+            cand.push_back({dx * dx + dy * dy + dz * dz, c});
+        }
+        std::partial_sort(cand.begin(), cand.begin() + std::min<size_t>(3, cand.size()), cand.end());
+        for (int w = 0; w < 3 && w < static_cast<int>(cand.size()); ++w) {
+            g[w + 1] = cand[w].second;
+            used[cand[w].second] = 1;
+        }
+        groups.push_back(g);
+        (void)head;
+    }
+    return groups;
+}
+
+struct HostBlock {
+    int rows[kRows];
+    int wlen[4];
+    int L;                     // row-length class (multiple of 4)
+    int us;                    // 4 * chunks + 4
+    std::vector<int> ccol;     // chunk start columns
+    std::vector<int4> runs;    // (col, chunks, staging offset, 0)
+    std::vector<unsigned short> lidx;  // k-major per warp, concatenated warps
+    std::vector<float> hi, lo;
+    int wbase_rel[4];
+};
+
+}  // namespace
+
+void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s) {
+    const i64 nsl = (m.n_dst + 31) / 32;
+    if (nsl == 0 || !dst.cap) return;
+    DBuf<float> d(3 * nsl);
+    k_slice_centroid<<<nblk(nsl, 256), 256, 0, s>>>(dst.cap, m.n_dst, nsl, d.p);
+    AXGB_CUDA(cudaGetLastError());
+    m.slice_xyz.resize(3 * nsl);
+    AXGB_CUDA(cudaMemcpyAsync(m.slice_xyz.data(), d.p, sizeof(float) * 3 * nsl, cudaMemcpyDeviceToHost, s));
+    AXGB_CUDA(cudaStreamSynchronize(s));
+}
+
+void build_blocked(Matrix &m, cudaStream_t s) {
+    Blocked &B = m.blocked;
+    if (B.built) return;
+    const i64 n = m.n_dst, nnz = m.nnz;
+    const i64 nsl = (n + 31) / 32;
+    std::vector<int> rp(n + 1), col(std::max<i64>(1, nnz));
+    std::vector<double> val(std::max<i64>(1, nnz));
+    AXGB_CUDA(cudaMemcpy(rp.data(), m.row_ptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    if (nnz) {
+        AXGB_CUDA(cudaMemcpy(col.data(), m.col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+        AXGB_CUDA(cudaMemcpy(val.data(), m.val.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost));
+    }
+    auto groups = group_slices(nsl, m.slice_xyz);
+    const i64 nb = static_cast<i64>(groups.size());
+    std::vector<HostBlock> hb(nb);
+    parallel_for_host(nb, [&](i64 b0, i64 b1) {
+        std::vector<std::pair<int, int>> rl;
+        std::vector<int> cols;
+        for (i64 b = b0; b < b1; ++b) {
+            HostBlock &H = hb[b];
+            rl.clear();
+            for (int g : groups[b])
+                if (g >= 0)
+                    for (i64 r = static_cast<i64>(g) * 32; r < std::min<i64>(n, static_cast<i64>(g) * 32 + 32); ++r)
+                        rl.push_back({-(rp[r + 1] - rp[r]), static_cast<int>(r)});
+            std::stable_sort(rl.begin(), rl.end());
+            for (int t = 0; t < kRows; ++t) H.rows[t] = t < static_cast<int>(rl.size()) ? rl[t].second : -1;
+            cols.clear();
+            for (auto &pr : rl)
+                for (int k = rp[pr.second]; k < rp[pr.second + 1]; ++k) cols.push_back(col[k] >> 2);
+            std::sort(cols.begin(), cols.end());
+            cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+            H.ccol.resize(cols.size());
+            for (size_t j = 0; j < cols.size(); ++j) H.ccol[j] = cols[j] * 4;
+            H.us = 4 * static_cast<int>(cols.size()) + 4;
+            const int zero = 4 * static_cast<int>(cols.size());
+            H.runs.clear();
+            for (size_t j = 0; j < cols.size();) {
+                size_t j1 = j + 1;
+                while (j1 < cols.size() && cols[j1] == cols[j1 - 1] + 1) ++j1;
+                H.runs.push_back(make_int4(cols[j] * 4, static_cast<int>(j1 - j), static_cast<int>(4 * j), 0));
+                j = j1;
+            }
+            int maxlen = 0;
+            for (int w = 0; w < 4; ++w) {
+                int mx = 0;
+                for (int t = 32 * w; t < 32 * w + 32; ++t)
+                    if (H.rows[t] >= 0) mx = std::max(mx, rp[H.rows[t] + 1] - rp[H.rows[t]]);
+                H.wlen[w] = mx;
+                maxlen = std::max(maxlen, mx);
+            }
+            H.L = std::max(4, (maxlen + 3) / 4 * 4);
+            H.lidx.clear();
+            H.hi.clear();
+            H.lo.clear();
+            int off = 0;
+            for (int w = 0; w < 4; ++w) {
+                H.wbase_rel[w] = off;
+                for (int k = 0; k < H.wlen[w]; ++k)
+                    for (int lane = 0; lane < 32; ++lane) {
+                        int r = H.rows[32 * w + lane];
+                        int q = zero;
+                        float hv = 0.f, lv = 0.f;
+                        if (r >= 0 && k < rp[r + 1] - rp[r]) {
+                            int e = rp[r] + k;
+                            int c = col[e];
+                            size_t pos = std::lower_bound(cols.begin(), cols.end(), c >> 2) - cols.begin();
+                            q = static_cast<int>(4 * pos) + (c & 3);
+                            hv = static_cast<float>(val[e]);
+                            lv = static_cast<float>(val[e] - static_cast<double>(hv));
+                        }
+                        H.lidx.push_back(static_cast<unsigned short>(q));
+                        H.hi.push_back(hv);
+                        H.lo.push_back(lv);
+                    }
+                off += 32 * H.wlen[w];
+            }
+        }
+    });
+    // classes and flattening
+    std::vector<int> brow(nb * kRows), wbase(nb * 4), wlen(nb * 4), cstart(nb + 1, 0), rstart(nb + 1, 0);
+    std::vector<int> ccol;
+    std::vector<int4> runs;
+    std::vector<unsigned short> lidx;
+    std::vector<float> hi, lo;
+    std::map<std::pair<int, int>, std::vector<int>> cls;
+    std::vector<int> fb;
+    for (i64 b = 0; b < nb; ++b) {
+        HostBlock &H = hb[b];
+        const int ebase = static_cast<int>(lidx.size());
+        for (int t = 0; t < kRows; ++t) brow[b * kRows + t] = H.rows[t];
+        for (int w = 0; w < 4; ++w) {
+            wbase[b * 4 + w] = ebase + H.wbase_rel[w];
+            wlen[b * 4 + w] = H.wlen[w];
+        }
+        cstart[b] = static_cast<int>(ccol.size());
+        ccol.insert(ccol.end(), H.ccol.begin(), H.ccol.end());
+        rstart[b] = static_cast<int>(runs.size());
+        runs.insert(runs.end(), H.runs.begin(), H.runs.end());
+        lidx.insert(lidx.end(), H.lidx.begin(), H.lidx.end());
+        hi.insert(hi.end(), H.hi.begin(), H.hi.end());
+        lo.insert(lo.end(), H.lo.begin(), H.lo.end());
+        int maxlen = std::max({H.wlen[0], H.wlen[1], H.wlen[2], H.wlen[3]});
+        if (maxlen <= kMaxL && H.us <= kMaxUS) {
+            int ub = 0;
+            while (kUsBuckets[ub] < H.us) ++ub;
+            cls[{H.L, kUsBuckets[ub]}].push_back(static_cast<int>(b));
+        } else {
+            for (int g : groups[b])
+                if (g >= 0) fb.push_back(g);
+        }
+        std::vector<int>().swap(H.ccol);
+        std::vector<unsigned short>().swap(H.lidx);
+        std::vector<float>().swap(H.hi);
+        std::vector<float>().swap(H.lo);
+    }
+    cstart[nb] = static_cast<int>(ccol.size());
+    rstart[nb] = static_cast<int>(runs.size());
+    AXGB_REQUIRE(lidx.size() < (size_t(1) << 31), "blocked layout: too many entries");
+    std::vector<int> ids;
+    B.launches.clear();
+    for (auto &kv : cls) {
+        Blocked::Launch l;
+        l.L = kv.first.first;
+        l.us = kv.first.second;
+        l.begin = static_cast<i64>(ids.size());
+        l.n = static_cast<i64>(kv.second.size());
+        ids.insert(ids.end(), kv.second.begin(), kv.second.end());
+        B.launches.push_back(l);
+    }
+    B.n_blocks = nb;
+    B.brow.upload(brow.data(), std::max<size_t>(1, brow.size()), s);
+    B.wbase.upload(wbase.data(), std::max<size_t>(1, wbase.size()), s);
+    B.wlen.upload(wlen.data(), std::max<size_t>(1, wlen.size()), s);
+    B.cstart.upload(cstart.data(), cstart.size(), s);
+    B.ccol.upload(ccol.data(), std::max<size_t>(1, ccol.size()), s);
+    B.rstart.upload(rstart.data(), rstart.size(), s);
+    B.runs.upload(runs.data(), std::max<size_t>(1, runs.size()), s);
+    B.lidx.upload(lidx.data(), std::max<size_t>(1, lidx.size()), s);
+    B.hi.upload(hi.data(), std::max<size_t>(1, hi.size()), s);
+    B.lo.upload(lo.data(), std::max<size_t>(1, lo.size()), s);
+    B.block_ids.upload(ids.data(), std::max<size_t>(1, ids.size()), s);
+    B.fallback_slices.upload(fb.data(), std::max<size_t>(1, fb.size()), s);
+    B.n_fallback = static_cast<i64>(fb.size());
+    if (!B.status.p) {
+        B.status.alloc(1);
+        B.status.zero(s);
+    }
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    B.built = true;
+}
+
+bool blocked_eligible(const Matrix &m, const void *x, i64 ldx) {
+    return (reinterpret_cast<std::uintptr_t>(x) % 16 == 0) && (ldx % 4 == 0) && (m.n_src % 4 == 0);
+}
+
+int blocked_launches(const Matrix &m) {
+    return static_cast<int>(m.blocked.launches.size()) + (m.blocked.n_fallback > 0 ? 1 : 0);
+}
+
+namespace {
+
+template <int L, int T>
+void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, const float *x, i64 ldx, float *y, i64 ldy,
+                i64 nrhs, cudaStream_t s) {
+    BlkArgs a;
+    a.blocks = B.block_ids.p + l.begin;
+    a.brow = B.brow.p;
+    a.wbase = B.wbase.p;
+    a.wlen = B.wlen.p;
+    a.lidx = B.lidx.p;
+    a.hi = B.hi.p;
+    a.lo = B.lo.p;
+    a.cstart = B.cstart.p;
+    a.ccol = B.ccol.p;
+    a.rstart = B.rstart.p;
+    a.runs = B.runs.p;
+    a.us = l.us;
+    a.status = B.status.p;
+    if (bulk) {
+        size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 2 * T;
+        AXGB_CUDA(cudaFuncSetAttribute(k_blk_bulk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(bytes)));
+        k_blk_bulk<L, T><<<static_cast<unsigned>(l.n), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+    } else {
+        size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 2 * T + sizeof(int) * static_cast<size_t>(l.us / 4);
+        AXGB_CUDA(cudaFuncSetAttribute(k_blk_chunk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(bytes)));
+        k_blk_chunk<L, T><<<static_cast<unsigned>(l.n), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+    }
+}
+
+template <int T>
+void launch_all(const Blocked &B, bool bulk, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    for (const auto &l : B.launches) {
+        if (l.n == 0) continue;
+        // T = 8 staging of the largest buckets would exceed shared memory: use 4 there
+        const bool big = static_cast<size_t>(l.us) * 2 * T * sizeof(float) > 200 * 1024;
+        if (T == 8 && big) {
+            switch (l.L) {
+                case 4: launch_one<4, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+                case 8: launch_one<8, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+                case 12: launch_one<12, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+                case 16: launch_one<16, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+                case 20: launch_one<20, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+                case 24: launch_one<24, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+                case 28: launch_one<28, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+                default: launch_one<32, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            }
+            continue;
+        }
+        switch (l.L) {
+            case 4: launch_one<4, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            case 8: launch_one<8, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            case 12: launch_one<12, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            case 16: launch_one<16, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            case 20: launch_one<20, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            case 24: launch_one<24, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            case 28: launch_one<28, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            default: launch_one<32, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+        }
+    }
+}
+
+}  // namespace
+
+void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T,
+                   cudaStream_t s) {
+    const Blocked &B = m.blocked;
+    if (T >= 8)
+        launch_all<8>(B, bulk, x, ldx, y, ldy, nrhs, s);
+    else if (T >= 4)
+        launch_all<4>(B, bulk, x, ldx, y, ldy, nrhs, s);
+    else
+        launch_all<2>(B, bulk, x, ldx, y, ldy, nrhs, s);
+    AXGB_CUDA(cudaGetLastError());
+}
+
+}  // namespace axgb

@@ -137,9 +137,9 @@ int axgb_generate_weights_c(int src_mesh, int dst_mesh, int method, int *matrix_
 /* Statistics of the last generation into this matrix. stats (int64[8]):
  * BVH candidate pairs, pairs passing the reference gates (float AABB, cap,
  * degenerate, area, mask), pairs clipped with the 32-vertex fallback,
- * kept pairs (nnz), LBVH nodes, and the kernel launches per split-FP32
- * apply of the direct, bulk-staged and cp.async-staged variants (each known
- * after axgb_matrix_prepare of its format). times_ms (double[8]): cell prep,
+ * kept pairs (nnz), LBVH nodes, the kernel launches per split-FP32 apply
+ * of the direct and of the blocked variants (each known after
+ * axgb_matrix_prepare of its format), 0. times_ms (double[8]): cell prep,
  * LBVH build, candidate search, clip, CSR assembly, total, 0, 0. */
 int axgb_matrix_stats(int matrix_handle, int64_t *stats, double *times_ms);
 
@@ -162,9 +162,9 @@ int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int6
                            const double *area_b, int *matrix_handle);
 
 /* Builds the apply layouts of a matrix ahead of time (format 0: FP64
- * sliced-ELL, 1: split-FP32 hi+lo sliced-ELL, 2: the cp.async-staged
- * split-FP32 layout on top of 1, 3: the bulk-copy staged layout on top of 2)
- * so that later apply calls allocate nothing. Synchronous. */
+ * sliced-ELL, 1: split-FP32 hi+lo sliced-ELL, 2: the blocked staged
+ * split-FP32 layout, which also builds 1) so that later apply calls
+ * allocate nothing. Synchronous. */
 int axgb_matrix_prepare(int matrix_handle, int format);
 
 /* Reads (and clears) the device status word of a matrix's bulk-staged apply:
@@ -191,13 +191,13 @@ int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *
 
 /* Same, kernel choice explicit. variant 0: direct gathers from global
  * memory, fields_per_pass = RHS tile width (0 = all), unroll = fields per
- * thread iteration (1, 2 or 4). variant 1: per 128-row block the unique
- * source values are staged in shared memory with cp.async, unroll = fields
- * per stage (2, 4 or 8), fields_per_pass ignored. variant 2: as 1 but the
- * block's source runs are staged as 16-byte chunks (cp.async.cg) and the row
- * loop is branch-free; variant 3: the runs are fetched with bulk (TMA) copies
- * completing on an mbarrier. Variants 2 and 3 need x 16-byte aligned and
- * ld_x, n_src multiples of 4; otherwise variant 1 runs. */
+ * thread iteration (1, 2 or 4). variants 1 and 2: rows in blocks of 4
+ * slices grouped by source locality; per block the source values are staged
+ * in shared memory as 16-byte chunks, variant 1 with cp.async by all
+ * threads, variant 2 with bulk (TMA) copies completing on an mbarrier;
+ * unroll = fields per stage (2, 4 or 8), fields_per_pass ignored. Variants
+ * 1 and 2 need x 16-byte aligned and ld_x, n_src multiples of 4; otherwise
+ * the direct kernel runs. */
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                               int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 
