@@ -77,6 +77,12 @@ struct DBuf {
         if (count > n) alloc(count);
         if (count) AXGB_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
     }
+    // Allocates at least one element and copies the vector's elements (none for an empty vector).
+    template <class V>
+    void upload_vec(const V &v, cudaStream_t s = 0) {
+        if (v.size() + 1 > n || !p) alloc(v.size() > 0 ? v.size() : 1);
+        if (!v.empty()) AXGB_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
     void download(T *h, size_t count, cudaStream_t s = 0) const {
         if (count) AXGB_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
     }

@@ -511,18 +511,18 @@ void build_blocked(Matrix &m, cudaStream_t s) {
         B.launches.push_back(l);
     }
     B.n_blocks = nb;
-    B.brow.upload(brow.data(), std::max<size_t>(1, brow.size()), s);
-    B.wbase.upload(wbase.data(), std::max<size_t>(1, wbase.size()), s);
-    B.wlen.upload(wlen.data(), std::max<size_t>(1, wlen.size()), s);
-    B.cstart.upload(cstart.data(), cstart.size(), s);
-    B.ccol.upload(ccol.data(), std::max<size_t>(1, ccol.size()), s);
-    B.rstart.upload(rstart.data(), rstart.size(), s);
-    B.runs.upload(runs.data(), std::max<size_t>(1, runs.size()), s);
-    B.lidx.upload(lidx.data(), std::max<size_t>(1, lidx.size()), s);
-    B.hi.upload(hi.data(), std::max<size_t>(1, hi.size()), s);
-    B.lo.upload(lo.data(), std::max<size_t>(1, lo.size()), s);
-    B.block_ids.upload(ids.data(), std::max<size_t>(1, ids.size()), s);
-    B.fallback_slices.upload(fb.data(), std::max<size_t>(1, fb.size()), s);
+    B.brow.upload_vec(brow, s);
+    B.wbase.upload_vec(wbase, s);
+    B.wlen.upload_vec(wlen, s);
+    B.cstart.upload_vec(cstart, s);
+    B.ccol.upload_vec(ccol, s);
+    B.rstart.upload_vec(rstart, s);
+    B.runs.upload_vec(runs, s);
+    B.lidx.upload_vec(lidx, s);
+    B.hi.upload_vec(hi, s);
+    B.lo.upload_vec(lo, s);
+    B.block_ids.upload_vec(ids, s);
+    B.fallback_slices.upload_vec(fb, s);
     B.n_fallback = static_cast<i64>(fb.size());
     if (!B.status.p) {
         B.status.alloc(1);
