@@ -225,9 +225,10 @@ void check_apply(const Matrix &m, const void *x, i64 ldx, const void *y, i64 ldy
 
 SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
     std::vector<SplitParams> cands;
-    for (int v : {1, 2})
-        for (int t : {2, 4, 8})
-            if (t <= std::max<i64>(2, nrhs)) cands.push_back({v, 0, t});
+    for (int t : {4, 8})
+        for (int fc : {0, 256, 128, 64, 32})
+            if (t <= std::max<i64>(2, nrhs) && (fc == 0 || fc < nrhs)) cands.push_back({1, fc, t});
+    cands.push_back({2, 128, 8});
     std::vector<i64> tiles = {nrhs};
     for (i64 t : {32, 8})
         if (t < nrhs) tiles.push_back(t);
@@ -302,7 +303,7 @@ SplitParams pick_params(Matrix &m, i64 nrhs) {
 SplitParams default_split_params(i64 nrhs) {
     SplitParams p;
     p.variant = 1;
-    p.fields_per_pass = 0;
+    p.fields_per_pass = 128;
     p.unroll = nrhs >= 8 ? 8 : 4;
     return p;
 }

@@ -183,7 +183,7 @@ struct Blocked {
 struct SplitParams {
     int variant = 1;          // 0 direct gathers, 1 blocked + cp.async chunk staging,
                               // 2 blocked + bulk-copy (TMA) staging
-    int fields_per_pass = 0;  // direct: RHS tile width (0 = all)
+    int fields_per_pass = 0;  // direct: RHS tile width; blocked: fields per work item (0 = all)
     int unroll = 4;           // direct: fields per thread iteration; staged: fields per stage
 };
 
@@ -221,7 +221,7 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
 // staged.cu
 void build_blocked(Matrix &m, cudaStream_t s);
 bool blocked_eligible(const Matrix &m, const void *x, i64 ldx);
-void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T,
+void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, i64 fchunk,
                    cudaStream_t s);
 int blocked_launches(const Matrix &m);
 void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s);

@@ -102,7 +102,23 @@ struct BlkArgs {
     const int4 *runs;
     int us;                    // staging stride of a field (floats)
     int *status;
+    i64 nbl;                   // blocks in this launch
+    i64 fchunk;                // fields per work item (multiple of the stage width)
 };
+
+// Work item of this CTA: (field chunk, block), chunk-major so that all CTAs
+// sweep the same fields at about the same time.
+__device__ __forceinline__ int item_setup(const BlkArgs &a, const float *&x, i64 ldx, float *&y, i64 ldy, i64 &nrhs) {
+    const i64 item = blockIdx.x;
+    const i64 chunk = item / a.nbl;
+    const int b = a.blocks[item - chunk * a.nbl];
+    const i64 f0 = chunk * a.fchunk;
+    const i64 n = nrhs - f0 < a.fchunk ? nrhs - f0 : a.fchunk;
+    x += f0 * ldx;
+    y += f0 * ldy;
+    nrhs = n;
+    return b;
+}
 
 // Row reduction of one staged tile of T fields. s/cn accumulators per pair.
 template <int L, int T>
@@ -176,7 +192,7 @@ __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__r
     const int us = a.us;
     float *xs = smem;                                   // [2][T][us]
     int *cc = reinterpret_cast<int *>(smem + 2 * T * us);  // chunk columns
-    const int b = a.blocks[blockIdx.x];
+    const int b = item_setup(a, x, ldx, y, ldy, nrhs);
     const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
     const int zero = 4 * nch;
     for (int j = threadIdx.x; j < nch; j += kRows) cc[j] = a.ccol[c0 + j];
@@ -225,7 +241,7 @@ __global__ void __launch_bounds__(kRows) k_blk_bulk(BlkArgs a, const float *__re
     __shared__ int abort_flag;
     const int us = a.us;
     float *xs = smem;  // [2][T][us]
-    const int b = a.blocks[blockIdx.x];
+    const int b = item_setup(a, x, ldx, y, ldy, nrhs);
     const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
     const int zero = 4 * nch;
     const int r0 = a.rstart[b], nr = a.rstart[b + 1] - r0;
@@ -544,8 +560,11 @@ namespace {
 
 template <int L, int T>
 void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, const float *x, i64 ldx, float *y, i64 ldy,
-                i64 nrhs, cudaStream_t s) {
+                i64 nrhs, i64 fchunk, cudaStream_t s) {
     BlkArgs a;
+    a.nbl = l.n;
+    a.fchunk = (fchunk <= 0 || fchunk >= nrhs) ? nrhs : (fchunk + T - 1) / T * T;
+    const i64 grid = l.n * ((nrhs + a.fchunk - 1) / a.fchunk);
     a.blocks = B.block_ids.p + l.begin;
     a.brow = B.brow.p;
     a.wbase = B.wbase.p;
@@ -563,58 +582,59 @@ void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, const flo
         size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 2 * T;
         AXGB_CUDA(cudaFuncSetAttribute(k_blk_bulk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(bytes)));
-        k_blk_bulk<L, T><<<static_cast<unsigned>(l.n), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+        k_blk_bulk<L, T><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
     } else {
         size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 2 * T + sizeof(int) * static_cast<size_t>(l.us / 4);
         AXGB_CUDA(cudaFuncSetAttribute(k_blk_chunk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(bytes)));
-        k_blk_chunk<L, T><<<static_cast<unsigned>(l.n), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+        k_blk_chunk<L, T><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
     }
 }
 
 template <int T>
-void launch_all(const Blocked &B, bool bulk, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+void launch_all(const Blocked &B, bool bulk, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, i64 fchunk,
+                cudaStream_t s) {
     for (const auto &l : B.launches) {
         if (l.n == 0) continue;
         // T = 8 staging of the largest buckets would exceed shared memory: use 4 there
         const bool big = static_cast<size_t>(l.us) * 2 * T * sizeof(float) > 200 * 1024;
         if (T == 8 && big) {
             switch (l.L) {
-                case 4: launch_one<4, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-                case 8: launch_one<8, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-                case 12: launch_one<12, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-                case 16: launch_one<16, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-                case 20: launch_one<20, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-                case 24: launch_one<24, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-                case 28: launch_one<28, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-                default: launch_one<32, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+                case 4: launch_one<4, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 8: launch_one<8, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 12: launch_one<12, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 16: launch_one<16, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 20: launch_one<20, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 24: launch_one<24, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 28: launch_one<28, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                default: launch_one<32, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
             }
             continue;
         }
         switch (l.L) {
-            case 4: launch_one<4, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-            case 8: launch_one<8, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-            case 12: launch_one<12, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-            case 16: launch_one<16, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-            case 20: launch_one<20, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-            case 24: launch_one<24, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-            case 28: launch_one<28, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
-            default: launch_one<32, T>(B, l, bulk, x, ldx, y, ldy, nrhs, s); break;
+            case 4: launch_one<4, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 8: launch_one<8, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 12: launch_one<12, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 16: launch_one<16, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 20: launch_one<20, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 24: launch_one<24, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 28: launch_one<28, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            default: launch_one<32, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
         }
     }
 }
 
 }  // namespace
 
-void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T,
+void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, i64 fchunk,
                    cudaStream_t s) {
     const Blocked &B = m.blocked;
     if (T >= 8)
-        launch_all<8>(B, bulk, x, ldx, y, ldy, nrhs, s);
+        launch_all<8>(B, bulk, x, ldx, y, ldy, nrhs, fchunk, s);
     else if (T >= 4)
-        launch_all<4>(B, bulk, x, ldx, y, ldy, nrhs, s);
+        launch_all<4>(B, bulk, x, ldx, y, ldy, nrhs, fchunk, s);
     else
-        launch_all<2>(B, bulk, x, ldx, y, ldy, nrhs, s);
+        launch_all<2>(B, bulk, x, ldx, y, ldy, nrhs, fchunk, s);
     AXGB_CUDA(cudaGetLastError());
 }
 
