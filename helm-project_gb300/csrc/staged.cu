@@ -108,7 +108,8 @@ struct BlkArgs {
 
 // Work item of this CTA: (field chunk, block), chunk-major so that all CTAs
 // sweep the same fields at about the same time.
-__device__ __forceinline__ int item_setup(const BlkArgs &a, const float *&x, i64 ldx, float *&y, i64 ldy, i64 &nrhs) {
+__device__ __forceinline__ int item_setup(const BlkArgs &a, const float *__restrict__ &x, i64 ldx,
+                                          float *__restrict__ &y, i64 ldy, i64 &nrhs) {
     const i64 item = blockIdx.x;
     const i64 chunk = item / a.nbl;
     const int b = a.blocks[item - chunk * a.nbl];
