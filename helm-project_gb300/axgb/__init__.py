@@ -396,11 +396,11 @@ def apply_f32split(matrix: Matrix, x, y=None, stream=None, fields_per_pass=None,
 
 def autotune_f32split(matrix: Matrix, x, y, stream=None):
     import torch
-    best = np.zeros(3, np.int32)
+    best = np.zeros(4, np.int32)
     _check(lib().axgb_autotune_f32split(matrix.handle, _ptr(x), x.stride(0), _ptr(y), y.stride(0), x.shape[0],
                                         _stream(stream if stream is not None else torch.cuda.current_stream()),
                                         _ptr(best)))
-    return dict(variant=int(best[0]), fields_per_pass=int(best[1]), unroll=int(best[2]))
+    return dict(variant=int(best[0]), fields_per_pass=int(best[1]), unroll=int(best[2]), stages=int(best[3]))
 
 
 def set_autotune(enable: bool):

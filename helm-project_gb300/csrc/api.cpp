@@ -226,9 +226,10 @@ void check_apply(const Matrix &m, const void *x, i64 ldx, const void *y, i64 ldy
 SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
     std::vector<SplitParams> cands;
     for (int t : {4, 8})
-        for (int fc : {0, 256, 128, 64, 32})
-            if (t <= std::max<i64>(2, nrhs) && (fc == 0 || fc < nrhs)) cands.push_back({1, fc, t});
-    cands.push_back({2, 128, 8});
+        for (int ns : {2, 3})
+            for (int fc : {0, 128, 64, 32})
+                if (t <= std::max<i64>(2, nrhs) && (fc == 0 || fc < nrhs)) cands.push_back({1, fc, t, ns});
+    cands.push_back({2, 64, 4, 2});
     std::vector<i64> tiles = {nrhs};
     for (i64 t : {32, 8})
         if (t < nrhs) tiles.push_back(t);
@@ -303,7 +304,8 @@ SplitParams pick_params(Matrix &m, i64 nrhs) {
 SplitParams default_split_params(i64 nrhs) {
     SplitParams p;
     p.variant = 1;
-    p.fields_per_pass = 128;
+    p.fields_per_pass = 64;
+    p.stages = 2;
     p.unroll = nrhs >= 8 ? 8 : 4;
     return p;
 }
@@ -670,7 +672,7 @@ int axgb_apply_f32split_tuned(int h, const float *x, int64_t ldx, float *y, int6
         } else {
             AXGB_REQUIRE(unroll == 2 || unroll == 4 || unroll == 8, "apply: staged fields per stage must be 2, 4 or 8");
         }
-        SplitParams p{variant, fields_per_pass, unroll};
+        SplitParams p{variant, fields_per_pass, unroll, 2};
         if (nrhs > 0) apply_split(*m, x, ldx, y, ldy, nrhs, p, static_cast<cudaStream_t>(stream));
     });
 }
@@ -690,6 +692,7 @@ int axgb_autotune_f32split(int h, const float *x, int64_t ldx, float *y, int64_t
             best[0] = p.variant;
             best[1] = p.fields_per_pass;
             best[2] = p.unroll;
+            best[3] = p.stages;
         }
     });
 }

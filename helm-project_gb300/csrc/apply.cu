@@ -506,7 +506,7 @@ void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs
     if (nrhs <= 0) return;
     if (p.variant >= 1 && blocked_eligible(m, x, ldx)) {
         if (!m.blocked.built) matrix_prepare(m, 2, s);
-        apply_blocked(m, x, ldx, y, ldy, nrhs, p.variant == 2, p.unroll, p.fields_per_pass, s);
+        apply_blocked(m, x, ldx, y, ldy, nrhs, p.variant == 2, p.unroll, p.stages, p.fields_per_pass, s);
         const Blocked &B = m.blocked;
         if (B.n_fallback > 0) {
             SellArgs a = sell_args(m, m.sell32, 4);

@@ -175,8 +175,19 @@ struct Blocked {
     DBuf<unsigned short> lidx;
     DBuf<float> hi, lo;
     std::vector<Launch> launches;
+    std::vector<int> order;  // launches by size, largest first
     i64 n_fallback = 0;
     DBuf<int> status;  // device status word: 1 = a bounded wait timed out
+    // stream pool for concurrent class launches (fork/join on the caller's stream)
+    std::mutex pool_mu;
+    std::vector<cudaStream_t> pool;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
+    ~Blocked() {
+        for (auto st : pool) cudaStreamDestroy(st);
+        for (auto ev : join) cudaEventDestroy(ev);
+        if (fork) cudaEventDestroy(fork);
+    }
 };
 
 // Kernel choice for the split-FP32 apply.
@@ -185,6 +196,7 @@ struct SplitParams {
                               // 2 blocked + bulk-copy (TMA) staging
     int fields_per_pass = 0;  // direct: RHS tile width; blocked: fields per work item (0 = all)
     int unroll = 4;           // direct: fields per thread iteration; staged: fields per stage
+    int stages = 2;           // blocked chunk variant: staging buffers (2 or 3)
 };
 
 struct Matrix {
@@ -221,8 +233,8 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
 // staged.cu
 void build_blocked(Matrix &m, cudaStream_t s);
 bool blocked_eligible(const Matrix &m, const void *x, i64 ldx);
-void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, i64 fchunk,
-                   cudaStream_t s);
+void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, int ns,
+                   i64 fchunk, cudaStream_t s);
 int blocked_launches(const Matrix &m);
 void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s);
 

@@ -33,6 +33,7 @@ namespace {
 constexpr int kRows = 128;       // rows per block (4 warps)
 constexpr int kMaxUS = 3072;     // staging floats per field a block may use
 constexpr int kMaxL = 32;        // longest row handled by the blocked kernels
+constexpr int kPool = 4;         // streams the class launches are spread over
 const int kUsBuckets[] = {256, 512, 768, 1024, 1280, 1536, 2048, 3072};
 
 inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
@@ -185,14 +186,15 @@ __device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, 
     }
 }
 
-template <int L, int T>
+template <int L, int T, int NS>
 __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__restrict__ x, i64 ldx,
                                                     float *__restrict__ y, i64 ldy, i64 nrhs) {
     static_assert(T % 2 == 0, "fields per stage must be even");
+    static_assert(NS == 2 || NS == 3, "two or three staging buffers");
     extern __shared__ __align__(128) float smem[];
     const int us = a.us;
-    float *xs = smem;                                   // [2][T][us]
-    int *cc = reinterpret_cast<int *>(smem + 2 * T * us);  // chunk columns
+    float *xs = smem;                                    // [NS][T][us]
+    int *cc = reinterpret_cast<int *>(smem + NS * T * us);  // chunk columns
     const int b = item_setup(a, x, ldx, y, ldy, nrhs);
     const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
     const int zero = 4 * nch;
@@ -202,33 +204,33 @@ __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__r
     int wl;
     i64 row;
     load_entries<L>(a, b, zero, li, h, lw, wl, row);
-    for (int q = threadIdx.x; q < 2 * T; q += kRows)
+    for (int q = threadIdx.x; q < NS * T; q += kRows)
         *reinterpret_cast<float4 *>(xs + q * us + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     const i64 ntile = (nrhs + T - 1) / T;
-    auto stage = [&](i64 t, float *dst) {
-        const i64 fa = t * T;
-        const int nf = static_cast<int>((nrhs - fa < static_cast<i64>(T)) ? nrhs - fa : static_cast<i64>(T));
-        const float *xt = x + fa * ldx;
-        for (int j = threadIdx.x; j < nch; j += kRows) {
-            const float *src = xt + cc[j];
+    // stage(t) commits one cp.async group; empty groups keep the count uniform
+    auto stage = [&](i64 t) {
+        if (t < ntile) {
+            float *dst = xs + (t % NS) * T * us;
+            const i64 fa = t * T;
+            const int nf = static_cast<int>((nrhs - fa < static_cast<i64>(T)) ? nrhs - fa : static_cast<i64>(T));
+            const float *xt = x + fa * ldx;
+            for (int j = threadIdx.x; j < nch; j += kRows) {
+                const float *src = xt + cc[j];
 #pragma unroll
-            for (int f = 0; f < T; ++f)
-                if (f < nf) cp_async16(dst + f * us + 4 * j, src + f * ldx);
+                for (int f = 0; f < T; ++f)
+                    if (f < nf) cp_async16(dst + f * us + 4 * j, src + f * ldx);
+            }
         }
         cp_async_commit();
     };
-    stage(0, xs);
+#pragma unroll
+    for (int q = 0; q < NS - 1; ++q) stage(q);
     for (i64 t = 0; t < ntile; ++t) {
-        const float *cur = xs + (t & 1) * T * us;
-        if (t + 1 < ntile) {
-            stage(t + 1, xs + ((t + 1) & 1) * T * us);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
+        stage(t + NS - 1);
+        cp_async_wait<NS - 1>();  // tile t's group has landed
         __syncthreads();
-        reduce_tile<L, T>(cur, us, li, h, lw, wl, t * T, nrhs, row, y, ldy);
+        reduce_tile<L, T>(xs + (t % NS) * T * us, us, li, h, lw, wl, t * T, nrhs, row, y, ldy);
         __syncthreads();
     }
 }
@@ -527,6 +529,10 @@ void build_blocked(Matrix &m, cudaStream_t s) {
         ids.insert(ids.end(), kv.second.begin(), kv.second.end());
         B.launches.push_back(l);
     }
+    B.order.resize(B.launches.size());
+    for (size_t q = 0; q < B.order.size(); ++q) B.order[q] = static_cast<int>(q);
+    std::stable_sort(B.order.begin(), B.order.end(),
+                     [&](int p1, int p2) { return B.launches[p1].n > B.launches[p2].n; });
     B.n_blocks = nb;
     B.brow.upload_vec(brow, s);
     B.wbase.upload_vec(wbase, s);
@@ -560,8 +566,8 @@ int blocked_launches(const Matrix &m) {
 namespace {
 
 template <int L, int T>
-void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, const float *x, i64 ldx, float *y, i64 ldy,
-                i64 nrhs, i64 fchunk, cudaStream_t s) {
+void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, const float *x, i64 ldx, float *y,
+                i64 ldy, i64 nrhs, i64 fchunk, cudaStream_t s) {
     BlkArgs a;
     a.nbl = l.n;
     a.fchunk = (fchunk <= 0 || fchunk >= nrhs) ? nrhs : (fchunk + T - 1) / T * T;
@@ -584,58 +590,87 @@ void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, const flo
         AXGB_CUDA(cudaFuncSetAttribute(k_blk_bulk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(bytes)));
         k_blk_bulk<L, T><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+    } else if (ns >= 3 && static_cast<size_t>(l.us) * 3 * T * sizeof(float) <= 200 * 1024) {
+        size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 3 * T + sizeof(int) * static_cast<size_t>(l.us / 4);
+        AXGB_CUDA(cudaFuncSetAttribute(k_blk_chunk<L, T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(bytes)));
+        k_blk_chunk<L, T, 3><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
     } else {
         size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 2 * T + sizeof(int) * static_cast<size_t>(l.us / 4);
-        AXGB_CUDA(cudaFuncSetAttribute(k_blk_chunk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        AXGB_CUDA(cudaFuncSetAttribute(k_blk_chunk<L, T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(bytes)));
-        k_blk_chunk<L, T><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+        k_blk_chunk<L, T, 2><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
     }
 }
 
 template <int T>
-void launch_all(const Blocked &B, bool bulk, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, i64 fchunk,
-                cudaStream_t s) {
-    for (const auto &l : B.launches) {
-        if (l.n == 0) continue;
+void launch_class(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, const float *x, i64 ldx, float *y,
+                  i64 ldy, i64 nrhs, i64 fchunk, cudaStream_t s) {
+    {
+        if (l.n == 0) return;
         // T = 8 staging of the largest buckets would exceed shared memory: use 4 there
         const bool big = static_cast<size_t>(l.us) * 2 * T * sizeof(float) > 200 * 1024;
         if (T == 8 && big) {
             switch (l.L) {
-                case 4: launch_one<4, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 8: launch_one<8, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 12: launch_one<12, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 16: launch_one<16, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 20: launch_one<20, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 24: launch_one<24, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 28: launch_one<28, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                default: launch_one<32, 4>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 4: launch_one<4, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 8: launch_one<8, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 12: launch_one<12, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 16: launch_one<16, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 20: launch_one<20, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 24: launch_one<24, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 28: launch_one<28, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                default: launch_one<32, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
             }
-            continue;
+            return;
         }
         switch (l.L) {
-            case 4: launch_one<4, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 8: launch_one<8, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 12: launch_one<12, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 16: launch_one<16, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 20: launch_one<20, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 24: launch_one<24, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 28: launch_one<28, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            default: launch_one<32, T>(B, l, bulk, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 4: launch_one<4, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 8: launch_one<8, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 12: launch_one<12, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 16: launch_one<16, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 20: launch_one<20, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 24: launch_one<24, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 28: launch_one<28, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            default: launch_one<32, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
         }
     }
 }
 
 }  // namespace
 
-void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, i64 fchunk,
-                   cudaStream_t s) {
-    const Blocked &B = m.blocked;
-    if (T >= 8)
-        launch_all<8>(B, bulk, x, ldx, y, ldy, nrhs, fchunk, s);
-    else if (T >= 4)
-        launch_all<4>(B, bulk, x, ldx, y, ldy, nrhs, fchunk, s);
-    else
-        launch_all<2>(B, bulk, x, ldx, y, ldy, nrhs, fchunk, s);
+void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, int ns,
+                   i64 fchunk, cudaStream_t s) {
+    Blocked &B = m.blocked;
+    // Classes run concurrently on a small stream pool (fork/join through
+    // events on the caller's stream, so the call stays stream-ordered and
+    // capturable); the largest classes are issued first.
+    std::lock_guard<std::mutex> lk(B.pool_mu);
+    if (B.pool.empty()) {
+        B.pool.resize(kPool);
+        B.join.resize(kPool);
+        for (int q = 0; q < kPool; ++q) {
+            AXGB_CUDA(cudaStreamCreateWithFlags(&B.pool[q], cudaStreamNonBlocking));
+            AXGB_CUDA(cudaEventCreateWithFlags(&B.join[q], cudaEventDisableTiming));
+        }
+        AXGB_CUDA(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming));
+    }
+    AXGB_CUDA(cudaEventRecord(B.fork, s));
+    const int used = static_cast<int>(std::min<size_t>(kPool, B.order.size()));
+    for (int q = 0; q < used; ++q) AXGB_CUDA(cudaStreamWaitEvent(B.pool[q], B.fork, 0));
+    for (size_t i = 0; i < B.order.size(); ++i) {
+        const Blocked::Launch &l = B.launches[B.order[i]];
+        cudaStream_t st = B.pool[i % kPool];
+        if (T >= 8)
+            launch_class<8>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, st);
+        else if (T >= 4)
+            launch_class<4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, st);
+        else
+            launch_class<2>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, st);
+    }
+    for (int q = 0; q < used; ++q) {
+        AXGB_CUDA(cudaEventRecord(B.join[q], B.pool[q]));
+        AXGB_CUDA(cudaStreamWaitEvent(s, B.join[q], 0));
+    }
     AXGB_CUDA(cudaGetLastError());
 }
 

@@ -201,10 +201,10 @@ int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                               int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 
-/* Autotuner: times the split apply over (variant, fields_per_pass, unroll)
- * choices on the given device buffers, caches the best per (matrix, nrhs)
- * and returns it in best[3]. Used automatically by axgb_apply_f32split when
- * enabled with axgb_set_autotune(1). */
+/* Autotuner: times the split apply over (variant, fields_per_pass, unroll,
+ * staging buffers) choices on the given device buffers, caches the best per
+ * (matrix, nrhs) and returns it in best[4]. Used automatically by
+ * axgb_apply_f32split when enabled with axgb_set_autotune(1). */
 int axgb_autotune_f32split(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                            axgb_stream_t stream, int32_t *best);
 int axgb_set_autotune(int enable);
