@@ -34,7 +34,7 @@ constexpr int kRows = 128;       // rows per block (4 warps)
 constexpr int kMaxUS = 3072;     // staging floats per field a block may use
 constexpr int kMaxL = 32;        // longest row handled by the blocked kernels
 constexpr int kPool = 4;         // streams the class launches are spread over
-const int kUsBuckets[] = {256, 512, 768, 1024, 1280, 1536, 2048, 3072};
+const int kUsBuckets[] = {1024, 3072};  // staging strides compiled into the chunk kernel
 
 inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
 
@@ -122,7 +122,61 @@ __device__ __forceinline__ int item_setup(const BlkArgs &a, const float *__restr
     return b;
 }
 
-// Row reduction of one staged tile of T fields. s/cn accumulators per pair.
+// Row reduction of one staged tile of T fields (field stride US floats in
+// shared memory). Per entry the packed weights (h, -h, -lo) are formed once
+// for the T/2 field pairs; per pair the compensated step is 11 FMA-pipe ops.
+template <int L, int T, int US>
+__device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, const float *h, const float *lw, int wl,
+                                              i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy) {
+    if (f0 + T <= nrhs) {
+        F2 sa[T / 2], cn[T / 2];
+#pragma unroll
+        for (int q = 0; q < T / 2; ++q) {
+            sa[q] = pk(0.f, 0.f);
+            cn[q] = pk(0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < L; ++k) {
+            if (k < wl) {  // warp-uniform
+                const F2 hp = pk(h[k], h[k]), hn = pk(-h[k], -h[k]), ln = pk(-lw[k], -lw[k]);
+                const float *p0 = cur + li[k];
+#pragma unroll
+                for (int q = 0; q < T / 2; ++q) {
+                    const F2 xv = pk(p0[(2 * q) * US], p0[(2 * q + 1) * US]);
+                    const F2 p = mul2(hp, xv);
+                    const F2 pen = fma2(hn, xv, p);  // p - h*x, exact
+                    const F2 t = add2(sa[q], p);
+                    const F2 bp = sub2(t, sa[q]);
+                    const F2 e = add2(sub2(sa[q], sub2(t, bp)), sub2(p, bp));
+                    const F2 u1 = fma2(ln, xv, pen);  // -(lo*x + product error)
+                    cn[q] = add2(cn[q], sub2(u1, e));
+                    sa[q] = t;
+                }
+            }
+        }
+        if (row >= 0) {
+#pragma unroll
+            for (int q = 0; q < T / 2; ++q) {
+                float ra, rb;
+                upk(sub2(sa[q], cn[q]), ra, rb);
+                y[(f0 + 2 * q) * ldy + row] = ra;
+                y[(f0 + 2 * q + 1) * ldy + row] = rb;
+            }
+        }
+    } else {
+        for (int f = 0; f < T; ++f) {
+            if (f0 + f >= nrhs) break;
+            float s1 = 0.f, c1 = 0.f;
+            const float *p0 = cur + f * US;
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (k < wl) csum1(s1, c1, h[k], lw[k], p0[li[k]]);
+            if (row >= 0) y[(f0 + f) * ldy + row] = __fadd_rn(s1, c1);
+        }
+    }
+}
+
+// Runtime-stride version used by the bulk-copy kernel.
 template <int L, int T>
 __device__ __forceinline__ void reduce_tile(const float *cur, int us, const int *li, const float *h, const float *lw,
                                             int wl, i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy) {
@@ -135,7 +189,7 @@ __device__ __forceinline__ void reduce_tile(const float *cur, int us, const int 
         }
 #pragma unroll
         for (int k = 0; k < L; ++k) {
-            if (k < wl) {  // warp-uniform
+            if (k < wl) {
                 const F2 h2 = pk(h[k], h[k]), l2 = pk(lw[k], lw[k]);
                 const float *p0 = cur + li[k];
 #pragma unroll
@@ -186,15 +240,14 @@ __device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, 
     }
 }
 
-template <int L, int T, int NS>
+template <int L, int T, int NS, int US>
 __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__restrict__ x, i64 ldx,
                                                     float *__restrict__ y, i64 ldy, i64 nrhs) {
     static_assert(T % 2 == 0, "fields per stage must be even");
     static_assert(NS == 2 || NS == 3, "two or three staging buffers");
     extern __shared__ __align__(128) float smem[];
-    const int us = a.us;
-    float *xs = smem;                                    // [NS][T][us]
-    int *cc = reinterpret_cast<int *>(smem + NS * T * us);  // chunk columns
+    float *xs = smem;                                    // [NS][T][US]
+    int *cc = reinterpret_cast<int *>(smem + NS * T * US);  // chunk columns
     const int b = item_setup(a, x, ldx, y, ldy, nrhs);
     const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
     const int zero = 4 * nch;
@@ -205,13 +258,14 @@ __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__r
     i64 row;
     load_entries<L>(a, b, zero, li, h, lw, wl, row);
     for (int q = threadIdx.x; q < NS * T; q += kRows)
-        *reinterpret_cast<float4 *>(xs + q * us + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4 *>(xs + q * US + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     const i64 ntile = (nrhs + T - 1) / T;
-    // stage(t) commits one cp.async group; empty groups keep the count uniform
+    // stage(t) commits one cp.async group (empty past the end, so group
+    // counting stays uniform)
     auto stage = [&](i64 t) {
         if (t < ntile) {
-            float *dst = xs + (t % NS) * T * us;
+            float *dst = xs + (t % NS) * T * US;
             const i64 fa = t * T;
             const int nf = static_cast<int>((nrhs - fa < static_cast<i64>(T)) ? nrhs - fa : static_cast<i64>(T));
             const float *xt = x + fa * ldx;
@@ -219,7 +273,7 @@ __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__r
                 const float *src = xt + cc[j];
 #pragma unroll
                 for (int f = 0; f < T; ++f)
-                    if (f < nf) cp_async16(dst + f * us + 4 * j, src + f * ldx);
+                    if (f < nf) cp_async16(dst + f * US + 4 * j, src + f * ldx);
             }
         }
         cp_async_commit();
@@ -227,11 +281,10 @@ __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__r
 #pragma unroll
     for (int q = 0; q < NS - 1; ++q) stage(q);
     for (i64 t = 0; t < ntile; ++t) {
-        stage(t + NS - 1);
-        cp_async_wait<NS - 1>();  // tile t's group has landed
-        __syncthreads();
-        reduce_tile<L, T>(xs + (t % NS) * T * us, us, li, h, lw, wl, t * T, nrhs, row, y, ldy);
-        __syncthreads();
+        cp_async_wait<NS - 2>();  // tile t has landed (NS-2 newer groups may be pending)
+        __syncthreads();          // ... for every thread, and tile t-1 is no longer read
+        stage(t + NS - 1);        // refill the buffer tile t-1 used
+        reduce_tile_c<L, T, US>(xs + (t % NS) * T * US, li, h, lw, wl, t * T, nrhs, row, y, ldy);
     }
 }
 
@@ -565,6 +618,28 @@ int blocked_launches(const Matrix &m) {
 
 namespace {
 
+template <int L, int T, int NS, int US>
+void launch_chunk_us(const BlkArgs &a, i64 grid, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    size_t bytes = sizeof(float) * static_cast<size_t>(US) * NS * T + sizeof(int) * static_cast<size_t>(US / 4);
+    AXGB_CUDA(cudaFuncSetAttribute(k_blk_chunk<L, T, NS, US>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(bytes)));
+    k_blk_chunk<L, T, NS, US><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+
+// Staging stride buckets compiled in: 1024 and 3072 floats per field.
+template <int L, int T>
+void launch_chunk(const BlkArgs &a, int us, int ns, i64 grid, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs,
+                  cudaStream_t s) {
+    if (us <= 1024) {
+        if (ns >= 3)
+            launch_chunk_us<L, T, 3, 1024>(a, grid, x, ldx, y, ldy, nrhs, s);
+        else
+            launch_chunk_us<L, T, 2, 1024>(a, grid, x, ldx, y, ldy, nrhs, s);
+    } else {
+        launch_chunk_us<L, (T > 4 ? 4 : T), 2, 3072>(a, grid, x, ldx, y, ldy, nrhs, s);
+    }
+}
+
 template <int L, int T>
 void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, const float *x, i64 ldx, float *y,
                 i64 ldy, i64 nrhs, i64 fchunk, cudaStream_t s) {
@@ -590,16 +665,8 @@ void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, c
         AXGB_CUDA(cudaFuncSetAttribute(k_blk_bulk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(bytes)));
         k_blk_bulk<L, T><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
-    } else if (ns >= 3 && static_cast<size_t>(l.us) * 3 * T * sizeof(float) <= 200 * 1024) {
-        size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 3 * T + sizeof(int) * static_cast<size_t>(l.us / 4);
-        AXGB_CUDA(cudaFuncSetAttribute(k_blk_chunk<L, T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(bytes)));
-        k_blk_chunk<L, T, 3><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
     } else {
-        size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 2 * T + sizeof(int) * static_cast<size_t>(l.us / 4);
-        AXGB_CUDA(cudaFuncSetAttribute(k_blk_chunk<L, T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(bytes)));
-        k_blk_chunk<L, T, 2><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+        launch_chunk<L, T>(a, l.us, ns, grid, x, ldx, y, ldy, nrhs, s);
     }
 }
 
