@@ -43,7 +43,7 @@ _SYMBOLS = [
     "axgb_apply_f64", "axgb_apply_f32split", "axgb_apply_f32split_tuned", "axgb_autotune_f32split",
     "axgb_set_autotune", "axgb_apply_c", "axgb_batch_apply_host_f64", "axgb_batch_apply_host_f32split",
     "axgb_batch_create", "axgb_batch_apply", "axgb_destroy_batch", "axgb_conservation_f64",
-    "axgb_conservation_f32", "axgb_matrix_device_status",
+    "axgb_conservation_f32", "axgb_matrix_device_status", "axgb_conservation_f64_noalloc",
 ]
 
 
@@ -111,6 +111,7 @@ def lib():
     L.axgb_destroy_batch.argtypes = [C.c_int]
     L.axgb_conservation_f64.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
     L.axgb_conservation_f32.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
+    L.axgb_conservation_f64_noalloc.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
     _L = L
     return L
 

@@ -813,6 +813,15 @@ int axgb_conservation_f64(int h, const double *src, const double *dst, int norm_
     });
 }
 
+int axgb_conservation_f64_noalloc(int h, const double *src, const double *dst, int norm_type, double *out,
+                                  axgb_stream_t stream) {
+    AXGB_TRY({
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        AXGB_REQUIRE(out && (m->n_src == 0 || src) && (m->n_dst == 0 || dst), "conservation_noalloc: NULL argument");
+        conservation_noalloc(*m, src, dst, norm_type, out, static_cast<cudaStream_t>(stream));
+    });
+}
+
 int axgb_conservation_f32(int h, const float *src, const float *dst, int norm_type, double *out,
                           axgb_stream_t stream) {
     AXGB_TRY({

@@ -427,6 +427,84 @@ double integral(const T *f, const double *area, const double *frac, i64 n, int m
     return acc;
 }
 
+// ─── conservation report without allocation ───────────────────────────────
+// For callers that cannot allocate device memory while they run (a model
+// whose memory is owned by its own pool, code between allocation-free
+// phases, or a stream that is later captured): the per-block partial sums
+// live in a fixed file-scope device array instead of cudaMalloc'd scratch.
+// Each block reduces a fixed span of 2048 cells; the partials are then
+// reduced by one block in a fixed order, so results are deterministic.
+
+constexpr int kNaThreads = 256;
+constexpr i64 kNaCellsPerBlock = 2048;                      // 8 cells per thread
+constexpr int kNaMaxBlocks = 8192;                          // per integral
+constexpr i64 kNaMaxCells = kNaCellsPerBlock * kNaMaxBlocks;  // 16,777,216 cells per side
+// [0, K): source partials, [K, 2K): destination partials, [2K, 2K+2): results.
+// Every slot a call reads is written earlier in the same call.
+static __device__ __align__(256) double g_noalloc_scratch[2 * kNaMaxBlocks + 2];
+
+template <class T>
+__global__ void k_integral_span(const T *f, const double *area, const double *frac, i64 n, int mode, double *partial) {
+    __shared__ double sh[kNaThreads];
+    const i64 b0 = static_cast<i64>(blockIdx.x) * kNaCellsPerBlock;
+    double acc = 0.0;
+    for (int q = 0; q < kNaCellsPerBlock / kNaThreads; ++q) {
+        const i64 i = b0 + q * kNaThreads + threadIdx.x;
+        if (i < n) {
+            double v = static_cast<double>(f[i]);
+            if (mode == 0)
+                acc += v * area[i] * frac[i];
+            else if (frac[i] != 0.0)
+                acc += v * area[i];
+        }
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = kNaThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// One block: result[w] = sum of partial[w*K .. w*K + nb[w]) for w = 0, 1.
+__global__ void k_sum_partials(const double *partial, int nb0, int nb1, double *result) {
+    __shared__ double sh[kNaThreads];
+    for (int w = 0; w < 2; ++w) {
+        const int nb = w == 0 ? nb0 : nb1;
+        const double *p = partial + static_cast<i64>(w) * kNaMaxBlocks;
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < nb; i += kNaThreads) acc += p[i];
+        sh[threadIdx.x] = acc;
+        __syncthreads();
+        for (int o = kNaThreads / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) result[w] = sh[0];
+        __syncthreads();
+    }
+}
+
+// Device address of g_noalloc_scratch for the current device, looked up
+// once per device (the host-side name is not a device address).
+double *noalloc_scratch() {
+    static std::mutex mu;
+    static double *ptr[256] = {};
+    int dev = 0;
+    AXGB_CUDA(cudaGetDevice(&dev));
+    AXGB_REQUIRE(dev >= 0 && dev < 256, "conservation_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            throw Error(AXGB_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+        ptr[dev] = static_cast<double *>(p);
+    }
+    return ptr[dev];
+}
+
 // ─── persistent batch kernel ───────────────────────────────────────────────
 // Items of all matrices are handed out by one atomic counter (no waiting):
 // item -> (matrix, tile, slice). Entries of up to 32 per row are cached in
@@ -553,6 +631,33 @@ void conservation(Matrix &m, const void *src, const void *dst, bool f32, int nor
     }
     double ae = std::abs(si - di);
     double den = std::max({std::abs(si), std::abs(di), 2.220446049250313e-16});
+    out[0] = si;
+    out[1] = di;
+    out[2] = ae;
+    out[3] = ae / den;
+}
+
+void conservation_noalloc(Matrix &m, const double *src, const double *dst, int norm_type, double *out,
+                          cudaStream_t s) {
+    if (m.n_src > kNaMaxCells || m.n_dst > kNaMaxCells)
+        throw Error(AXGB_ERR_INVALID, "conservation_noalloc: n_src (" + std::to_string(m.n_src) + ") or n_dst (" +
+                                          std::to_string(m.n_dst) + ") exceeds the fixed scratch limit of " +
+                                          std::to_string(kNaMaxCells) + " cells; use axgb_conservation_f64");
+    double *scr = noalloc_scratch();
+    const int nbs = static_cast<int>((m.n_src + kNaCellsPerBlock - 1) / kNaCellsPerBlock);
+    const int nbd = static_cast<int>((m.n_dst + kNaCellsPerBlock - 1) / kNaCellsPerBlock);
+    if (nbs > 0) k_integral_span<double><<<nbs, kNaThreads, 0, s>>>(src, m.area_a.p, m.frac_a.p, m.n_src, 0, scr);
+    if (nbd > 0)
+        k_integral_span<double><<<nbd, kNaThreads, 0, s>>>(dst, m.area_b.p, m.frac_b.p, m.n_dst,
+                                                           norm_type == 0 ? 1 : 0, scr + kNaMaxBlocks);
+    k_sum_partials<<<1, kNaThreads, 0, s>>>(scr, nbs, nbd, scr + 2 * kNaMaxBlocks);
+    AXGB_CUDA(cudaGetLastError());
+    double two[2] = {0.0, 0.0};
+    AXGB_CUDA(cudaMemcpyAsync(two, scr + 2 * kNaMaxBlocks, sizeof(two), cudaMemcpyDeviceToHost, s));
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    const double si = two[0], di = two[1];
+    const double ae = std::abs(si - di);
+    const double den = std::max({std::abs(si), std::abs(di), 2.220446049250313e-16});
     out[0] = si;
     out[1] = di;
     out[2] = ae;

@@ -243,6 +243,21 @@ int axgb_conservation_f64(int matrix_handle, const double *src, const double *ds
 int axgb_conservation_f32(int matrix_handle, const float *src, const float *dst, int norm_type, double *out,
                           axgb_stream_t stream);
 
+/* axgb_conservation_f64 for callers that cannot allocate device memory
+ * while they run (a model whose device memory belongs to its own pool, or
+ * code that must not call cudaMalloc between its set-up and tear-down). It
+ * allocates nothing: its partial sums live in a fixed 128 KiB array that the
+ * library places in every GPU that loads it, kept until the process exits.
+ * Limit: n_src and n_dst at most 16,777,216 cells each; larger matrices get
+ * AXGB_ERR_INVALID (use axgb_conservation_f64). The first call on a device
+ * looks the array's device address up once; make that first call before
+ * any stream capture. All calls share the one array, so calls that overlap
+ * on the GPU (other streams or host threads) race; no slot needs clearing
+ * between calls. Synchronous. It has no counterpart in the reference, which
+ * always allocates its reduction scratch. */
+int axgb_conservation_f64_noalloc(int matrix_handle, const double *src, const double *dst, int norm_type,
+                                  double *out, axgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
