@@ -113,18 +113,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_fields(xyz_t, seed: int = 2024):
-    """[1016, n] float32 on the device: 8 SH(l<=128) tracers x lognormal level scales."""
+def make_fields(xyz_t, nrhs: int = NRHS, seed: int = 2024):
+    """[nrhs, n] float32 on the device: the first nrhs of the 1016 fields
+    [tracer][level][cell], 8 SH(l<=128) tracers x lognormal level scales."""
     import torch
 
     from axgb import fields
-    base = fields.sh_fields(xyz_t, 128, [seed + t for t in range(N_TRACERS)])
+    n_tr = (nrhs + N_LEVELS - 1) // N_LEVELS
+    base = fields.sh_fields(xyz_t, 128, [seed + t for t in range(n_tr)])
     rng = np.random.default_rng(seed)
     scales = rng.lognormal(0.0, 1.0, size=(N_TRACERS, N_LEVELS))
-    X = torch.empty((NRHS, xyz_t.shape[0]), dtype=torch.float32, device=xyz_t.device)
-    for t in range(N_TRACERS):
-        sc = torch.tensor(scales[t], dtype=torch.float64, device=xyz_t.device)
-        X[t * N_LEVELS:(t + 1) * N_LEVELS] = (base[t][None, :] * sc[:, None]).to(torch.float32)
+    X = torch.empty((nrhs, xyz_t.shape[0]), dtype=torch.float32, device=xyz_t.device)
+    for t in range(n_tr):
+        nl = min(N_LEVELS, nrhs - t * N_LEVELS)
+        sc = torch.tensor(scales[t][:nl], dtype=torch.float64, device=xyz_t.device)
+        X[t * N_LEVELS:t * N_LEVELS + nl] = (base[t][None, :] * sc[:, None]).to(torch.float32)
     del base
     return X, scales
 
@@ -194,6 +197,14 @@ def main():
     ap.add_argument("--impl", default="axgb", choices=["axgb", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nrhs", type=int, default=NRHS,
+                    help="fields per step (default 1016 = 8 tracers x 127 levels; smaller values make "
+                         "profiling cases of the same kernel; the first nrhs fields of the workload)")
+    ap.add_argument("--kernel", default=None,
+                    help="fixed kernel choice variant,fields_per_pass,unroll,stages instead of the autotuner")
+    ap.add_argument("--apply-only", action="store_true",
+                    help="time only the split apply (no FP64 apply, oracle parity, e2e, weight generation "
+                         "or CPU baseline reports); for profiler captures")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -236,19 +247,25 @@ def main():
     # ── fields ──
     xyz = torch.tensor(grids.cell_centroids_xyz(src_g), device=dev)
     t0 = time.perf_counter()
-    X, scales = make_fields(xyz)
+    nrhs = max(1, min(args.nrhs, NRHS))
+    X, scales = make_fields(xyz, nrhs)
     torch.cuda.synchronize()
     log(f"fields {time.perf_counter() - t0:.1f}s")
-    Y = torch.empty((NRHS, M.n_dst), dtype=torch.float32, device=dev)
+    Y = torch.empty((nrhs, M.n_dst), dtype=torch.float32, device=dev)
     M.prepare(2)
-    tuned = axgb.autotune_f32split(M, X, Y)
+    if args.kernel:
+        v, fpp, un, stg = (int(t) for t in args.kernel.split(","))
+        tuned = {"variant": v, "fields_per_pass": fpp, "unroll": un, "stages": stg}
+        axgb.set_kernel_choice(M, nrhs, **tuned)
+    else:
+        tuned = axgb.autotune_f32split(M, X, Y)
     launches_per_step = axgb_launches(M, tuned["variant"])
-    log(f"autotune: {tuned} launches/step={launches_per_step}")
+    log(f"kernel: {tuned} launches/step={launches_per_step}")
 
     stream = torch.cuda.current_stream()
 
     def run_split():
-        axgb.apply_f32split(M, X, Y, stream=stream)  # the tuned kernel
+        axgb.apply_f32split(M, X, Y, stream=stream)  # the tuned (or fixed) kernel
 
     for _ in range(args.warmup):
         run_split()
@@ -271,16 +288,40 @@ def main():
         tt = torch.tensor([ms_step], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms_step = float(tt.item())
-    dst_vals = M.n_dst * NRHS
+    dst_vals = M.n_dst * nrhs
     value = world * dst_vals / (ms_step / 1e3)
-    bytes_split = 4 * M.n_src * NRHS + 4 * M.n_dst * NRHS + 12 * M.nnz + 4 * (M.n_dst + 1)
+    bytes_split = 4 * M.n_src * nrhs + 4 * M.n_dst * nrhs + 12 * M.nnz + 4 * (M.n_dst + 1)
     peak, peak_kind = peaks()
     achieved = bytes_split / (ms_step / 1e3) / 1e9
     log(f"split: {ms_step:.3f} ms/step  {achieved:.0f} GB/s ({achieved / peak:.2%} of {peak_kind} {peak:.0f})")
 
+    workload = WORKLOAD if nrhs == NRHS else f"C768->0.25deg conservative, batched split-FP32 SpMM, {nrhs} RHS"
+    result = {
+        "metric": METRIC if nrhs == NRHS else METRIC.replace("1016 RHS", f"{nrhs} RHS"), "value": value,
+        "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload, "n_src": M.n_src, "n_dst": M.n_dst, "nnz": M.nnz, "nrhs": nrhs,
+                   "kernel": tuned, "l2": f"inputs {4 * M.n_src * nrhs / 1e9:.1f} GB per step > L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": profiled_traffic() if nrhs == NRHS else None,
+                     "peak_kind": peak_kind, "bytes_per_step": bytes_split},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+        "weightgen_c768_to_0p25": {"seconds": t_gen3, "nnz": M.nnz, "pairs_per_s": M.nnz / t_gen3,
+                                   "candidates": st3["bvh_candidates"], "gated": st3["gated_pairs"],
+                                   "stages_ms": {k: st3[k] for k in st3 if k.startswith("t_")}},
+    }
+    if args.apply_only:
+        if rank == 0:
+            print(json.dumps(result), flush=True)
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
+
     # ── plain FP64 SpMM on FP64 copies of the same fields ──
     X64 = X.to(torch.float64)
-    Y64 = torch.empty((NRHS, M.n_dst), dtype=torch.float64, device=dev)
+    Y64 = torch.empty((nrhs, M.n_dst), dtype=torch.float64, device=dev)
     M.prepare(0)
     for _ in range(args.warmup):
         axgb.apply_f64(M, X64, Y64, stream=stream)
@@ -291,26 +332,10 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     ms64 = e0.elapsed_time(e1) / args.steps
-    bytes_f64 = 8 * M.n_src * NRHS + 8 * M.n_dst * NRHS + 12 * M.nnz + 4 * (M.n_dst + 1)
+    bytes_f64 = 8 * M.n_src * nrhs + 8 * M.n_dst * nrhs + 12 * M.nnz + 4 * (M.n_dst + 1)
     log(f"fp64: {ms64:.3f} ms/step  {bytes_f64 / ms64 / 1e6:.0f} GB/s; split speed-up {ms64 / ms_step:.2f}x")
 
-    result = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_src": M.n_src, "n_dst": M.n_dst, "nnz": M.nnz, "nrhs": NRHS,
-                   "kernel": tuned, "l2": "inputs 14.4 GB per step > L2",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": profiled_traffic(), "peak_kind": peak_kind,
-                     "bytes_per_step": bytes_split},
-        "fp64_apply": {"ms_per_step": ms64, "GBps": bytes_f64 / ms64 / 1e6, "split_speedup": ms64 / ms_step},
-        "gpu_launches": launches_per_step * args.steps,
-        "clocks": clocks,
-        "weightgen_c768_to_0p25": {"seconds": t_gen3, "nnz": M.nnz, "pairs_per_s": M.nnz / t_gen3,
-                                   "candidates": st3["bvh_candidates"], "gated": st3["gated_pairs"],
-                                   "stages_ms": {k: st3[k] for k in st3 if k.startswith("t_")}},
-    }
+    result["fp64_apply"] = {"ms_per_step": ms64, "GBps": bytes_f64 / ms64 / 1e6, "split_speedup": ms64 / ms_step}
 
     if rank == 0:
         # ── errors and conservation against the CPU oracle ──
@@ -324,7 +349,7 @@ def main():
         rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
         same = M.nnz == wo.nnz and np.array_equal(rows, wo.row) and np.array_equal(csr["col"], wo.col)
         wrel = float(np.max(np.abs(csr["val"] - wo.w) / wo.w)) if same else None
-        sample = [0, 1, 500, NRHS - 1]
+        sample = sorted({0, 1, min(500, nrhs - 1), nrhs - 1})
         Xs = X[sample].to(torch.float64).cpu().numpy()
         ref = o.apply_csr(wo, Xs, compensated=True)
         e_split = rel_errors(Y[sample].cpu().numpy(), ref)
@@ -352,11 +377,17 @@ def main():
         result["weightgen_0p25_to_c384"] = weightgen_c384(md, dst_g)
         # ── CPU baseline: oracle CSR apply on this host ──
         if not args.no_cpu:
-            ns = 16
+            ns = min(64, nrhs)
             xs = X[:ns].to(torch.float64).cpu().numpy()
-            rate, dt = cpu_apply_rate(o, wo, xs)
+            reps, total = 0, 0.0
+            while total < 10.0 and reps < 1000:  # about 10 s of CPU work
+                _, dt = cpu_apply_rate(o, wo, xs)
+                reps += 1
+                total += dt
+            rate = reps * ns * wo.n_dst / total
             result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                      "sample": f"{ns} of {NRHS} RHS, FP64 CSR row loop (OpenMP), {dt:.2f} s"}
+                                      "sample": f"{ns} of {nrhs} RHS x {reps} repeats, FP64 CSR row loop "
+                                                f"(OpenMP, oracle port), {total:.1f} s"}
         print(json.dumps(result), flush=True)
     if world > 1:
         dist.destroy_process_group()

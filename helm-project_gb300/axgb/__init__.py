@@ -44,6 +44,7 @@ _SYMBOLS = [
     "axgb_set_autotune", "axgb_apply_c", "axgb_batch_apply_host_f64", "axgb_batch_apply_host_f32split",
     "axgb_batch_create", "axgb_batch_apply", "axgb_destroy_batch", "axgb_conservation_f64",
     "axgb_conservation_f32", "axgb_matrix_device_status", "axgb_conservation_f64_noalloc",
+    "axgb_set_kernel_choice", "axgb_get_kernel_choice",
 ]
 
 
@@ -112,6 +113,8 @@ def lib():
     L.axgb_conservation_f64.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
     L.axgb_conservation_f32.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
     L.axgb_conservation_f64_noalloc.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
+    L.axgb_set_kernel_choice.argtypes = [C.c_int, C.c_int64, vp]
+    L.axgb_get_kernel_choice.argtypes = [C.c_int, C.c_int64, vp, vp]
     _L = L
     return L
 
@@ -402,6 +405,21 @@ def autotune_f32split(matrix: Matrix, x, y, stream=None):
                                         _stream(stream if stream is not None else torch.cuda.current_stream()),
                                         _ptr(best)))
     return dict(variant=int(best[0]), fields_per_pass=int(best[1]), unroll=int(best[2]), stages=int(best[3]))
+
+
+def set_kernel_choice(matrix: Matrix, nrhs: int, variant: int, fields_per_pass: int, unroll: int, stages: int = 2):
+    """Seed the cached kernel choice that apply_f32split uses for (matrix, nrhs)."""
+    ch = np.array([variant, fields_per_pass, unroll, stages], np.int32)
+    _check(lib().axgb_set_kernel_choice(matrix.handle, int(nrhs), _ptr(ch)))
+
+
+def get_kernel_choice(matrix: Matrix, nrhs: int):
+    """The kernel choice apply_f32split would use for (matrix, nrhs), and whether it is cached."""
+    ch = np.zeros(4, np.int32)
+    cached = np.zeros(1, np.int32)
+    _check(lib().axgb_get_kernel_choice(matrix.handle, int(nrhs), _ptr(ch), _ptr(cached)))
+    return dict(variant=int(ch[0]), fields_per_pass=int(ch[1]), unroll=int(ch[2]), stages=int(ch[3]),
+                cached=bool(cached[0]))
 
 
 def set_autotune(enable: bool):

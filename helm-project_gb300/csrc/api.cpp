@@ -702,6 +702,48 @@ int axgb_set_autotune(int enable) {
     return AXGB_SUCCESS;
 }
 
+int axgb_set_kernel_choice(int h, int64_t nrhs, const int32_t *choice) {
+    AXGB_TRY({
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        AXGB_REQUIRE(choice && nrhs > 0, "set_kernel_choice: NULL choice or nrhs <= 0");
+        SplitParams p{choice[0], choice[1], choice[2], choice[3]};
+        AXGB_REQUIRE(p.variant >= 0 && p.variant <= 2, "set_kernel_choice: variant must be 0, 1 or 2");
+        AXGB_REQUIRE(p.fields_per_pass >= 0, "set_kernel_choice: fields_per_pass must be >= 0");
+        if (p.variant == 0) {
+            AXGB_REQUIRE(p.unroll == 1 || p.unroll == 2 || p.unroll == 4, "set_kernel_choice: direct unroll must be 1, 2 or 4");
+        } else {
+            AXGB_REQUIRE(p.unroll == 2 || p.unroll == 4 || p.unroll == 8,
+                         "set_kernel_choice: staged fields per stage must be 2, 4 or 8");
+        }
+        AXGB_REQUIRE(p.stages == 2 || (p.stages == 3 && p.variant == 1),
+                     "set_kernel_choice: stages must be 2 (or 3 with variant 1)");
+        std::lock_guard<std::mutex> lk(m->mu);
+        m->tuned[nrhs] = p;
+    });
+}
+
+int axgb_get_kernel_choice(int h, int64_t nrhs, int32_t *choice, int32_t *cached) {
+    AXGB_TRY({
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        AXGB_REQUIRE(choice && nrhs > 0, "get_kernel_choice: NULL choice or nrhs <= 0");
+        SplitParams p = default_split_params(nrhs);
+        int32_t c = 0;
+        {
+            std::lock_guard<std::mutex> lk(m->mu);
+            auto it = m->tuned.find(nrhs);
+            if (it != m->tuned.end()) {
+                p = it->second;
+                c = 1;
+            }
+        }
+        choice[0] = p.variant;
+        choice[1] = p.fields_per_pass;
+        choice[2] = p.unroll;
+        choice[3] = p.stages;
+        if (cached) *cached = c;
+    });
+}
+
 int axgb_apply_f32split(int h, const float *x, int64_t ldx, float *y, int64_t ldy, int64_t nrhs,
                         axgb_stream_t stream) {
     AXGB_TRY({

@@ -194,10 +194,10 @@ int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *
  * thread iteration (1, 2 or 4). variants 1 and 2: rows in blocks of 4
  * slices grouped by source locality; per block the source values are staged
  * in shared memory as 16-byte chunks, variant 1 with cp.async by all
- * threads, variant 2 with bulk (TMA) copies completing on an mbarrier;
- * unroll = fields per stage (2, 4 or 8), fields_per_pass ignored. Variants
- * 1 and 2 need x 16-byte aligned and ld_x, n_src multiples of 4; otherwise
- * the direct kernel runs. */
+ * threads (two staging buffers), variant 2 with bulk (TMA) copies completing
+ * on an mbarrier; unroll = fields per stage (2, 4 or 8), fields_per_pass =
+ * fields per work item of a block (0 = all). Variants 1 and 2 need x 16-byte
+ * aligned and ld_x, n_src multiples of 4; otherwise the direct kernel runs. */
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                               int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 
@@ -208,6 +208,15 @@ int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, f
 int axgb_autotune_f32split(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                            axgb_stream_t stream, int32_t *best);
 int axgb_set_autotune(int enable);
+
+/* Read or seed the cached kernel choice of (matrix, nrhs) that
+ * axgb_apply_f32split uses: choice[4] = variant, fields_per_pass, unroll,
+ * stages (stages 2 or 3, variant 1 only), as axgb_autotune_f32split returns
+ * it. Seeding lets a caller reuse a choice tuned in an earlier process
+ * without timing again. When nothing is cached for (matrix, nrhs), get
+ * sets *cached = 0 and returns the default choice. */
+int axgb_set_kernel_choice(int matrix_handle, int64_t nrhs, const int32_t *choice);
+int axgb_get_kernel_choice(int matrix_handle, int64_t nrhs, int32_t *choice, int32_t *cached);
 
 /* ─── Apply (host pointers, synchronous) ─────────────────────────────────
  * Replaces axis_apply_c (axis_c_interop.cpp:217-236): FP64, one field,

@@ -243,3 +243,19 @@ def test_conservation_parity(gpu, oracle, cfg1):
     ro = oracle.conservation(wo, f, oracle.apply_csr(wo, f)[0])
     assert abs(rep["src_integral"] - ro["src_integral"]) / abs(ro["src_integral"]) < 1e-13
     assert rep["relative_error"] < 1e-12
+
+
+def test_kernel_choice_seed_and_read(gpu, oracle, cfg1):
+    import torch
+    src, dst, M, wo, f = cfg1
+    nrhs = 6
+    assert gpu.get_kernel_choice(M, nrhs)["cached"] is False
+    gpu.set_kernel_choice(M, nrhs, variant=1, fields_per_pass=4, unroll=2, stages=3)
+    ch = gpu.get_kernel_choice(M, nrhs)
+    assert ch == dict(variant=1, fields_per_pass=4, unroll=2, stages=3, cached=True)
+    X = torch.tensor(np.stack([f * (1 + k) for k in range(nrhs)]).astype(np.float32), device="cuda")
+    y = gpu.apply_f32split(M, X).cpu().numpy().astype(np.float64)
+    ref = oracle.apply_csr(wo, X.cpu().numpy().astype(np.float64), compensated=True)
+    assert np.max(np.abs(y - ref) / np.abs(ref)) < SPLIT_RTOL
+    with pytest.raises(gpu.InvalidArgument):
+        gpu.set_kernel_choice(M, nrhs, variant=2, fields_per_pass=0, unroll=4, stages=3)
