@@ -252,7 +252,9 @@ def main():
     torch.cuda.synchronize()
     log(f"fields {time.perf_counter() - t0:.1f}s")
     Y = torch.empty((nrhs, M.n_dst), dtype=torch.float32, device=dev)
+    t0 = time.perf_counter()
     M.prepare(2)
+    log(f"apply layouts built in {time.perf_counter() - t0:.2f}s")
     if args.kernel:
         v, fpp, un, stg = (int(t) for t in args.kernel.split(","))
         tuned = {"variant": v, "fields_per_pass": fpp, "unroll": un, "stages": stg}

@@ -197,9 +197,17 @@ void mesh_upload_impl(Mesh &m) {
 }
 
 // Reusable device staging for the host-pointer entry points.
+// Device staging for the host-buffer batched apply: a ring of field-chunk
+// buffers and three streams (copy in, compute, copy out) with events, kept
+// across calls (one set per process, for the device current at first use;
+// re-created if the device changes).
 struct Staging {
+    static constexpr int kRing = 3;
     std::mutex mu;
     DBuf<char> a, b;
+    int device = -1;
+    cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
+    cudaEvent_t loaded[kRing] = {}, computed[kRing] = {}, drained[kRing] = {};
     void *get_a(size_t bytes) {
         if (a.n < bytes) a.alloc(bytes);
         return a.p;
@@ -207,6 +215,30 @@ struct Staging {
     void *get_b(size_t bytes) {
         if (b.n < bytes) b.alloc(bytes);
         return b.p;
+    }
+    void ensure_streams() {
+        int dev = 0;
+        AXGB_CUDA(cudaGetDevice(&dev));
+        if (dev == device && h2d) return;
+        release_streams();
+        a.release();
+        b.release();
+        for (cudaStream_t *st : {&h2d, &comp, &d2h}) AXGB_CUDA(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+        for (int q = 0; q < kRing; ++q)
+            for (cudaEvent_t *ev : {&loaded[q], &computed[q], &drained[q]})
+                AXGB_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+        device = dev;
+    }
+    void release_streams() {
+        for (cudaStream_t st : {h2d, comp, d2h})
+            if (st) cudaStreamDestroy(st);
+        h2d = comp = d2h = nullptr;
+        for (int q = 0; q < kRing; ++q)
+            for (cudaEvent_t *ev : {&loaded[q], &computed[q], &drained[q]})
+                if (*ev) {
+                    cudaEventDestroy(*ev);
+                    *ev = nullptr;
+                }
     }
     static Staging &get() {
         static Staging s;
@@ -263,34 +295,44 @@ SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i6
 // Host-buffer batch apply, LayoutLeft [n, n_vars]. Fields are streamed in
 // chunks through two device staging halves on two streams, so the copies of
 // one chunk overlap the apply of the other.
+// Host-buffer batched apply: fields [n_vars][n] in host memory (pinned for
+// full copy speed). Chunks of fields flow through a 3-deep ring of device
+// buffers: copy in (stream h2d) -> apply (stream comp) -> copy out (stream
+// d2h), so host-to-device copies, the apply and device-to-host copies of
+// different chunks overlap. A chunk holds about 2^26 values (256 MiB FP32).
+// Synchronous: returns when every result is in dst.
 template <class T, class F>
 void host_batch(Matrix &m, const T *src, T *dst, int64_t n_vars, F apply_fn) {
     auto &st = Staging::get();
     std::lock_guard<std::mutex> lk(st.mu);
+    st.ensure_streams();
+    constexpr int R = Staging::kRing;
     const int64_t ns = std::max<int64_t>(1, m.n_src), nd = std::max<int64_t>(1, m.n_dst);
-    const int64_t per = std::max<int64_t>(1, std::min<int64_t>(n_vars, (int64_t(1) << 28) / (ns + nd)));
-    T *dx = static_cast<T *>(st.get_a(sizeof(T) * ns * per * 2));
-    T *dy = static_cast<T *>(st.get_b(sizeof(T) * nd * per * 2));
-    cudaStream_t cs[2];
-    AXGB_CUDA(cudaStreamCreateWithFlags(&cs[0], cudaStreamNonBlocking));
-    AXGB_CUDA(cudaStreamCreateWithFlags(&cs[1], cudaStreamNonBlocking));
+    const int64_t per = std::max<int64_t>(1, std::min<int64_t>(n_vars, (int64_t(1) << 26) / (ns + nd)));
+    T *dx = static_cast<T *>(st.get_a(sizeof(T) * ns * per * R));
+    T *dy = static_cast<T *>(st.get_b(sizeof(T) * nd * per * R));
     int64_t chunk = 0;
     for (int64_t v0 = 0; v0 < n_vars; v0 += per, ++chunk) {
-        int64_t nv = std::min(per, n_vars - v0);
-        int b = static_cast<int>(chunk & 1);
-        cudaStream_t s = cs[b];
+        const int64_t nv = std::min(per, n_vars - v0);
+        const int b = static_cast<int>(chunk % R);
         T *x = dx + static_cast<int64_t>(b) * ns * per;
         T *y = dy + static_cast<int64_t>(b) * nd * per;
+        if (chunk >= R) AXGB_CUDA(cudaStreamWaitEvent(st.h2d, st.computed[b], 0));  // x[b] no longer read
         if (m.n_src)
-            AXGB_CUDA(cudaMemcpyAsync(x, src + v0 * m.n_src, sizeof(T) * m.n_src * nv, cudaMemcpyHostToDevice, s));
-        apply_fn(x, ns, y, nd, nv, s);
+            AXGB_CUDA(cudaMemcpyAsync(x, src + v0 * m.n_src, sizeof(T) * m.n_src * nv, cudaMemcpyHostToDevice, st.h2d));
+        AXGB_CUDA(cudaEventRecord(st.loaded[b], st.h2d));
+        AXGB_CUDA(cudaStreamWaitEvent(st.comp, st.loaded[b], 0));
+        if (chunk >= R) AXGB_CUDA(cudaStreamWaitEvent(st.comp, st.drained[b], 0));  // y[b] copied out
+        apply_fn(x, ns, y, nd, nv, st.comp);
+        AXGB_CUDA(cudaEventRecord(st.computed[b], st.comp));
+        AXGB_CUDA(cudaStreamWaitEvent(st.d2h, st.computed[b], 0));
         if (m.n_dst)
-            AXGB_CUDA(cudaMemcpyAsync(dst + v0 * m.n_dst, y, sizeof(T) * m.n_dst * nv, cudaMemcpyDeviceToHost, s));
+            AXGB_CUDA(cudaMemcpyAsync(dst + v0 * m.n_dst, y, sizeof(T) * m.n_dst * nv, cudaMemcpyDeviceToHost, st.d2h));
+        AXGB_CUDA(cudaEventRecord(st.drained[b], st.d2h));
     }
-    AXGB_CUDA(cudaStreamSynchronize(cs[0]));
-    AXGB_CUDA(cudaStreamSynchronize(cs[1]));
-    cudaStreamDestroy(cs[0]);
-    cudaStreamDestroy(cs[1]);
+    AXGB_CUDA(cudaStreamSynchronize(st.h2d));
+    AXGB_CUDA(cudaStreamSynchronize(st.comp));
+    AXGB_CUDA(cudaStreamSynchronize(st.d2h));
 }
 
 SplitParams default_split_params(i64 nrhs);

@@ -250,9 +250,10 @@ __global__ void k_slice_len(const int *rp, i64 n_rows, i64 n_slices, int *len) {
     len[s] = m * 32;  // entries of the slice; scanned into base
 }
 
-__global__ void k_sell_fill(const int *rp, const int *ccol, const double *val, i64 n_rows, i64 n_slices,
-                            const int *base, const int *slen32, int *rlen, int *col, float *hi, float *lo,
-                            double *w64) {
+// perm (optional): CSR index of the k-th entry of each row (split layouts).
+__global__ void k_sell_fill(const int *rp, const int *ccol, const double *val, const int *perm, i64 n_rows,
+                            i64 n_slices, const int *base, const int *slen32, int *rlen, int *col, float *hi,
+                            float *lo, double *w64) {
     i64 r = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (r >= n_slices * 32) return;
     i64 s = r >> 5;
@@ -269,8 +270,9 @@ __global__ void k_sell_fill(const int *rp, const int *ccol, const double *val, i
     for (int k = 0; k < L; ++k) {
         int e = b + k * 32 + lane;
         if (k < n) {
-            double w = val[r0 + k];
-            col[e] = ccol[r0 + k];
+            const int src = perm ? perm[r0 + k] : r0 + k;
+            double w = val[src];
+            col[e] = ccol[src];
             if (hi) {
                 float h = __double2float_rn(w);
                 hi[e] = h;
@@ -314,7 +316,8 @@ void build_sell(Matrix &m, int fmt, cudaStream_t s) {
         S.w64.alloc(total);
     }
     if (n_slices > 0) {
-        k_sell_fill<<<nblk(n_slices * 32, 256), 256, 0, s>>>(m.row_ptr.p, m.col.p, m.val.p, n_rows, n_slices,
+        const int *perm = (fmt == 1 && m.split_perm.p) ? m.split_perm.p : nullptr;
+        k_sell_fill<<<nblk(n_slices * 32, 256), 256, 0, s>>>(m.row_ptr.p, m.col.p, m.val.p, perm, n_rows, n_slices,
                                                             S.base.p, slen32.p, rlen.p, S.col.p,
                                                             fmt == 1 ? S.hi.p : nullptr, fmt == 1 ? S.lo.p : nullptr,
                                                             fmt == 0 ? S.w64.p : nullptr);
@@ -563,9 +566,9 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
 
 void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(m.mu);
+    if (format >= 1) build_blocked(m, s);  // fixes the split entry order (split_perm) first
     if (format == 2) {
         build_sell(m, 1, s);  // slices of blocks that do not fit the blocked kernels use the direct kernel
-        build_blocked(m, s);
         m.stats[6] = blocked_launches(m);
         return;
     }

@@ -207,6 +207,11 @@ struct Matrix {
     double times_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     Sell sell64, sell32;
     Blocked blocked;
+    // Order of each row's entries in the split-FP32 layouts: split_perm[rp[r] + k]
+    // is the CSR index of the k-th entry of row r. Chosen by the blocked build
+    // against shared-memory bank conflicts and shared by every split layout,
+    // so all split kernels sum in the same order (same bits).
+    DBuf<int> split_perm;
     std::vector<float> slice_xyz;  // mean unit vector of each 32-row slice (locality hint), may be empty
     std::map<i64, SplitParams> tuned;  // nrhs -> best kernel choice
     std::mutex mu;

@@ -439,6 +439,86 @@ struct HostBlock {
     int wbase_rel[4];
 };
 
+struct OrderScratch {
+    std::vector<int> cand[32];  // per lane: (CSR index, staging address) of the entries not yet placed
+    std::vector<int> addr[32];
+};
+
+// Order of each row's entries in the block (written to perm). At step k the
+// 32 lanes of a warp gather entry k of their rows from shared memory; lanes
+// hitting one bank at different addresses serialise. For k = 0, 1, ... each
+// row (fewest remaining entries first) takes the remaining entry whose bank
+// holds the fewest other addresses so far at this step (ties: CSR order).
+// Any order gives the same compensated row sum up to its last bits; the
+// chosen one is used by every split-FP32 layout.
+void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::vector<int> &col,
+                   const std::vector<int> &cols, std::vector<int> &perm, OrderScratch &S) {
+    const int zero = 4 * static_cast<int>(cols.size());
+    for (int w = 0; w < 4; ++w) {
+        int r_of[32], n_of[32], left[32];
+        for (int lane = 0; lane < 32; ++lane) {
+            const int r = H.rows[32 * w + lane];
+            r_of[lane] = r;
+            n_of[lane] = r >= 0 ? rp[r + 1] - rp[r] : 0;
+            left[lane] = n_of[lane];
+            S.cand[lane].clear();
+            S.addr[lane].clear();
+            for (int q = 0; q < n_of[lane]; ++q) {
+                const int c = col[rp[r] + q];
+                const int pos =
+                    static_cast<int>(std::lower_bound(cols.begin(), cols.end(), c >> 2) - cols.begin());
+                S.cand[lane].push_back(rp[r] + q);
+                S.addr[lane].push_back(4 * pos + (c & 3));
+            }
+        }
+        for (int k = 0; k < H.wlen[w]; ++k) {
+            int bank_n[32];
+            int bank_a[32][33];
+            for (int b = 0; b < 32; ++b) bank_n[b] = 0;
+            auto present = [&](int a) {
+                const int b = a & 31;
+                for (int i = 0; i < bank_n[b]; ++i)
+                    if (bank_a[b][i] == a) return true;
+                return false;
+            };
+            auto add = [&](int a) {
+                if (!present(a)) {
+                    const int b = a & 31;
+                    bank_a[b][bank_n[b]++] = a;
+                }
+            };
+            int lanes[32], nl = 0;
+            bool pad = false;
+            for (int lane = 0; lane < 32; ++lane) {
+                if (left[lane] > 0)
+                    lanes[nl++] = lane;
+                else
+                    pad = true;
+            }
+            if (pad) add(zero);
+            std::stable_sort(lanes, lanes + nl, [&](int a, int b) { return left[a] < left[b]; });
+            for (int i = 0; i < nl; ++i) {
+                const int lane = lanes[i];
+                std::vector<int> &cd = S.cand[lane], &ad = S.addr[lane];
+                int best = -1, bcost = 1 << 30;
+                for (int q = 0; q < static_cast<int>(cd.size()); ++q) {
+                    if (cd[q] < 0) continue;
+                    const int cost = present(ad[q]) ? 0 : bank_n[ad[q] & 31];
+                    if (cost < bcost) {
+                        bcost = cost;
+                        best = q;
+                        if (cost == 0) break;
+                    }
+                }
+                add(ad[best]);
+                perm[rp[r_of[lane]] + (n_of[lane] - left[lane])] = cd[best];
+                cd[best] = -1;
+                --left[lane];
+            }
+        }
+    }
+}
+
 }  // namespace
 
 void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s) {
@@ -467,9 +547,11 @@ void build_blocked(Matrix &m, cudaStream_t s) {
     auto groups = group_slices(nsl, m.slice_xyz);
     const i64 nb = static_cast<i64>(groups.size());
     std::vector<HostBlock> hb(nb);
+    std::vector<int> perm(std::max<i64>(1, nnz));
     parallel_for_host(nb, [&](i64 b0, i64 b1) {
         std::vector<std::pair<int, int>> rl;
         std::vector<int> cols;
+        OrderScratch scratch;
         for (i64 b = b0; b < b1; ++b) {
             HostBlock &H = hb[b];
             rl.clear();
@@ -504,6 +586,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
                 maxlen = std::max(maxlen, mx);
             }
             H.L = std::max(4, (maxlen + 3) / 4 * 4);
+            order_entries(H, rp, col, cols, perm, scratch);
             H.lidx.clear();
             H.hi.clear();
             H.lo.clear();
@@ -516,7 +599,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
                         int q = zero;
                         float hv = 0.f, lv = 0.f;
                         if (r >= 0 && k < rp[r + 1] - rp[r]) {
-                            int e = rp[r] + k;
+                            int e = perm[rp[r] + k];
                             int c = col[e];
                             size_t pos = std::lower_bound(cols.begin(), cols.end(), c >> 2) - cols.begin();
                             q = static_cast<int>(4 * pos) + (c & 3);
@@ -599,6 +682,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
     B.lo.upload_vec(lo, s);
     B.block_ids.upload_vec(ids, s);
     B.fallback_slices.upload_vec(fb, s);
+    m.split_perm.upload_vec(perm, s);
     B.n_fallback = static_cast<i64>(fb.size());
     if (!B.status.p) {
         B.status.alloc(1);
