@@ -1,0 +1,105 @@
+"""Generate the golden fixtures in this folder from the reference's own code.
+
+Run where the reference checkout is present (it is not on the GPU machines):
+
+    python tests/golden/make_golden.py
+
+The reference's geometry headers (spherical clipper, cap filter, Morton
+order, degenerate-cell handler, grid detector, trig cache) are compiled
+unmodified through the host shim by ``oracle/build.py`` into
+``oracle/_ref/libaxisref.so``; its ``ref_conservative`` glue runs the
+reference's first-order conservative algorithm around them. Every fixture
+stores its input meshes as well, so the tests need neither the reference
+nor the grid generators to reproduce the inputs:
+
+* ``conservative_<case>.npz``: src/dst meshes, and the reference's CSR
+  (row, col, w), frac_a/b and area_a/b;
+* ``clip.npz``: 200 random spherical polygon pairs and the reference
+  clipper's overlap area and output polygon;
+* ``cellprep_<grid>.npz``: a mesh and the reference's cell areas, bounding
+  caps, float AABBs and degenerate flags.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+for p in (ROOT, os.path.join(ROOT, "helm-project_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+from axgb import grids  # noqa: E402
+from oracle import RefLib  # noqa: E402
+from oracle import build as obuild  # noqa: E402
+
+CONSERVATIVE = {
+    "5deg_to_C8": lambda: (grids.latlon_deg(5.0), grids.cubed_sphere(8)),
+    "C12_to_C8": lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8)),
+    "C8_to_10deg": lambda: (grids.cubed_sphere(8), grids.latlon_deg(10.0)),
+    "tripole48x36_to_10deg": lambda: (grids.tripole(48, 36, seed=4, jitter=0.1), grids.latlon_deg(10.0)),
+}
+CELLPREP = {
+    "C8": lambda: grids.cubed_sphere(8),
+    "5deg": lambda: grids.latlon_deg(5.0),
+    "tripole48x36": lambda: grids.tripole(48, 36, seed=4, jitter=0.1),
+}
+
+
+def mesh_dict(prefix, m):
+    return {f"{prefix}_lonlat": m.node_lonlat, f"{prefix}_off": m.conn_offsets, f"{prefix}_idx": m.conn_indices}
+
+
+def cap_poly(center, radius, nv, rng):
+    """Convex spherical polygon: nv points on a small circle, CCW seen from outside."""
+    c = center / np.linalg.norm(center)
+    a = np.cross(c, [0.0, 0.0, 1.0] if abs(c[2]) < 0.9 else [1.0, 0.0, 0.0])
+    a /= np.linalg.norm(a)
+    b = np.cross(c, a)
+    th = np.sort(rng.uniform(0, 2 * np.pi, nv))
+    pts = [np.cos(radius) * c + np.sin(radius) * (np.cos(t) * a + np.sin(t) * b) for t in th]
+    return np.array(pts)
+
+
+def main():
+    path = obuild.build_ref()
+    if path is None:
+        raise SystemExit("the reference checkout is needed to generate the golden fixtures")
+    ref = RefLib(path)
+    for name, make in CONSERVATIVE.items():
+        src, dst = make()
+        w = ref.conservative(src, dst)
+        np.savez_compressed(os.path.join(HERE, f"conservative_{name}.npz"), **mesh_dict("src", src),
+                            **mesh_dict("dst", dst), row=w.row, col=w.col, w=w.w, frac_a=w.frac_a, frac_b=w.frac_b,
+                            area_a=w.area_a, area_b=w.area_b)
+        print(name, "nnz", w.nnz)
+    for name, make in CELLPREP.items():
+        m = make()
+        c = ref.cell_prep(m)
+        np.savez_compressed(os.path.join(HERE, f"cellprep_{name}.npz"), **mesh_dict("mesh", m), **c)
+        print("cellprep", name, m.n_cells)
+    rng = np.random.default_rng(20240)
+    subj, clipp, nsub, ncl, area, nout, outp = [], [], [], [], [], [], []
+    for _ in range(200):
+        def ll(lo, la):
+            return np.array([np.cos(la) * np.cos(lo), np.cos(la) * np.sin(lo), np.sin(la)])
+        a = cap_poly(ll(rng.uniform(-3, 3), rng.uniform(-1.5, 1.5)), rng.uniform(0.001, 0.5), rng.integers(3, 12), rng)
+        b = cap_poly(ll(rng.uniform(-3, 3), rng.uniform(-1.5, 1.5)), rng.uniform(0.001, 0.5), rng.integers(3, 12), rng)
+        if rng.uniform() < 0.5:  # overlapping pair: move b onto a
+            b = cap_poly(a.mean(0), rng.uniform(0.001, 0.5), rng.integers(3, 12), rng)
+        ar, poly = ref.clip(a, b)
+        pad = lambda p: np.concatenate([p, np.zeros((32 - len(p), 3))])
+        subj.append(pad(a)); clipp.append(pad(b)); nsub.append(len(a)); ncl.append(len(b))
+        area.append(ar); nout.append(len(poly)); outp.append(pad(poly))
+    np.savez_compressed(os.path.join(HERE, "clip.npz"), subj=np.array(subj), clip=np.array(clipp),
+                        n_subj=np.array(nsub), n_clip=np.array(ncl), area=np.array(area), n_out=np.array(nout),
+                        out=np.array(outp))
+    print("clip pairs", len(area), "overlapping", int(np.sum(np.array(area) > 0)))
+
+
+if __name__ == "__main__":
+    main()
