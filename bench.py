@@ -212,23 +212,17 @@ def main():
         return reference_arm(args)
 
     import torch
-    import torch.distributed as dist
 
     import axgb
-    from axgb import grids
+    from axgb import grids, replicas
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl")
+    rank, world, local = replicas.world_info()
     torch.cuda.set_device(local)
+    replicas.init()  # NCCL process group when launched with more than one rank
     axgb.init(local)
     dev = torch.device("cuda", local)
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
+    barrier = replicas.barrier
 
     # ── weights for the headline workload ──
     t0 = time.perf_counter()
@@ -285,13 +279,9 @@ def main():
     torch.cuda.synchronize()
     barrier()
     clocks = clk.stop()
-    ms_step = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        tt = torch.tensor([ms_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_step = float(tt.item())
+    ms_step = replicas.max_over_ranks(e0.elapsed_time(e1) / args.steps)
     dst_vals = M.n_dst * nrhs
-    value = world * dst_vals / (ms_step / 1e3)
+    value = replicas.aggregate_rate(dst_vals, ms_step / 1e3, world)
     bytes_split = 4 * M.n_src * nrhs + 4 * M.n_dst * nrhs + 12 * M.nnz + 4 * (M.n_dst + 1)
     peak, peak_kind = peaks()
     achieved = bytes_split / (ms_step / 1e3) / 1e9
@@ -317,8 +307,7 @@ def main():
     if args.apply_only:
         if rank == 0:
             print(json.dumps(result), flush=True)
-        if world > 1:
-            dist.destroy_process_group()
+        replicas.finalize()
         return 0
 
     # ── plain FP64 SpMM on FP64 copies of the same fields ──
@@ -391,8 +380,7 @@ def main():
                                       "sample": f"{ns} of {nrhs} RHS x {reps} repeats, FP64 CSR row loop "
                                                 f"(OpenMP, oracle port), {total:.1f} s"}
         print(json.dumps(result), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    replicas.finalize()
     return 0
 
 
