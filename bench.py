@@ -366,6 +366,9 @@ def main():
             result["e2e"] = e2e(M, X, args)
         # ── weight generation for 0.25 deg -> C384 ──
         result["weightgen_0p25_to_c384"] = weightgen_c384(md, dst_g)
+        # ── uneven batch of 17 grid pairs in one persistent launch ──
+        result["batch_17_pairs"] = batch_pairs(args)
+        log("batch", {k: v for k, v in result["batch_17_pairs"].items() if k not in ("pairs", "nrhs")})
         # ── CPU baseline: oracle CSR apply on this host ──
         if not args.no_cpu:
             ns = min(64, nrhs)
@@ -439,6 +442,83 @@ def e2e(M, X, args):
     return {"value": M.n_dst * nrhs / s, "unit": UNIT, "h2d_bytes_per_step": 4 * M.n_src * nrhs,
             "d2h_bytes_per_step": 4 * M.n_dst * nrhs, "ms_per_step": 1e3 * s, "nrhs": nrhs,
             "api": "axgb_batch_apply_host_f32split (pinned host buffers)"}
+
+
+def batch_pairs(args):
+    """Uneven batch of grid pairs in one persistent, graph-captured launch:
+    every cubed-sphere (C48, C96, C192, C384) x lat-lon (2, 1, 0.5, 0.25 deg)
+    combination, the direction alternating with the parity of the two grid
+    indices so each grid is source and destination, plus a 1440 x 1080
+    tripole-style grid -> 0.5 deg (17 pairs). Each pair carries a seeded
+    uniform 1..64 FP32 fields. Reports weight generation of all pairs, the
+    batch apply (dst-vals/s, algorithmic GB/s) and the same work as one
+    tuned apply call per pair, and checks the batch bitwise against them."""
+    import torch
+
+    import axgb
+    from axgb import grids
+    cs = {n: grids.cubed_sphere(n) for n in (48, 96, 192, 384)}
+    ll = {d: grids.latlon_deg(d) for d in (2.0, 1.0, 0.5, 0.25)}
+    meshes = {}
+
+    def mesh(key, g):
+        if key not in meshes:
+            meshes[key] = axgb.Mesh.from_grid(g)
+        return meshes[key]
+
+    pairs = []
+    for a, n in enumerate(cs):
+        for b, d in enumerate(ll):
+            if (a + b) % 2 == 0:
+                pairs.append((f"C{n}->{d}deg", ("cs", n), cs[n], ("ll", d), ll[d]))
+            else:
+                pairs.append((f"{d}deg->C{n}", ("ll", d), ll[d], ("cs", n), cs[n]))
+    pairs.append(("tripole1440x1080->0.5deg", ("tp",), grids.tripole(1440, 1080, seed=4, jitter=0.1), ("ll", 0.5),
+                  ll[0.5]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mats = [axgb.generate_weights(mesh(ks, gs), mesh(kd, gd), {"method": "conservative"}) for _, ks, gs, kd, gd in pairs]
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    rng = np.random.default_rng(404)
+    nrhs = [int(v) for v in rng.integers(1, 65, len(pairs))]
+    gen = torch.Generator(device="cuda").manual_seed(404)
+    xs = [torch.rand((k, M.n_src), device="cuda", generator=gen, dtype=torch.float32) for k, M in zip(nrhs, mats)]
+    ys = [torch.empty((k, M.n_dst), device="cuda", dtype=torch.float32) for k, M in zip(nrhs, mats)]
+    B = axgb.Batch(mats, nrhs)
+    for _ in range(args.warmup):
+        B.apply(xs, ys)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        B.apply(xs, ys)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_b = e0.elapsed_time(e1) / args.steps
+    # the same work as one tuned call per pair
+    for M, x, y in zip(mats, xs, ys):
+        M.prepare(2)
+        axgb.autotune_f32split(M, x, y)
+    yp = [torch.empty_like(y) for y in ys]
+    for _ in range(args.warmup):
+        for M, x, y in zip(mats, xs, yp):
+            axgb.apply_f32split(M, x, y)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        for M, x, y in zip(mats, xs, yp):
+            axgb.apply_f32split(M, x, y)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_p = e0.elapsed_time(e1) / args.steps
+    same = all(torch.equal(a, b) for a, b in zip(ys, yp))
+    dst_vals = sum(k * M.n_dst for k, M in zip(nrhs, mats))
+    nbytes = sum(4 * k * (M.n_src + M.n_dst) + 12 * M.nnz + 4 * (M.n_dst + 1) for k, M in zip(nrhs, mats))
+    return {"pairs": [p[0] for p in pairs], "nrhs": nrhs, "nnz_total": int(sum(M.nnz for M in mats)),
+            "weightgen_s": t_gen, "batch_ms": ms_b, "batch_dst_vals_per_s": dst_vals / (ms_b / 1e3),
+            "batch_GBps": nbytes / ms_b / 1e6, "per_pair_calls_ms": ms_p, "bitwise_equal_to_per_pair": bool(same),
+            "launches": "1 persistent kernel per batch apply, replayed from a CUDA graph"}
 
 
 def weightgen_c384(md_0p25, latlon_g):

@@ -29,9 +29,17 @@
 namespace axgb {
 
 struct Batch {
+    // One descriptor per (matrix, slice kind): mode 0 covers the slices whose
+    // rows have at most 32 entries (lane per row, items = field tile x
+    // slice), mode 1 the slices with longer rows (warp per row and 32
+    // fields, items = field chunk x row).
     struct Desc {
         const int *base, *len, *rlen, *col;
         const float *hi, *lo;
+        const int *ids;  // slice ids
+        i64 n_ids;
+        int mode;
+        int mat;  // index of the matrix in the batch
         i64 n_rows, n_slices;
         const float *x;
         i64 ldx;
@@ -77,8 +85,8 @@ struct SellArgs {
 __device__ __forceinline__ float ldg_f(const float *p) { return __ldg(p); }
 
 // ─── split-FP32 kernel ─────────────────────────────────────────────────────
-// L > 0: entries cached in registers (slice length <= L).
-// L == 0: entries re-read from global memory (long slices).
+// Lane per row for slices whose rows have at most L <= 32 entries, entries
+// cached in registers (longer rows: k_split_rows).
 template <int L, int U>
 __global__ void __launch_bounds__(256) k_split(SellArgs a, const float *__restrict__ x, i64 ldx, float *__restrict__ y,
                                                i64 ldy, i64 nrhs, i64 tile) {
@@ -93,7 +101,8 @@ __global__ void __launch_bounds__(256) k_split(SellArgs a, const float *__restri
     const int rl = a.rlen[static_cast<i64>(sid) * 32 + lane];
     const i64 f0 = t * tile, f1 = min(f0 + tile, nrhs);
     const bool store = row < a.n_rows;
-    if constexpr (L > 0) {
+    static_assert(L > 0 && L <= 32, "lane-per-row kernels cache at most 32 entries");
+    {
         int c[L];
         float h[L], lw[L];
 #pragma unroll
@@ -157,20 +166,12 @@ __global__ void __launch_bounds__(256) k_split(SellArgs a, const float *__restri
                 if (k < rl) csum1(s, cc, h[k], lw[k], ldg_f(xf + c[k]));
             if (store) y[f * ldy + row] = __fadd_rn(s, cc);
         }
-    } else {
-        for (i64 f = f0; f < f1; ++f) {
-            float s = 0.f, cc = 0.f;
-            const float *xf = x + f * ldx;
-            for (int k = 0; k < rl; ++k) {
-                int e = base + k * 32 + lane;
-                csum1(s, cc, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
-            }
-            if (store) y[f * ldy + row] = __fadd_rn(s, cc);
-        }
     }
 }
 
 // ─── FP64 kernel ───────────────────────────────────────────────────────────
+// Lane per row, slices of rows with at most L <= 32 entries (longer rows:
+// k_f64_rows); s = fma(w, x, s) in entry order.
 template <int L, int U>
 __global__ void __launch_bounds__(256) k_f64(SellArgs a, const double *__restrict__ x, i64 ldx, double *__restrict__ y,
                                              i64 ldy, i64 nrhs, i64 tile) {
@@ -185,7 +186,8 @@ __global__ void __launch_bounds__(256) k_f64(SellArgs a, const double *__restric
     const int rl = a.rlen[static_cast<i64>(sid) * 32 + lane];
     const i64 f0 = t * tile, f1 = min(f0 + tile, nrhs);
     const bool store = row < a.n_rows;
-    if constexpr (L > 0) {
+    static_assert(L > 0 && L <= 32, "lane-per-row kernels cache at most 32 entries");
+    {
         int c[L];
         double w[L];
 #pragma unroll
@@ -224,17 +226,57 @@ __global__ void __launch_bounds__(256) k_f64(SellArgs a, const double *__restric
                 if (k < rl) s = fma(w[k], __ldg(xf + c[k]), s);
             if (store) y[f * ldy + row] = s;
         }
-    } else {
-        for (i64 f = f0; f < f1; ++f) {
-            double s = 0.0;
-            const double *xf = x + f * ldx;
-            for (int k = 0; k < rl; ++k) {
-                int e = base + k * 32 + lane;
-                s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
-            }
-            if (store) y[f * ldy + row] = s;
-        }
     }
+}
+
+// ─── long rows: one warp per (row, 32 fields) ─────────────────────────────
+// Slices holding rows of more than 32 entries (coarse destination cells over
+// a fine source). A warp takes one row and 32 fields, lane = field; each
+// lane sums its row in entry order with the same steps as the lane-per-row
+// kernels, so results are bitwise the same. Items run field chunk outer and
+// rows inner, so neighbouring warps gather neighbouring source cells.
+__device__ __forceinline__ bool row_item(const SellArgs &a, i64 nrhs, i64 &row, int &sid, int &p, i64 &f) {
+    const int lane = threadIdx.x & 31;
+    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const i64 per = a.n_ids * 32;
+    if (w >= per * ((nrhs + 31) / 32)) return false;
+    const i64 fc = w / per;
+    const i64 q = w - fc * per;
+    sid = a.ids[q >> 5];
+    p = static_cast<int>(q & 31);
+    row = static_cast<i64>(sid) * 32 + p;
+    f = fc * 32 + lane;
+    return row < a.n_rows && f < nrhs;
+}
+
+__global__ void __launch_bounds__(256) k_split_rows(SellArgs a, const float *__restrict__ x, i64 ldx,
+                                                    float *__restrict__ y, i64 ldy, i64 nrhs) {
+    i64 row, f;
+    int sid, p;
+    if (!row_item(a, nrhs, row, sid, p, f)) return;
+    const int n = a.rlen[row], base = a.base[sid];
+    const float *xf = x + f * ldx;
+    float s = 0.f, cc = 0.f;
+    for (int k = 0; k < n; ++k) {
+        const int e = base + k * 32 + p;  // same address in every lane: one broadcast load
+        csum1(s, cc, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
+    }
+    y[f * ldy + row] = __fadd_rn(s, cc);
+}
+
+__global__ void __launch_bounds__(256) k_f64_rows(SellArgs a, const double *__restrict__ x, i64 ldx,
+                                                  double *__restrict__ y, i64 ldy, i64 nrhs) {
+    i64 row, f;
+    int sid, p;
+    if (!row_item(a, nrhs, row, sid, p, f)) return;
+    const int n = a.rlen[row], base = a.base[sid];
+    const double *xf = x + f * ldx;
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const int e = base + k * 32 + p;
+        s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
+    }
+    y[f * ldy + row] = s;
 }
 
 // ─── layout build ──────────────────────────────────────────────────────────
@@ -381,6 +423,18 @@ void launch_split(const SellArgs &a, const float *x, i64 ldx, float *y, i64 ldy,
         k_split<L, 1><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
 }
 
+void launch_split_rows(const SellArgs &a, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    const i64 warps = a.n_ids * 32 * ((nrhs + 31) / 32);
+    if (warps == 0) return;
+    k_split_rows<<<nblk(warps * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+
+void launch_f64_rows(const SellArgs &a, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    const i64 warps = a.n_ids * 32 * ((nrhs + 31) / 32);
+    if (warps == 0) return;
+    k_f64_rows<<<nblk(warps * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+
 template <int L>
 void launch_f64(const SellArgs &a, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, i64 tile, cudaStream_t s) {
     i64 items = ((nrhs + tile - 1) / tile) * a.n_ids;
@@ -523,15 +577,35 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
         int m = 0;
         while (m + 1 < n_desc && desc[m + 1].item_begin <= static_cast<i64>(it)) ++m;
         const Batch::Desc &d = desc[m];
-        i64 local = static_cast<i64>(it) - d.item_begin;
-        i64 t = local / d.n_slices;
-        i64 sid = local - t * d.n_slices;
-        i64 row = sid * 32 + lane;
-        int base = d.base[sid];
-        int rl = d.rlen[sid * 32 + lane];
-        i64 f0 = t * d.tile, f1 = min(f0 + d.tile, d.nrhs);
-        bool store = row < d.n_rows;
-        constexpr int L = 32;
+        const i64 local = static_cast<i64>(it) - d.item_begin;
+        if (d.mode == 1) {  // long rows: lane = field
+            const i64 per = d.n_ids * 32;
+            const i64 fc = local / per;
+            const i64 q = local - fc * per;
+            const int sid = d.ids[q >> 5];
+            const int p = static_cast<int>(q & 31);
+            const i64 row = static_cast<i64>(sid) * 32 + p;
+            const i64 f = fc * 32 + lane;
+            if (row < d.n_rows && f < d.nrhs) {
+                const int n = d.rlen[row], base = d.base[sid];
+                const float *xf = d.x + f * d.ldx;
+                float s = 0.f, cc = 0.f;
+                for (int k = 0; k < n; ++k) {
+                    const int e = base + k * 32 + p;
+                    csum1(s, cc, d.hi[e], d.lo[e], __ldg(xf + d.col[e]));
+                }
+                d.y[f * d.ldy + row] = __fadd_rn(s, cc);
+            }
+            continue;
+        }
+        const i64 t = local / d.n_ids;
+        const i64 sid = d.ids[local - t * d.n_ids];
+        const i64 row = sid * 32 + lane;
+        const int base = d.base[sid];
+        const int rl = d.rlen[sid * 32 + lane];
+        const i64 f0 = t * d.tile, f1 = min(f0 + d.tile, d.nrhs);
+        const bool store = row < d.n_rows;
+        constexpr int L = 16;
         int c[L];
         float h[L], lw[L];
 #pragma unroll
@@ -553,7 +627,7 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
 #pragma unroll
             for (int k = 0; k < L; ++k)
                 if (k < rl) csum1(s, cc, h[k], lw[k], __ldg(xf + c[k]));
-            for (int k = L; k < rl; ++k) {
+            for (int k = L; k < rl; ++k) {  // rows of 17..32 entries: the tail from global memory
                 int e = base + k * 32 + lane;
                 csum1(s, cc, d.hi[e], d.lo[e], __ldg(xf + d.col[e]));
             }
@@ -593,7 +667,7 @@ void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs
             SellArgs a = sell_args(m, m.sell32, 4);
             a.ids = B.fallback_slices.p;
             a.n_ids = B.n_fallback;
-            launch_split<0>(a, x, ldx, y, ldy, nrhs, nrhs, 1, s);
+            launch_split_rows(a, x, ldx, y, ldy, nrhs, s);
         }
         AXGB_CUDA(cudaGetLastError());
         return;
@@ -605,8 +679,8 @@ void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs
     launch_split<8>(sell_args(m, S, 0), x, ldx, y, ldy, nrhs, tile, unroll, s);
     launch_split<16>(sell_args(m, S, 1), x, ldx, y, ldy, nrhs, tile, unroll, s);
     launch_split<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, unroll, s);
-    launch_split<64>(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, tile, unroll, s);
-    launch_split<0>(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    launch_split_rows(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, s);
+    launch_split_rows(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, s);
     AXGB_CUDA(cudaGetLastError());
 }
 
@@ -618,8 +692,8 @@ void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs
     launch_f64<8>(sell_args(m, S, 0), x, ldx, y, ldy, nrhs, tile, s);
     launch_f64<16>(sell_args(m, S, 1), x, ldx, y, ldy, nrhs, tile, s);
     launch_f64<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, s);
-    launch_f64<64>(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, tile, s);
-    launch_f64<0>(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, tile, s);
+    launch_f64_rows(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, s);
+    launch_f64_rows(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, s);
     AXGB_CUDA(cudaGetLastError());
 }
 
@@ -675,21 +749,32 @@ std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &
     for (size_t q = 0; q < mats.size(); ++q) {
         Matrix &m = *mats[q];
         matrix_prepare(m, 1, 0);
-        Batch::Desc d{};
-        d.base = m.sell32.base.p;
-        d.len = nullptr;
-        d.rlen = m.sell32.len.p;
-        d.col = m.sell32.col.p;
-        d.hi = m.sell32.hi.p;
-        d.lo = m.sell32.lo.p;
-        d.n_rows = m.n_dst;
-        d.n_slices = m.sell32.n_slices;
-        d.nrhs = nrhs[q];
-        d.tile = std::max<i64>(1, std::min<i64>(nrhs[q], 8));
-        d.n_tiles = (nrhs[q] + d.tile - 1) / d.tile;
-        d.item_begin = items;
-        items += d.n_tiles * d.n_slices;
-        b->desc.push_back(d);
+        const Sell &S = m.sell32;
+        for (int mode = 0; mode < 2; ++mode) {
+            // classes 0..2: rows of at most 32 entries; 3..4: longer rows
+            const i64 c0 = S.class_begin[mode == 0 ? 0 : 3], c1 = S.class_begin[mode == 0 ? 3 : 5];
+            Batch::Desc d{};
+            d.base = S.base.p;
+            d.len = nullptr;
+            d.rlen = S.len.p;
+            d.col = S.col.p;
+            d.hi = S.hi.p;
+            d.lo = S.lo.p;
+            d.ids = S.class_ids.p + c0;
+            d.n_ids = c1 - c0;
+            d.mode = mode;
+            d.mat = static_cast<int>(q);
+            d.n_rows = m.n_dst;
+            d.n_slices = S.n_slices;
+            d.nrhs = nrhs[q];
+            d.tile = std::max<i64>(1, std::min<i64>(nrhs[q], 8));
+            d.n_tiles = (nrhs[q] + d.tile - 1) / d.tile;
+            const i64 n_items = mode == 0 ? d.n_tiles * d.n_ids : d.n_ids * 32 * ((nrhs[q] + 31) / 32);
+            if (n_items == 0) continue;
+            d.item_begin = items;
+            items += n_items;
+            b->desc.push_back(d);
+        }
     }
     b->total_items = items;
     b->d_desc.alloc(std::max<size_t>(1, b->desc.size()));
@@ -707,7 +792,7 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
     std::lock_guard<std::mutex> lk(b.mu);
     const size_t k = b.desc.size();
     std::vector<const void *> ptrs;
-    for (size_t q = 0; q < k; ++q) {
+    for (size_t q = 0; q < b.mats.size(); ++q) {
         AXGB_REQUIRE(ldx[q] >= b.mats[q]->n_src && ldy[q] >= b.mats[q]->n_dst, "batch_apply: leading dimension");
         ptrs.push_back(x[q]);
         ptrs.push_back(y[q]);
@@ -716,10 +801,11 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
     }
     if (ptrs != b.last_ptrs) {
         for (size_t q = 0; q < k; ++q) {
-            b.desc[q].x = x[q];
-            b.desc[q].ldx = ldx[q];
-            b.desc[q].y = y[q];
-            b.desc[q].ldy = ldy[q];
+            const int mi = b.desc[q].mat;
+            b.desc[q].x = x[mi];
+            b.desc[q].ldx = ldx[mi];
+            b.desc[q].y = y[mi];
+            b.desc[q].ldy = ldy[mi];
         }
         // stream-ordered update of the descriptors the graph reads
         AXGB_CUDA(cudaMemcpyAsync(b.d_desc.p, b.desc.data(), sizeof(Batch::Desc) * k, cudaMemcpyHostToDevice, s));
