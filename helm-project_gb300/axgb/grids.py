@@ -211,6 +211,94 @@ def tripole(ni: int = 1440, nj: int = 1080, seed: int = 4, jitter: float = 0.1) 
     return MeshArrays(node, off, idx, name=f"tripole{ni}x{nj}", shape=(ni, nj))
 
 
+def _fibonacci_points(n: int) -> np.ndarray:
+    i = np.arange(n, dtype=np.float64) + 0.5
+    z = 1.0 - 2.0 * i / n
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    th = np.pi * (1.0 + 5.0 ** 0.5) * i
+    return np.stack([r * np.cos(th), r * np.sin(th), z], axis=1)
+
+
+def _tangent_basis(p: np.ndarray):
+    a = np.where(np.abs(p[:, 2:3]) < 0.9, np.array([[0.0, 0.0, 1.0]]), np.array([[1.0, 0.0, 0.0]]))
+    e1 = np.cross(a, p)
+    e1 /= np.linalg.norm(e1, axis=1, keepdims=True)
+    e2 = np.cross(p, e1)
+    return e1, e2
+
+
+def _delaunay(p: np.ndarray):
+    """Spherical Delaunay triangles (convex hull), oriented counter-clockwise
+    seen from outside, and their circumcentres (the Voronoi vertices)."""
+    from scipy.spatial import ConvexHull
+    tri = ConvexHull(p).simplices.astype(np.int64)
+    a, b, c = p[tri[:, 0]], p[tri[:, 1]], p[tri[:, 2]]
+    nrm = np.cross(b - a, c - a)
+    flip = np.einsum("ij,ij->i", nrm, a) < 0.0
+    tri[flip, 1], tri[flip, 2] = tri[flip, 2], tri[flip, 1].copy()
+    nrm[flip] *= -1.0
+    cc = nrm / np.linalg.norm(nrm, axis=1, keepdims=True)
+    return tri, cc
+
+
+def _fans(p: np.ndarray, tri: np.ndarray, cc: np.ndarray):
+    """For every point, its incident triangles in counter-clockwise order
+    around it (seen from outside): CSR offsets and triangle ids."""
+    n = p.shape[0]
+    owner = tri.reshape(-1)
+    tid = np.repeat(np.arange(tri.shape[0], dtype=np.int64), 3)
+    e1, e2 = _tangent_basis(p)
+    d = cc[tid] - p[owner]
+    ang = np.arctan2(np.einsum("ij,ij->i", d, e2[owner]), np.einsum("ij,ij->i", d, e1[owner]))
+    order = np.lexsort((ang, owner))
+    off = np.zeros(n + 1, dtype=np.int64)
+    off[1:] = np.cumsum(np.bincount(owner, minlength=n))
+    return off, tid[order]
+
+
+def voronoi(n: int = 2621442, seed: int = 5, jitter: float = 0.2, lloyd: int = 5) -> MeshArrays:
+    """Spherical Voronoi mesh of n cells (5- to 7-gons).
+
+    Generators: Fibonacci-sphere points, each moved by a seeded uniform
+    random tangent offset of up to ``jitter`` times the mean spacing, then
+    ``lloyd`` Lloyd iterations (every generator moved to the centroid of its
+    cell). The Lloyd steps keep the initial Delaunay triangulation (the
+    points move by a fraction of the spacing, so the fans of incident
+    triangles stay valid to first order) and the final cells come from an
+    exact convex hull of the relaxed generators. Cell vertices are the
+    circumcentres of the Delaunay triangles, shared between cells, listed
+    counter-clockwise seen from outside."""
+    rng = np.random.default_rng(seed)
+    p = _fibonacci_points(n)
+    spacing = np.sqrt(4.0 * np.pi / n)
+    e1, e2 = _tangent_basis(p)
+    r = jitter * spacing * np.sqrt(rng.uniform(0.0, 1.0, n))
+    t = rng.uniform(0.0, 2.0 * np.pi, n)
+    p = p + (r * np.cos(t))[:, None] * e1 + (r * np.sin(t))[:, None] * e2
+    p /= np.linalg.norm(p, axis=1, keepdims=True)
+    if lloyd > 0:
+        tri, cc = _delaunay(p)
+        off, fan = _fans(p, tri, cc)
+        owner = np.repeat(np.arange(n, dtype=np.int64), np.diff(off))
+        nxt = np.arange(fan.shape[0], dtype=np.int64) + 1
+        last = off[1:] - 1
+        nxt[last] = off[:-1]  # wrap around each fan
+        for _ in range(lloyd):
+            a, b = tri[:, 0], tri[:, 1]
+            nrm = np.cross(p[b] - p[a], p[tri[:, 2]] - p[a])
+            cc = nrm / np.linalg.norm(nrm, axis=1, keepdims=True)
+            v0, v1 = cc[fan], cc[fan[nxt]]
+            g = p[owner]
+            w = np.linalg.norm(np.cross(v0 - g, v1 - g), axis=1)  # 2 x planar fan triangle area
+            q = w[:, None] * (g + v0 + v1)
+            cen = np.stack([np.bincount(owner, weights=q[:, d], minlength=n) for d in range(3)], axis=1)
+            p = cen / np.linalg.norm(cen, axis=1, keepdims=True)
+    tri, cc = _delaunay(p)
+    off, fan = _fans(p, tri, cc)
+    node = _xyz_to_lonlat_deg(cc)
+    return MeshArrays(node, off, fan, name=f"voronoi{n}")
+
+
 def cell_centroids_xyz(mesh: MeshArrays) -> np.ndarray:
     """Normalised mean of the unit-sphere vertex vectors of every cell: the
     cap centroid of ``compute_cell_centroid_xyz``

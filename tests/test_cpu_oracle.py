@@ -142,3 +142,17 @@ def test_bilinear_rect_source(oracle):
     rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
     assert np.allclose(rs, 1.0, atol=1e-14)
     assert np.all(w.w >= 0) and np.all(w.col < src.n_cells)
+
+
+def test_voronoi_mesh(oracle):
+    """The spherical Voronoi generator: closed, counter-clockwise cells that
+    tile the sphere, mostly 5- to 7-gons, conservative row sums of 1."""
+    g = grids.voronoi(10242, seed=5, jitter=0.2, lloyd=5)
+    nv = np.diff(g.conn_offsets)
+    assert g.n_cells == 10242 and np.mean((nv >= 5) & (nv <= 7)) > 0.98
+    c = oracle.cell_prep(g)
+    assert np.all(c["degen"] == 0)
+    assert abs(c["area"].sum() / (4 * np.pi) - 1.0) < 1e-12
+    w = oracle.conservative(g, grids.latlon_deg(5.0))
+    rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
+    assert np.all(np.abs(rs - 1.0) < 1e-11)

@@ -45,6 +45,8 @@ PAIRS = [
     ("5deg->C8", lambda: (grids.latlon_deg(5.0), grids.cubed_sphere(8))),
     ("C12->C8", lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8))),
     ("2deg->C96", lambda: (grids.latlon_deg(2.0), grids.cubed_sphere(96))),
+    ("voronoi40962->2deg", lambda: (grids.voronoi(40962, seed=5), grids.latlon_deg(2.0))),
+    ("tripole360x270->1deg", lambda: (grids.tripole(360, 270, seed=4), grids.latlon_deg(1.0))),
 ]
 
 
