@@ -371,6 +371,9 @@ def main():
             result["e2e"] = e2e(M, X, args)
         # ── weight generation for 0.25 deg -> C384 ──
         result["weightgen_0p25_to_c384"] = weightgen_c384(md, dst_g)
+        # ── single-field configurations (1 deg -> C48, 0.25 deg -> C384) ──
+        result["single_field_configs"] = small_configs(o)
+        log("single-field", result["single_field_configs"])
         # ── uneven batch of 17 grid pairs in one persistent launch ──
         result["batch_17_pairs"] = batch_pairs(args)
         log("batch", {k: v for k, v in result["batch_17_pairs"].items() if k not in ("pairs", "nrhs")})
@@ -631,6 +634,79 @@ def batch_pairs(args):
             "weightgen_s": t_gen, "batch_ms": ms_b, "batch_dst_vals_per_s": dst_vals / (ms_b / 1e3),
             "batch_GBps": nbytes / ms_b / 1e6, "per_pair_calls_ms": ms_p, "bitwise_equal_to_per_pair": bool(same),
             "launches": "1 persistent kernel per batch apply, replayed from a CUDA graph"}
+
+
+def small_configs(o):
+    """The single-field configurations: 1 deg -> C48 (weights + one FP64
+    SpMV, against the oracle's weights and output) and 0.25 deg -> C384 (one
+    FP32 field with l <= 64: plain FP64 apply vs split-FP32 apply, errors
+    against the FP64 oracle and conservation). Also times the oracle's
+    faithful (serial, as the reference's loop) weight generation for
+    1 deg -> C48 on one host core."""
+    import torch
+
+    import axgb
+    from axgb import fields, grids
+    out = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def dev_time(fn, reps=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # config 1
+    src, dst = grids.latlon_deg(1.0), grids.cubed_sphere(48)
+    ms, md = axgb.Mesh.from_grid(src), axgb.Mesh.from_grid(dst)
+    M = axgb.generate_weights(ms, md, {"method": "conservative"})
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    M = axgb.generate_weights(ms, md, {"method": "conservative"})
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    wf = o.conservative(src, dst, faithful=True)
+    t_faithful = time.perf_counter() - t0
+    f = fields.sh_field(grids.cell_centroids_xyz(src), 16, seed=1, offset=280.0).numpy()
+    x = torch.tensor(f, device="cuda")
+    y = torch.empty(M.n_dst, dtype=torch.float64, device="cuda")
+    ms1 = dev_time(lambda: axgb.apply_f64(M, x, y))
+    ref = o.apply_csr(wf, f, compensated=True)[0]
+    csr = M.to_csr()
+    rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
+    out["c1_1deg_to_C48"] = {
+        "nnz": M.nnz, "weightgen_s": t_gen, "pairs_per_s": M.nnz / t_gen,
+        "oracle_faithful_weightgen_s_1core": t_faithful,
+        "index_set_identical": bool(M.nnz == wf.nnz and np.array_equal(rows, wf.row)
+                                    and np.array_equal(csr["col"], wf.col)),
+        "spmv_fp64_ms": ms1, "spmv_dst_vals_per_s": M.n_dst / (ms1 / 1e3),
+        "fp64": rel_errors(y.cpu().numpy()[None], ref[None]),
+        "conservation_fp64": axgb.check_conservation(M, x, y)["relative_error"]}
+    # config 2
+    src, dst = grids.latlon_deg(0.25), grids.cubed_sphere(384)
+    M = axgb.generate_weights(axgb.Mesh.from_grid(src), axgb.Mesh.from_grid(dst), {"method": "conservative"})
+    f32 = fields.sh_field(torch.tensor(grids.cell_centroids_xyz(src), device="cuda"), 64, seed=2).to(torch.float32)
+    x32 = f32.view(1, -1).contiguous()
+    x64 = x32.to(torch.float64)
+    y32 = torch.empty((1, M.n_dst), dtype=torch.float32, device="cuda")
+    y64 = torch.empty((1, M.n_dst), dtype=torch.float64, device="cuda")
+    M.prepare(2)
+    axgb.autotune_f32split(M, x32, y32)
+    ms_s = dev_time(lambda: axgb.apply_f32split(M, x32, y32))
+    ms_d = dev_time(lambda: axgb.apply_f64(M, x64, y64))
+    wo = o.conservative(src, dst)
+    ref = o.apply_csr(wo, x64.cpu().numpy(), compensated=True)
+    out["c2_0p25deg_to_C384_one_field"] = {
+        "nnz": M.nnz, "split_ms": ms_s, "fp64_ms": ms_d, "split_speedup": ms_d / ms_s,
+        "split": rel_errors(y32.cpu().numpy(), ref), "fp64": rel_errors(y64.cpu().numpy(), ref),
+        "conservation_split": axgb.check_conservation(M, x32[0], y32[0])["relative_error"],
+        "conservation_fp64": axgb.check_conservation(M, x64[0], y64[0])["relative_error"]}
+    return out
 
 
 def weightgen_c384(md_0p25, latlon_g):

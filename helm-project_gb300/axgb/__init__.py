@@ -373,6 +373,8 @@ def apply_f64(matrix: Matrix, x, y=None, stream=None):
         x = x.view(1, -1)
     if y is None:
         y = torch.empty((x.shape[0], matrix.n_dst), dtype=torch.float64, device=x.device)
+    elif y.dim() == 1:
+        y = y.view(1, -1)
     _check(lib().axgb_apply_f64(matrix.handle, _ptr(x), x.stride(0), _ptr(y), y.stride(0), x.shape[0],
                                 _stream(stream if stream is not None else torch.cuda.current_stream())))
     return y
@@ -387,6 +389,8 @@ def apply_f32split(matrix: Matrix, x, y=None, stream=None, fields_per_pass=None,
         x = x.view(1, -1)
     if y is None:
         y = torch.empty((x.shape[0], matrix.n_dst), dtype=torch.float32, device=x.device)
+    elif y.dim() == 1:
+        y = y.view(1, -1)
     s = _stream(stream if stream is not None else torch.cuda.current_stream())
     if fields_per_pass is None and unroll is None and variant is None:
         _check(lib().axgb_apply_f32split(matrix.handle, _ptr(x), x.stride(0), _ptr(y), y.stride(0), x.shape[0], s))

@@ -229,12 +229,17 @@ __global__ void __launch_bounds__(256) k_f64(SellArgs a, const double *__restric
     }
 }
 
-// ─── long rows: one warp per (row, 32 fields) ─────────────────────────────
+// ─── long rows ─────────────────────────────────────────────────────────────
 // Slices holding rows of more than 32 entries (coarse destination cells over
-// a fine source). A warp takes one row and 32 fields, lane = field; each
-// lane sums its row in entry order with the same steps as the lane-per-row
-// kernels, so results are bitwise the same. Items run field chunk outer and
-// rows inner, so neighbouring warps gather neighbouring source cells.
+// a fine source, e.g. polar cells over a lat-lon source). Rows of more than
+// 32 entries follow the leaf + pairwise-tree order of fp32x2.cuh (rows of at
+// most 32 entries in these slices: entry order), in two forms:
+//   k_split_rows: one warp per (row, 32 fields), lane = field, leaves in
+//                 turn; for many fields.
+//   k_split_coop: one warp per row, lane = leaf, fields in turn; for few
+//                 fields (a single field of a 1500-entry polar row is then
+//                 47 steps per lane instead of 1500 on one lane).
+// Entry k of row p of slice sid sits at base[sid] + 32k + p.
 __device__ __forceinline__ bool row_item(const SellArgs &a, i64 nrhs, i64 &row, int &sid, int &p, i64 &f) {
     const int lane = threadIdx.x & 31;
     const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -249,19 +254,116 @@ __device__ __forceinline__ bool row_item(const SellArgs &a, i64 nrhs, i64 &row, 
     return row < a.n_rows && f < nrhs;
 }
 
+// One lane: the value of a row (n entries at e0 + 32k) for one field.
+__device__ __forceinline__ float row_value_lane(const int *col, const float *hi, const float *lo, int e0, int n,
+                                                const float *xf) {
+    float s = 0.f, c = 0.f;
+    if (n <= 32) {
+        for (int k = 0; k < n; ++k) {
+            const int e = e0 + 32 * k;
+            csum1(s, c, hi[e], lo[e], ldg_f(xf + col[e]));
+        }
+        return __fadd_rn(s, c);
+    }
+    float ss[5], sc[5];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        float ls = 0.f, lc = 0.f;
+        for (int k = j; k < n; k += 32) {
+            const int e = e0 + 32 * k;
+            csum1(ls, lc, hi[e], lo[e], ldg_f(xf + col[e]));
+        }
+        // in-order pairwise tree: fold in the finished left subtrees
+#pragma unroll
+        for (int b = 0; b < 5; ++b) {
+            if (((j >> b) & 1) == 0) {
+                ss[b] = ls;
+                sc[b] = lc;
+                break;
+            }
+            float ts = ss[b], tc = sc[b];
+            lcombine(ts, tc, ls, lc);
+            ls = ts;
+            lc = tc;
+            if (b == 4) {
+                s = ls;
+                c = lc;
+            }
+        }
+    }
+    return __fadd_rn(s, c);
+}
+
 __global__ void __launch_bounds__(256) k_split_rows(SellArgs a, const float *__restrict__ x, i64 ldx,
                                                     float *__restrict__ y, i64 ldy, i64 nrhs) {
     i64 row, f;
     int sid, p;
     if (!row_item(a, nrhs, row, sid, p, f)) return;
-    const int n = a.rlen[row], base = a.base[sid];
-    const float *xf = x + f * ldx;
-    float s = 0.f, cc = 0.f;
-    for (int k = 0; k < n; ++k) {
-        const int e = base + k * 32 + p;  // same address in every lane: one broadcast load
-        csum1(s, cc, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
+    y[f * ldy + row] = row_value_lane(a.col, a.hi, a.lo, a.base[sid] + p, a.rlen[row], x + f * ldx);
+}
+
+// Warp per row, all fields in turn; lane = leaf for rows of more than 32
+// entries, lane 0 alone for shorter rows (entry order).
+__global__ void __launch_bounds__(256) k_split_coop(SellArgs a, const float *__restrict__ x, i64 ldx,
+                                                    float *__restrict__ y, i64 ldy, i64 nrhs) {
+    const int lane = threadIdx.x & 31;
+    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (w >= a.n_ids * 32) return;
+    const int sid = a.ids[w >> 5], p = static_cast<int>(w & 31);
+    const i64 row = static_cast<i64>(sid) * 32 + p;
+    if (row >= a.n_rows) return;
+    const int n = a.rlen[row], e0 = a.base[sid] + p;
+    for (i64 f = 0; f < nrhs; ++f) {
+        const float *xf = x + f * ldx;
+        if (n <= 32) {
+            if (lane == 0) y[f * ldy + row] = row_value_lane(a.col, a.hi, a.lo, e0, n, xf);
+            continue;
+        }
+        float s = 0.f, c = 0.f;
+        for (int k = lane; k < n; k += 32) {
+            const int e = e0 + 32 * k;
+            csum1(s, c, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const float s2 = __shfl_xor_sync(0xffffffffu, s, off), c2 = __shfl_xor_sync(0xffffffffu, c, off);
+            lcombine(s, c, s2, c2);
+        }
+        if (lane == 0) y[f * ldy + row] = __fadd_rn(s, c);
     }
-    y[f * ldy + row] = __fadd_rn(s, cc);
+}
+
+// FP64 long rows: leaves of s = fma(w, x, s), in-order pairwise tree of
+// plain additions (rows of at most 32 entries: entry order).
+__device__ __forceinline__ double row_value_lane64(const int *col, const double *w64, int e0, int n,
+                                                   const double *xf) {
+    double s = 0.0;
+    if (n <= 32) {
+        for (int k = 0; k < n; ++k) {
+            const int e = e0 + 32 * k;
+            s = fma(w64[e], __ldg(xf + col[e]), s);
+        }
+        return s;
+    }
+    double st[5];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        double l = 0.0;
+        for (int k = j; k < n; k += 32) {
+            const int e = e0 + 32 * k;
+            l = fma(w64[e], __ldg(xf + col[e]), l);
+        }
+#pragma unroll
+        for (int b = 0; b < 5; ++b) {
+            if (((j >> b) & 1) == 0) {
+                st[b] = l;
+                break;
+            }
+            l = st[b] + l;
+            if (b == 4) s = l;
+        }
+    }
+    return s;
 }
 
 __global__ void __launch_bounds__(256) k_f64_rows(SellArgs a, const double *__restrict__ x, i64 ldx,
@@ -269,14 +371,33 @@ __global__ void __launch_bounds__(256) k_f64_rows(SellArgs a, const double *__re
     i64 row, f;
     int sid, p;
     if (!row_item(a, nrhs, row, sid, p, f)) return;
-    const int n = a.rlen[row], base = a.base[sid];
-    const double *xf = x + f * ldx;
-    double s = 0.0;
-    for (int k = 0; k < n; ++k) {
-        const int e = base + k * 32 + p;
-        s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
+    y[f * ldy + row] = row_value_lane64(a.col, a.w64, a.base[sid] + p, a.rlen[row], x + f * ldx);
+}
+
+__global__ void __launch_bounds__(256) k_f64_coop(SellArgs a, const double *__restrict__ x, i64 ldx,
+                                                  double *__restrict__ y, i64 ldy, i64 nrhs) {
+    const int lane = threadIdx.x & 31;
+    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (w >= a.n_ids * 32) return;
+    const int sid = a.ids[w >> 5], p = static_cast<int>(w & 31);
+    const i64 row = static_cast<i64>(sid) * 32 + p;
+    if (row >= a.n_rows) return;
+    const int n = a.rlen[row], e0 = a.base[sid] + p;
+    for (i64 f = 0; f < nrhs; ++f) {
+        const double *xf = x + f * ldx;
+        if (n <= 32) {
+            if (lane == 0) y[f * ldy + row] = row_value_lane64(a.col, a.w64, e0, n, xf);
+            continue;
+        }
+        double s = 0.0;
+        for (int k = lane; k < n; k += 32) {
+            const int e = e0 + 32 * k;
+            s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) y[f * ldy + row] = s;
     }
-    y[f * ldy + row] = s;
 }
 
 // ─── layout build ──────────────────────────────────────────────────────────
@@ -423,15 +544,27 @@ void launch_split(const SellArgs &a, const float *x, i64 ldx, float *y, i64 ldy,
         k_split<L, 1><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
 }
 
+// Long-row slices: a warp per row and field chunk with few fields, lane =
+// field with many (same bits either way).
+constexpr i64 kCoopMaxFields = 8;
+
 void launch_split_rows(const SellArgs &a, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    if (a.n_ids == 0 || nrhs == 0) return;
+    if (nrhs <= kCoopMaxFields) {
+        k_split_coop<<<nblk(a.n_ids * 32 * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
+        return;
+    }
     const i64 warps = a.n_ids * 32 * ((nrhs + 31) / 32);
-    if (warps == 0) return;
     k_split_rows<<<nblk(warps * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
 }
 
 void launch_f64_rows(const SellArgs &a, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    if (a.n_ids == 0 || nrhs == 0) return;
+    if (nrhs <= kCoopMaxFields) {
+        k_f64_coop<<<nblk(a.n_ids * 32 * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
+        return;
+    }
     const i64 warps = a.n_ids * 32 * ((nrhs + 31) / 32);
-    if (warps == 0) return;
     k_f64_rows<<<nblk(warps * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
 }
 
@@ -578,24 +711,42 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
         while (m + 1 < n_desc && desc[m + 1].item_begin <= static_cast<i64>(it)) ++m;
         const Batch::Desc &d = desc[m];
         const i64 local = static_cast<i64>(it) - d.item_begin;
-        if (d.mode == 1) {  // long rows: lane = field
-            const i64 per = d.n_ids * 32;
+        if (d.mode == 1) {  // long-row slices, order of fp32x2.cuh
+            if (d.nrhs <= kCoopMaxFields) {  // warp per row: lane = leaf, fields in turn
+                const int sid = d.ids[local >> 5], p = static_cast<int>(local & 31);
+                const i64 row = static_cast<i64>(sid) * 32 + p;
+                if (row >= d.n_rows) continue;
+                const int n = d.rlen[row], e0 = d.base[sid] + p;
+                for (i64 f = 0; f < d.nrhs; ++f) {
+                    const float *xf = d.x + f * d.ldx;
+                    if (n <= 32) {
+                        if (lane == 0) d.y[f * d.ldy + row] = row_value_lane(d.col, d.hi, d.lo, e0, n, xf);
+                        continue;
+                    }
+                    float s = 0.f, c = 0.f;
+                    for (int k = lane; k < n; k += 32) {
+                        const int e = e0 + 32 * k;
+                        csum1(s, c, d.hi[e], d.lo[e], __ldg(xf + d.col[e]));
+                    }
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const float s2 = __shfl_xor_sync(0xffffffffu, s, off);
+                        const float c2 = __shfl_xor_sync(0xffffffffu, c, off);
+                        lcombine(s, c, s2, c2);
+                    }
+                    if (lane == 0) d.y[f * d.ldy + row] = __fadd_rn(s, c);
+                }
+                continue;
+            }
+            const i64 per = d.n_ids * 32;  // lane = field
             const i64 fc = local / per;
             const i64 q = local - fc * per;
             const int sid = d.ids[q >> 5];
             const int p = static_cast<int>(q & 31);
             const i64 row = static_cast<i64>(sid) * 32 + p;
             const i64 f = fc * 32 + lane;
-            if (row < d.n_rows && f < d.nrhs) {
-                const int n = d.rlen[row], base = d.base[sid];
-                const float *xf = d.x + f * d.ldx;
-                float s = 0.f, cc = 0.f;
-                for (int k = 0; k < n; ++k) {
-                    const int e = base + k * 32 + p;
-                    csum1(s, cc, d.hi[e], d.lo[e], __ldg(xf + d.col[e]));
-                }
-                d.y[f * d.ldy + row] = __fadd_rn(s, cc);
-            }
+            if (row < d.n_rows && f < d.nrhs)
+                d.y[f * d.ldy + row] = row_value_lane(d.col, d.hi, d.lo, d.base[sid] + p, d.rlen[row], d.x + f * d.ldx);
             continue;
         }
         const i64 t = local / d.n_ids;
@@ -769,7 +920,9 @@ std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &
             d.nrhs = nrhs[q];
             d.tile = std::max<i64>(1, std::min<i64>(nrhs[q], 8));
             d.n_tiles = (nrhs[q] + d.tile - 1) / d.tile;
-            const i64 n_items = mode == 0 ? d.n_tiles * d.n_ids : d.n_ids * 32 * ((nrhs[q] + 31) / 32);
+            const i64 n_items = mode == 0                      ? d.n_tiles * d.n_ids
+                                : nrhs[q] <= kCoopMaxFields ? d.n_ids * 32
+                                                            : d.n_ids * 32 * ((nrhs[q] + 31) / 32);
             if (n_items == 0) continue;
             d.item_begin = items;
             items += n_items;

@@ -402,7 +402,6 @@ std::vector<std::array<int, 4>> group_slices(i64 nsl, const std::vector<float> &
     for (i64 q = 0; q < nsl; ++q) order[q] = code[q].second;
     std::vector<char> used(nsl, 0);
     constexpr int kWindow = 48;
-    i64 head = 0;
     for (i64 q = 0; q < nsl; ++q) {
         int s = order[q];
         if (used[s]) continue;
@@ -422,7 +421,6 @@ std::vector<std::array<int, 4>> group_slices(i64 nsl, const std::vector<float> &
             used[cand[w].second] = 1;
         }
         groups.push_back(g);
-        (void)head;
     }
     return groups;
 }

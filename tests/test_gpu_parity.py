@@ -291,3 +291,48 @@ def test_long_rows_parity(gpu, oracle):
         B.apply([xs], [yb])
         torch.cuda.synchronize()
         assert np.array_equal(yb.cpu().numpy(), outs[0])
+
+
+def test_one_dimensional_fields(gpu, oracle, cfg1):
+    """1-D x and y (one field) through the device entry points."""
+    import torch
+    src, dst, M, wo, f = cfg1
+    x = torch.tensor(f, device="cuda")
+    y = torch.empty(M.n_dst, dtype=torch.float64, device="cuda")
+    gpu.apply_f64(M, x, y)
+    ref = oracle.apply_csr(wo, f, compensated=True)[0]
+    assert np.max(np.abs(y.cpu().numpy() - ref) / np.abs(ref)) < F64_RTOL
+    y32 = torch.empty(M.n_dst, dtype=torch.float32, device="cuda")
+    gpu.apply_f32split(M, x.to(torch.float32), y32)
+    assert np.max(np.abs(y32.cpu().numpy() - ref) / np.abs(ref)) < SPLIT_RTOL
+
+
+def test_very_long_rows_few_fields(gpu, oracle):
+    """Polar destination cells over a lat-lon source: rows of hundreds of
+    entries. One, three and forty fields (warp-per-row and lane-per-field
+    forms of the long-row order) give the same bits per field, and match
+    the oracle."""
+    import torch
+    src, dst = grids.latlon_deg(1.0), grids.cubed_sphere(6)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    wo = oracle.conservative(src, dst)
+    assert np.diff(wo.row_ptr()).max() > 200
+    rng = np.random.default_rng(9)
+    X = (rng.standard_normal((40, M.n_src)) + 3.0).astype(np.float32)
+    ref = oracle.apply_csr(wo, X.astype(np.float64), compensated=True)
+    xs = torch.tensor(X, device="cuda")
+    y40 = gpu.apply_f32split(M, xs).cpu().numpy()
+    y1 = gpu.apply_f32split(M, xs[:1]).cpu().numpy()
+    y3 = gpu.apply_f32split(M, xs[:3], variant=0, unroll=1, fields_per_pass=0).cpu().numpy()
+    assert np.array_equal(y1, y40[:1]) and np.array_equal(y3, y40[:3])
+    assert np.max(np.abs(y40 - ref) / np.abs(ref)) < SPLIT_RTOL
+    d40 = gpu.apply_f64(M, xs.to(torch.float64)).cpu().numpy()
+    d1 = gpu.apply_f64(M, xs[:1].to(torch.float64)).cpu().numpy()
+    assert np.array_equal(d1, d40[:1])
+    assert np.max(np.abs(d40 - ref) / np.abs(ref)) < F64_RTOL
+    B = gpu.Batch([M, M], [2, 40])
+    yb2 = torch.empty((2, M.n_dst), dtype=torch.float32, device="cuda")
+    yb40 = torch.empty((40, M.n_dst), dtype=torch.float32, device="cuda")
+    B.apply([xs[:2], xs], [yb2, yb40])
+    torch.cuda.synchronize()
+    assert np.array_equal(yb2.cpu().numpy(), y40[:2]) and np.array_equal(yb40.cpu().numpy(), y40)
