@@ -165,7 +165,7 @@ def reference_arm(args):
     gen_s = time.perf_counter() - t0
     xyz = grids.cell_centroids_xyz(src)
     base = fields.sh_fields(xyz, 32, [2024]).numpy()[0]
-    sample = 16
+    sample = 64
     rng = np.random.default_rng(2024)
     X = np.stack([base * s for s in rng.lognormal(0, 1, sample)]).astype(np.float32).astype(np.float64)
     for _ in range(args.warmup):
@@ -408,7 +408,7 @@ def axgb_launches(M, variant):
 
 def profiled_traffic():
     """Per-step DRAM bytes of the apply from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "apply_split_c768_0p25_1016rhs.md")
+    p = os.path.join(ROOT, "profiles", "apply_split_blk_chunk_c768_0p25.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
