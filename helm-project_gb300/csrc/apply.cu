@@ -29,15 +29,18 @@
 namespace axgb {
 
 struct Batch {
-    // One descriptor per (matrix, slice kind): mode 0 covers the slices whose
-    // rows have at most 32 entries (lane per row, items = field tile x
-    // slice), mode 1 the slices with longer rows (warp per row and 32
-    // fields, items = field chunk x row).
+    // One descriptor per (matrix, kind): mode 0 covers the slices whose rows
+    // have at most 32 entries (lane per row, items = field tile x slice);
+    // mode 1 the rows of at most 32 entries of the other slices (lane per
+    // field, items = 32-field chunk x row); mode 2 the rows of more than 32
+    // entries (lane per leaf, items = 8-field chunk x row).
     struct Desc {
         const int *base, *len, *rlen, *col;
         const float *hi, *lo;
-        const int *ids;  // slice ids
-        i64 n_ids;
+        const int *lrow, *lptr, *lcol;  // mode 2: row-contiguous long rows
+        const float *lhi, *llo;
+        const int *ids;  // slice ids (modes 0, 1)
+        i64 n_ids;       // slices (modes 0, 1) or long rows (mode 2)
         int mode;
         int mat;  // index of the matrix in the batch
         i64 n_rows, n_slices;
@@ -230,15 +233,15 @@ __global__ void __launch_bounds__(256) k_f64(SellArgs a, const double *__restric
 }
 
 // ─── long rows ─────────────────────────────────────────────────────────────
-// Slices holding rows of more than 32 entries (coarse destination cells over
-// a fine source, e.g. polar cells over a lat-lon source). Rows of more than
-// 32 entries follow the leaf + pairwise-tree order of fp32x2.cuh (rows of at
-// most 32 entries in these slices: entry order), in two forms:
-//   k_split_rows: one warp per (row, 32 fields), lane = field, leaves in
-//                 turn; for many fields.
-//   k_split_coop: one warp per row, lane = leaf, fields in turn; for few
-//                 fields (a single field of a 1500-entry polar row is then
-//                 47 steps per lane instead of 1500 on one lane).
+// Slices in the long classes (some row has more than 32 entries; coarse
+// destination cells over a fine source, e.g. polar cells over a lat-lon
+// source) run in two launches:
+//   k_split_rows: rows of at most 32 entries of those slices, one warp per
+//                 (row, 32 fields), lane = field, entry order;
+//   k_split_long: rows of more than 32 entries, one warp per (row, F
+//                 fields), lane = leaf of the order in fp32x2.cuh, the F
+//                 fields carried side by side, entries read row-contiguous
+//                 (Sell::lcol/lhi/llo), shuffle butterfly at the end.
 // Entry k of row p of slice sid sits at base[sid] + 32k + p.
 __device__ __forceinline__ bool row_item(const SellArgs &a, i64 nrhs, i64 &row, int &sid, int &p, i64 &f) {
     const int lane = threadIdx.x & 31;
@@ -254,116 +257,21 @@ __device__ __forceinline__ bool row_item(const SellArgs &a, i64 nrhs, i64 &row, 
     return row < a.n_rows && f < nrhs;
 }
 
-// One lane: the value of a row (n entries at e0 + 32k) for one field.
-__device__ __forceinline__ float row_value_lane(const int *col, const float *hi, const float *lo, int e0, int n,
-                                                const float *xf) {
-    float s = 0.f, c = 0.f;
-    if (n <= 32) {
-        for (int k = 0; k < n; ++k) {
-            const int e = e0 + 32 * k;
-            csum1(s, c, hi[e], lo[e], ldg_f(xf + col[e]));
-        }
-        return __fadd_rn(s, c);
-    }
-    float ss[5], sc[5];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        float ls = 0.f, lc = 0.f;
-        for (int k = j; k < n; k += 32) {
-            const int e = e0 + 32 * k;
-            csum1(ls, lc, hi[e], lo[e], ldg_f(xf + col[e]));
-        }
-        // in-order pairwise tree: fold in the finished left subtrees
-#pragma unroll
-        for (int b = 0; b < 5; ++b) {
-            if (((j >> b) & 1) == 0) {
-                ss[b] = ls;
-                sc[b] = lc;
-                break;
-            }
-            float ts = ss[b], tc = sc[b];
-            lcombine(ts, tc, ls, lc);
-            ls = ts;
-            lc = tc;
-            if (b == 4) {
-                s = ls;
-                c = lc;
-            }
-        }
-    }
-    return __fadd_rn(s, c);
-}
-
 __global__ void __launch_bounds__(256) k_split_rows(SellArgs a, const float *__restrict__ x, i64 ldx,
                                                     float *__restrict__ y, i64 ldy, i64 nrhs) {
     i64 row, f;
     int sid, p;
     if (!row_item(a, nrhs, row, sid, p, f)) return;
-    y[f * ldy + row] = row_value_lane(a.col, a.hi, a.lo, a.base[sid] + p, a.rlen[row], x + f * ldx);
-}
-
-// Warp per row, all fields in turn; lane = leaf for rows of more than 32
-// entries, lane 0 alone for shorter rows (entry order).
-__global__ void __launch_bounds__(256) k_split_coop(SellArgs a, const float *__restrict__ x, i64 ldx,
-                                                    float *__restrict__ y, i64 ldy, i64 nrhs) {
-    const int lane = threadIdx.x & 31;
-    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (w >= a.n_ids * 32) return;
-    const int sid = a.ids[w >> 5], p = static_cast<int>(w & 31);
-    const i64 row = static_cast<i64>(sid) * 32 + p;
-    if (row >= a.n_rows) return;
-    const int n = a.rlen[row], e0 = a.base[sid] + p;
-    for (i64 f = 0; f < nrhs; ++f) {
-        const float *xf = x + f * ldx;
-        if (n <= 32) {
-            if (lane == 0) y[f * ldy + row] = row_value_lane(a.col, a.hi, a.lo, e0, n, xf);
-            continue;
-        }
-        float s = 0.f, c = 0.f;
-        for (int k = lane; k < n; k += 32) {
-            const int e = e0 + 32 * k;
-            csum1(s, c, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
-        }
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const float s2 = __shfl_xor_sync(0xffffffffu, s, off), c2 = __shfl_xor_sync(0xffffffffu, c, off);
-            lcombine(s, c, s2, c2);
-        }
-        if (lane == 0) y[f * ldy + row] = __fadd_rn(s, c);
+    const int n = a.rlen[row];
+    if (n > 32) return;  // k_split_long
+    const int e0 = a.base[sid] + p;
+    const float *xf = x + f * ldx;
+    float s = 0.f, c = 0.f;
+    for (int k = 0; k < n; ++k) {
+        const int e = e0 + 32 * k;
+        csum1(s, c, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
     }
-}
-
-// FP64 long rows: leaves of s = fma(w, x, s), in-order pairwise tree of
-// plain additions (rows of at most 32 entries: entry order).
-__device__ __forceinline__ double row_value_lane64(const int *col, const double *w64, int e0, int n,
-                                                   const double *xf) {
-    double s = 0.0;
-    if (n <= 32) {
-        for (int k = 0; k < n; ++k) {
-            const int e = e0 + 32 * k;
-            s = fma(w64[e], __ldg(xf + col[e]), s);
-        }
-        return s;
-    }
-    double st[5];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        double l = 0.0;
-        for (int k = j; k < n; k += 32) {
-            const int e = e0 + 32 * k;
-            l = fma(w64[e], __ldg(xf + col[e]), l);
-        }
-#pragma unroll
-        for (int b = 0; b < 5; ++b) {
-            if (((j >> b) & 1) == 0) {
-                st[b] = l;
-                break;
-            }
-            l = st[b] + l;
-            if (b == 4) s = l;
-        }
-    }
-    return s;
+    y[f * ldy + row] = __fadd_rn(s, c);
 }
 
 __global__ void __launch_bounds__(256) k_f64_rows(SellArgs a, const double *__restrict__ x, i64 ldx,
@@ -371,32 +279,118 @@ __global__ void __launch_bounds__(256) k_f64_rows(SellArgs a, const double *__re
     i64 row, f;
     int sid, p;
     if (!row_item(a, nrhs, row, sid, p, f)) return;
-    y[f * ldy + row] = row_value_lane64(a.col, a.w64, a.base[sid] + p, a.rlen[row], x + f * ldx);
+    const int n = a.rlen[row];
+    if (n > 32) return;  // k_f64_long
+    const int e0 = a.base[sid] + p;
+    const double *xf = x + f * ldx;
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const int e = e0 + 32 * k;
+        s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
+    }
+    y[f * ldy + row] = s;
 }
 
-__global__ void __launch_bounds__(256) k_f64_coop(SellArgs a, const double *__restrict__ x, i64 ldx,
+struct LongRows {
+    const int *row, *ptr, *col;
+    const float *hi, *lo;
+    const double *w64;
+    i64 n;
+};
+constexpr int kLongF = 8;  // fields per warp in the long-row kernels
+
+// Warp w: long row w % n, fields [F*(w / n), ...). Lane j sums entries
+// j, j+32, ... of the row for each of the F fields (leaves), then a
+// butterfly over lane offsets 1..16 combines the leaves; lane f stores
+// field f.
+__device__ __forceinline__ void split_long_row(const LongRows &L, i64 w, const float *x, i64 ldx, float *y,
+                                               i64 ldy, i64 nrhs) {
+    const int lane = threadIdx.x & 31;
+    const i64 i = w % L.n, fc = w / L.n;
+    const i64 row = L.row[i];
+    const int b = L.ptr[i], n = L.ptr[i + 1] - b;
+    const i64 f0 = fc * kLongF;
+    const int nf = static_cast<int>(nrhs - f0 < kLongF ? nrhs - f0 : kLongF);
+    float s[kLongF], c[kLongF];
+#pragma unroll
+    for (int f = 0; f < kLongF; ++f) {
+        s[f] = 0.f;
+        c[f] = 0.f;
+    }
+    for (int k = lane; k < n; k += 32) {
+        const int col = L.col[b + k];
+        const float h = L.hi[b + k], l = L.lo[b + k];
+#pragma unroll
+        for (int f = 0; f < kLongF; ++f)
+            if (f < nf) csum1(s[f], c[f], h, l, ldg_f(x + (f0 + f) * ldx + col));
+    }
+#pragma unroll
+    for (int f = 0; f < kLongF; ++f) {
+        if (f < nf) {  // warp-uniform
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const float s2 = __shfl_xor_sync(0xffffffffu, s[f], off);
+                const float c2 = __shfl_xor_sync(0xffffffffu, c[f], off);
+                lcombine(s[f], c[f], s2, c2);
+            }
+            if (lane == f) y[(f0 + f) * ldy + row] = __fadd_rn(s[f], c[f]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_split_long(LongRows L, const float *__restrict__ x, i64 ldx,
+                                                    float *__restrict__ y, i64 ldy, i64 nrhs) {
+    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (w >= L.n * ((nrhs + kLongF - 1) / kLongF)) return;
+    split_long_row(L, w, x, ldx, y, ldy, nrhs);
+}
+
+__global__ void __launch_bounds__(256) k_f64_long(LongRows L, const double *__restrict__ x, i64 ldx,
                                                   double *__restrict__ y, i64 ldy, i64 nrhs) {
     const int lane = threadIdx.x & 31;
     const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (w >= a.n_ids * 32) return;
-    const int sid = a.ids[w >> 5], p = static_cast<int>(w & 31);
-    const i64 row = static_cast<i64>(sid) * 32 + p;
-    if (row >= a.n_rows) return;
-    const int n = a.rlen[row], e0 = a.base[sid] + p;
-    for (i64 f = 0; f < nrhs; ++f) {
-        const double *xf = x + f * ldx;
-        if (n <= 32) {
-            if (lane == 0) y[f * ldy + row] = row_value_lane64(a.col, a.w64, e0, n, xf);
-            continue;
-        }
-        double s = 0.0;
-        for (int k = lane; k < n; k += 32) {
-            const int e = e0 + 32 * k;
-            s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
-        }
+    if (w >= L.n * ((nrhs + kLongF - 1) / kLongF)) return;
+    const i64 i = w % L.n, fc = w / L.n;
+    const i64 row = L.row[i];
+    const int b = L.ptr[i], n = L.ptr[i + 1] - b;
+    const i64 f0 = fc * kLongF;
+    const int nf = static_cast<int>(nrhs - f0 < kLongF ? nrhs - f0 : kLongF);
+    double s[kLongF];
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
-        if (lane == 0) y[f * ldy + row] = s;
+    for (int f = 0; f < kLongF; ++f) s[f] = 0.0;
+    for (int k = lane; k < n; k += 32) {
+        const int col = L.col[b + k];
+        const double wv = L.w64[b + k];
+#pragma unroll
+        for (int f = 0; f < kLongF; ++f)
+            if (f < nf) s[f] = fma(wv, __ldg(x + (f0 + f) * ldx + col), s[f]);
+    }
+#pragma unroll
+    for (int f = 0; f < kLongF; ++f) {
+        if (f < nf) {
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) s[f] = s[f] + __shfl_xor_sync(0xffffffffu, s[f], off);
+            if (lane == f) y[(f0 + f) * ldy + row] = s[f];
+        }
+    }
+}
+
+// Row-contiguous copy of the long rows' entries (in the layout's order).
+__global__ void k_long_fill(const int *rp, const int *ccol, const double *val, const int *perm, const int *lrow,
+                            const int *lptr, i64 n_lrows, int *lcol, float *lhi, float *llo, double *lw64) {
+    const i64 i = blockIdx.x;
+    if (i >= n_lrows) return;
+    const int r = lrow[i], r0 = rp[r], b = lptr[i], n = lptr[i + 1] - b;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int src = perm ? perm[r0 + k] : r0 + k;
+        const double w = val[src];
+        lcol[b + k] = ccol[src];
+        if (lhi) {
+            const float h = __double2float_rn(w);
+            lhi[b + k] = h;
+            llo[b + k] = __double2float_rn(w - static_cast<double>(h));
+        }
+        if (lw64) lw64[b + k] = w;
     }
 }
 
@@ -506,6 +500,35 @@ void build_sell(Matrix &m, int fmt, cudaStream_t s) {
         ids.insert(ids.end(), cls[c].begin(), cls[c].end());
     }
     S.class_begin[5] = static_cast<i64>(ids.size());
+    // rows of more than 32 entries, row-contiguous
+    {
+        std::vector<int> rp(n_rows + 1);
+        AXGB_CUDA(cudaMemcpy(rp.data(), m.row_ptr.p, sizeof(int) * (n_rows + 1), cudaMemcpyDeviceToHost));
+        std::vector<int> lrow, lptr(1, 0);
+        for (i64 r = 0; r < n_rows; ++r)
+            if (rp[r + 1] - rp[r] > 32) {
+                lrow.push_back(static_cast<int>(r));
+                lptr.push_back(lptr.back() + rp[r + 1] - rp[r]);
+            }
+        S.n_lrows = static_cast<i64>(lrow.size());
+        S.lrow.upload_vec(lrow, s);
+        S.lptr.upload_vec(lptr, s);
+        const size_t ne = std::max<size_t>(1, lptr.back());
+        S.lcol.alloc(ne);
+        if (fmt == 1) {
+            S.lhi.alloc(ne);
+            S.llo.alloc(ne);
+        } else {
+            S.lw64.alloc(ne);
+        }
+        if (S.n_lrows > 0) {
+            const int *perm = (fmt == 1 && m.split_perm.p) ? m.split_perm.p : nullptr;
+            k_long_fill<<<static_cast<unsigned>(S.n_lrows), 128, 0, s>>>(
+                m.row_ptr.p, m.col.p, m.val.p, perm, S.lrow.p, S.lptr.p, S.n_lrows, S.lcol.p,
+                fmt == 1 ? S.lhi.p : nullptr, fmt == 1 ? S.llo.p : nullptr, fmt == 0 ? S.lw64.p : nullptr);
+            AXGB_CUDA(cudaGetLastError());
+        }
+    }
     S.class_ids.upload(ids.data(), ids.size(), s);
     S.h_slice_len.resize(n_slices);
     for (i64 q = 0; q < n_slices; ++q) S.h_slice_len[q] = h_len[q] / 32;
@@ -544,28 +567,39 @@ void launch_split(const SellArgs &a, const float *x, i64 ldx, float *y, i64 ldy,
         k_split<L, 1><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
 }
 
-// Long-row slices: a warp per row and field chunk with few fields, lane =
-// field with many (same bits either way).
-constexpr i64 kCoopMaxFields = 8;
+LongRows long_rows(const Sell &S) {
+    LongRows L;
+    L.row = S.lrow.p;
+    L.ptr = S.lptr.p;
+    L.col = S.lcol.p;
+    L.hi = S.lhi.p;
+    L.lo = S.llo.p;
+    L.w64 = S.lw64.p;
+    L.n = S.n_lrows;
+    return L;
+}
 
+// Slices of the long classes: their short rows (k_*_rows), then every row
+// of more than 32 entries (k_*_long).
 void launch_split_rows(const SellArgs &a, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
     if (a.n_ids == 0 || nrhs == 0) return;
-    if (nrhs <= kCoopMaxFields) {
-        k_split_coop<<<nblk(a.n_ids * 32 * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
-        return;
-    }
     const i64 warps = a.n_ids * 32 * ((nrhs + 31) / 32);
     k_split_rows<<<nblk(warps * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
 }
-
+void launch_split_long(const Sell &S, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    if (S.n_lrows == 0 || nrhs == 0) return;
+    const i64 warps = S.n_lrows * ((nrhs + kLongF - 1) / kLongF);
+    k_split_long<<<nblk(warps * 32, 256), 256, 0, s>>>(long_rows(S), x, ldx, y, ldy, nrhs);
+}
 void launch_f64_rows(const SellArgs &a, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s) {
     if (a.n_ids == 0 || nrhs == 0) return;
-    if (nrhs <= kCoopMaxFields) {
-        k_f64_coop<<<nblk(a.n_ids * 32 * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
-        return;
-    }
     const i64 warps = a.n_ids * 32 * ((nrhs + 31) / 32);
     k_f64_rows<<<nblk(warps * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+void launch_f64_long(const Sell &S, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    if (S.n_lrows == 0 || nrhs == 0) return;
+    const i64 warps = S.n_lrows * ((nrhs + kLongF - 1) / kLongF);
+    k_f64_long<<<nblk(warps * 32, 256), 256, 0, s>>>(long_rows(S), x, ldx, y, ldy, nrhs);
 }
 
 template <int L>
@@ -711,42 +745,39 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
         while (m + 1 < n_desc && desc[m + 1].item_begin <= static_cast<i64>(it)) ++m;
         const Batch::Desc &d = desc[m];
         const i64 local = static_cast<i64>(it) - d.item_begin;
-        if (d.mode == 1) {  // long-row slices, order of fp32x2.cuh
-            if (d.nrhs <= kCoopMaxFields) {  // warp per row: lane = leaf, fields in turn
-                const int sid = d.ids[local >> 5], p = static_cast<int>(local & 31);
-                const i64 row = static_cast<i64>(sid) * 32 + p;
-                if (row >= d.n_rows) continue;
-                const int n = d.rlen[row], e0 = d.base[sid] + p;
-                for (i64 f = 0; f < d.nrhs; ++f) {
-                    const float *xf = d.x + f * d.ldx;
-                    if (n <= 32) {
-                        if (lane == 0) d.y[f * d.ldy + row] = row_value_lane(d.col, d.hi, d.lo, e0, n, xf);
-                        continue;
-                    }
-                    float s = 0.f, c = 0.f;
-                    for (int k = lane; k < n; k += 32) {
-                        const int e = e0 + 32 * k;
-                        csum1(s, c, d.hi[e], d.lo[e], __ldg(xf + d.col[e]));
-                    }
-#pragma unroll
-                    for (int off = 1; off < 32; off <<= 1) {
-                        const float s2 = __shfl_xor_sync(0xffffffffu, s, off);
-                        const float c2 = __shfl_xor_sync(0xffffffffu, c, off);
-                        lcombine(s, c, s2, c2);
-                    }
-                    if (lane == 0) d.y[f * d.ldy + row] = __fadd_rn(s, c);
-                }
-                continue;
-            }
-            const i64 per = d.n_ids * 32;  // lane = field
+        if (d.mode == 2) {  // rows of more than 32 entries
+            LongRows L;
+            L.row = d.lrow;
+            L.ptr = d.lptr;
+            L.col = d.lcol;
+            L.hi = d.lhi;
+            L.lo = d.llo;
+            L.w64 = nullptr;
+            L.n = d.n_ids;
+            split_long_row(L, local, d.x, d.ldx, d.y, d.ldy, d.nrhs);
+            continue;
+        }
+        if (d.mode == 1) {  // short rows of long-class slices: lane = field
+            const i64 per = d.n_ids * 32;
             const i64 fc = local / per;
             const i64 q = local - fc * per;
             const int sid = d.ids[q >> 5];
             const int p = static_cast<int>(q & 31);
             const i64 row = static_cast<i64>(sid) * 32 + p;
             const i64 f = fc * 32 + lane;
-            if (row < d.n_rows && f < d.nrhs)
-                d.y[f * d.ldy + row] = row_value_lane(d.col, d.hi, d.lo, d.base[sid] + p, d.rlen[row], d.x + f * d.ldx);
+            if (row < d.n_rows && f < d.nrhs) {
+                const int n = d.rlen[row];
+                if (n <= 32) {
+                    const int e0 = d.base[sid] + p;
+                    const float *xf = d.x + f * d.ldx;
+                    float s = 0.f, c = 0.f;
+                    for (int k = 0; k < n; ++k) {
+                        const int e = e0 + 32 * k;
+                        csum1(s, c, d.hi[e], d.lo[e], __ldg(xf + d.col[e]));
+                    }
+                    d.y[f * d.ldy + row] = __fadd_rn(s, c);
+                }
+            }
             continue;
         }
         const i64 t = local / d.n_ids;
@@ -820,6 +851,7 @@ void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs
             a.n_ids = B.n_fallback;
             launch_split_rows(a, x, ldx, y, ldy, nrhs, s);
         }
+        launch_split_long(m.sell32, x, ldx, y, ldy, nrhs, s);
         AXGB_CUDA(cudaGetLastError());
         return;
     }
@@ -832,6 +864,7 @@ void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs
     launch_split<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, unroll, s);
     launch_split_rows(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, s);
     launch_split_rows(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, s);
+    launch_split_long(S, x, ldx, y, ldy, nrhs, s);
     AXGB_CUDA(cudaGetLastError());
 }
 
@@ -845,6 +878,7 @@ void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs
     launch_f64<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, s);
     launch_f64_rows(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, s);
     launch_f64_rows(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, s);
+    launch_f64_long(S, x, ldx, y, ldy, nrhs, s);
     AXGB_CUDA(cudaGetLastError());
 }
 
@@ -901,8 +935,8 @@ std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &
         Matrix &m = *mats[q];
         matrix_prepare(m, 1, 0);
         const Sell &S = m.sell32;
-        for (int mode = 0; mode < 2; ++mode) {
-            // classes 0..2: rows of at most 32 entries; 3..4: longer rows
+        for (int mode = 0; mode < 3; ++mode) {
+            // classes 0..2: slices of rows of at most 32 entries; 3..4: the others
             const i64 c0 = S.class_begin[mode == 0 ? 0 : 3], c1 = S.class_begin[mode == 0 ? 3 : 5];
             Batch::Desc d{};
             d.base = S.base.p;
@@ -911,8 +945,13 @@ std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &
             d.col = S.col.p;
             d.hi = S.hi.p;
             d.lo = S.lo.p;
+            d.lrow = S.lrow.p;
+            d.lptr = S.lptr.p;
+            d.lcol = S.lcol.p;
+            d.lhi = S.lhi.p;
+            d.llo = S.llo.p;
             d.ids = S.class_ids.p + c0;
-            d.n_ids = c1 - c0;
+            d.n_ids = mode == 2 ? S.n_lrows : c1 - c0;
             d.mode = mode;
             d.mat = static_cast<int>(q);
             d.n_rows = m.n_dst;
@@ -920,9 +959,9 @@ std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &
             d.nrhs = nrhs[q];
             d.tile = std::max<i64>(1, std::min<i64>(nrhs[q], 8));
             d.n_tiles = (nrhs[q] + d.tile - 1) / d.tile;
-            const i64 n_items = mode == 0                      ? d.n_tiles * d.n_ids
-                                : nrhs[q] <= kCoopMaxFields ? d.n_ids * 32
-                                                            : d.n_ids * 32 * ((nrhs[q] + 31) / 32);
+            const i64 n_items = mode == 0   ? d.n_tiles * d.n_ids
+                                : mode == 1 ? d.n_ids * 32 * ((nrhs[q] + 31) / 32)
+                                            : d.n_ids * ((nrhs[q] + kLongF - 1) / kLongF);
             if (n_items == 0) continue;
             d.item_begin = items;
             items += n_items;

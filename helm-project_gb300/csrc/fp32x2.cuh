@@ -103,14 +103,14 @@ __device__ __forceinline__ void cstep2i(F2 &s, F2 &cn, F2 h, F2 l, F2 x) {
 }
 
 // ─── rows longer than 32 entries ──────────────────────────────────────────
-// Canonical order for a row of n > 32 entries: leaf j (j = 0..31) sums
-// entries j, j+32, j+64, ... in order with csum1; the 32 leaves are then
-// combined by an in-order pairwise tree (leaves 2m and 2m+1 first, and so
-// on) with lcombine; the row value is s + c of the root. The warp-parallel
-// form (lane = leaf, shuffle butterfly over lane offsets 1, 2, ..., 16) and
-// the one-lane form (leaves in turn, a five-deep stack) give the same bits:
-// TwoSum's error is exact in either operand order and the other additions
-// are commutative. Rows of at most 32 entries are summed in entry order.
+// Order for a row of n > 32 entries: leaf j (j = 0..31) sums entries j,
+// j+32, j+64, ... in order with csum1; the 32 leaves are combined by an
+// in-order pairwise tree (leaves 2m and 2m+1 first, and so on) with
+// lcombine; the row value is s + c of the root. Computed with lane = leaf
+// and a shuffle butterfly over lane offsets 1, 2, ..., 16: every lane ends
+// with the root, since TwoSum's error is exact in either operand order and
+// the other additions are commutative. Rows of at most 32 entries are
+// summed in entry order.
 __device__ __forceinline__ void lcombine(float &s, float &c, float s2, float c2) {
     const float t = __fadd_rn(s, s2);
     const float bp = __fsub_rn(t, s);

@@ -154,6 +154,12 @@ struct Sell {
     DBuf<int> class_ids;
     std::vector<int> class_maxlen;
     std::vector<int> h_slice_len;  // entries per row slot of each slice
+    // Rows of more than 32 entries, row-contiguous in the layout's entry
+    // order (for the warp-per-row kernels): row ids, offsets, entries.
+    i64 n_lrows = 0;
+    DBuf<int> lrow, lptr, lcol;
+    DBuf<float> lhi, llo;   // format 1
+    DBuf<double> lw64;      // format 0
 };
 
 // Blocked split-FP32 layout (staged.cu). Rows are grouped in blocks of up to
