@@ -484,7 +484,10 @@ def voronoi_main(args):
     xyz = torch.tensor(grids.cell_centroids_xyz(src_g), device=dev)
     base = fields.sh_fields(xyz, 256, [7000 + k for k in range(8)], chunk=1 << 20)
     scales = np.random.default_rng(7000).lognormal(0.0, 1.0, size=(8, 8))
-    X = torch.empty((nrhs, M.n_src), dtype=torch.float32, device=dev)
+    # leading dimension padded to a multiple of 4 floats (16-byte aligned field
+    # starts, which the shared-memory staged kernels need; n_src = 2,621,442)
+    ld = (M.n_src + 3) // 4 * 4
+    X = torch.empty((nrhs, ld), dtype=torch.float32, device=dev)[:, :M.n_src]
     for k in range(8):
         sc = torch.tensor(scales[k], dtype=torch.float64, device=dev)
         X[8 * k:8 * k + 8] = (base[k][None, :] * sc[:, None]).to(torch.float32)
@@ -633,7 +636,9 @@ def batch_pairs(args):
     return {"pairs": [p[0] for p in pairs], "nrhs": nrhs, "nnz_total": int(sum(M.nnz for M in mats)),
             "weightgen_s": t_gen, "batch_ms": ms_b, "batch_dst_vals_per_s": dst_vals / (ms_b / 1e3),
             "batch_GBps": nbytes / ms_b / 1e6, "per_pair_calls_ms": ms_p, "bitwise_equal_to_per_pair": bool(same),
-            "launches": "1 persistent kernel per batch apply, replayed from a CUDA graph"}
+            "launches": "one CUDA graph per batch apply: a persistent staged kernel per row-length class "
+                        "(work queue over the blocks of all pairs) and one persistent direct kernel for "
+                        "the slices the staged layout leaves out and the rows of more than 32 entries"}
 
 
 def small_configs(o):

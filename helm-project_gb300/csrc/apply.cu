@@ -60,6 +60,11 @@ struct Batch {
     DBuf<unsigned long long> counter;
     i64 total_items = 0;
     int blocks = 0;
+    // matrices whose fields take the persistent staged kernels (blocked
+    // layout) in the current plan, and that plan
+    std::vector<char> use;
+    bool planned = false;
+    std::shared_ptr<BlkBatch> blk;
     // graph per stream, replayed while descriptors are updated in place
     std::map<cudaStream_t, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
     std::vector<const void *> last_ptrs;
@@ -930,14 +935,30 @@ std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &
     auto b = std::make_shared<Batch>();
     b->mats = mats;
     b->nrhs = nrhs;
+    for (auto &m : mats) matrix_prepare(*m, 2, 0);
+    int dev = 0, sms = 0;
+    AXGB_CUDA(cudaGetDevice(&dev));
+    AXGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int per_sm = 0;
+    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0));
+    b->blocks = std::max(1, sms * std::max(1, per_sm));
+    b->counter.alloc(1);
+    return b;
+}
+
+namespace {
+
+// Work of the direct persistent kernel: for a matrix on the staged kernels,
+// the slices the blocked layout leaves out (their rows of at most 32
+// entries) and the rows of more than 32 entries; for the others, all of it.
+void plan_direct(Batch &b) {
+    b.desc.clear();
     i64 items = 0;
-    for (size_t q = 0; q < mats.size(); ++q) {
-        Matrix &m = *mats[q];
-        matrix_prepare(m, 1, 0);
+    for (size_t q = 0; q < b.mats.size(); ++q) {
+        Matrix &m = *b.mats[q];
         const Sell &S = m.sell32;
+        const i64 k = b.nrhs[q];
         for (int mode = 0; mode < 3; ++mode) {
-            // classes 0..2: slices of rows of at most 32 entries; 3..4: the others
-            const i64 c0 = S.class_begin[mode == 0 ? 0 : 3], c1 = S.class_begin[mode == 0 ? 3 : 5];
             Batch::Desc d{};
             d.base = S.base.p;
             d.len = nullptr;
@@ -950,61 +971,90 @@ std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &
             d.lcol = S.lcol.p;
             d.lhi = S.lhi.p;
             d.llo = S.llo.p;
-            d.ids = S.class_ids.p + c0;
-            d.n_ids = mode == 2 ? S.n_lrows : c1 - c0;
             d.mode = mode;
             d.mat = static_cast<int>(q);
             d.n_rows = m.n_dst;
             d.n_slices = S.n_slices;
-            d.nrhs = nrhs[q];
-            d.tile = std::max<i64>(1, std::min<i64>(nrhs[q], 8));
-            d.n_tiles = (nrhs[q] + d.tile - 1) / d.tile;
+            d.nrhs = k;
+            d.tile = std::max<i64>(1, std::min<i64>(k, 8));
+            d.n_tiles = (k + d.tile - 1) / d.tile;
+            if (mode == 2) {
+                d.n_ids = S.n_lrows;
+            } else if (b.use[q]) {
+                if (mode == 0) continue;
+                d.ids = m.blocked.fallback_slices.p;  // classes of the blocked layout's left-out slices
+                d.n_ids = m.blocked.n_fallback;
+            } else {
+                // classes 0..2: slices of rows of at most 32 entries; 3..4: the others
+                const i64 c0 = S.class_begin[mode == 0 ? 0 : 3], c1 = S.class_begin[mode == 0 ? 3 : 5];
+                d.ids = S.class_ids.p + c0;
+                d.n_ids = c1 - c0;
+            }
             const i64 n_items = mode == 0   ? d.n_tiles * d.n_ids
-                                : mode == 1 ? d.n_ids * 32 * ((nrhs[q] + 31) / 32)
-                                            : d.n_ids * ((nrhs[q] + kLongF - 1) / kLongF);
+                                : mode == 1 ? d.n_ids * 32 * ((k + 31) / 32)
+                                            : d.n_ids * ((k + kLongF - 1) / kLongF);
             if (n_items == 0) continue;
             d.item_begin = items;
             items += n_items;
-            b->desc.push_back(d);
+            b.desc.push_back(d);
         }
     }
-    b->total_items = items;
-    b->d_desc.alloc(std::max<size_t>(1, b->desc.size()));
-    b->counter.alloc(1);
-    int dev = 0, sms = 0;
-    AXGB_CUDA(cudaGetDevice(&dev));
-    AXGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    int per_sm = 0;
-    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0));
-    b->blocks = std::max(1, sms * std::max(1, per_sm));
-    return b;
+    b.total_items = items;
+    b.d_desc.alloc(std::max<size_t>(1, b.desc.size()));
 }
 
+void drop_graphs(Batch &b) {
+    for (auto &g : b.graphs) {
+        cudaGraphExecDestroy(g.second.second);
+        cudaGraphDestroy(g.second.first);
+    }
+    b.graphs.clear();
+}
+
+}  // namespace
+
+// Stream-ordered. The first call (and a call whose fields change which
+// matrices can use the staged kernels) plans the work and captures a CUDA
+// graph per stream; later calls update the field pointers in the device
+// descriptors the graph reads and replay it.
 void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *y, const i64 *ldy, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(b.mu);
-    const size_t k = b.desc.size();
+    const size_t nm = b.mats.size();
     std::vector<const void *> ptrs;
-    for (size_t q = 0; q < b.mats.size(); ++q) {
+    std::vector<char> use(nm, 0);
+    for (size_t q = 0; q < nm; ++q) {
         AXGB_REQUIRE(ldx[q] >= b.mats[q]->n_src && ldy[q] >= b.mats[q]->n_dst, "batch_apply: leading dimension");
         ptrs.push_back(x[q]);
         ptrs.push_back(y[q]);
         ptrs.push_back(reinterpret_cast<const void *>(ldx[q]));
         ptrs.push_back(reinterpret_cast<const void *>(ldy[q]));
+        use[q] = (b.nrhs[q] > 0 && b.mats[q]->blocked.built && blocked_eligible(*b.mats[q], x[q], ldx[q])) ? 1 : 0;
+    }
+    if (!b.planned || use != b.use) {
+        b.use = use;
+        plan_direct(b);
+        std::vector<Matrix *> raw;
+        for (auto &m : b.mats) raw.push_back(m.get());
+        b.blk = blk_batch_create(raw, b.nrhs, b.use);
+        drop_graphs(b);
+        b.last_ptrs.clear();
+        b.planned = true;
     }
     if (ptrs != b.last_ptrs) {
-        for (size_t q = 0; q < k; ++q) {
-            const int mi = b.desc[q].mat;
-            b.desc[q].x = x[mi];
-            b.desc[q].ldx = ldx[mi];
-            b.desc[q].y = y[mi];
-            b.desc[q].ldy = ldy[mi];
+        for (auto &d : b.desc) {
+            d.x = x[d.mat];
+            d.ldx = ldx[d.mat];
+            d.y = y[d.mat];
+            d.ldy = ldy[d.mat];
         }
         // stream-ordered update of the descriptors the graph reads
-        AXGB_CUDA(cudaMemcpyAsync(b.d_desc.p, b.desc.data(), sizeof(Batch::Desc) * k, cudaMemcpyHostToDevice, s));
+        if (!b.desc.empty())
+            AXGB_CUDA(cudaMemcpyAsync(b.d_desc.p, b.desc.data(), sizeof(Batch::Desc) * b.desc.size(),
+                                      cudaMemcpyHostToDevice, s));
+        blk_batch_set_fields(*b.blk, x, ldx, y, ldy, s);
         AXGB_CUDA(cudaStreamSynchronize(s));
         b.last_ptrs = ptrs;
     }
-    if (b.total_items == 0) return;
     auto it = b.graphs.find(s);
     if (it == b.graphs.end()) {
         cudaStream_t cap = s;
@@ -1016,8 +1066,12 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
         cudaGraph_t g;
         cudaGraphExec_t ge;
         AXGB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        cudaMemsetAsync(b.counter.p, 0, sizeof(unsigned long long), cap);
-        k_batch<<<b.blocks, 256, 0, cap>>>(b.d_desc.p, static_cast<int>(k), b.total_items, b.counter.p);
+        blk_batch_launch(*b.blk, cap);
+        if (b.total_items > 0) {
+            cudaMemsetAsync(b.counter.p, 0, sizeof(unsigned long long), cap);
+            k_batch<<<b.blocks, 256, 0, cap>>>(b.d_desc.p, static_cast<int>(b.desc.size()), b.total_items,
+                                                b.counter.p);
+        }
         AXGB_CUDA(cudaStreamEndCapture(cap, &g));
         AXGB_CUDA(cudaGraphInstantiate(&ge, g, 0));
         if (own) AXGB_CUDA(cudaStreamDestroy(cap));

@@ -249,6 +249,14 @@ bool blocked_eligible(const Matrix &m, const void *x, i64 ldx);
 void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, int ns,
                    i64 fchunk, cudaStream_t s);
 int blocked_launches(const Matrix &m);
+// persistent staged kernels over the blocked layouts of several matrices
+// (batches); use[q] selects the matrices whose fields allow the staged kernels
+struct BlkBatch;
+std::shared_ptr<BlkBatch> blk_batch_create(const std::vector<Matrix *> &mats, const std::vector<i64> &nrhs,
+                                           const std::vector<char> &use);
+void blk_batch_set_fields(BlkBatch &bb, const float *const *x, const i64 *ldx, float *const *y, const i64 *ldy,
+                          cudaStream_t s);
+void blk_batch_launch(BlkBatch &bb, cudaStream_t s);
 void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s);
 
 // scan_sort.cu: device primitives (own implementations)

@@ -22,6 +22,8 @@
 #include <algorithm>
 #include <array>
 #include <cstdint>
+#include <map>
+#include <memory>
 #include <thread>
 
 #include "fp32x2.cuh"
@@ -240,15 +242,15 @@ __device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, 
     }
 }
 
+// One work item: block b for the fields of x/y (nrhs of them), staged T
+// fields at a time through NS shared-memory buffers of US floats per field.
 template <int L, int T, int NS, int US>
-__global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__restrict__ x, i64 ldx,
-                                                    float *__restrict__ y, i64 ldy, i64 nrhs) {
+__device__ __forceinline__ void blk_item(const BlkArgs &a, int b, const float *__restrict__ x, i64 ldx,
+                                         float *__restrict__ y, i64 ldy, i64 nrhs, float *smem) {
     static_assert(T % 2 == 0, "fields per stage must be even");
     static_assert(NS == 2 || NS == 3, "two or three staging buffers");
-    extern __shared__ __align__(128) float smem[];
-    float *xs = smem;                                    // [NS][T][US]
+    float *xs = smem;                                       // [NS][T][US]
     int *cc = reinterpret_cast<int *>(smem + NS * T * US);  // chunk columns
-    const int b = item_setup(a, x, ldx, y, ldy, nrhs);
     const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
     const int zero = 4 * nch;
     for (int j = threadIdx.x; j < nch; j += kRows) cc[j] = a.ccol[c0 + j];
@@ -285,6 +287,54 @@ __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__r
         __syncthreads();          // ... for every thread, and tile t-1 is no longer read
         stage(t + NS - 1);        // refill the buffer tile t-1 used
         reduce_tile_c<L, T, US>(xs + (t % NS) * T * US, li, h, lw, wl, t * T, nrhs, row, y, ldy);
+    }
+    cp_async_wait<0>();
+}
+
+template <int L, int T, int NS, int US>
+__global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__restrict__ x, i64 ldx,
+                                                    float *__restrict__ y, i64 ldy, i64 nrhs) {
+    extern __shared__ __align__(128) float smem[];
+    const int b = item_setup(a, x, ldx, y, ldy, nrhs);
+    blk_item<L, T, NS, US>(a, b, x, ldx, y, ldy, nrhs, smem);
+}
+
+// ─── persistent form for batches of matrices ───────────────────────────────
+// One descriptor per (matrix, row-length class): the class's blocks of that
+// matrix and its fields. Items (descriptor, field chunk, block) are handed
+// out by an atomic counter; each CTA loops until the counter passes the
+// total, so blocks of all matrices of the class share one launch.
+struct BlkDesc {
+    BlkArgs a;  // a.blocks / a.nbl: the class's blocks; a.fchunk: fields per item
+    const float *x;
+    i64 ldx;
+    float *y;
+    i64 ldy;
+    i64 nrhs;
+    i64 item_begin;
+};
+
+template <int L, int T, int NS, int US>
+__global__ void __launch_bounds__(kRows) k_blk_persist(const BlkDesc *__restrict__ d, int nd, i64 total,
+                                                      unsigned long long *counter) {
+    extern __shared__ __align__(128) float smem[];
+    __shared__ long long s_item;
+    while (true) {
+        if (threadIdx.x == 0) s_item = static_cast<long long>(atomicAdd(counter, 1ull));
+        __syncthreads();
+        const i64 it = s_item;
+        __syncthreads();  // every thread has read s_item
+        if (it >= total) return;
+        int q = 0;
+        while (q + 1 < nd && d[q + 1].item_begin <= it) ++q;
+        const BlkDesc &D = d[q];
+        const i64 local = it - D.item_begin;
+        const i64 chunk = local / D.a.nbl;
+        const int b = D.a.blocks[local - chunk * D.a.nbl];
+        const i64 f0 = chunk * D.a.fchunk;
+        const i64 n = D.nrhs - f0 < D.a.fchunk ? D.nrhs - f0 : D.a.fchunk;
+        blk_item<L, T, NS, US>(D.a, b, D.x + f0 * D.ldx, D.ldx, D.y + f0 * D.ldy, D.ldy, n, smem);
+        __syncthreads();  // shared memory is reused by the next item
     }
 }
 
@@ -786,6 +836,144 @@ void launch_class(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns,
 }
 
 }  // namespace
+
+// ─── batches ────────────────────────────────────────────────────────────────
+namespace {
+
+constexpr int kBatchT = 4, kBatchNS = 2;
+constexpr i64 kBatchFChunk = 32;  // fields per work item
+
+BlkArgs blk_args(const Blocked &B, const Blocked::Launch &l) {
+    BlkArgs a{};
+    a.nbl = l.n;
+    a.blocks = B.block_ids.p + l.begin;
+    a.brow = B.brow.p;
+    a.wbase = B.wbase.p;
+    a.wlen = B.wlen.p;
+    a.lidx = B.lidx.p;
+    a.hi = B.hi.p;
+    a.lo = B.lo.p;
+    a.cstart = B.cstart.p;
+    a.ccol = B.ccol.p;
+    a.rstart = B.rstart.p;
+    a.runs = B.runs.p;
+    a.us = l.us;
+    a.status = B.status.p;
+    return a;
+}
+
+template <int L, int US>
+void persist_launch(const BlkDesc *d, int nd, i64 total, unsigned long long *counter, cudaStream_t s) {
+    constexpr size_t bytes = sizeof(float) * US * kBatchNS * kBatchT + sizeof(int) * (US / 4);
+    auto k = k_blk_persist<L, kBatchT, kBatchNS, US>;
+    AXGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+    int dev = 0, sms = 0, per = 0;
+    AXGB_CUDA(cudaGetDevice(&dev));
+    AXGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kRows, bytes));
+    const i64 grid = std::min<i64>(total, static_cast<i64>(sms) * std::max(1, per));
+    k<<<static_cast<unsigned>(grid), kRows, bytes, s>>>(d, nd, total, counter);
+}
+
+template <int US>
+void persist_dispatch(int L, const BlkDesc *d, int nd, i64 total, unsigned long long *counter, cudaStream_t s) {
+    switch (L) {
+        case 4: persist_launch<4, US>(d, nd, total, counter, s); break;
+        case 8: persist_launch<8, US>(d, nd, total, counter, s); break;
+        case 12: persist_launch<12, US>(d, nd, total, counter, s); break;
+        case 16: persist_launch<16, US>(d, nd, total, counter, s); break;
+        case 20: persist_launch<20, US>(d, nd, total, counter, s); break;
+        case 24: persist_launch<24, US>(d, nd, total, counter, s); break;
+        case 28: persist_launch<28, US>(d, nd, total, counter, s); break;
+        default: persist_launch<32, US>(d, nd, total, counter, s); break;
+    }
+}
+
+}  // namespace
+
+struct BlkBatch {
+    struct Group {
+        int L = 0, us = 0;
+        std::vector<std::pair<int, int>> parts;  // (matrix index, launch index)
+        std::vector<BlkDesc> desc;
+        DBuf<BlkDesc> d_desc;
+        DBuf<unsigned long long> counter;
+        i64 total = 0;
+    };
+    std::vector<Matrix *> mats;
+    std::vector<i64> nrhs;
+    std::vector<Group> groups;
+};
+
+std::shared_ptr<BlkBatch> blk_batch_create(const std::vector<Matrix *> &mats, const std::vector<i64> &nrhs,
+                                           const std::vector<char> &use) {
+    auto bb = std::make_shared<BlkBatch>();
+    bb->mats = mats;
+    bb->nrhs = nrhs;
+    std::map<std::pair<int, int>, int> gi;
+    for (size_t q = 0; q < mats.size(); ++q) {
+        if (!use[q] || nrhs[q] <= 0) continue;
+        const Blocked &B = mats[q]->blocked;
+        for (size_t li = 0; li < B.launches.size(); ++li) {
+            const Blocked::Launch &l = B.launches[li];
+            if (l.n == 0) continue;
+            auto key = std::make_pair(l.L, l.us);
+            auto it = gi.find(key);
+            if (it == gi.end()) {
+                it = gi.emplace(key, static_cast<int>(bb->groups.size())).first;
+                bb->groups.emplace_back();
+                bb->groups.back().L = l.L;
+                bb->groups.back().us = l.us;
+            }
+            bb->groups[it->second].parts.push_back({static_cast<int>(q), static_cast<int>(li)});
+        }
+    }
+    for (auto &g : bb->groups) {
+        g.d_desc.alloc(g.parts.size());
+        g.counter.alloc(1);
+        g.desc.resize(g.parts.size());
+        i64 items = 0;
+        for (size_t i = 0; i < g.parts.size(); ++i) {
+            const int q = g.parts[i].first;
+            const Blocked &B = mats[q]->blocked;
+            BlkDesc &D = g.desc[i];
+            D.a = blk_args(B, B.launches[g.parts[i].second]);
+            D.a.fchunk = std::min<i64>(kBatchFChunk, nrhs[q]);
+            D.nrhs = nrhs[q];
+            D.item_begin = items;
+            items += D.a.nbl * ((nrhs[q] + D.a.fchunk - 1) / D.a.fchunk);
+        }
+        g.total = items;
+    }
+    return bb;
+}
+
+void blk_batch_set_fields(BlkBatch &bb, const float *const *x, const i64 *ldx, float *const *y, const i64 *ldy,
+                          cudaStream_t s) {
+    for (auto &g : bb.groups) {
+        for (size_t i = 0; i < g.parts.size(); ++i) {
+            const int q = g.parts[i].first;
+            g.desc[i].x = x[q];
+            g.desc[i].ldx = ldx[q];
+            g.desc[i].y = y[q];
+            g.desc[i].ldy = ldy[q];
+        }
+        AXGB_CUDA(cudaMemcpyAsync(g.d_desc.p, g.desc.data(), sizeof(BlkDesc) * g.desc.size(), cudaMemcpyHostToDevice,
+                                  s));
+    }
+}
+
+void blk_batch_launch(BlkBatch &bb, cudaStream_t s) {
+    for (auto &g : bb.groups) {
+        if (g.total == 0) continue;
+        AXGB_CUDA(cudaMemsetAsync(g.counter.p, 0, sizeof(unsigned long long), s));
+        if (g.us <= 1024)
+            persist_dispatch<1024>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
+        else
+            persist_dispatch<3072>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
+    }
+    AXGB_CUDA(cudaGetLastError());
+}
 
 void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, int ns,
                    i64 fchunk, cudaStream_t s) {
