@@ -298,7 +298,7 @@ def main():
         "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload, "n_src": M.n_src, "n_dst": M.n_dst, "nnz": M.nnz, "nrhs": nrhs,
-                   "kernel": tuned, "l2": f"inputs {4 * M.n_src * nrhs / 1e9:.1f} GB per step > L2",
+                   "kernel": tuned, "source_renumbered": M.stats()["source_renumbered"], "l2": f"inputs {4 * M.n_src * nrhs / 1e9:.1f} GB per step > L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic() if nrhs == NRHS else None,
@@ -494,7 +494,13 @@ def voronoi_main(args):
     del base
     Y = torch.empty((nrhs, M.n_dst), dtype=torch.float32, device=dev)
     M.prepare(2)
-    tuned = axgb.autotune_f32split(M, X, Y)
+    if args.kernel:
+        v, fpp, un, stg = (int(t) for t in args.kernel.split(","))
+        tuned = {"variant": v, "fields_per_pass": fpp, "unroll": un, "stages": stg}
+        axgb.set_kernel_choice(M, nrhs, **tuned)
+    else:
+        tuned = axgb.autotune_f32split(M, X, Y)
+    log(f"kernel: {tuned}")
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -513,6 +519,9 @@ def voronoi_main(args):
     clk.start()
     ms_split = timed(lambda: axgb.apply_f32split(M, X, Y, stream=stream))
     clocks = clk.stop()
+    if args.apply_only:
+        log(f"split {ms_split:.3f} ms")
+        return 0
     X64 = X.to(torch.float64)
     Y64 = torch.empty((nrhs, M.n_dst), dtype=torch.float64, device=dev)
     M.prepare(0)
@@ -542,6 +551,7 @@ def voronoi_main(args):
         "config": {"workload": "spherical Voronoi 2,621,442 cells (5 Lloyd iterations) -> 0.1deg lat-lon "
                                "6,480,000 cells, conservative, split-FP32 SpMM, 64 RHS",
                    "n_src": M.n_src, "n_dst": M.n_dst, "nnz": M.nnz, "nrhs": nrhs, "kernel": tuned,
+                   "source_renumbered": M.stats()["source_renumbered"],
                    "l2": f"inputs {4 * M.n_src * nrhs / 1e9:.2f} GB per step > L2", "parallelism": "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_kind": peak_kind, "bytes_per_step": bytes_split},

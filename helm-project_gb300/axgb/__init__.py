@@ -295,8 +295,8 @@ class Matrix:
         tm = np.zeros(8)
         _check(lib().axgb_matrix_stats(self.handle, _ptr(st), _ptr(tm)))
         return dict(bvh_candidates=int(st[0]), gated_pairs=int(st[1]), fallback_clips=int(st[2]), nnz=int(st[3]),
-                    bvh_nodes=int(st[4]), t_prep_ms=tm[0], t_bvh_ms=tm[1], t_search_ms=tm[2], t_clip_ms=tm[3],
-                    t_assemble_ms=tm[4], t_total_ms=tm[5])
+                    bvh_nodes=int(st[4]), source_renumbered=bool(st[7]), t_prep_ms=tm[0], t_bvh_ms=tm[1],
+                    t_search_ms=tm[2], t_clip_ms=tm[3], t_assemble_ms=tm[4], t_total_ms=tm[5])
 
     def prepare(self, fmt: int):
         _check(lib().axgb_matrix_prepare(self.handle, fmt))

@@ -259,7 +259,7 @@ SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i6
     std::vector<SplitParams> cands;
     for (int t : {4, 8})
         for (int ns : {2, 3})
-            for (int fc : {0, 128, 64, 32})
+            for (int fc : {0, 128, 64, 32, 16, 8})
                 if (t <= std::max<i64>(2, nrhs) && (fc == 0 || fc < nrhs)) cands.push_back({1, fc, t, ns});
     cands.push_back({2, 64, 4, 2});
     std::vector<i64> tiles = {nrhs};
@@ -582,7 +582,10 @@ int axgb_generate_weights_c(int src, int dst, int method, int *mat) {
 int axgb_matrix_stats(int h, int64_t *stats, double *times_ms) {
     AXGB_TRY({
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
-        if (stats) std::copy(m->stats, m->stats + 8, stats);
+        if (stats) {
+            std::copy(m->stats, m->stats + 8, stats);
+            stats[7] = m->src_renum ? 1 : 0;
+        }
         if (times_ms) std::copy(m->times_ms, m->times_ms + 8, times_ms);
     });
 }

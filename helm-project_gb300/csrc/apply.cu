@@ -28,6 +28,16 @@
 
 namespace axgb {
 
+// Arguments of the source gather of a batch member (renumbered sources).
+struct GatherDesc {
+    const float *x;
+    i64 ldx;
+    const int *inv;
+    i64 n, nrhs;
+    float *xr;
+    i64 ldr;
+};
+
 struct Batch {
     // One descriptor per (matrix, kind): mode 0 covers the slices whose rows
     // have at most 32 entries (lane per row, items = field tile x slice);
@@ -65,6 +75,10 @@ struct Batch {
     std::vector<char> use;
     bool planned = false;
     std::shared_ptr<BlkBatch> blk;
+    // members with renumbered sources: fields gathered into xr first
+    std::vector<DBuf<float>> xr;
+    std::vector<GatherDesc> gdesc;
+    DBuf<GatherDesc> d_gdesc;
     // graph per stream, replayed while descriptors are updated in place
     std::map<cudaStream_t, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
     std::vector<const void *> last_ptrs;
@@ -479,7 +493,8 @@ void build_sell(Matrix &m, int fmt, cudaStream_t s) {
     }
     if (n_slices > 0) {
         const int *perm = (fmt == 1 && m.split_perm.p) ? m.split_perm.p : nullptr;
-        k_sell_fill<<<nblk(n_slices * 32, 256), 256, 0, s>>>(m.row_ptr.p, m.col.p, m.val.p, perm, n_rows, n_slices,
+        const int *ccol = (fmt == 1 && m.src_renum) ? m.split_col.p : m.col.p;
+        k_sell_fill<<<nblk(n_slices * 32, 256), 256, 0, s>>>(m.row_ptr.p, ccol, m.val.p, perm, n_rows, n_slices,
                                                             S.base.p, slen32.p, rlen.p, S.col.p,
                                                             fmt == 1 ? S.hi.p : nullptr, fmt == 1 ? S.lo.p : nullptr,
                                                             fmt == 0 ? S.w64.p : nullptr);
@@ -528,8 +543,9 @@ void build_sell(Matrix &m, int fmt, cudaStream_t s) {
         }
         if (S.n_lrows > 0) {
             const int *perm = (fmt == 1 && m.split_perm.p) ? m.split_perm.p : nullptr;
+            const int *ccol = (fmt == 1 && m.src_renum) ? m.split_col.p : m.col.p;
             k_long_fill<<<static_cast<unsigned>(S.n_lrows), 128, 0, s>>>(
-                m.row_ptr.p, m.col.p, m.val.p, perm, S.lrow.p, S.lptr.p, S.n_lrows, S.lcol.p,
+                m.row_ptr.p, ccol, m.val.p, perm, S.lrow.p, S.lptr.p, S.n_lrows, S.lcol.p,
                 fmt == 1 ? S.lhi.p : nullptr, fmt == 1 ? S.llo.p : nullptr, fmt == 0 ? S.lw64.p : nullptr);
             AXGB_CUDA(cudaGetLastError());
         }
@@ -843,10 +859,63 @@ void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
     }
 }
 
+namespace {
+// xr[f][j] = x[f][inv[j]]: fields into the split layouts' source numbering.
+__global__ void k_gather_src(const float *__restrict__ x, i64 ldx, const int *__restrict__ inv, i64 n, i64 nrhs,
+                             float *__restrict__ xr, i64 ldr) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const i64 f = blockIdx.y;
+    if (j >= n || f >= nrhs) return;
+    xr[f * ldr + j] = __ldg(x + f * ldx + inv[j]);
+}
+}  // namespace
+
+// Same for a batch member: arguments read from device memory, so a captured
+// graph picks up new field pointers.
+__global__ void k_gather_desc(const GatherDesc *__restrict__ g) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const GatherDesc d = *g;
+    if (j >= d.n) return;
+    for (i64 f = blockIdx.y; f < d.nrhs; f += gridDim.y) d.xr[f * d.ldr + j] = __ldg(d.x + f * d.ldx + d.inv[j]);
+}
+
+i64 renum_ld(const Matrix &m) { return (m.n_src + 3) / 4 * 4; }
+
+void gather_source(const Matrix &m, const float *x, i64 ldx, i64 nrhs, float *xr, cudaStream_t s) {
+    for (i64 f0 = 0; f0 < nrhs; f0 += 65535) {
+        const i64 nf = std::min<i64>(65535, nrhs - f0);
+        dim3 grid(nblk(m.n_src, 256), static_cast<unsigned>(nf));
+        k_gather_src<<<grid, 256, 0, s>>>(x + f0 * ldx, ldx, m.src_inv.p, m.n_src, nf, xr + f0 * renum_ld(m),
+                                           renum_ld(m));
+    }
+    AXGB_CUDA(cudaGetLastError());
+}
+
+void apply_split_layouts(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
+                         cudaStream_t s);
+
+// A renumbered matrix first gathers the fields into stream-ordered scratch
+// (cudaMallocAsync, freed on the same stream after the apply).
 void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
                  cudaStream_t s) {
     if (nrhs <= 0) return;
-    if (p.variant >= 1 && blocked_eligible(m, x, ldx)) {
+    if (!m.blocked.built) matrix_prepare(m, 2, s);
+    if (!m.src_renum) {
+        apply_split_layouts(m, x, ldx, y, ldy, nrhs, p, s);
+        return;
+    }
+    const i64 ldr = renum_ld(m);
+    float *xr = nullptr;
+    AXGB_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&xr), sizeof(float) * static_cast<size_t>(ldr * nrhs), s));
+    gather_source(m, x, ldx, nrhs, xr, s);
+    apply_split_layouts(m, xr, ldr, y, ldy, nrhs, p, s);
+    AXGB_CUDA(cudaFreeAsync(xr, s));
+}
+
+void apply_split_layouts(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
+                         cudaStream_t s) {
+    if (nrhs <= 0) return;
+    if (p.variant >= 1 && blocked_eligible(m, x, ldx, p.variant == 2)) {
         if (!m.blocked.built) matrix_prepare(m, 2, s);
         apply_blocked(m, x, ldx, y, ldy, nrhs, p.variant == 2, p.unroll, p.stages, p.fields_per_pass, s);
         const Blocked &B = m.blocked;
@@ -1022,13 +1091,30 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
     const size_t nm = b.mats.size();
     std::vector<const void *> ptrs;
     std::vector<char> use(nm, 0);
+    // members with renumbered sources read their fields from b.xr (gathered first)
+    if (b.xr.size() != nm) b.xr.resize(nm);
+    std::vector<const float *> ex(nm);
+    std::vector<i64> eld(nm);
     for (size_t q = 0; q < nm; ++q) {
-        AXGB_REQUIRE(ldx[q] >= b.mats[q]->n_src && ldy[q] >= b.mats[q]->n_dst, "batch_apply: leading dimension");
+        const Matrix &m = *b.mats[q];
+        AXGB_REQUIRE(ldx[q] >= m.n_src && ldy[q] >= m.n_dst, "batch_apply: leading dimension");
         ptrs.push_back(x[q]);
         ptrs.push_back(y[q]);
         ptrs.push_back(reinterpret_cast<const void *>(ldx[q]));
         ptrs.push_back(reinterpret_cast<const void *>(ldy[q]));
-        use[q] = (b.nrhs[q] > 0 && b.mats[q]->blocked.built && blocked_eligible(*b.mats[q], x[q], ldx[q])) ? 1 : 0;
+        if (m.src_renum) {
+            const size_t need = static_cast<size_t>(std::max<i64>(1, renum_ld(m) * b.nrhs[q]));
+            if (b.xr[q].n < need) {
+                b.xr[q].alloc(need);
+                b.planned = false;  // new scratch address: re-plan and re-capture
+            }
+            ex[q] = b.xr[q].p;
+            eld[q] = renum_ld(m);
+        } else {
+            ex[q] = x[q];
+            eld[q] = ldx[q];
+        }
+        use[q] = (b.nrhs[q] > 0 && m.blocked.built && blocked_eligible(m, ex[q], eld[q], false)) ? 1 : 0;
     }
     if (!b.planned || use != b.use) {
         b.use = use;
@@ -1042,16 +1128,24 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
     }
     if (ptrs != b.last_ptrs) {
         for (auto &d : b.desc) {
-            d.x = x[d.mat];
-            d.ldx = ldx[d.mat];
+            d.x = ex[d.mat];
+            d.ldx = eld[d.mat];
             d.y = y[d.mat];
             d.ldy = ldy[d.mat];
         }
+        b.gdesc.clear();
+        for (size_t q = 0; q < nm; ++q)
+            if (b.mats[q]->src_renum && b.nrhs[q] > 0)
+                b.gdesc.push_back({x[q], ldx[q], b.mats[q]->src_inv.p, b.mats[q]->n_src, b.nrhs[q], b.xr[q].p, eld[q]});
+        if (b.d_gdesc.n < b.gdesc.size()) b.d_gdesc.alloc(b.gdesc.size());
         // stream-ordered update of the descriptors the graph reads
         if (!b.desc.empty())
             AXGB_CUDA(cudaMemcpyAsync(b.d_desc.p, b.desc.data(), sizeof(Batch::Desc) * b.desc.size(),
                                       cudaMemcpyHostToDevice, s));
-        blk_batch_set_fields(*b.blk, x, ldx, y, ldy, s);
+        if (!b.gdesc.empty())
+            AXGB_CUDA(cudaMemcpyAsync(b.d_gdesc.p, b.gdesc.data(), sizeof(GatherDesc) * b.gdesc.size(),
+                                      cudaMemcpyHostToDevice, s));
+        blk_batch_set_fields(*b.blk, ex.data(), eld.data(), y, ldy, s);
         AXGB_CUDA(cudaStreamSynchronize(s));
         b.last_ptrs = ptrs;
     }
@@ -1066,6 +1160,11 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
         cudaGraph_t g;
         cudaGraphExec_t ge;
         AXGB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        for (size_t i = 0; i < b.gdesc.size(); ++i) {  // renumbered members: gather their fields first
+            const GatherDesc &g = b.gdesc[i];
+            dim3 grid(nblk(g.n, 256), static_cast<unsigned>(std::min<i64>(g.nrhs, 65535)));
+            k_gather_desc<<<grid, 256, 0, cap>>>(b.d_gdesc.p + i);
+        }
         blk_batch_launch(*b.blk, cap);
         if (b.total_items > 0) {
             cudaMemsetAsync(b.counter.p, 0, sizeof(unsigned long long), cap);

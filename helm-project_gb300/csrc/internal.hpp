@@ -176,6 +176,7 @@ struct Blocked {
     };
     bool built = false;
     i64 n_blocks = 0;
+    i64 n_src = 0;  // source cells of the matrix (bounds the last staged chunk)
     DBuf<int> brow, wbase, wlen, cstart, ccol, rstart, block_ids, fallback_slices;
     DBuf<int4> runs;  // (global col of first chunk, chunks, staging offset, 0)
     DBuf<unsigned short> lidx;
@@ -218,6 +219,13 @@ struct Matrix {
     // against shared-memory bank conflicts and shared by every split layout,
     // so all split kernels sum in the same order (same bits).
     DBuf<int> split_perm;
+    // Source renumbering of the split layouts (chosen by the blocked build
+    // when the source cells' own numbering scatters each block's sources
+    // over many 16-byte chunks): split_col holds the renumbered column of
+    // every CSR entry, src_inv the original cell of every new index. A split
+    // apply first gathers the fields into the new order.
+    bool src_renum = false;
+    DBuf<int> split_col, src_inv;
     std::vector<float> slice_xyz;  // mean unit vector of each 32-row slice (locality hint), may be empty
     std::map<i64, SplitParams> tuned;  // nrhs -> best kernel choice
     std::mutex mu;
@@ -245,7 +253,7 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
 
 // staged.cu
 void build_blocked(Matrix &m, cudaStream_t s);
-bool blocked_eligible(const Matrix &m, const void *x, i64 ldx);
+bool blocked_eligible(const Matrix &m, const void *x, i64 ldx, bool bulk);
 void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, int ns,
                    i64 fchunk, cudaStream_t s);
 int blocked_launches(const Matrix &m);

@@ -63,6 +63,12 @@ __device__ __forceinline__ unsigned smem_u32(const void *p) {
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
 }
+// 16-byte copy of which only the first `bytes` come from global memory; the
+// rest of the 16 shared-memory bytes is zero-filled.
+__device__ __forceinline__ void cp_async16_part(void *smem, const void *gmem, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem), "r"(bytes)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -107,6 +113,7 @@ struct BlkArgs {
     int *status;
     i64 nbl;                   // blocks in this launch
     i64 fchunk;                // fields per work item (multiple of the stage width)
+    i64 n_src;                 // source cells: the last chunk may be partial
 };
 
 // Work item of this CTA: (field chunk, block), chunk-major so that all CTAs
@@ -273,9 +280,16 @@ __device__ __forceinline__ void blk_item(const BlkArgs &a, int b, const float *_
             const float *xt = x + fa * ldx;
             for (int j = threadIdx.x; j < nch; j += kRows) {
                 const float *src = xt + cc[j];
+                const i64 left = a.n_src - cc[j];  // the chunk of the last source cells may be partial
+                if (left >= 4) {
 #pragma unroll
-                for (int f = 0; f < T; ++f)
-                    if (f < nf) cp_async16(dst + f * US + 4 * j, src + f * ldx);
+                    for (int f = 0; f < T; ++f)
+                        if (f < nf) cp_async16(dst + f * US + 4 * j, src + f * ldx);
+                } else {
+#pragma unroll
+                    for (int f = 0; f < T; ++f)
+                        if (f < nf) cp_async16_part(dst + f * US + 4 * j, src + f * ldx, static_cast<int>(4 * left));
+                }
             }
         }
         cp_async_commit();
@@ -580,6 +594,44 @@ void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s) {
     AXGB_CUDA(cudaStreamSynchronize(s));
 }
 
+// Source renumbering: new index = rank of first use when the rows are read
+// in order (unused cells last, in their own order). Adopted when it cuts the
+// 16-byte chunks the 128-row groups of consecutive rows touch by more than
+// 1.5x; then col is rewritten in place and the renumbering uploaded.
+void plan_source_order(Matrix &m, const std::vector<int> &rp, std::vector<int> &col, cudaStream_t s) {
+    const i64 n = m.n_dst, nnz = m.nnz, ns = m.n_src;
+    m.src_renum = false;
+    if (nnz == 0 || ns == 0) return;
+    std::vector<int> rank(ns, -1);
+    int next = 0;
+    for (i64 e = 0; e < nnz; ++e)
+        if (rank[col[e]] < 0) rank[col[e]] = next++;
+    for (i64 c = 0; c < ns; ++c)
+        if (rank[c] < 0) rank[c] = next++;
+    i64 ch0 = 0, ch1 = 0;
+    std::vector<int> a, b;
+    for (i64 r0 = 0; r0 < n; r0 += kRows) {
+        const i64 e0 = rp[r0], e1 = rp[std::min<i64>(n, r0 + kRows)];
+        a.clear();
+        b.clear();
+        for (i64 e = e0; e < e1; ++e) {
+            a.push_back(col[e] >> 2);
+            b.push_back(rank[col[e]] >> 2);
+        }
+        std::sort(a.begin(), a.end());
+        std::sort(b.begin(), b.end());
+        ch0 += std::unique(a.begin(), a.end()) - a.begin();
+        ch1 += std::unique(b.begin(), b.end()) - b.begin();
+    }
+    if (ch0 <= ch1 + ch1 / 2) return;
+    std::vector<int> inv(ns);
+    for (i64 c = 0; c < ns; ++c) inv[rank[c]] = static_cast<int>(c);
+    for (i64 e = 0; e < nnz; ++e) col[e] = rank[col[e]];
+    m.src_inv.upload_vec(inv, s);
+    m.split_col.upload_vec(col, s);
+    m.src_renum = true;
+}
+
 void build_blocked(Matrix &m, cudaStream_t s) {
     Blocked &B = m.blocked;
     if (B.built) return;
@@ -592,6 +644,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
         AXGB_CUDA(cudaMemcpy(col.data(), m.col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
         AXGB_CUDA(cudaMemcpy(val.data(), m.val.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost));
     }
+    plan_source_order(m, rp, col, s);  // columns below are in the split layouts' numbering
     auto groups = group_slices(nsl, m.slice_xyz);
     const i64 nb = static_cast<i64>(groups.size());
     std::vector<HostBlock> hb(nb);
@@ -718,6 +771,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
     std::stable_sort(B.order.begin(), B.order.end(),
                      [&](int p1, int p2) { return B.launches[p1].n > B.launches[p2].n; });
     B.n_blocks = nb;
+    B.n_src = m.n_src;
     B.brow.upload_vec(brow, s);
     B.wbase.upload_vec(wbase, s);
     B.wlen.upload_vec(wlen, s);
@@ -740,8 +794,9 @@ void build_blocked(Matrix &m, cudaStream_t s) {
     B.built = true;
 }
 
-bool blocked_eligible(const Matrix &m, const void *x, i64 ldx) {
-    return (reinterpret_cast<std::uintptr_t>(x) % 16 == 0) && (ldx % 4 == 0) && (m.n_src % 4 == 0);
+bool blocked_eligible(const Matrix &m, const void *x, i64 ldx, bool bulk) {
+    // 16-byte aligned field starts; the bulk copies also need whole chunks
+    return (reinterpret_cast<std::uintptr_t>(x) % 16 == 0) && (ldx % 4 == 0) && (!bulk || m.n_src % 4 == 0);
 }
 
 int blocked_launches(const Matrix &m) {
@@ -792,6 +847,7 @@ void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, c
     a.runs = B.runs.p;
     a.us = l.us;
     a.status = B.status.p;
+    a.n_src = B.n_src;
     if (bulk) {
         size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 2 * T;
         AXGB_CUDA(cudaFuncSetAttribute(k_blk_bulk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -843,8 +899,9 @@ namespace {
 constexpr int kBatchT = 4, kBatchNS = 2;
 constexpr i64 kBatchFChunk = 32;  // fields per work item
 
-BlkArgs blk_args(const Blocked &B, const Blocked::Launch &l) {
+BlkArgs blk_args(const Blocked &B, const Blocked::Launch &l, i64 n_src) {
     BlkArgs a{};
+    a.n_src = n_src;
     a.nbl = l.n;
     a.blocks = B.block_ids.p + l.begin;
     a.brow = B.brow.p;
@@ -937,7 +994,7 @@ std::shared_ptr<BlkBatch> blk_batch_create(const std::vector<Matrix *> &mats, co
             const int q = g.parts[i].first;
             const Blocked &B = mats[q]->blocked;
             BlkDesc &D = g.desc[i];
-            D.a = blk_args(B, B.launches[g.parts[i].second]);
+            D.a = blk_args(B, B.launches[g.parts[i].second], mats[q]->n_src);
             D.a.fchunk = std::min<i64>(kBatchFChunk, nrhs[q]);
             D.nrhs = nrhs[q];
             D.item_begin = items;

@@ -139,7 +139,11 @@ int axgb_generate_weights_c(int src_mesh, int dst_mesh, int method, int *matrix_
  * degenerate, area, mask), pairs clipped with the 32-vertex fallback,
  * kept pairs (nnz), LBVH nodes, the kernel launches per split-FP32 apply
  * of the direct and of the blocked variants (each known after
- * axgb_matrix_prepare of its format), 0. times_ms (double[8]): cell prep,
+ * axgb_matrix_prepare of its format), and 1 when the split layouts renumber
+ * the source cells (known after axgb_matrix_prepare of format 1 or 2; a
+ * split apply then first gathers the fields into that order, in scratch of
+ * the fields' size taken with cudaMallocAsync on the apply's stream).
+ * times_ms (double[8]): cell prep,
  * LBVH build, candidate search, clip, CSR assembly, total, 0, 0. */
 int axgb_matrix_stats(int matrix_handle, int64_t *stats, double *times_ms);
 
@@ -197,7 +201,8 @@ int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *
  * threads (two staging buffers), variant 2 with bulk (TMA) copies completing
  * on an mbarrier; unroll = fields per stage (2, 4 or 8), fields_per_pass =
  * fields per work item of a block (0 = all). Variants 1 and 2 need x 16-byte
- * aligned and ld_x, n_src multiples of 4; otherwise the direct kernel runs. */
+ * aligned and ld_x a multiple of 4 (variant 2 also n_src a multiple of 4);
+ * otherwise the direct kernel runs. */
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                               int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 

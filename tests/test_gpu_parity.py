@@ -336,3 +336,34 @@ def test_very_long_rows_few_fields(gpu, oracle):
     B.apply([xs[:2], xs], [yb2, yb40])
     torch.cuda.synchronize()
     assert np.array_equal(yb2.cpu().numpy(), y40[:2]) and np.array_equal(yb40.cpu().numpy(), y40)
+
+
+def test_staged_kernels_partial_last_chunk(gpu, oracle):
+    """n_src not a multiple of 4 (a Voronoi source): with a padded leading
+    dimension the staged kernels run, the last source chunk is copied in
+    part and zero-filled; results agree bitwise with the direct kernel and
+    with the batch."""
+    import torch
+    src, dst = grids.voronoi(40962, seed=5), grids.latlon_deg(0.5)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    assert M.n_src % 4 == 2
+    wo = oracle.conservative(src, dst)
+    rng = np.random.default_rng(11)
+    X = (rng.standard_normal((9, M.n_src)) + 2.0).astype(np.float32)
+    ref = oracle.apply_csr(wo, X.astype(np.float64), compensated=True)
+    ld = (M.n_src + 3) // 4 * 4
+    buf = torch.zeros((9, ld), dtype=torch.float32, device="cuda")
+    buf[:, : M.n_src] = torch.tensor(X, device="cuda")
+    xs = buf[:, : M.n_src]
+    y1 = gpu.apply_f32split(M, xs, fields_per_pass=0, unroll=4, variant=1).cpu().numpy()
+    y0 = gpu.apply_f32split(M, xs, fields_per_pass=0, unroll=1, variant=0).cpu().numpy()
+    assert np.array_equal(y1, y0)
+    # a Voronoi mesh numbers its cells along a spiral: a 128-row strip of the
+    # 0.5 deg grid touches every few cells of a latitude band
+    assert M.stats()["source_renumbered"]
+    assert np.max(np.abs(y1 - ref) / np.abs(ref)) < SPLIT_RTOL
+    B = gpu.Batch([M], [9])
+    yb = torch.empty((9, M.n_dst), dtype=torch.float32, device="cuda")
+    B.apply([xs], [yb])
+    torch.cuda.synchronize()
+    assert np.array_equal(yb.cpu().numpy(), y1)
