@@ -716,6 +716,24 @@ def small_configs(o):
     ms_d = dev_time(lambda: axgb.apply_f64(M, x64, y64))
     wo = o.conservative(src, dst)
     ref = o.apply_csr(wo, x64.cpu().numpy(), compensated=True)
+    # NaN-aware batched FP64 apply (skipna) on the same matrix: 16 fields, 5% NaN sources
+    nf = 16
+    gen = torch.Generator(device="cuda").manual_seed(77)
+    xn = 280.0 + torch.randn((nf, M.n_src), device="cuda", dtype=torch.float64, generator=gen)
+    xn[torch.rand((nf, M.n_src), device="cuda", generator=gen) < 0.05] = float("nan")
+    yn = torch.empty((nf, M.n_dst), device="cuda", dtype=torch.float64)
+    ms_nan = dev_time(lambda: axgb.nan_apply_f64(M, xn, 0.5, yn))
+    xs = xn[:2].cpu().numpy()
+    from oracle import Weights
+    csr = M.to_csr()
+    wg = Weights(M.n_src, M.n_dst, np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"])).astype(np.int64),
+                 csr["col"].astype(np.int64), csr["val"], csr["frac_a"], csr["frac_b"], csr["area_a"], csr["area_b"])
+    ref_nan = o.nan_batch_apply(wg, xs, 0.5)  # the oracle's loop on the GPU's weights
+    nan_bytes = 8 * (M.n_src + M.n_dst) * nf + 12 * M.nnz + 4 * (M.n_dst + 1)
+    out["c2_nan_batch_apply_16_fields"] = {
+        "ms": ms_nan, "GBps": nan_bytes / ms_nan / 1e6,
+        "bitwise_equal_to_oracle_loop": bool(np.array_equal(yn[:2].cpu().numpy(), ref_nan, equal_nan=True)),
+        "nan_outputs": int(torch.isnan(yn).sum().item())}
     out["c2_0p25deg_to_C384_one_field"] = {
         "nnz": M.nnz, "split_ms": ms_s, "fp64_ms": ms_d, "split_speedup": ms_d / ms_s,
         "split": rel_errors(y32.cpu().numpy(), ref), "fp64": rel_errors(y64.cpu().numpy(), ref),

@@ -44,7 +44,8 @@ _SYMBOLS = [
     "axgb_set_autotune", "axgb_apply_c", "axgb_batch_apply_host_f64", "axgb_batch_apply_host_f32split",
     "axgb_batch_create", "axgb_batch_apply", "axgb_destroy_batch", "axgb_conservation_f64",
     "axgb_conservation_f32", "axgb_matrix_device_status", "axgb_conservation_f64_noalloc",
-    "axgb_set_kernel_choice", "axgb_get_kernel_choice",
+    "axgb_set_kernel_choice", "axgb_get_kernel_choice", "axgb_nan_batch_apply_f64", "axgb_apply_masked_f64",
+    "axgb_nan_batch_apply_host", "axgb_matrix_serialize", "axgb_matrix_deserialize",
 ]
 
 
@@ -114,6 +115,11 @@ def lib():
     L.axgb_conservation_f32.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
     L.axgb_conservation_f64_noalloc.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
     L.axgb_set_kernel_choice.argtypes = [C.c_int, C.c_int64, vp]
+    L.axgb_nan_batch_apply_f64.argtypes = [C.c_int, vp, C.c_int64, vp, C.c_int64, C.c_int64, C.c_double, vp]
+    L.axgb_apply_masked_f64.argtypes = [C.c_int, vp, vp, vp, vp]
+    L.axgb_nan_batch_apply_host.argtypes = [C.c_int, vp, C.c_int64, vp, C.c_int64, C.c_int64, C.c_double]
+    L.axgb_matrix_serialize.argtypes = [C.c_int, vp, C.c_int64, vp]
+    L.axgb_matrix_deserialize.argtypes = [vp, C.c_int64, vp]
     L.axgb_get_kernel_choice.argtypes = [C.c_int, C.c_int64, vp, vp]
     _L = L
     return L
@@ -306,6 +312,21 @@ class Matrix:
         _check(lib().axgb_matrix_device_status(self.handle, _ptr(st)))
         return int(st[0])
 
+    def serialize(self) -> bytes:
+        """WeightCache blob (weight_cache.hpp:49-157)."""
+        n = C.c_int64()
+        _check(lib().axgb_matrix_serialize(self.handle, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        _check(lib().axgb_matrix_serialize(self.handle, buf, n.value, C.byref(n)))
+        return buf.raw
+
+    @classmethod
+    def deserialize(cls, blob: bytes):
+        _ensure_init()
+        h = C.c_int()
+        _check(lib().axgb_matrix_deserialize(C.c_char_p(blob), len(blob), C.byref(h)))
+        return cls(h.value)
+
     @classmethod
     def from_csr(cls, n_src, n_dst, row_ptr, col, val, frac_a=None, frac_b=None, area_a=None, area_b=None):
         _ensure_init()
@@ -444,6 +465,44 @@ def batch_apply_host_f64(matrix: Matrix, x_host, y_host):
     _check(lib().axgb_batch_apply_host_f64(matrix.handle, _ptr(x_host), matrix.n_src, _ptr(y_host), matrix.n_dst,
                                            n_vars))
     return y_host
+
+
+def nan_batch_apply(matrix: Matrix, src, na_thres: float):
+    """nan_batch_apply (python/axis_py.cpp:764-821): numpy src [n_src, n_vars]
+    with NaNs -> [n_dst, n_vars], through the host C ABI."""
+    a = np.asarray(src, dtype=np.float64)
+    if a.ndim != 2:
+        raise InvalidArgument(ERR_INVALID, "nan_batch_apply: src must be 2-D [n_src, n_vars]")
+    n_vars = a.shape[1]
+    x = np.ascontiguousarray(a.T)  # LayoutLeft [n_src, n_vars]
+    y = np.zeros((n_vars, matrix.n_dst))
+    _check(lib().axgb_nan_batch_apply_host(matrix.handle, _ptr(x), a.shape[0], _ptr(y), matrix.n_dst, n_vars,
+                                           float(na_thres)))
+    return np.ascontiguousarray(y.T)
+
+
+def nan_apply_f64(matrix: Matrix, x, na_thres: float, y=None, stream=None):
+    """Device NaN-aware FP64 apply: x, y CUDA tensors [nrhs, n]."""
+    import torch
+    if x.dim() == 1:
+        x = x.view(1, -1)
+    if y is None:
+        y = torch.empty((x.shape[0], matrix.n_dst), dtype=torch.float64, device=x.device)
+    elif y.dim() == 1:
+        y = y.view(1, -1)
+    _check(lib().axgb_nan_batch_apply_f64(matrix.handle, _ptr(x), x.stride(0), _ptr(y), y.stride(0), x.shape[0],
+                                          float(na_thres),
+                                          _stream(stream if stream is not None else torch.cuda.current_stream())))
+    return y
+
+
+def apply_masked(matrix: Matrix, x, y, dst_mask=None, stream=None):
+    """Masked apply (apply.hpp:458-532) on device FP64 tensors: rows whose
+    int32 mask is 0 keep y's value."""
+    import torch
+    _check(lib().axgb_apply_masked_f64(matrix.handle, _ptr(x), _ptr(y), _ptr(dst_mask),
+                                       _stream(stream if stream is not None else torch.cuda.current_stream())))
+    return y
 
 
 def check_conservation(matrix: Matrix, src, dst, norm_type: int = 0, stream=None):

@@ -624,6 +624,116 @@ int axgb_matrix_export_csr(int h, int64_t *row_ptr, int64_t *col_idx, double *va
     });
 }
 
+// ─── weight cache blob (include/axis/solver/weight_cache.hpp:49-157) ─────
+// [magic u32 0x43574841, the reference's value (little-endian bytes "AHWC")]
+// [version u32 = 1][endian u8][pad 7][n_src u64][n_dst u64]
+// [nnz u64] then factor_list f64[nnz], factor_row i64[nnz], factor_col
+// i64[nnz], frac_a f64[n_src], frac_b f64[n_dst], area_a f64[n_src], area_b
+// f64[n_dst]. The COO triplets are written in CSR order.
+namespace {
+constexpr uint32_t kCacheMagic = 0x43574841u;
+constexpr uint32_t kCacheVersion = 1;
+constexpr int64_t kCacheHeader = 40;
+inline uint8_t native_endian() {
+    const uint16_t one = 1;
+    uint8_t b;
+    std::memcpy(&b, &one, 1);
+    return b == 1 ? 0x01 : 0x02;
+}
+inline int64_t cache_size(int64_t ns, int64_t nd, int64_t nnz) { return kCacheHeader + 24 * nnz + 16 * ns + 16 * nd; }
+}  // namespace
+
+int axgb_matrix_serialize(int h, void *buf, int64_t buf_size, int64_t *written) {
+    AXGB_TRY({
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        const int64_t need = cache_size(m->n_src, m->n_dst, m->nnz);
+        if (written) *written = need;
+        if (!buf) return AXGB_SUCCESS;  // size query
+        AXGB_REQUIRE(buf_size >= need, "matrix_serialize: buf_size (" + std::to_string(buf_size) + ") < required (" +
+                                           std::to_string(need) + ")");
+        std::vector<int> rp(m->n_dst + 1), c(m->nnz);
+        m->row_ptr.download(rp.data(), rp.size());
+        m->col.download(c.data(), c.size());
+        uint8_t *p = static_cast<uint8_t *>(buf);
+        const uint64_t ns = m->n_src, nd = m->n_dst, nz = m->nnz;
+        std::memset(p, 0, kCacheHeader);
+        std::memcpy(p, &kCacheMagic, 4);
+        std::memcpy(p + 4, &kCacheVersion, 4);
+        p[8] = native_endian();
+        std::memcpy(p + 16, &ns, 8);
+        std::memcpy(p + 24, &nd, 8);
+        std::memcpy(p + 32, &nz, 8);
+        double *vals = reinterpret_cast<double *>(p + kCacheHeader);
+        m->val.download(vals, m->nnz);
+        AXGB_CUDA(cudaDeviceSynchronize());
+        int64_t *rows = reinterpret_cast<int64_t *>(p + kCacheHeader + 8 * nz);
+        int64_t *cols = rows + nz;
+        for (int64_t j = 0; j < m->n_dst; ++j)
+            for (int k = rp[j]; k < rp[j + 1]; ++k) rows[k] = j;
+        for (int64_t k = 0; k < m->nnz; ++k) cols[k] = c[k];
+        double *fa = reinterpret_cast<double *>(cols + nz);
+        double *fb = fa + ns, *aa = fb + nd, *ab = aa + ns;
+        m->frac_a.download(fa, ns);
+        m->frac_b.download(fb, nd);
+        m->area_a.download(aa, ns);
+        m->area_b.download(ab, nd);
+        AXGB_CUDA(cudaDeviceSynchronize());
+    });
+}
+
+int axgb_matrix_deserialize(const void *buf, int64_t buf_size, int *h) {
+    AXGB_TRY({
+        AXGB_REQUIRE(buf && h, "matrix_deserialize: NULL argument");
+        AXGB_REQUIRE(buf_size >= kCacheHeader, "matrix_deserialize: buf_size (" + std::to_string(buf_size) +
+                                                   ") < minimum header size (40)");
+        const uint8_t *p = static_cast<const uint8_t *>(buf);
+        uint32_t magic, version;
+        uint64_t ns, nd, nz;
+        std::memcpy(&magic, p, 4);
+        std::memcpy(&version, p + 4, 4);
+        std::memcpy(&ns, p + 16, 8);
+        std::memcpy(&nd, p + 24, 8);
+        std::memcpy(&nz, p + 32, 8);
+        AXGB_REQUIRE(magic == kCacheMagic, "matrix_deserialize: invalid magic bytes");
+        AXGB_REQUIRE(version == kCacheVersion, "matrix_deserialize: format version mismatch (expected 1, got " +
+                                                   std::to_string(version) + ")");
+        AXGB_REQUIRE(p[8] == native_endian(), "matrix_deserialize: endianness mismatch");
+        AXGB_REQUIRE(ns < (uint64_t(1) << 31) && nd < (uint64_t(1) << 31) && nz < (uint64_t(1) << 31),
+                     "matrix_deserialize: sizes above 2^31");
+        const int64_t need = cache_size(static_cast<int64_t>(ns), static_cast<int64_t>(nd), static_cast<int64_t>(nz));
+        AXGB_REQUIRE(buf_size >= need, "matrix_deserialize: blob size mismatch (buf_size=" + std::to_string(buf_size) +
+                                           ", expected=" + std::to_string(need) + ")");
+        // unaligned-safe copies of the body
+        std::vector<double> vals(nz), fa(ns), fb(nd), aa(ns), ab(nd);
+        std::vector<int64_t> rows(nz), cols(nz);
+        const uint8_t *q = p + kCacheHeader;
+        std::memcpy(vals.data(), q, 8 * nz);
+        std::memcpy(rows.data(), q + 8 * nz, 8 * nz);
+        std::memcpy(cols.data(), q + 16 * nz, 8 * nz);
+        q += 24 * nz;
+        std::memcpy(fa.data(), q, 8 * ns);
+        std::memcpy(fb.data(), q + 8 * ns, 8 * nd);
+        std::memcpy(aa.data(), q + 8 * ns + 8 * nd, 8 * ns);
+        std::memcpy(ab.data(), q + 16 * ns + 8 * nd, 8 * nd);
+        // COO -> CSR, stable by row (to_csr order: rows ascending, then columns)
+        std::vector<int64_t> rp(nd + 1, 0);
+        for (uint64_t k = 0; k < nz; ++k) {
+            AXGB_REQUIRE(rows[k] >= 0 && static_cast<uint64_t>(rows[k]) < nd, "matrix_deserialize: row out of range");
+            rp[rows[k] + 1]++;
+        }
+        for (uint64_t j = 0; j < nd; ++j) rp[j + 1] += rp[j];
+        std::vector<int64_t> pos(rp.begin(), rp.end() - 1), cc(nz);
+        std::vector<double> vv(nz);
+        for (uint64_t k = 0; k < nz; ++k) {
+            const int64_t at = pos[rows[k]]++;
+            cc[at] = cols[k];
+            vv[at] = vals[k];
+        }
+        return axgb_matrix_import_csr(static_cast<int64_t>(ns), static_cast<int64_t>(nd), static_cast<int64_t>(nz),
+                                      rp.data(), cc.data(), vv.data(), fa.data(), fb.data(), aa.data(), ab.data(), h);
+    });
+}
+
 int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int64_t *row_ptr, const int64_t *col_idx,
                            const double *values, const double *frac_a, const double *frac_b, const double *area_a,
                            const double *area_b, int *h) {
@@ -833,6 +943,37 @@ int axgb_apply_c(int h, const double *src, double *dst, int n_src, int n_dst) {
         if (n_src) AXGB_CUDA(cudaMemcpy(dx, src, sizeof(double) * n_src, cudaMemcpyHostToDevice));
         apply_f64(*m, dx, std::max<int64_t>(1, n_src), dy, std::max<int64_t>(1, n_dst), 1, 0);
         if (n_dst) AXGB_CUDA(cudaMemcpy(dst, dy, sizeof(double) * n_dst, cudaMemcpyDeviceToHost));
+    });
+}
+
+int axgb_nan_batch_apply_f64(int h, const double *x, int64_t ldx, double *y, int64_t ldy, int64_t nrhs,
+                             double na_thres, axgb_stream_t stream) {
+    AXGB_TRY({
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        check_apply(*m, x, ldx, y, ldy, nrhs);
+        nan_batch_apply_f64(*m, x, ldx, y, ldy, nrhs, na_thres, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int axgb_apply_masked_f64(int h, const double *x, double *y, const int32_t *dst_mask, axgb_stream_t stream) {
+    AXGB_TRY({
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        check_apply(*m, x, std::max<int64_t>(1, m->n_src), y, std::max<int64_t>(1, m->n_dst), 1);
+        apply_masked_f64(*m, x, dst_mask, y, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int axgb_nan_batch_apply_host(int h, const double *src, int64_t n_src, double *dst, int64_t n_dst, int64_t n_vars,
+                              double na_thres) {
+    AXGB_TRY({
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        AXGB_REQUIRE(n_src == m->n_src && n_dst == m->n_dst, "nan_batch_apply: extents do not match the matrix");
+        AXGB_REQUIRE(n_vars >= 0, "nan_batch_apply: n_vars < 0");
+        if (n_vars > 0)
+            host_batch<double>(*m, src, dst, n_vars,
+                               [&](const double *x, int64_t lx, double *y, int64_t ly, int64_t nv, cudaStream_t s) {
+                                   nan_batch_apply_f64(*m, x, lx, y, ly, nv, na_thres, s);
+                               });
     });
 }
 

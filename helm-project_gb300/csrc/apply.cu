@@ -634,6 +634,99 @@ void launch_f64(const SellArgs &a, const double *x, i64 ldx, double *y, i64 ldy,
         k_f64<L, 1><<<blocks, 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, tile);
 }
 
+// ─── NaN-aware and masked FP64 applies ────────────────────────────────────
+// nan_batch_apply of include/axis/solver/apply.hpp:359-437 on the FP64
+// sliced-ELL layout (each row's entries in CSR order), lane per row: per row
+// the total weight, per field the weighted sum and the valid weight, with
+// unfused multiply and add in entry order, so the NaN decisions and the
+// values match the reference loop bit for bit. 0 < L <= 32: entries cached
+// in registers; L == 0: rows of any length, entries re-read per field.
+__device__ __forceinline__ double nan_result(double total, double wsum, double valid, double na_thres) {
+    if (valid == 0.0 || total == 0.0) return __longlong_as_double(0x7ff8000000000000ll);
+    const double frac = __ddiv_rn(valid, total);
+    return frac < __dsub_rn(__dsub_rn(1.0, na_thres), 1e-6) ? __longlong_as_double(0x7ff8000000000000ll)
+                                                            : __ddiv_rn(wsum, valid);
+}
+
+template <int L>
+__global__ void __launch_bounds__(256) k_nan_sell(SellArgs a, const double *__restrict__ x, i64 ldx,
+                                                  double *__restrict__ y, i64 ldy, i64 nrhs, double na_thres) {
+    const int lane = threadIdx.x & 31;
+    const i64 item = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (item >= a.n_ids) return;
+    const int sid = a.ids[item];
+    const i64 row = static_cast<i64>(sid) * 32 + lane;
+    if (row >= a.n_rows) return;
+    const int base = a.base[sid] + lane, rl = a.rlen[row];
+    if constexpr (L > 0) {
+        int c[L];
+        double w[L];
+        double total = 0.0;
+#pragma unroll
+        for (int k = 0; k < L; ++k) {
+            if (k < rl) {
+                c[k] = a.col[base + 32 * k];
+                w[k] = a.w64[base + 32 * k];
+                total = __dadd_rn(total, w[k]);
+            }
+        }
+        for (i64 v = 0; v < nrhs; ++v) {
+            const double *xv = x + v * ldx;
+            double wsum = 0.0, valid = 0.0;
+#pragma unroll
+            for (int k = 0; k < L; ++k) {
+                if (k < rl) {
+                    const double xk = __ldg(xv + c[k]);
+                    if (!isnan(xk)) {
+                        wsum = __dadd_rn(wsum, __dmul_rn(w[k], xk));
+                        valid = __dadd_rn(valid, w[k]);
+                    }
+                }
+            }
+            y[v * ldy + row] = nan_result(total, wsum, valid, na_thres);
+        }
+    } else {
+        // rows of any length (the long classes): fields over gridDim.y, the
+        // loads of 8 entries issued ahead of their in-order accumulation
+        double total = 0.0;
+        for (int k = 0; k < rl; ++k) total = __dadd_rn(total, a.w64[base + 32 * k]);
+        for (i64 v = blockIdx.y; v < nrhs; v += gridDim.y) {
+            const double *xv = x + v * ldx;
+            double wsum = 0.0, valid = 0.0;
+            for (int k0 = 0; k0 < rl; k0 += 8) {
+                double wk[8], xk[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    if (k0 + u < rl) {
+                        wk[u] = a.w64[base + 32 * (k0 + u)];
+                        xk[u] = __ldg(xv + a.col[base + 32 * (k0 + u)]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    if (k0 + u < rl && !isnan(xk[u])) {
+                        wsum = __dadd_rn(wsum, __dmul_rn(wk[u], xk[u]));
+                        valid = __dadd_rn(valid, wk[u]);
+                    }
+                }
+            }
+            y[v * ldy + row] = nan_result(total, wsum, valid, na_thres);
+        }
+    }
+}
+
+// Masked apply of include/axis/solver/apply.hpp:458-532: rows with mask 0
+// are not written; the others get the row sum in CSR order.
+__global__ void k_masked_apply(const int *__restrict__ rp, const int *__restrict__ col,
+                               const double *__restrict__ val, i64 n_dst, const double *__restrict__ x,
+                               const int *__restrict__ mask, double *__restrict__ y) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n_dst || (mask && mask[j] == 0)) return;
+    double s = 0.0;
+    for (int k = rp[j]; k < rp[j + 1]; ++k) s = __dadd_rn(s, __dmul_rn(val[k], __ldg(x + col[k])));
+    y[j] = s;
+}
+
 // ─── conservation ──────────────────────────────────────────────────────────
 
 template <class T>
@@ -998,6 +1091,30 @@ void conservation_noalloc(Matrix &m, const double *src, const double *dst, int n
     out[1] = di;
     out[2] = ae;
     out[3] = ae / den;
+}
+
+void nan_batch_apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, double na_thres,
+                         cudaStream_t s) {
+    if (nrhs <= 0 || m.n_dst == 0) return;
+    if (!m.sell64.built) matrix_prepare(m, 0, s);
+    const Sell &S = m.sell64;
+    auto launch = [&](auto kernel, int cls, unsigned gy) {
+        const SellArgs a = sell_args(m, S, cls);
+        if (a.n_ids > 0) kernel<<<dim3(nblk(a.n_ids * 32, 256), gy), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs, na_thres);
+    };
+    const unsigned fy = static_cast<unsigned>(std::min<i64>(nrhs, 65535));
+    launch(k_nan_sell<8>, 0, 1);
+    launch(k_nan_sell<16>, 1, 1);
+    launch(k_nan_sell<32>, 2, 1);
+    launch(k_nan_sell<0>, 3, fy);
+    launch(k_nan_sell<0>, 4, fy);
+    AXGB_CUDA(cudaGetLastError());
+}
+
+void apply_masked_f64(Matrix &m, const double *x, const int *mask, double *y, cudaStream_t s) {
+    if (m.n_dst == 0) return;
+    k_masked_apply<<<nblk(m.n_dst, 256), 256, 0, s>>>(m.row_ptr.p, m.col.p, m.val.p, m.n_dst, x, mask, y);
+    AXGB_CUDA(cudaGetLastError());
 }
 
 std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &mats, const std::vector<i64> &nrhs) {

@@ -246,6 +246,9 @@ void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs
 void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
                  cudaStream_t s);
 void conservation(Matrix &m, const void *src, const void *dst, bool f32, int norm_type, double *out, cudaStream_t s);
+void nan_batch_apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, double na_thres,
+                         cudaStream_t s);
+void apply_masked_f64(Matrix &m, const double *x, const int *mask, double *y, cudaStream_t s);
 void conservation_noalloc(Matrix &m, const double *src, const double *dst, int norm_type, double *out,
                           cudaStream_t s);
 std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &mats, const std::vector<i64> &nrhs);

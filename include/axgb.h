@@ -161,6 +161,20 @@ int axgb_matrix_export_csr(int matrix_handle, int64_t *row_ptr, int64_t *col_idx
  * [0, n_src); rows need not be column-sorted). frac/area may be NULL
  * (filled with 1 and 0). Mirrors the InterpolationMatrix adopting
  * constructor (interpolation_matrix.hpp:80-92) followed by to_csr(). */
+/* Weight cache blob: the binary format of WeightCache
+ * (include/axis/solver/weight_cache.hpp:49-157), so weights round-trip with
+ * the reference. 40-byte header [magic u32 0x43574841 (bytes "AHWC")]
+ * [version 1 u32][endian u8]
+ * [pad 7][n_src u64][n_dst u64][nnz u64], then factor_list f64[nnz],
+ * factor_row i64[nnz], factor_col i64[nnz], frac_a f64[n_src], frac_b
+ * f64[n_dst], area_a f64[n_src], area_b f64[n_dst]; the triplets are written
+ * in CSR order. serialize: buf NULL returns the size in *written; a smaller
+ * buf_size is AXGB_ERR_INVALID. deserialize validates magic, version,
+ * endianness and size (AXGB_ERR_INVALID otherwise) and builds a matrix as
+ * axgb_matrix_import_csr does (triplets in any order). */
+int axgb_matrix_serialize(int matrix_handle, void *buf, int64_t buf_size, int64_t *written);
+int axgb_matrix_deserialize(const void *buf, int64_t buf_size, int *matrix_handle);
+
 int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int64_t *row_ptr, const int64_t *col_idx,
                            const double *values, const double *frac_a, const double *frac_b, const double *area_a,
                            const double *area_b, int *matrix_handle);
@@ -223,6 +237,23 @@ int axgb_set_autotune(int enable);
 int axgb_set_kernel_choice(int matrix_handle, int64_t nrhs, const int32_t *choice);
 int axgb_get_kernel_choice(int matrix_handle, int64_t nrhs, int32_t *choice, int32_t *cached);
 
+/* NaN-aware batched FP64 apply; replaces nan_batch_apply
+ * (include/axis/solver/apply.hpp:359-437, python/axis_py.cpp:764-821).
+ * Device pointers, x [nrhs][ld_x], y [nrhs][ld_y] (y overwritten). Per row:
+ * the total weight; per field: the weighted sum and the weight of the
+ * sources that are not NaN. y is NaN where no source is valid or the valid
+ * weight fraction is below 1 - na_thres - 1e-6, else the weighted sum over
+ * the valid weight. Sums run in CSR order with separate multiply and add, as
+ * the reference's loop, so NaN positions and values match it exactly. */
+int axgb_nan_batch_apply_f64(int matrix_handle, const double *x, int64_t ld_x, double *y, int64_t ld_y,
+                             int64_t nrhs, double na_thres, axgb_stream_t stream);
+
+/* Masked single-field FP64 apply; replaces the masked solver::apply
+ * (include/axis/solver/apply.hpp:458-532). Device pointers; dst_mask
+ * [n_dst] int32 (0 = masked: y left unchanged) or NULL (every row). */
+int axgb_apply_masked_f64(int matrix_handle, const double *x, double *y, const int32_t *dst_mask,
+                          axgb_stream_t stream);
+
 /* ─── Apply (host pointers, synchronous) ─────────────────────────────────
  * Replaces axis_apply_c (axis_c_interop.cpp:217-236): FP64, one field,
  * host arrays; returns AXGB_ERR_INVALID before touching dst on extent
@@ -231,6 +262,11 @@ int axgb_apply_c(int matrix_handle, const double *src, double *dst, int n_src, i
 
 /* Replaces python batch_apply (axis_py.cpp:690-759) for host arrays laid
  * out LayoutLeft [n_src, n_vars] / [n_dst, n_vars]. */
+/* axgb_nan_batch_apply_f64 on host arrays: src [n_src, n_vars] and dst
+ * [n_dst, n_vars] column-major (LayoutLeft, one field after another), the
+ * layout nan_batch_apply takes. Synchronous. */
+int axgb_nan_batch_apply_host(int matrix_handle, const double *src, int64_t n_src, double *dst, int64_t n_dst,
+                              int64_t n_vars, double na_thres);
 int axgb_batch_apply_host_f64(int matrix_handle, const double *src, int64_t n_src, double *dst, int64_t n_dst,
                               int64_t n_vars);
 int axgb_batch_apply_host_f32split(int matrix_handle, const float *src, int64_t n_src, float *dst, int64_t n_dst,

@@ -83,6 +83,9 @@ class Oracle:
         L.orc_result_stats.argtypes = [C.c_void_p, _i64p]
         L.orc_result_copy.argtypes = [C.c_void_p, _i64p, _i64p, _f64p, _f64p, _f64p, _f64p, _f64p]
         L.orc_result_free.argtypes = [C.c_void_p]
+        L.orc_nan_batch_apply.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_int64, _f64p, C.c_int64,
+                                          C.c_int64, C.c_double]
+        L.orc_apply_masked.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_void_p, _f64p]
         L.orc_apply_csr.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_int64, _f64p, C.c_int64, C.c_int64,
                                     C.c_int]
         L.orc_apply_coo_atomic.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_int64, _f64p, C.c_int64,
@@ -184,6 +187,24 @@ class Oracle:
         y = np.zeros((nrhs, wts.n_dst))
         self.L.orc_apply_csr(wts.n_dst, wts.row_ptr(), np.ascontiguousarray(wts.col), np.ascontiguousarray(wts.w),
                              x.reshape(-1), x.shape[1], y.reshape(-1), wts.n_dst, nrhs, int(compensated))
+        return y
+
+    def nan_batch_apply(self, wts: Weights, x, na_thres: float):
+        """x: [nrhs, n_src] float64 with NaNs; returns [nrhs, n_dst]."""
+        x = np.ascontiguousarray(np.atleast_2d(x), np.float64)
+        nrhs = x.shape[0]
+        y = np.zeros((nrhs, wts.n_dst))
+        self.L.orc_nan_batch_apply(wts.n_dst, wts.row_ptr(), np.ascontiguousarray(wts.col),
+                                   np.ascontiguousarray(wts.w), x.reshape(-1), x.shape[1], y.reshape(-1), wts.n_dst,
+                                   nrhs, float(na_thres))
+        return y
+
+    def apply_masked(self, wts: Weights, x, mask, y0):
+        """One field; rows with mask 0 keep y0's value."""
+        y = np.array(y0, np.float64, copy=True)
+        m = np.ascontiguousarray(mask, np.int32)
+        self.L.orc_apply_masked(wts.n_dst, wts.row_ptr(), np.ascontiguousarray(wts.col), np.ascontiguousarray(wts.w),
+                                np.ascontiguousarray(x, np.float64), m.ctypes.data_as(C.c_void_p), y)
         return y
 
     def apply_coo_atomic(self, wts: Weights, x):

@@ -944,6 +944,52 @@ void orc_apply_coo_atomic(i64 nnz, const i64 *row, const i64 *col, const double 
     }
 }
 
+// NaN-aware batch apply of include/axis/solver/apply.hpp:359-437: per row
+// the total weight, per field the weighted sum and the weight of the non-NaN
+// sources (entries in CSR order, plain multiply then add); NaN where no
+// source is valid or the valid fraction is below 1 - na_thres - 1e-6, else
+// the renormalised mean. x/y column-major with leading dims ldx/ldy.
+void orc_nan_batch_apply(i64 n_dst, const i64 *row_ptr, const i64 *col, const double *val, const double *x,
+                         i64 ldx, double *y, i64 ldy, i64 nrhs, double na_thres) {
+#pragma omp parallel for schedule(static)
+    for (i64 j = 0; j < n_dst; ++j) {
+        double total = 0.0;
+        for (i64 k = row_ptr[j]; k < row_ptr[j + 1]; ++k) total += val[k];
+        for (i64 v = 0; v < nrhs; ++v) {
+            double wsum = 0.0, valid = 0.0;
+            for (i64 k = row_ptr[j]; k < row_ptr[j + 1]; ++k) {
+                const double xv = x[v * ldx + col[k]];
+                if (!std::isnan(xv)) {
+                    wsum += val[k] * xv;
+                    valid += val[k];
+                }
+            }
+            double r;
+            if (valid == 0.0 || total == 0.0) {
+                r = std::numeric_limits<double>::quiet_NaN();
+            } else {
+                const double frac = valid / total;
+                r = frac < (1.0 - na_thres - 1e-6) ? std::numeric_limits<double>::quiet_NaN() : wsum / valid;
+            }
+            y[v * ldy + j] = r;
+        }
+    }
+}
+
+// Masked single-field apply of include/axis/solver/apply.hpp:458-532 (CSR
+// path): rows with mask 0 keep their value; the others get the row sum
+// (entries in CSR order).
+void orc_apply_masked(i64 n_dst, const i64 *row_ptr, const i64 *col, const double *val, const double *x,
+                      const int *mask, double *y) {
+#pragma omp parallel for schedule(static)
+    for (i64 j = 0; j < n_dst; ++j) {
+        if (mask && mask[j] == 0) continue;
+        double s = 0.0;
+        for (i64 k = row_ptr[j]; k < row_ptr[j + 1]; ++k) s += val[k] * x[col[k]];
+        y[j] = s;
+    }
+}
+
 // Conservation report of src/solver/conservation.cpp:24-96.
 // out = (src_integral, dst_integral, absolute_error, relative_error).
 void orc_conservation(i64 n_src, const double *src, const double *area_a, const double *frac_a, i64 n_dst,

@@ -48,3 +48,19 @@ def test_last_error_without_device():
     assert rc == axgb.ERR_HANDLE
     assert "unknown mesh handle" in axgb.last_error()
     assert L.axgb_destroy_matrix(999) != 0
+
+
+def test_weight_cache_header_checks_without_device():
+    """The blob header is validated before any device work (magic, version,
+    truncation), as WeightCache::deserialize does (prop_weight_cache.cpp)."""
+    import struct
+
+    import axgb
+    L = axgb.lib()
+    h = ctypes.c_int()
+    good = struct.pack("<IIB7xQQQ", 0x43574841, 1, 1, 2, 2, 1) + bytes(24 + 32 + 32)
+    for blob, msg in ((b"XXXX" + good[4:], "magic"), (good[:4] + struct.pack("<I", 7) + good[8:], "version"),
+                      (good[:30], "header"), (good[:60], "size")):
+        rc = L.axgb_matrix_deserialize(ctypes.c_char_p(blob), len(blob), ctypes.byref(h))
+        assert rc == axgb.ERR_INVALID, msg
+        assert axgb.last_error()

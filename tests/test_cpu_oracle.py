@@ -156,3 +156,44 @@ def test_voronoi_mesh(oracle):
     w = oracle.conservative(g, grids.latlon_deg(5.0))
     rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
     assert np.all(np.abs(rs - 1.0) < 1e-11)
+
+
+def _nan_case(oracle):
+    # the source mesh and NaN pattern of the reference's fused NaN SpMV test
+    # (tests_python/test_fused_nan_spmv.py:23-60); the destination is a
+    # cubed sphere (its regular -> regular bilinear fast path is not restated)
+    src = grids.regular_latlon(10, 5, 0.0, -90.0, 36.0, 36.0)
+    dst = grids.cubed_sphere(4)
+    w = oracle.bilinear(src, dst)
+    x = np.ones((3, w.n_src))
+    x[0, ::3] = np.nan
+    x[1, 1::4] = np.nan
+    x[2, ::2] = np.nan
+    return w, x
+
+
+def test_nan_batch_apply_oracle(oracle):
+    """The fused NaN-aware apply against the reference test's manual
+    formula (masked sum / valid weight, NaN below the valid fraction)."""
+    w, x = _nan_case(oracle)
+    got = oracle.nan_batch_apply(w, x, 0.5)
+    mask = np.isnan(x)
+    num = oracle.apply_csr(w, np.where(mask, 0.0, x), compensated=False)
+    den = oracle.apply_csr(w, (~mask).astype(np.float64), compensated=False)
+    tot = oracle.apply_csr(w, np.ones((1, w.n_src)), compensated=False)[0]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        exp = np.where(den / tot[None, :] < (1.0 - 0.5 - 1e-6), np.nan, num / den)
+    np.testing.assert_allclose(got, exp, rtol=1e-12, equal_nan=True)
+    assert np.isnan(got).any() and np.isfinite(got).any()
+
+
+def test_apply_masked_oracle(oracle):
+    src, dst = grids.latlon_deg(5.0), grids.cubed_sphere(8)
+    w = oracle.conservative(src, dst)
+    x = np.cos(np.radians(np.repeat(np.arange(-87.5, 90, 5.0), 72))) + 280.0
+    mask = (np.arange(w.n_dst) % 3 != 0).astype(np.int32)
+    y0 = np.full(w.n_dst, -7.0)
+    y = oracle.apply_masked(w, x, mask, y0)
+    full = oracle.apply_csr(w, x, compensated=False)[0]
+    assert np.all(y[mask == 0] == -7.0)
+    assert np.allclose(y[mask == 1], full[mask == 1], rtol=1e-14)

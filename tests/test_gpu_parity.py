@@ -367,3 +367,102 @@ def test_staged_kernels_partial_last_chunk(gpu, oracle):
     B.apply([xs], [yb])
     torch.cuda.synchronize()
     assert np.array_equal(yb.cpu().numpy(), y1)
+
+
+def _oracle_weights_of(M):
+    """The GPU's own CSR as oracle weights (the two generators agree to an
+    ulp on a few weights, where CUDA's and glibc's atan2 differ)."""
+    from oracle import Weights
+    csr = M.to_csr()
+    rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
+    return Weights(M.n_src, M.n_dst, rows.astype(np.int64), csr["col"].astype(np.int64), csr["val"], csr["frac_a"],
+                   csr["frac_b"], csr["area_a"], csr["area_b"])
+
+
+def test_nan_batch_apply_parity(gpu, oracle):
+    """NaN-aware batched apply on the GPU against the oracle on the same
+    weights: NaN positions and values bit for bit (device and host entry
+    points)."""
+    import torch
+    src, dst = grids.latlon_deg(2.0), grids.cubed_sphere(24)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    wo = _oracle_weights_of(M)
+    rng = np.random.default_rng(17)
+    X = rng.standard_normal((6, M.n_src)) + 280.0
+    for v, p in enumerate((0.0, 0.05, 0.3, 0.6, 0.9, 1.0)):
+        X[v, rng.uniform(size=M.n_src) < p] = np.nan
+    for thres in (0.0, 0.25, 0.5, 1.0):
+        ref = oracle.nan_batch_apply(wo, X, thres)
+        got = gpu.nan_apply_f64(M, torch.tensor(X, device="cuda"), thres).cpu().numpy()
+        np.testing.assert_array_equal(got, ref)
+        host = gpu.nan_batch_apply(M, X.T, thres)  # [n_src, n_vars] like axis_py.nan_batch_apply
+        np.testing.assert_array_equal(host, ref.T)
+
+
+def test_apply_masked_parity(gpu, oracle):
+    import torch
+    src, dst = grids.latlon_deg(2.0), grids.cubed_sphere(24)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    wo = _oracle_weights_of(M)
+    x = np.random.default_rng(19).standard_normal(M.n_src) + 280.0
+    mask = (np.arange(M.n_dst) % 5 != 1).astype(np.int32)
+    y0 = np.full(M.n_dst, -3.0)
+    ref = oracle.apply_masked(wo, x, mask, y0)
+    y = torch.tensor(y0, device="cuda")
+    gpu.apply_masked(M, torch.tensor(x, device="cuda"), y, torch.tensor(mask, device="cuda"))
+    np.testing.assert_array_equal(y.cpu().numpy(), ref)
+    y2 = torch.tensor(y0, device="cuda")
+    gpu.apply_masked(M, torch.tensor(x, device="cuda"), y2)  # no mask: every row
+    full = oracle.apply_masked(wo, x, np.ones(M.n_dst, np.int32), y0)
+    np.testing.assert_array_equal(y2.cpu().numpy(), full)
+
+
+def _read_blob(blob):
+    """Independent reader of the weight cache layout (weight_cache.hpp:14-26)."""
+    import struct
+    magic, version, endian = struct.unpack_from("<IIB", blob, 0)
+    ns, nd, nz = struct.unpack_from("<QQQ", blob, 16)
+    off = 40
+    arrs = {}
+    for name, n, dt in (("w", nz, "<f8"), ("row", nz, "<i8"), ("col", nz, "<i8"), ("frac_a", ns, "<f8"),
+                        ("frac_b", nd, "<f8"), ("area_a", ns, "<f8"), ("area_b", nd, "<f8")):
+        arrs[name] = np.frombuffer(blob, dtype=dt, count=n, offset=off)
+        off += 8 * n
+    return magic, version, endian, ns, nd, nz, off, arrs
+
+
+def test_weight_cache_round_trip(gpu, oracle):
+    """WeightCache blob: layout read back independently, deserialize
+    reproduces the CSR bit for bit (the reference's round-trip property),
+    triplets in any order accepted, and bad magic / version / truncation
+    rejected (prop_weight_cache.cpp)."""
+    import torch
+    src, dst = grids.latlon_deg(5.0), grids.cubed_sphere(8)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    blob = M.serialize()
+    magic, version, endian, ns, nd, nz, size, a = _read_blob(blob)
+    # the reference's magic value 0x43574841 (its comment calls it "AXWC"; the
+    # little-endian bytes of the value are b"AHWC")
+    assert (magic, version, endian) == (0x43574841, 1, 1) and blob[:4] == b"AHWC"
+    assert (ns, nd, nz) == (M.n_src, M.n_dst, M.nnz) and size == len(blob)
+    csr = M.to_csr()
+    rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
+    assert np.array_equal(a["row"], rows) and np.array_equal(a["col"], csr["col"]) and np.array_equal(a["w"], csr["val"])
+    M2 = gpu.Matrix.deserialize(blob)
+    csr2 = M2.to_csr()
+    for k in csr:
+        assert np.array_equal(csr[k], csr2[k]), k
+    x = torch.tensor(np.random.default_rng(2).standard_normal(M.n_src), device="cuda")
+    assert torch.equal(gpu.apply_f64(M, x), gpu.apply_f64(M2, x))
+    # triplets shuffled: the same matrix
+    perm = np.random.default_rng(3).permutation(nz)
+    b = bytearray(blob)
+    for name, off in (("w", 40), ("row", 40 + 8 * nz), ("col", 40 + 16 * nz)):
+        b[off:off + 8 * nz] = a[name][perm].tobytes()
+    csr3 = gpu.Matrix.deserialize(bytes(b)).to_csr()
+    for k in csr:
+        assert np.array_equal(csr[k], csr3[k]), k
+    # rejections
+    for bad in (b"XXXX" + blob[4:], blob[:4] + (2).to_bytes(4, "little") + blob[8:], blob[:41], blob[:20]):
+        with pytest.raises(gpu.InvalidArgument):
+            gpu.Matrix.deserialize(bad)
