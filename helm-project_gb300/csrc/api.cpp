@@ -536,14 +536,19 @@ int axgb_generate_weights(int src, int dst, const axgb_regrid_config *cfg_in, in
         auto M = std::make_shared<Matrix>();
         if (cfg.method == AXGB_CONSERVATIVE) {
             // dispatch of generate_conservative (weight_generator.cpp:3246-3302)
-            if (S->grid.regular && D->grid.regular)
-                throw Error(AXGB_ERR_UNSUPPORTED, "conservative: both meshes regular (regular fast path not provided)");
-            if (S->grid.rectilinear && D->grid.rectilinear)
+            bool done = false;
+            if (S->grid.regular && D->grid.regular) {
+                done = generate_conservative_regular(*S, *D, cfg, *M);  // may decline
+                if (!done) M = std::make_shared<Matrix>();
+            } else if (S->grid.rectilinear && D->grid.rectilinear) {
                 throw Error(AXGB_ERR_UNSUPPORTED,
                             "conservative: both meshes rectilinear (rectilinear fast path not provided)");
-            if (cfg.line_type != AXGB_GREAT_CIRCLE)
-                throw Error(AXGB_ERR_UNSUPPORTED, "conservative: Cartesian line type not provided");
-            generate_conservative(*S, *D, cfg, *M);
+            }
+            if (!done) {
+                if (cfg.line_type != AXGB_GREAT_CIRCLE)
+                    throw Error(AXGB_ERR_UNSUPPORTED, "conservative: Cartesian line type not provided");
+                generate_conservative(*S, *D, cfg, *M);
+            }
         } else if (cfg.method == AXGB_BILINEAR) {
             // dispatch of generate_bilinear (weight_generator.cpp:2306-2345)
             if (S->grid.regular && D->grid.regular)

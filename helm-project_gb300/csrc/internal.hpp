@@ -238,6 +238,8 @@ void mesh_prepare(Mesh &m, cudaStream_t s);  // cell prep kernel (once)
 
 // weights.cu
 void generate_conservative(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
+// regular x regular fast path; false = declined (use generate_conservative)
+bool generate_conservative_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 
 // apply.cu

@@ -443,12 +443,165 @@ __global__ void k_fill(double *a, i64 n, double v) {
 
 inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
 
+// ─── regular x regular conservative fast path ──────────────────────────────
+// generate_conservative_rect (src/solver/weight_generator_conservative_rect.cpp
+// :87-415): per destination cell the overlapping source cells by index
+// arithmetic and their exact spherical-rectangle overlap (:50-66), one thread
+// per destination cell, counted (pass 1) then written (pass 2) in the
+// reference's (js, is) loop order.
+struct RectGrid {
+    i64 ni, nj;
+    double lon_min, dlon, lat_min, dlat;
+};
+struct RectArgs {
+    RectGrid sg, dg;
+    bool src_global;
+    const double *sa, *da;  // cell areas
+    const int *smask, *dmask;
+    i64 n_src, n_dst;
+};
+
+__device__ __forceinline__ double band_area(double lo, double dlat, double dlon) {
+    constexpr double d2r = 3.14159265358979323846 / 180.0;
+    const double hi = lo + dlat;
+    return (dlon * d2r) * (sin(hi * d2r) - sin(lo * d2r));
+}
+
+__global__ void k_band_area(RectGrid g, const double *user, i64 n, double *area) {
+    const i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    area[c] = user ? user[c] : band_area(g.lat_min + static_cast<double>(c / g.ni) * g.dlat, g.dlat, g.dlon);
+}
+
+template <bool FILL>
+__global__ void k_rect(RectArgs a, int *count, const i64 *offs, int *cs, int *cd, double *ov) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= a.n_dst) return;
+    int n = 0;
+    i64 at = FILL ? offs[j] : 0;
+    const i64 jd = j / a.dg.ni, id = j - jd * a.dg.ni;
+    if (!(a.dmask && a.dmask[j] == 0) && a.da[j] > 0.0) {
+        const double d_lo_x = a.dg.lon_min + static_cast<double>(id) * a.dg.dlon, d_hi_x = d_lo_x + a.dg.dlon;
+        const double d_lo_y = a.dg.lat_min + static_cast<double>(jd) * a.dg.dlat, d_hi_y = d_lo_y + a.dg.dlat;
+        double dlx = d_lo_x, dhx = d_hi_x;
+        if (a.src_global) {
+            const double shift = 360.0 * floor((d_lo_x - a.sg.lon_min) / 360.0);
+            dlx = d_lo_x - shift;
+            dhx = d_hi_x - shift;
+        }
+        const int sni = static_cast<int>(a.sg.ni), snj = static_cast<int>(a.sg.nj);
+        int is_lo = static_cast<int>(floor((dlx - a.sg.lon_min) / a.sg.dlon));
+        int is_hi = static_cast<int>(floor((dhx - a.sg.lon_min) / a.sg.dlon));
+        int js_lo = static_cast<int>(floor((d_lo_y - a.sg.lat_min) / a.sg.dlat));
+        int js_hi = static_cast<int>(floor((d_hi_y - a.sg.lat_min) / a.sg.dlat));
+        if (!a.src_global) {
+            is_lo = max(0, is_lo);
+            is_hi = min(sni - 1, is_hi);
+        }
+        js_lo = max(0, js_lo);
+        js_hi = min(snj - 1, js_hi);
+        constexpr double d2r = 3.14159265358979323846 / 180.0;
+        if (is_lo <= is_hi && js_lo <= js_hi) {
+            for (int js = js_lo; js <= js_hi; ++js)
+                for (int is = is_lo; is <= is_hi; ++is) {
+                    const int ia = a.src_global ? ((is % sni) + sni) % sni : is;
+                    const i64 c = static_cast<i64>(js) * sni + ia;
+                    if (c >= a.n_src || (a.smask && a.smask[c] == 0) || a.sa[c] <= 0.0) continue;
+                    const double s_lo_x = a.sg.lon_min + static_cast<double>(is) * a.sg.dlon, s_hi_x = s_lo_x + a.sg.dlon;
+                    const double s_lo_y = a.sg.lat_min + static_cast<double>(js) * a.sg.dlat, s_hi_y = s_lo_y + a.sg.dlat;
+                    const double dx = fmax(0.0, fmin(s_hi_x, dhx) - fmax(s_lo_x, dlx));
+                    const double lo_y = fmax(s_lo_y, d_lo_y), hi_y = fmin(s_hi_y, d_hi_y);
+                    if (hi_y <= lo_y || dx <= 0.0) continue;
+                    const double o = (dx * d2r) * (sin(hi_y * d2r) - sin(lo_y * d2r));
+                    if (o <= 0.0) continue;
+                    if (FILL) {
+                        cs[at] = static_cast<int>(c);
+                        cd[at] = static_cast<int>(j);
+                        ov[at] = o;
+                        ++at;
+                    } else {
+                        ++n;
+                    }
+                }
+        }
+    }
+    if (!FILL) count[j] = n;
+}
+
 using Clock = std::chrono::steady_clock;
 inline double ms_since(Clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
 }
 
 }  // namespace
+
+// Kept pairs (overlap > 0, weight_generator.cpp:3682) of the candidate list
+// (cs, cd, ov) into the CSR of out: weights, frac_b per row and frac_a per
+// column (the steps of :3684-3724), areas copied from area_src / area_dst.
+static void assemble(DBuf<int> &cs, DBuf<int> &cd, DBuf<double> &ov, i64 n_cand, const double *area_src,
+                     const double *area_dst, const MeshView &D, const axgb_regrid_config &cfg, Matrix &out,
+                     cudaStream_t s) {
+    const i64 n_src = out.n_src, n_dst = out.n_dst;
+    DBuf<int> keep(n_cand);
+    DBuf<i64> pos(n_cand + 1);
+    i64 nnz = 0;
+    if (n_cand > 0) {
+        k_keep_flags<<<nblk(n_cand, 256), 256, 0, s>>>(ov.p, n_cand, keep.p);
+        scan_exclusive_i32_to_i64(keep.p, pos.p, n_cand, s);
+        AXGB_CUDA(cudaMemcpy(&nnz, pos.p + n_cand, sizeof(i64), cudaMemcpyDeviceToHost));
+    }
+    DBuf<std::uint64_t> key(nnz), key2(nnz);
+    DBuf<int> vals(nnz), vals2(nnz);
+    DBuf<double> kov(nnz);
+    out.row_ptr.alloc(n_dst + 1);
+    out.col.alloc(nnz);
+    out.val.alloc(nnz);
+    out.frac_a.alloc(n_src);
+    out.frac_b.alloc(n_dst);
+    out.area_a.alloc(n_src);
+    out.area_b.alloc(n_dst);
+    DBuf<double> ovs(nnz);
+    DBuf<int> rcnt(n_dst), ccnt(n_src), col_ptr(n_src + 1);
+    rcnt.zero(s);
+    ccnt.zero(s);
+    if (nnz > 0) {
+        k_compact<<<nblk(n_cand, 256), 256, 0, s>>>(ov.p, cs.p, cd.p, pos.p, n_cand, key.p, vals.p, kov.p);
+        int rbits = 32;
+        while (rbits < 64 && (static_cast<unsigned long long>(n_dst) >> (rbits - 32)) > 0) ++rbits;
+        radix_sort_pairs_u64(key.p, vals.p, nnz, rbits, s);
+        k_count_keys<<<nblk(nnz, 256), 256, 0, s>>>(key.p, nnz, rcnt.p);
+        k_csr_cols<<<nblk(nnz, 256), 256, 0, s>>>(key.p, vals.p, kov.p, nnz, out.col.p, ovs.p, key2.p, vals2.p);
+        AXGB_CUDA(cudaGetLastError());
+        int cbits = 32;
+        while (cbits < 64 && (static_cast<unsigned long long>(n_src) >> (cbits - 32)) > 0) ++cbits;
+        radix_sort_pairs_u64(key2.p, vals2.p, nnz, cbits, s);
+        k_count_keys<<<nblk(nnz, 256), 256, 0, s>>>(key2.p, nnz, ccnt.p);
+        AXGB_CUDA(cudaGetLastError());
+    }
+    scan_exclusive_i32(rcnt.p, out.row_ptr.p, n_dst, s);
+    scan_exclusive_i32(ccnt.p, col_ptr.p, n_src, s);
+    AXGB_CUDA(cudaMemcpyAsync(out.area_a.p, area_src, sizeof(double) * n_src, cudaMemcpyDeviceToDevice, s));
+    AXGB_CUDA(cudaMemcpyAsync(out.area_b.p, area_dst, sizeof(double) * n_dst, cudaMemcpyDeviceToDevice, s));
+    if (n_dst > 0)
+        k_rows<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, ovs.p, area_dst, n_dst,
+                                               cfg.norm_type == AXGB_FRACAREA ? 1 : 0, out.val.p, out.frac_b.p);
+    if (n_src > 0)
+        k_cols<<<nblk(n_src, 256), 256, 0, s>>>(col_ptr.p, vals2.p, ovs.p, area_src, n_src, out.frac_a.p);
+    AXGB_CUDA(cudaGetLastError());
+    if (cfg.unmapped == AXGB_UNMAPPED_ERROR && n_dst > 0) {
+        DBuf<int> bad(1);
+        bad.zero(s);
+        k_unmapped<<<nblk(n_dst, 256), 256, 0, s>>>(D, out.row_ptr.p, bad.p);
+        int h_bad = 0;
+        AXGB_CUDA(cudaMemcpy(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h_bad > 0)
+            throw Error(AXGB_ERR_UNMAPPED,
+                        "generate_conservative: " + std::to_string(h_bad) + " unmapped destination cell(s)");
+    }
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    out.nnz = nnz;
+    out.stats[3] = nnz;
+}
 
 void generate_conservative(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {
     cudaStream_t s = 0;
@@ -545,68 +698,63 @@ void generate_conservative(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, 
 
     // 5. assembly
     t0 = Clock::now();
-    DBuf<int> keep(n_cand);
-    DBuf<i64> pos(n_cand + 1);
-    i64 nnz = 0;
-    if (n_cand > 0) {
-        k_keep_flags<<<nblk(n_cand, 256), 256, 0, s>>>(ov.p, n_cand, keep.p);
-        scan_exclusive_i32_to_i64(keep.p, pos.p, n_cand, s);
-        AXGB_CUDA(cudaMemcpy(&nnz, pos.p + n_cand, sizeof(i64), cudaMemcpyDeviceToHost));
-    }
-    DBuf<std::uint64_t> key(nnz), key2(nnz);
-    DBuf<int> vals(nnz), vals2(nnz);
-    DBuf<double> kov(nnz);
-    out.row_ptr.alloc(n_dst + 1);
-    out.col.alloc(nnz);
-    out.val.alloc(nnz);
-    out.frac_a.alloc(n_src);
-    out.frac_b.alloc(n_dst);
-    out.area_a.alloc(n_src);
-    out.area_b.alloc(n_dst);
-    DBuf<double> ovs(nnz);
-    DBuf<int> rcnt(n_dst), ccnt(n_src), col_ptr(n_src + 1);
-    rcnt.zero(s);
-    ccnt.zero(s);
-    if (nnz > 0) {
-        k_compact<<<nblk(n_cand, 256), 256, 0, s>>>(ov.p, cs.p, cd.p, pos.p, n_cand, key.p, vals.p, kov.p);
-        int rbits = 32;
-        while (rbits < 64 && (static_cast<unsigned long long>(n_dst) >> (rbits - 32)) > 0) ++rbits;
-        radix_sort_pairs_u64(key.p, vals.p, nnz, rbits, s);
-        k_count_keys<<<nblk(nnz, 256), 256, 0, s>>>(key.p, nnz, rcnt.p);
-        k_csr_cols<<<nblk(nnz, 256), 256, 0, s>>>(key.p, vals.p, kov.p, nnz, out.col.p, ovs.p, key2.p, vals2.p);
-        AXGB_CUDA(cudaGetLastError());
-        int cbits = 32;
-        while (cbits < 64 && (static_cast<unsigned long long>(n_src) >> (cbits - 32)) > 0) ++cbits;
-        radix_sort_pairs_u64(key2.p, vals2.p, nnz, cbits, s);
-        k_count_keys<<<nblk(nnz, 256), 256, 0, s>>>(key2.p, nnz, ccnt.p);
-        AXGB_CUDA(cudaGetLastError());
-    }
-    scan_exclusive_i32(rcnt.p, out.row_ptr.p, n_dst, s);
-    scan_exclusive_i32(ccnt.p, col_ptr.p, n_src, s);
-    AXGB_CUDA(cudaMemcpyAsync(out.area_a.p, S.area, sizeof(double) * n_src, cudaMemcpyDeviceToDevice, s));
-    AXGB_CUDA(cudaMemcpyAsync(out.area_b.p, D.area, sizeof(double) * n_dst, cudaMemcpyDeviceToDevice, s));
-    if (n_dst > 0)
-        k_rows<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, ovs.p, D.area, n_dst,
-                                               cfg.norm_type == AXGB_FRACAREA ? 1 : 0, out.val.p, out.frac_b.p);
-    if (n_src > 0)
-        k_cols<<<nblk(n_src, 256), 256, 0, s>>>(col_ptr.p, vals2.p, ovs.p, S.area, n_src, out.frac_a.p);
-    AXGB_CUDA(cudaGetLastError());
-    if (cfg.unmapped == AXGB_UNMAPPED_ERROR && n_dst > 0) {
-        DBuf<int> bad(1);
-        bad.zero(s);
-        k_unmapped<<<nblk(n_dst, 256), 256, 0, s>>>(D, out.row_ptr.p, bad.p);
-        int h_bad = 0;
-        AXGB_CUDA(cudaMemcpy(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
-        if (h_bad > 0)
-            throw Error(AXGB_ERR_UNMAPPED,
-                        "generate_conservative: " + std::to_string(h_bad) + " unmapped destination cell(s)");
-    }
-    AXGB_CUDA(cudaStreamSynchronize(s));
-    out.nnz = nnz;
-    out.stats[3] = nnz;
+    assemble(cs, cd, ov, n_cand, S.area, D.area, D, cfg, out, s);
     out.times_ms[4] = ms_since(t0);
     out.times_ms[5] = ms_since(t_all);
     slice_centroids(D, out, s);  // locality hint for the blocked apply layout (not timed)
+}
+
+bool generate_conservative_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {
+    const GridInfo &sg = src.grid, &dg = dst.grid;
+    // decline non-global grids whose longitude ranges do not fit (:127-147)
+    const bool src_global = static_cast<double>(sg.ni) * sg.dlon > 350.0;
+    const bool dst_global = static_cast<double>(dg.ni) * dg.dlon > 350.0;
+    if (!src_global && !dst_global &&
+        (dg.lon_min < sg.lon_min - sg.dlon * 0.5 || dg.lon_max > sg.lon_max + sg.dlon * 0.5))
+        return false;
+    cudaStream_t s = 0;
+    auto t_all = Clock::now();
+    mesh_prepare(src, s);
+    mesh_prepare(dst, s);
+    MeshView D = dst.view();
+    const i64 n_src = src.n_cells, n_dst = dst.n_cells;
+    AXGB_REQUIRE(n_src < (i64(1) << 31) - 1 && n_dst < (i64(1) << 31) - 1, "meshes above 2^31 cells");
+    out.n_src = n_src;
+    out.n_dst = n_dst;
+    RectArgs a;
+    a.sg = {sg.ni, sg.nj, sg.lon_min, sg.dlon, sg.lat_min, sg.dlat};
+    a.dg = {dg.ni, dg.nj, dg.lon_min, dg.dlon, dg.lat_min, dg.dlat};
+    a.src_global = src_global;
+    a.n_src = n_src;
+    a.n_dst = n_dst;
+    a.smask = src.has_mask ? src.d_mask.p : nullptr;
+    a.dmask = dst.has_mask ? dst.d_mask.p : nullptr;
+    DBuf<double> sa(n_src), da(n_dst);
+    if (n_src) k_band_area<<<nblk(n_src, 256), 256, 0, s>>>(a.sg, src.has_area ? src.d_user_area.p : nullptr, n_src, sa.p);
+    if (n_dst) k_band_area<<<nblk(n_dst, 256), 256, 0, s>>>(a.dg, dst.has_area ? dst.d_user_area.p : nullptr, n_dst, da.p);
+    a.sa = sa.p;
+    a.da = da.p;
+    DBuf<int> counts(n_dst);
+    DBuf<i64> offs(n_dst + 1);
+    if (n_dst) k_rect<false><<<nblk(n_dst, 128), 128, 0, s>>>(a, counts.p, nullptr, nullptr, nullptr, nullptr);
+    AXGB_CUDA(cudaGetLastError());
+    scan_exclusive_i32_to_i64(counts.p, offs.p, n_dst, s);
+    i64 n_cand = 0;
+    AXGB_CUDA(cudaMemcpy(&n_cand, offs.p + n_dst, sizeof(i64), cudaMemcpyDeviceToHost));
+    AXGB_REQUIRE(n_cand < (i64(1) << 31), "more than 2^31 overlapping pairs");
+    if (cfg.unmapped == AXGB_UNMAPPED_ERROR && n_cand == 0) return false;  // the general path diagnoses it
+    DBuf<int> cs(n_cand), cd(n_cand);
+    DBuf<double> ov(n_cand);
+    if (n_cand) k_rect<true><<<nblk(n_dst, 128), 128, 0, s>>>(a, nullptr, offs.p, cs.p, cd.p, ov.p);
+    AXGB_CUDA(cudaGetLastError());
+    out.stats[0] = out.stats[1] = n_cand;
+    auto t0 = Clock::now();
+    assemble(cs, cd, ov, n_cand, sa.p, da.p, D, cfg, out, s);
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    out.times_ms[4] = ms_since(t0);
+    out.times_ms[5] = ms_since(t_all);
+    slice_centroids(D, out, s);
+    return true;
 }
 
 void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {

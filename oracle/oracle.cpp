@@ -576,6 +576,109 @@ struct orc_result {
     double seconds = 0.0;
 };
 
+// Regular x regular conservative fast path: generate_conservative_rect
+// (src/solver/weight_generator_conservative_rect.cpp:87-415) with its
+// rect_overlap_spherical (:50-66). Returns false to decline (non-global grids
+// whose longitude ranges do not fit, :127-147), leaving *res untouched.
+static bool conservative_rect(const Mesh &S, const Mesh &D, const GridInfo &sg, const GridInfo &dg, int norm_type,
+                              orc_result *res) {
+    const i64 n_src = S.n_cells, n_dst = D.n_cells;
+    const i64 sni = sg.ni, snj = sg.nj, dni = dg.ni;
+    const double wrap = 350.0;  // degrees
+    const bool src_global = static_cast<double>(sni) * sg.dlon > wrap;
+    const bool dst_global = static_cast<double>(dni) * dg.dlon > wrap;
+    if (!src_global && !dst_global) {
+        if (dg.lon_min < sg.lon_min - sg.dlon * 0.5 || dg.lon_max > sg.lon_max + sg.dlon * 0.5) return false;
+    }
+    constexpr double d2r = 3.14159265358979323846 / 180.0;
+    auto band_area = [&](double lo, double dlat, double dlon) {
+        double hi = lo + dlat;
+        double dl = dlon * d2r, lo_r = lo * d2r, hi_r = hi * d2r;
+        return dl * (std::sin(hi_r) - std::sin(lo_r));
+    };
+    std::vector<double> sa(n_src), da(n_dst);
+    for (i64 c = 0; c < n_src; ++c)
+        sa[c] = S.areas ? S.areas[c] : band_area(sg.lat_min + static_cast<double>(c / sni) * sg.dlat, sg.dlat, sg.dlon);
+    for (i64 c = 0; c < n_dst; ++c)
+        da[c] = D.areas ? D.areas[c] : band_area(dg.lat_min + static_cast<double>(c / dni) * dg.dlat, dg.dlat, dg.dlon);
+    std::vector<i64> rows, cols;
+    std::vector<double> ovs;
+    const i64 dnj = dg.nj;
+    for (i64 jd = 0; jd < dnj; ++jd)
+        for (i64 id = 0; id < dni; ++id) {
+            const i64 j = jd * dni + id;
+            if (D.mask && D.mask[j] == 0) continue;
+            const double d_lo_x = dg.lon_min + static_cast<double>(id) * dg.dlon, d_hi_x = d_lo_x + dg.dlon;
+            const double d_lo_y = dg.lat_min + static_cast<double>(jd) * dg.dlat, d_hi_y = d_lo_y + dg.dlat;
+            double dlx = d_lo_x, dhx = d_hi_x;
+            if (src_global) {
+                const double shift = 360.0 * std::floor((d_lo_x - sg.lon_min) / 360.0);
+                dlx = d_lo_x - shift;
+                dhx = d_hi_x - shift;
+            }
+            if (da[j] <= 0.0) continue;
+            int is_lo = static_cast<int>(std::floor((dlx - sg.lon_min) / sg.dlon));
+            int is_hi = static_cast<int>(std::floor((dhx - sg.lon_min) / sg.dlon));
+            int js_lo = static_cast<int>(std::floor((d_lo_y - sg.lat_min) / sg.dlat));
+            int js_hi = static_cast<int>(std::floor((d_hi_y - sg.lat_min) / sg.dlat));
+            if (!src_global) {
+                is_lo = std::max(0, is_lo);
+                is_hi = std::min(static_cast<int>(sni) - 1, is_hi);
+            }
+            js_lo = std::max(0, js_lo);
+            js_hi = std::min(static_cast<int>(snj) - 1, js_hi);
+            if (is_lo > is_hi || js_lo > js_hi) continue;
+            for (int js = js_lo; js <= js_hi; ++js)
+                for (int is = is_lo; is <= is_hi; ++is) {
+                    int ia = is;
+                    if (src_global) ia = ((is % static_cast<int>(sni)) + static_cast<int>(sni)) % static_cast<int>(sni);
+                    const i64 c = static_cast<i64>(js) * sni + ia;
+                    if (c >= n_src) continue;
+                    if (S.mask && S.mask[c] == 0) continue;
+                    if (sa[c] <= 0.0) continue;
+                    const double s_lo_x = sg.lon_min + static_cast<double>(is) * sg.dlon, s_hi_x = s_lo_x + sg.dlon;
+                    const double s_lo_y = sg.lat_min + static_cast<double>(js) * sg.dlat, s_hi_y = s_lo_y + sg.dlat;
+                    double dx = std::fmax(0.0, std::fmin(s_hi_x, dhx) - std::fmax(s_lo_x, dlx));
+                    double lo_y = std::fmax(s_lo_y, d_lo_y), hi_y = std::fmin(s_hi_y, d_hi_y);
+                    if (hi_y <= lo_y || dx <= 0.0) continue;
+                    const double ov = (dx * d2r) * (std::sin(hi_y * d2r) - std::sin(lo_y * d2r));
+                    if (ov <= 0.0) continue;
+                    rows.push_back(j);
+                    cols.push_back(c);
+                    ovs.push_back(ov);
+                }
+        }
+    // weights, FracArea, fractions (:323-345), then (row, col) order as to_csr
+    std::vector<double> fa(n_src, 0.0), fb(n_dst, 0.0), w(ovs.size());
+    for (size_t k = 0; k < ovs.size(); ++k) {
+        w[k] = std::max(ovs[k] / da[rows[k]], 0.0);
+        fa[cols[k]] += ovs[k] / sa[cols[k]];
+        fb[rows[k]] += ovs[k] / da[rows[k]];
+    }
+    if (norm_type == 1)
+        for (size_t k = 0; k < w.size(); ++k)
+            if (fb[rows[k]] > 0.0) w[k] /= fb[rows[k]];
+    for (auto &v : fa) v = std::min(v, 1.0);
+    for (auto &v : fb) v = std::min(v, 1.0);
+    std::vector<size_t> perm(w.size());
+    std::iota(perm.begin(), perm.end(), 0);
+    std::sort(perm.begin(), perm.end(), [&](size_t a, size_t b) {
+        return rows[a] != rows[b] ? rows[a] < rows[b] : cols[a] < cols[b];
+    });
+    res->n_src = n_src;
+    res->n_dst = n_dst;
+    for (size_t q : perm) {
+        res->row.push_back(rows[q]);
+        res->col.push_back(cols[q]);
+        res->w.push_back(w[q]);
+    }
+    res->frac_a = fa;
+    res->frac_b = fb;
+    res->area_a = sa;
+    res->area_b = da;
+    return true;
+}
+
 extern "C" {
 
 int orc_num_threads() {
@@ -685,7 +788,17 @@ int orc_conservative(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i6
     Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, sareas, smask};
     Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, dareas, dmask};
     GridInfo sg = detect(S), dg = detect(D);
-    if ((sg.regular && dg.regular) || (sg.rectilinear && dg.rectilinear)) return -2;
+    // dispatch of generate_conservative (src/solver/weight_generator.cpp:3260-3296)
+    if (sg.regular && dg.regular) {
+        auto *res = new orc_result;
+        if (conservative_rect(S, D, sg, dg, norm_type, res) && (unmapped != 0 || !res->w.empty())) {
+            *out = res;
+            return 0;
+        }
+        delete res;  // declined: the general path below
+    } else if (sg.rectilinear && dg.rectilinear) {
+        return -2;  // the non-uniform rectilinear fast path is not restated
+    }
 
     auto sxyz = node_xyz(S), dxyz = node_xyz(D);
     // degenerate scan

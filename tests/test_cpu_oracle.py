@@ -197,3 +197,18 @@ def test_apply_masked_oracle(oracle):
     full = oracle.apply_csr(w, x, compensated=False)[0]
     assert np.all(y[mask == 0] == -7.0)
     assert np.allclose(y[mask == 1], full[mask == 1], rtol=1e-14)
+
+
+def test_conservative_regular_known_answer(oracle):
+    """The regular x regular fast path: a 2 deg cell over four 1 deg cells
+    gets the exact spherical-band area fractions; row sums and source
+    fractions are 1 for global grids."""
+    w = oracle.conservative(grids.latlon_deg(1.0), grids.latlon_deg(2.0))
+    d2r = np.pi / 180.0
+    band = lambda lo, hi: np.sin(hi * d2r) - np.sin(lo * d2r)
+    sel = w.row == 0
+    assert np.array_equal(w.col[sel], [0, 1, 360, 361])
+    exp = np.array([band(-90, -89), band(-90, -89), band(-89, -88), band(-89, -88)]) / band(-90, -88) / 2
+    assert np.allclose(w.w[sel], exp, rtol=1e-14)
+    rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
+    assert np.all(np.abs(rs - 1) < 1e-14) and np.all(np.abs(w.frac_a - 1) < 1e-14)

@@ -104,8 +104,8 @@ def test_bilinear_parity(gpu, oracle):
 def test_unsupported_and_unmapped(gpu, oracle):
     a = gpu.make_regular_mesh(36, 18, 0.0, -90.0, 10.0, 10.0)
     b = gpu.make_regular_mesh(18, 9, 0.0, -90.0, 20.0, 20.0)
-    with pytest.raises(gpu.Unsupported):
-        gpu.generate_weights(a, b, {"method": "conservative"})
+    with pytest.raises(gpu.Unsupported):  # regular x regular bilinear fast path not provided
+        gpu.generate_weights(a, b, {"method": "bilinear"})
     with pytest.raises(gpu.Unsupported):
         gpu.generate_weights(a, b, {"method": "patch"})
     # a regional source leaves most of a global destination unmapped
@@ -466,3 +466,26 @@ def test_weight_cache_round_trip(gpu, oracle):
     for bad in (b"XXXX" + blob[4:], blob[:4] + (2).to_bytes(4, "little") + blob[8:], blob[:41], blob[:20]):
         with pytest.raises(gpu.InvalidArgument):
             gpu.Matrix.deserialize(bad)
+
+
+REGULAR_PAIRS = [
+    ("1deg->2deg", lambda: (grids.latlon_deg(1.0), grids.latlon_deg(2.0))),
+    ("2deg->1deg", lambda: (grids.latlon_deg(2.0), grids.latlon_deg(1.0))),
+    ("0.5deg->0.75deg", lambda: (grids.latlon_deg(0.5), grids.latlon_deg(0.75))),
+    ("regional 1deg->global 2deg", lambda: (grids.regular_latlon(40, 30, 20.0, -10.0, 1.0, 1.0), grids.latlon_deg(2.0))),
+    ("shifted global", lambda: (grids.regular_latlon(360, 180, -180.0, -90.0, 1.0, 1.0), grids.latlon_deg(3.0))),
+]
+
+
+@pytest.mark.parametrize("name,make", REGULAR_PAIRS)
+def test_conservative_regular_fast_path(gpu, oracle, name, make):
+    """Regular x regular conservative weights (the analytic fast path of
+    weight_generator_conservative_rect.cpp) against the oracle's restatement:
+    the index set bit-exact, values within 1e-12."""
+    src, dst = make()
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    wo = oracle.conservative(src, dst)
+    _check_weights(M, wo)
+    Mf = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst),
+                              {"method": "conservative", "norm_type": "FracArea"})
+    _check_weights(Mf, oracle.conservative(src, dst, norm_type=1))
