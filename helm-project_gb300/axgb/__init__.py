@@ -272,6 +272,15 @@ def parse_regrid_config(config: dict | None) -> RegridConfig:
                 setattr(cfg, field, int(v))
     if "use_limiter" in config:
         cfg.use_limiter = int(bool(config["use_limiter"]))
+    if "extrap_method" in config:  # ExtrapolationAction (regrid_config.hpp:65-88); not parsed by axis_py
+        v = config["extrap_method"]
+        table = {"none": 0, "nearest_wet": 1}
+        if isinstance(v, str):
+            if v not in table:
+                raise ValueError(f"Unknown extrap_method: {v}")
+            cfg.extrap_method = table[v]
+        else:
+            cfg.extrap_method = int(v)
     return cfg
 
 

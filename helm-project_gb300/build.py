@@ -29,6 +29,7 @@ UNITS = [
     ("apply.cu", []),
     ("staged.cu", []),
     ("scan_sort.cu", []),
+    ("coastal.cu", []),
 ]
 HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", os.path.join("..", "..", "include", "axgb.h")]
 

@@ -560,6 +560,8 @@ int axgb_generate_weights(int src, int dst, const axgb_regrid_config *cfg_in, in
             throw Error(AXGB_ERR_UNSUPPORTED, "generate_weights: method " + std::to_string(cfg.method) +
                                                   " not provided (Conservative1stOrder and Bilinear are)");
         }
+        // generate() applies the coastal post-pass to every method (weight_generator.cpp:2014)
+        coastal_postpass(*S, *D, cfg, *M);
         *mat = R.add(R.mats, M);
     });
 }

@@ -242,6 +242,10 @@ void generate_conservative(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, 
 bool generate_conservative_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 
+// coastal.cu: wet renormalisation and NearestWet extrapolation after any
+// method when the source mesh has a cell mask
+void coastal_postpass(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &m);
+
 // apply.cu
 void matrix_prepare(Matrix &m, int format, cudaStream_t s);
 void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s);

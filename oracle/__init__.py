@@ -50,6 +50,25 @@ class Weights:
         return np.cumsum(rp)
 
 
+def centroid_xy(m):
+    """compute_cell_centroids_xy (src/solver/weight_generator.cpp:75-138) for a
+    spherical-degree mesh, as float32 (lon, lat) degrees."""
+    pi = 3.14159265358979323846
+    lon = m.node_lonlat[:, 0] * pi / 180.0
+    lat = m.node_lonlat[:, 1] * pi / 180.0
+    nv = np.diff(m.conn_offsets)
+    cell = np.repeat(np.arange(m.n_cells), nv)
+    idx = m.conn_indices
+    sx = np.bincount(cell, weights=np.cos(lat[idx]) * np.cos(lon[idx]), minlength=m.n_cells)
+    sy = np.bincount(cell, weights=np.cos(lat[idx]) * np.sin(lon[idx]), minlength=m.n_cells)
+    sz = np.bincount(cell, weights=np.sin(lat[idx]), minlength=m.n_cells)
+    inv = 1.0 / nv
+    la = np.arcsin(sz * inv)
+    lo = np.arctan2(sy * inv, sx * inv)
+    lo = np.where(lo < 0.0, lo + 2.0 * pi, lo)
+    return (lo * 180.0 / pi).astype(np.float32), (la * 180.0 / pi).astype(np.float32)
+
+
 class Oracle:
     def __init__(self, path: str | None = None):
         if path is None:
@@ -145,15 +164,53 @@ class Oracle:
         self.L.orc_result_stats(h, st)
         return nnz, st
 
-    def conservative(self, src, dst, norm_type: int = 0, unmapped: int = 1, faithful: bool = False) -> Weights:
+    def conservative(self, src, dst, norm_type: int = 0, unmapped: int = 1, faithful: bool = False,
+                     src_mask=None, dst_mask=None) -> Weights:
         h = C.c_void_p()
         t0 = time.perf_counter()
-        rc = self.L.orc_conservative(*_mesh_args(src), None, None, *_mesh_args(dst), None, None, norm_type, unmapped,
-                                     int(faithful), C.byref(h))
+        sm = None if src_mask is None else np.ascontiguousarray(src_mask, np.int32)
+        dm = None if dst_mask is None else np.ascontiguousarray(dst_mask, np.int32)
+        rc = self.L.orc_conservative(*_mesh_args(src), None, None if sm is None else sm.ctypes.data_as(C.c_void_p),
+                                     *_mesh_args(dst), None, None if dm is None else dm.ctypes.data_as(C.c_void_p),
+                                     norm_type, unmapped, int(faithful), C.byref(h))
         dt = time.perf_counter() - t0
         if rc != 0:
             raise RuntimeError(f"oracle conservative failed rc={rc}")
         return self._collect(h, src.n_cells, dst.n_cells, dt)
+
+    def coastal(self, w: Weights, src, dst, src_mask, nearest_wet: bool = True) -> Weights:
+        """coastal_renormalize_and_extrapolate (src/solver/weight_generator.cpp:
+        1736-1881) on CSR-ordered weights: wet entries (mask > 0) kept, a row
+        whose wet weights sum to s in (0, 1) divided by s (sums in CSR order),
+        and with NearestWet every row left empty given the wet source (mask != 0)
+        whose float (lon, lat) centroid (compute_cell_centroids_xy, :75-138) is
+        nearest, weight 1, ties to the lower index. Brute-force search."""
+        mask = np.asarray(src_mask)
+        keep = mask[w.col] > 0
+        s = np.zeros(w.n_dst)
+        for k in np.nonzero(keep)[0]:  # in CSR order, as the device pass sums
+            s[w.row[k]] += w.w[k]
+        row, col, val = w.row[keep], w.col[keep], w.w[keep].copy()
+        ren = (s[row] > 0.0) & (s[row] < 1.0)
+        val[ren] = val[ren] / s[row][ren]
+        if nearest_wet:
+            wet = np.nonzero(mask != 0)[0]
+            dry = np.setdiff1d(np.arange(w.n_dst), np.unique(row))
+            if len(wet) and len(dry):
+                sx, sy = centroid_xy(src)
+                dx, dy = centroid_xy(dst)
+                px, py = sx[wet], sy[wet]
+                add_c = []
+                for j in dry:
+                    ex = np.float32(dx[j]) - px
+                    ey = np.float32(dy[j]) - py
+                    d = ex * ex + ey * ey  # float32, no fused multiply-add
+                    add_c.append(wet[int(np.argmin(d))])
+                row = np.concatenate([row, dry])
+                col = np.concatenate([col, np.array(add_c, np.int64)])
+                val = np.concatenate([val, np.ones(len(dry))])
+        order = np.lexsort((col, row))
+        return Weights(w.n_src, w.n_dst, row[order], col[order], val[order], w.frac_a, w.frac_b, w.area_a, w.area_b)
 
     def bilinear(self, src, dst) -> Weights:
         h = C.c_void_p()

@@ -212,3 +212,29 @@ def test_conservative_regular_known_answer(oracle):
     assert np.allclose(w.w[sel], exp, rtol=1e-14)
     rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
     assert np.all(np.abs(rs - 1) < 1e-14) and np.all(np.abs(w.frac_a - 1) < 1e-14)
+
+
+def _land_mask(src):
+    # a rectangular "continent" of masked source cells
+    c = grids.cell_centroids_xyz(src)
+    lat = np.degrees(np.arcsin(c[:, 2]))
+    lon = np.degrees(np.arctan2(c[:, 1], c[:, 0])) % 360
+    return (~((lat > -30) & (lat < 40) & (lon > 20) & (lon < 110))).astype(np.int32)
+
+
+def test_coastal_postpass_oracle(oracle):
+    """Wet renormalisation and NearestWet extrapolation: coastal rows sum to
+    1, land rows take the nearest wet source with weight 1."""
+    src, dst = grids.latlon_deg(5.0), grids.cubed_sphere(8)
+    mask = _land_mask(src)
+    w = oracle.conservative(src, dst, src_mask=mask)
+    assert np.all(mask[w.col] > 0)
+    wc = oracle.coastal(w, src, dst, mask)
+    rs = np.bincount(wc.row, weights=wc.w, minlength=wc.n_dst)
+    counts = np.bincount(wc.row, minlength=wc.n_dst)
+    assert np.all(counts > 0)
+    assert np.all(np.abs(rs - 1.0) < 1e-12)
+    dry = np.setdiff1d(np.arange(w.n_dst), np.unique(w.row))
+    assert len(dry) > 0 and np.all(counts[dry] == 1)
+    none = oracle.coastal(w, src, dst, mask, nearest_wet=False)
+    assert set(np.unique(none.row)) == set(np.unique(w.row))

@@ -489,3 +489,29 @@ def test_conservative_regular_fast_path(gpu, oracle, name, make):
     Mf = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst),
                               {"method": "conservative", "norm_type": "FracArea"})
     _check_weights(Mf, oracle.conservative(src, dst, norm_type=1))
+
+
+def _land_mask(src):
+    c = grids.cell_centroids_xyz(src)
+    lat = np.degrees(np.arcsin(c[:, 2]))
+    lon = np.degrees(np.arctan2(c[:, 1], c[:, 0])) % 360
+    return (~((lat > -30) & (lat < 40) & (lon > 20) & (lon < 110))).astype(np.int32)
+
+
+@pytest.mark.parametrize("name,make", [
+    ("5deg->C8", lambda: (grids.latlon_deg(5.0), grids.cubed_sphere(8))),
+    ("C24->2deg", lambda: (grids.cubed_sphere(24), grids.latlon_deg(2.0))),
+])
+def test_coastal_postpass_parity(gpu, oracle, name, make):
+    """A masked source: generate_weights applies the coastal post-pass (wet
+    renormalisation, NearestWet extrapolation) as the reference's generate()
+    does; against the oracle on the same kept pairs."""
+    src, dst = make()
+    mask = _land_mask(src)
+    ms = gpu.Mesh.from_arrays(src.node_lonlat, src.conn_offsets, src.conn_indices, mask=mask)
+    md = gpu.Mesh.from_grid(dst)
+    wo = oracle.conservative(src, dst, src_mask=mask)
+    for extrap, nearest in (("nearest_wet", True), ("none", False)):
+        M = gpu.generate_weights(ms, md, {"method": "conservative", "extrap_method": extrap})
+        ref = oracle.coastal(wo, src, dst, mask, nearest_wet=nearest)
+        _check_weights(M, ref)
