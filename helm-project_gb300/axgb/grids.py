@@ -80,6 +80,32 @@ def regular_latlon(ni: int, nj: int, lon_start: float = 0.0, lat_start: float = 
     return MeshArrays(node, off, idx, name=f"latlon{ni}x{nj}", shape=(ni, nj))
 
 
+def rectilinear(lon_edges, lat_edges) -> MeshArrays:
+    """Rectilinear lat-lon mesh on given (strictly increasing) cell edges, in
+    the node and cell layout of ``regular_latlon``: cell ``i + j*ni`` spans
+    ``lon_edges[i:i+2]`` x ``lat_edges[j:j+2]``."""
+    lon = np.asarray(lon_edges, dtype=np.float64)
+    lat = np.asarray(lat_edges, dtype=np.float64)
+    ni, nj = lon.size - 1, lat.size - 1
+    lon2 = np.broadcast_to(lon[None, :], (nj + 1, ni + 1)).reshape(-1)
+    lat2 = np.broadcast_to(lat[:, None], (nj + 1, ni + 1)).reshape(-1)
+    node = np.stack([lon2, lat2], axis=1).copy()
+    off = np.arange(0, 4 * ni * nj + 1, 4, dtype=np.int64)
+    return MeshArrays(node, off, _quad_connectivity(ni, nj), name=f"rect{ni}x{nj}", shape=(ni, nj))
+
+
+def equal_area_latlon(ni: int, nj: int, lon_start: float = 0.0, stretch: float = 0.0) -> MeshArrays:
+    """Global rectilinear mesh with equal-area latitude bands (edges at
+    asin of evenly spaced sines) and, for ``stretch`` > 0, longitudes packed
+    toward ``lon_start + 180``: a non-uniform grid on both axes."""
+    lat = np.degrees(np.arcsin(np.linspace(-1.0, 1.0, nj + 1)))
+    lat[0], lat[-1] = -90.0, 90.0
+    t = np.linspace(0.0, 1.0, ni + 1)
+    lon = lon_start + 360.0 * (t + stretch * np.sin(2.0 * np.pi * t) / (2.0 * np.pi))
+    lon[0], lon[-1] = lon_start, lon_start + 360.0
+    return rectilinear(lon, lat)
+
+
 def latlon_deg(res_deg: float) -> MeshArrays:
     """Global lat-lon grid with cell edges on integer multiples of ``res_deg``
     (lon 0..360, lat -90..90)."""

@@ -540,9 +540,10 @@ int axgb_generate_weights(int src, int dst, const axgb_regrid_config *cfg_in, in
             if (S->grid.regular && D->grid.regular) {
                 done = generate_conservative_regular(*S, *D, cfg, *M);  // may decline
                 if (!done) M = std::make_shared<Matrix>();
-            } else if (S->grid.rectilinear && D->grid.rectilinear) {
-                throw Error(AXGB_ERR_UNSUPPORTED,
-                            "conservative: both meshes rectilinear (rectilinear fast path not provided)");
+            }
+            if (!done && S->grid.rectilinear && D->grid.rectilinear) {
+                done = generate_conservative_rectilinear(*S, *D, cfg, *M);
+                if (!done) M = std::make_shared<Matrix>();
             }
             if (!done) {
                 if (cfg.line_type != AXGB_GREAT_CIRCLE)
@@ -551,11 +552,13 @@ int axgb_generate_weights(int src, int dst, const axgb_regrid_config *cfg_in, in
             }
         } else if (cfg.method == AXGB_BILINEAR) {
             // dispatch of generate_bilinear (weight_generator.cpp:2306-2345)
-            if (S->grid.regular && D->grid.regular)
-                throw Error(AXGB_ERR_UNSUPPORTED, "bilinear: both meshes regular (regular fast path not provided)");
-            if (!S->grid.rectilinear)
-                throw Error(AXGB_ERR_UNSUPPORTED, "bilinear: source is not rectilinear (BVH bilinear not provided)");
-            generate_bilinear(*S, *D, cfg, *M);
+            bool done = false;
+            if (S->grid.regular && D->grid.regular) done = generate_bilinear_regular(*S, *D, cfg, *M);
+            if (!done) {
+                if (!S->grid.rectilinear)
+                    throw Error(AXGB_ERR_UNSUPPORTED, "bilinear: source is not rectilinear (BVH bilinear not provided)");
+                generate_bilinear(*S, *D, cfg, *M);
+            }
         } else {
             throw Error(AXGB_ERR_UNSUPPORTED, "generate_weights: method " + std::to_string(cfg.method) +
                                                   " not provided (Conservative1stOrder and Bilinear are)");

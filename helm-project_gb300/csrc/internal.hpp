@@ -240,6 +240,11 @@ void mesh_prepare(Mesh &m, cudaStream_t s);  // cell prep kernel (once)
 void generate_conservative(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 // regular x regular fast path; false = declined (use generate_conservative)
 bool generate_conservative_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
+// rectilinear x rectilinear fast path (non-uniform edges); false = an empty
+// matrix under UnmappedAction::Error (use generate_conservative)
+bool generate_conservative_rectilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
+// regular x regular bilinear fast path; false = no destination cells (fall through)
+bool generate_bilinear_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 
 // coastal.cu: wet renormalisation and NearestWet extrapolation after any

@@ -318,8 +318,8 @@ __global__ void k_keep_flags(const double *ov, i64 n, int *keep) {
     if (k < n) keep[k] = ov[k] > 0.0 ? 1 : 0;
 }
 
-__global__ void k_compact(const double *ov, const int *cs, const int *cd, const i64 *pos, i64 n,
-                          std::uint64_t *key, int *vals, double *kov) {
+__global__ void k_compact(const double *ov, const double *fac, const int *cs, const int *cd, const i64 *pos, i64 n,
+                          std::uint64_t *key, int *vals, double *kov, double *kfac) {
     i64 k = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= n) return;
     if (ov[k] > 0.0) {
@@ -327,6 +327,7 @@ __global__ void k_compact(const double *ov, const int *cs, const int *cd, const 
         key[p] = (static_cast<unsigned long long>(cd[k]) << 32) | static_cast<unsigned>(cs[k]);
         vals[p] = static_cast<int>(p);
         kov[p] = ov[k];
+        if (fac) kfac[p] = fac[k];
     }
 }
 
@@ -335,8 +336,8 @@ __global__ void k_count_keys(const std::uint64_t *key, i64 n, int *cnt) {
     if (k < n) atomicAdd(&cnt[key[k] >> 32], 1);
 }
 
-__global__ void k_csr_cols(const std::uint64_t *key, const int *perm, const double *kov, i64 n, int *col,
-                           double *ov_sorted, std::uint64_t *key2, int *vals2) {
+__global__ void k_csr_cols(const std::uint64_t *key, const int *perm, const double *kov, const double *kfac, i64 n,
+                           int *col, double *ov_sorted, double *fac_sorted, std::uint64_t *key2, int *vals2) {
     i64 k = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= n) return;
     unsigned long long kk = key[k];
@@ -344,13 +345,15 @@ __global__ void k_csr_cols(const std::uint64_t *key, const int *perm, const doub
     unsigned j = static_cast<unsigned>(kk >> 32);
     col[k] = static_cast<int>(i);
     ov_sorted[k] = kov[perm[k]];
+    if (kfac) fac_sorted[k] = kfac[perm[k]];
     key2[k] = (static_cast<unsigned long long>(i) << 32) | j;
     vals2[k] = static_cast<int>(k);
 }
 
-// Weights and frac_b per row (weight_generator.cpp:3684-3716).
-__global__ void k_rows(const int *row_ptr, const double *ov, const double *area_dst, i64 n_dst, int fracarea,
-                       double *w, double *frac_b) {
+// Weights and frac_b per row (weight_generator.cpp:3684-3716); fb_pre, when
+// given, holds the row sums already taken in the generator's own order.
+__global__ void k_rows(const int *row_ptr, const double *ov, const double *area_dst, const double *fb_pre, i64 n_dst,
+                       int fracarea, double *w, double *frac_b) {
     i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n_dst) return;
     double ad = area_dst[j];
@@ -361,19 +364,21 @@ __global__ void k_rows(const int *row_ptr, const double *ov, const double *area_
         w[k] = fmax(wij, 0.0);
         fb += o / ad;
     }
+    if (fb_pre) fb = fb_pre[j];
     if (fracarea && fb > 0.0)
         for (int k = row_ptr[j]; k < row_ptr[j + 1]; ++k) w[k] /= fb;
     frac_b[j] = fmin(fb, 1.0);
 }
 
-// frac_a per source cell, contributions in ascending row order.
-__global__ void k_cols(const int *col_ptr, const int *perm2, const double *ov, const double *area_src, i64 n_src,
-                       double *frac_a) {
+// frac_a per source cell, contributions in ascending row order: ov / area,
+// or the per-pair contributions fac when the generator gives them.
+__global__ void k_cols(const int *col_ptr, const int *perm2, const double *ov, const double *fac,
+                       const double *area_src, i64 n_src, double *frac_a) {
     i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n_src) return;
     double as = area_src[i];
     double fa = 0.0;
-    for (int k = col_ptr[i]; k < col_ptr[i + 1]; ++k) fa += ov[perm2[k]] / as;
+    for (int k = col_ptr[i]; k < col_ptr[i + 1]; ++k) fa += fac ? fac[perm2[k]] : ov[perm2[k]] / as;
     frac_a[i] = fmin(fa, 1.0);
 }
 
@@ -436,6 +441,84 @@ __global__ void k_bilinear(MeshView D, const double *clon, int ni, const double 
     w[o + 3] = tx * ty;
 }
 
+// Regular x regular bilinear: generate_bilinear_rect
+// (src/solver/weight_generator_bilinear_rect.cpp:31-320), one thread per
+// destination cell. The point is the mean of the cell's vertex (lon, lat)
+// degrees, wrapped into [lon_min, lon_min + 360) on a periodic source; its
+// fractional cell-centre index is bounds-tested with a 1e-9 slack, floored,
+// clamped (wrapped in longitude when periodic), and the four weights are
+// written column-ascending (ties in emission order, as a stable to_csr).
+// cnt = 4 for a mapped row, 0 otherwise.
+struct BilRegArgs {
+    double lon_min, lat_min, dlon, dlat;
+    int ni, nj;
+    bool periodic;
+};
+
+__global__ void k_bilinear_reg(MeshView D, BilRegArgs g, int *cnt, int *col4, double *w4, int *n_unmapped) {
+    const i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= D.n_cells) return;
+    const int b = D.off[c], e = D.off[c + 1];
+    double ls = 0.0, ts = 0.0;
+    for (int k = b; k < e; ++k) {
+        const i64 n = D.idx[k];
+        ls += D.lonlat[n];
+        ts += D.lonlat[n + D.n_nodes];
+    }
+    double ld = ls / static_cast<double>(e - b);
+    const double td = ts / static_cast<double>(e - b);
+    if (g.periodic) {
+        double off = ld - g.lon_min;
+        off = off - floor(off / 360.0) * 360.0;
+        ld = g.lon_min + off;
+    }
+    const double fi = (ld - g.lon_min) / g.dlon - 0.5, fj = (td - g.lat_min) / g.dlat - 0.5;
+    const double tol = 1.0e-9;
+    bool inside = fj >= -0.5 - tol && fj <= static_cast<double>(g.nj) - 0.5 + tol;
+    if (!g.periodic) inside = inside && fi >= -0.5 - tol && fi <= static_cast<double>(g.ni) - 0.5 + tol;
+    if (!inside) {
+        cnt[c] = 0;
+        atomicAdd(n_unmapped, 1);
+        return;
+    }
+    int i = static_cast<int>(floor(fi)), j = static_cast<int>(floor(fj));
+    j = max(0, min(j, g.nj - 2));
+    i = g.periodic ? ((i % g.ni) + g.ni) % g.ni : max(0, min(i, g.ni - 2));
+    const double tx = fmin(1.0, fmax(0.0, fi - static_cast<double>(i)));
+    const double ty = fmin(1.0, fmax(0.0, fj - static_cast<double>(j)));
+    int i1 = i + 1;
+    if (i1 >= g.ni) i1 = g.periodic ? 0 : g.ni - 1;
+    const int j1 = min(j + 1, g.nj - 1);
+    int cc[4] = {j * g.ni + i, j * g.ni + i1, j1 * g.ni + i, j1 * g.ni + i1};
+    double ww[4] = {(1.0 - tx) * (1.0 - ty), tx * (1.0 - ty), (1.0 - tx) * ty, tx * ty};
+    for (int a = 1; a < 4; ++a)  // stable insertion sort by column
+        for (int q = a; q > 0 && cc[q - 1] > cc[q]; --q) {
+            const int tc = cc[q];
+            cc[q] = cc[q - 1];
+            cc[q - 1] = tc;
+            const double tw = ww[q];
+            ww[q] = ww[q - 1];
+            ww[q - 1] = tw;
+        }
+    cnt[c] = 4;
+    for (int k = 0; k < 4; ++k) {
+        col4[4 * c + k] = cc[k];
+        w4[4 * c + k] = ww[k];
+    }
+}
+
+__global__ void k_bilinear_reg_pack(const int *row_ptr, const int *cnt, const int *col4, const double *w4, i64 n_dst,
+                                    int *col, double *w, double *frac_b) {
+    const i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= n_dst) return;
+    const int p = row_ptr[c];
+    for (int k = 0; k < cnt[c]; ++k) {
+        col[p + k] = col4[4 * c + k];
+        w[p + k] = w4[4 * c + k];
+    }
+    frac_b[c] = cnt[c] ? 1.0 : 0.0;
+}
+
 __global__ void k_fill(double *a, i64 n, double v) {
     i64 k = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k < n) a[k] = v;
@@ -474,10 +557,11 @@ __global__ void k_band_area(RectGrid g, const double *user, i64 n, double *area)
 }
 
 template <bool FILL>
-__global__ void k_rect(RectArgs a, int *count, const i64 *offs, int *cs, int *cd, double *ov) {
+__global__ void k_rect(RectArgs a, int *count, const i64 *offs, int *cs, int *cd, double *ov, double *fb) {
     const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= a.n_dst) return;
     int n = 0;
+    double fbj = 0.0;  // frac_b in the reference's emission order
     i64 at = FILL ? offs[j] : 0;
     const i64 jd = j / a.dg.ni, id = j - jd * a.dg.ni;
     if (!(a.dmask && a.dmask[j] == 0) && a.da[j] > 0.0) {
@@ -518,6 +602,7 @@ __global__ void k_rect(RectArgs a, int *count, const i64 *offs, int *cs, int *cd
                         cs[at] = static_cast<int>(c);
                         cd[at] = static_cast<int>(j);
                         ov[at] = o;
+                        fbj += o / a.da[j];
                         ++at;
                     } else {
                         ++n;
@@ -526,6 +611,129 @@ __global__ void k_rect(RectArgs a, int *count, const i64 *offs, int *cs, int *cd
         }
     }
     if (!FILL) count[j] = n;
+    if (FILL) fb[j] = fbj;
+}
+
+// Non-uniform rectilinear grids: generate_conservative_rect_nonuniform
+// (src/solver/weight_generator_conservative_rect_nonuniform.cpp:52-311). Cell
+// c is (c % ni, c / ni) on the sorted unique edge coordinates ulon/ulat.
+struct RectNuGrid {
+    int ni, nj;
+    const double *ulon, *ulat;  // ni+1, nj+1 edges
+};
+struct RectNuArgs {
+    RectNuGrid sg, dg;
+    bool src_global;
+    double s_lon_min, s_lon_max;
+    const double *s_user, *d_user;  // mesh cell areas, or null
+    const int *smask, *dmask;
+    i64 n_src, n_dst;
+};
+
+__device__ __forceinline__ double band_area_edges(double lo_x, double hi_x, double lo_y, double hi_y) {
+    constexpr double d2r = 3.14159265358979323846 / 180.0;
+    double dlon = hi_x - lo_x;
+    dlon *= d2r;
+    return dlon * (sin(hi_y * d2r) - sin(lo_y * d2r));
+}
+
+__device__ __forceinline__ int lower_bound_d(const double *a, int n, double v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int upper_bound_e(const double *a, int n, double v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (!(v < a[mid])) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Reported areas from the unshifted edges (:251-300).
+__global__ void k_edge_area(RectNuGrid g, const double *user, i64 n, double *area) {
+    const i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const i64 ci = c % g.ni, cj = c / g.ni;
+    area[c] = user ? user[c] : band_area_edges(g.ulon[ci], g.ulon[ci + 1], g.ulat[cj], g.ulat[cj + 1]);
+}
+
+// One thread per destination cell, in the reference's loop order: the
+// destination box (shifted by whole turns onto a global source), its area
+// from those shifted edges, binary searches for the source index ranges
+// (:140-156), then every (js, is) with overlap > 1e-12 and a positive source
+// area, that area taken from the source edges as placed (+360 past the last
+// column). FILL writes the pairs, the overlap, the frac_a contribution, the
+// row's frac_b (emission order) and the area the weights divide by.
+template <bool FILL>
+__global__ void k_rect_nu(RectNuArgs a, int *count, const i64 *offs, int *cs, int *cd, double *ov, double *fac,
+                          double *fb, double *da_w) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= a.n_dst) return;
+    int n = 0;
+    i64 at = FILL ? offs[j] : 0;
+    double fbj = 0.0, area_dst = 0.0;
+    const int sni = a.sg.ni, snj = a.sg.nj;
+    const i64 jd = j / a.dg.ni, id = j - jd * a.dg.ni;
+    if (!(a.dmask && a.dmask[j] == 0)) {
+        const double d_lo_y = a.dg.ulat[jd], d_hi_y = a.dg.ulat[jd + 1];
+        double dlx = a.dg.ulon[id], dhx = a.dg.ulon[id + 1];
+        if (a.src_global) {
+            const double shift = 360.0 * floor((dlx - a.s_lon_min) / 360.0);
+            dlx = dlx - shift;
+            dhx = dhx - shift;
+        }
+        area_dst = a.d_user ? a.d_user[j] : band_area_edges(dlx, dhx, d_lo_y, d_hi_y);
+        if (area_dst > 0.0) {
+            const int is0 = max(0, lower_bound_d(a.sg.ulon, sni + 1, dlx) - 1);
+            int is1 = upper_bound_e(a.sg.ulon, sni + 1, dhx);
+            if (!a.src_global || dhx <= a.s_lon_max) is1 = min(sni - 1, is1);
+            const int js0 = max(0, lower_bound_d(a.sg.ulat, snj + 1, d_lo_y) - 1);
+            const int js1 = min(snj - 1, upper_bound_e(a.sg.ulat, snj + 1, d_hi_y));
+            constexpr double d2r = 3.14159265358979323846 / 180.0;
+            for (int js = js0; js <= js1; ++js)
+                for (int is = is0; is <= is1; ++is) {
+                    const int ia = a.src_global ? ((is % sni) + sni) % sni : is;
+                    const i64 c = ia + static_cast<i64>(js) * sni;
+                    if (a.smask && a.smask[c] == 0) continue;
+                    double s_lo_x = a.sg.ulon[ia], s_hi_x = a.sg.ulon[ia + 1];
+                    if (a.src_global && is >= sni) {
+                        s_lo_x += 360.0;
+                        s_hi_x += 360.0;
+                    }
+                    const double s_lo_y = a.sg.ulat[js], s_hi_y = a.sg.ulat[js + 1];
+                    const double dx = fmax(0.0, fmin(s_hi_x, dhx) - fmax(s_lo_x, dlx));
+                    const double lo_y = fmax(s_lo_y, d_lo_y), hi_y = fmin(s_hi_y, d_hi_y);
+                    if (hi_y <= lo_y || dx <= 0.0) continue;
+                    const double o = (dx * d2r) * (sin(hi_y * d2r) - sin(lo_y * d2r));
+                    if (!(o > 1e-12)) continue;
+                    const double area_src = a.s_user ? a.s_user[c] : band_area_edges(s_lo_x, s_hi_x, s_lo_y, s_hi_y);
+                    if (area_src <= 0.0) continue;
+                    if (FILL) {
+                        cs[at] = static_cast<int>(c);
+                        cd[at] = static_cast<int>(j);
+                        ov[at] = o;
+                        fac[at] = o / area_src;
+                        fbj += o / area_dst;
+                        ++at;
+                    } else {
+                        ++n;
+                    }
+                }
+        }
+    }
+    if (!FILL) count[j] = n;
+    if (FILL) {
+        fb[j] = fbj;
+        da_w[j] = area_dst;
+    }
 }
 
 using Clock = std::chrono::steady_clock;
@@ -535,12 +743,21 @@ inline double ms_since(Clock::time_point t0) {
 
 }  // namespace
 
+// What a fast path hands the assembly besides (cs, cd, ov).
+struct AssembleOpts {
+    const double *fac = nullptr;         // per-pair frac_a contribution (instead of ov / area_src)
+    const double *fb_pre = nullptr;      // per-row frac_b, summed in the generator's order
+    const double *area_a_out = nullptr;  // reported areas, when not the ones the weights divide by
+    const double *area_b_out = nullptr;
+    bool check_unmapped = true;          // the general path's UnmappedAction::Error check
+};
+
 // Kept pairs (overlap > 0, weight_generator.cpp:3682) of the candidate list
 // (cs, cd, ov) into the CSR of out: weights, frac_b per row and frac_a per
 // column (the steps of :3684-3724), areas copied from area_src / area_dst.
 static void assemble(DBuf<int> &cs, DBuf<int> &cd, DBuf<double> &ov, i64 n_cand, const double *area_src,
                      const double *area_dst, const MeshView &D, const axgb_regrid_config &cfg, Matrix &out,
-                     cudaStream_t s) {
+                     cudaStream_t s, const AssembleOpts &o = AssembleOpts{}) {
     const i64 n_src = out.n_src, n_dst = out.n_dst;
     DBuf<int> keep(n_cand);
     DBuf<i64> pos(n_cand + 1);
@@ -552,7 +769,7 @@ static void assemble(DBuf<int> &cs, DBuf<int> &cd, DBuf<double> &ov, i64 n_cand,
     }
     DBuf<std::uint64_t> key(nnz), key2(nnz);
     DBuf<int> vals(nnz), vals2(nnz);
-    DBuf<double> kov(nnz);
+    DBuf<double> kov(nnz), kfac(o.fac ? nnz : 0), facs(o.fac ? nnz : 0);
     out.row_ptr.alloc(n_dst + 1);
     out.col.alloc(nnz);
     out.val.alloc(nnz);
@@ -565,12 +782,14 @@ static void assemble(DBuf<int> &cs, DBuf<int> &cd, DBuf<double> &ov, i64 n_cand,
     rcnt.zero(s);
     ccnt.zero(s);
     if (nnz > 0) {
-        k_compact<<<nblk(n_cand, 256), 256, 0, s>>>(ov.p, cs.p, cd.p, pos.p, n_cand, key.p, vals.p, kov.p);
+        k_compact<<<nblk(n_cand, 256), 256, 0, s>>>(ov.p, o.fac, cs.p, cd.p, pos.p, n_cand, key.p, vals.p, kov.p,
+                                                    kfac.p);
         int rbits = 32;
         while (rbits < 64 && (static_cast<unsigned long long>(n_dst) >> (rbits - 32)) > 0) ++rbits;
         radix_sort_pairs_u64(key.p, vals.p, nnz, rbits, s);
         k_count_keys<<<nblk(nnz, 256), 256, 0, s>>>(key.p, nnz, rcnt.p);
-        k_csr_cols<<<nblk(nnz, 256), 256, 0, s>>>(key.p, vals.p, kov.p, nnz, out.col.p, ovs.p, key2.p, vals2.p);
+        k_csr_cols<<<nblk(nnz, 256), 256, 0, s>>>(key.p, vals.p, kov.p, o.fac ? kfac.p : nullptr, nnz, out.col.p,
+                                                  ovs.p, facs.p, key2.p, vals2.p);
         AXGB_CUDA(cudaGetLastError());
         int cbits = 32;
         while (cbits < 64 && (static_cast<unsigned long long>(n_src) >> (cbits - 32)) > 0) ++cbits;
@@ -580,15 +799,18 @@ static void assemble(DBuf<int> &cs, DBuf<int> &cd, DBuf<double> &ov, i64 n_cand,
     }
     scan_exclusive_i32(rcnt.p, out.row_ptr.p, n_dst, s);
     scan_exclusive_i32(ccnt.p, col_ptr.p, n_src, s);
-    AXGB_CUDA(cudaMemcpyAsync(out.area_a.p, area_src, sizeof(double) * n_src, cudaMemcpyDeviceToDevice, s));
-    AXGB_CUDA(cudaMemcpyAsync(out.area_b.p, area_dst, sizeof(double) * n_dst, cudaMemcpyDeviceToDevice, s));
+    AXGB_CUDA(cudaMemcpyAsync(out.area_a.p, o.area_a_out ? o.area_a_out : area_src, sizeof(double) * n_src,
+                              cudaMemcpyDeviceToDevice, s));
+    AXGB_CUDA(cudaMemcpyAsync(out.area_b.p, o.area_b_out ? o.area_b_out : area_dst, sizeof(double) * n_dst,
+                              cudaMemcpyDeviceToDevice, s));
     if (n_dst > 0)
-        k_rows<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, ovs.p, area_dst, n_dst,
+        k_rows<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, ovs.p, area_dst, o.fb_pre, n_dst,
                                                cfg.norm_type == AXGB_FRACAREA ? 1 : 0, out.val.p, out.frac_b.p);
     if (n_src > 0)
-        k_cols<<<nblk(n_src, 256), 256, 0, s>>>(col_ptr.p, vals2.p, ovs.p, area_src, n_src, out.frac_a.p);
+        k_cols<<<nblk(n_src, 256), 256, 0, s>>>(col_ptr.p, vals2.p, ovs.p, o.fac ? facs.p : nullptr, area_src, n_src,
+                                               out.frac_a.p);
     AXGB_CUDA(cudaGetLastError());
-    if (cfg.unmapped == AXGB_UNMAPPED_ERROR && n_dst > 0) {
+    if (o.check_unmapped && cfg.unmapped == AXGB_UNMAPPED_ERROR && n_dst > 0) {
         DBuf<int> bad(1);
         bad.zero(s);
         k_unmapped<<<nblk(n_dst, 256), 256, 0, s>>>(D, out.row_ptr.p, bad.p);
@@ -736,7 +958,7 @@ bool generate_conservative_regular(Mesh &src, Mesh &dst, const axgb_regrid_confi
     a.da = da.p;
     DBuf<int> counts(n_dst);
     DBuf<i64> offs(n_dst + 1);
-    if (n_dst) k_rect<false><<<nblk(n_dst, 128), 128, 0, s>>>(a, counts.p, nullptr, nullptr, nullptr, nullptr);
+    if (n_dst) k_rect<false><<<nblk(n_dst, 128), 128, 0, s>>>(a, counts.p, nullptr, nullptr, nullptr, nullptr, nullptr);
     AXGB_CUDA(cudaGetLastError());
     scan_exclusive_i32_to_i64(counts.p, offs.p, n_dst, s);
     i64 n_cand = 0;
@@ -744,16 +966,127 @@ bool generate_conservative_regular(Mesh &src, Mesh &dst, const axgb_regrid_confi
     AXGB_REQUIRE(n_cand < (i64(1) << 31), "more than 2^31 overlapping pairs");
     if (cfg.unmapped == AXGB_UNMAPPED_ERROR && n_cand == 0) return false;  // the general path diagnoses it
     DBuf<int> cs(n_cand), cd(n_cand);
-    DBuf<double> ov(n_cand);
-    if (n_cand) k_rect<true><<<nblk(n_dst, 128), 128, 0, s>>>(a, nullptr, offs.p, cs.p, cd.p, ov.p);
+    DBuf<double> ov(n_cand), fb(n_dst);
+    fb.zero(s);
+    if (n_cand) k_rect<true><<<nblk(n_dst, 128), 128, 0, s>>>(a, nullptr, offs.p, cs.p, cd.p, ov.p, fb.p);
     AXGB_CUDA(cudaGetLastError());
     out.stats[0] = out.stats[1] = n_cand;
     auto t0 = Clock::now();
-    assemble(cs, cd, ov, n_cand, sa.p, da.p, D, cfg, out, s);
+    AssembleOpts o;
+    o.fb_pre = fb.p;
+    o.check_unmapped = false;  // the fast path returns its matrix as it is (:380-415)
+    assemble(cs, cd, ov, n_cand, sa.p, da.p, D, cfg, out, s, o);
     AXGB_CUDA(cudaStreamSynchronize(s));
     out.times_ms[4] = ms_since(t0);
     out.times_ms[5] = ms_since(t_all);
     slice_centroids(D, out, s);
+    return true;
+}
+
+bool generate_conservative_rectilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {
+    const GridInfo &sg = src.grid, &dg = dst.grid;
+    cudaStream_t s = 0;
+    auto t_all = Clock::now();
+    mesh_prepare(src, s);
+    mesh_prepare(dst, s);
+    MeshView D = dst.view();
+    const i64 n_src = src.n_cells, n_dst = dst.n_cells;
+    AXGB_REQUIRE(n_src < (i64(1) << 31) - 1 && n_dst < (i64(1) << 31) - 1, "meshes above 2^31 cells");
+    out.n_src = n_src;
+    out.n_dst = n_dst;
+    DBuf<double> sl, st, dl, dt;
+    sl.upload(sg.ulon.data(), sg.ulon.size(), s);
+    st.upload(sg.ulat.data(), sg.ulat.size(), s);
+    dl.upload(dg.ulon.data(), dg.ulon.size(), s);
+    dt.upload(dg.ulat.data(), dg.ulat.size(), s);
+    RectNuArgs a;
+    a.sg = {static_cast<int>(sg.ni), static_cast<int>(sg.nj), sl.p, st.p};
+    a.dg = {static_cast<int>(dg.ni), static_cast<int>(dg.nj), dl.p, dt.p};
+    a.s_lon_min = sg.ulon.front();
+    a.s_lon_max = sg.ulon.back();
+    a.src_global = (a.s_lon_max - a.s_lon_min) > 350.0;  // degrees (:81-83)
+    a.s_user = src.has_area ? src.d_user_area.p : nullptr;
+    a.d_user = dst.has_area ? dst.d_user_area.p : nullptr;
+    a.smask = src.has_mask ? src.d_mask.p : nullptr;
+    a.dmask = dst.has_mask ? dst.d_mask.p : nullptr;
+    a.n_src = n_src;
+    a.n_dst = n_dst;
+    DBuf<int> counts(n_dst);
+    DBuf<i64> offs(n_dst + 1);
+    if (n_dst)
+        k_rect_nu<false><<<nblk(n_dst, 128), 128, 0, s>>>(a, counts.p, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                          nullptr, nullptr);
+    AXGB_CUDA(cudaGetLastError());
+    scan_exclusive_i32_to_i64(counts.p, offs.p, n_dst, s);
+    i64 n_cand = 0;
+    AXGB_CUDA(cudaMemcpy(&n_cand, offs.p + n_dst, sizeof(i64), cudaMemcpyDeviceToHost));
+    AXGB_REQUIRE(n_cand < (i64(1) << 31), "more than 2^31 overlapping pairs");
+    // under UnmappedAction::Error an empty matrix goes on to the general path (weight_generator.cpp:3286-3295)
+    if (n_dst == 0 || (cfg.unmapped == AXGB_UNMAPPED_ERROR && n_cand == 0)) return false;
+    DBuf<int> cs(n_cand), cd(n_cand);
+    DBuf<double> ov(n_cand), fac(n_cand), fb(n_dst), da_w(n_dst), sa(n_src), da(n_dst);
+    k_rect_nu<true><<<nblk(n_dst, 128), 128, 0, s>>>(a, nullptr, offs.p, cs.p, cd.p, ov.p, fac.p, fb.p, da_w.p);
+    if (n_src) k_edge_area<<<nblk(n_src, 256), 256, 0, s>>>(a.sg, a.s_user, n_src, sa.p);
+    k_edge_area<<<nblk(n_dst, 256), 256, 0, s>>>(a.dg, a.d_user, n_dst, da.p);
+    AXGB_CUDA(cudaGetLastError());
+    out.stats[0] = out.stats[1] = n_cand;
+    auto t0 = Clock::now();
+    AssembleOpts o;
+    o.fac = fac.p;
+    o.fb_pre = fb.p;
+    o.area_b_out = da.p;
+    o.check_unmapped = false;
+    assemble(cs, cd, ov, n_cand, sa.p, da_w.p, D, cfg, out, s, o);
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    out.times_ms[4] = ms_since(t0);
+    out.times_ms[5] = ms_since(t_all);
+    slice_centroids(D, out, s);
+    return true;
+}
+
+bool generate_bilinear_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {
+    const GridInfo &g = src.grid;
+    const i64 n_src = src.n_cells, n_dst = dst.n_cells;
+    if (n_dst == 0 || g.ni == 0 || g.nj == 0) return false;  // the reference's fall-through signal
+    cudaStream_t s = 0;
+    auto t_all = Clock::now();
+    mesh_prepare(dst, s);
+    AXGB_REQUIRE(4 * n_dst < (i64(1) << 31) && n_src < (i64(1) << 31), "bilinear: meshes too large");
+    BilRegArgs a{g.lon_min, g.lat_min, g.dlon, g.dlat, static_cast<int>(g.ni), static_cast<int>(g.nj),
+                 std::abs((g.lon_max - g.lon_min) - 360.0) < 1.0e-10 * g.dlon};
+    DBuf<int> cnt(n_dst), col4(4 * n_dst), bad(1);
+    DBuf<double> w4(4 * n_dst);
+    bad.zero(s);
+    k_bilinear_reg<<<nblk(n_dst, 128), 128, 0, s>>>(dst.view(), a, cnt.p, col4.p, w4.p, bad.p);
+    AXGB_CUDA(cudaGetLastError());
+    int h_bad = 0;
+    AXGB_CUDA(cudaMemcpy(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h_bad > 0 && cfg.unmapped == AXGB_UNMAPPED_ERROR)
+        throw Error(AXGB_ERR_UNMAPPED, "bilinear: " + std::to_string(h_bad) +
+                                           " unmapped destination cell(s) in the regular-grid fast path");
+    out.n_src = n_src;
+    out.n_dst = n_dst;
+    out.row_ptr.alloc(n_dst + 1);
+    scan_exclusive_i32(cnt.p, out.row_ptr.p, n_dst, s);
+    int nnz = 0;
+    AXGB_CUDA(cudaMemcpy(&nnz, out.row_ptr.p + n_dst, sizeof(int), cudaMemcpyDeviceToHost));
+    out.nnz = nnz;
+    out.col.alloc(std::max(1, nnz));
+    out.val.alloc(std::max(1, nnz));
+    out.frac_a.alloc(n_src);
+    out.frac_b.alloc(n_dst);
+    out.area_a.alloc(n_src);
+    out.area_b.alloc(n_dst);
+    k_bilinear_reg_pack<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, cnt.p, col4.p, w4.p, n_dst, out.col.p,
+                                                         out.val.p, out.frac_b.p);
+    if (n_src) k_fill<<<nblk(n_src, 256), 256, 0, s>>>(out.frac_a.p, n_src, 1.0);
+    out.area_a.zero(s);
+    out.area_b.zero(s);
+    AXGB_CUDA(cudaGetLastError());
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    out.stats[3] = nnz;
+    out.times_ms[5] = ms_since(t_all);
+    slice_centroids(dst.view(), out, s);
     return true;
 }
 

@@ -96,7 +96,7 @@ class Oracle:
         L.orc_conservative.argtypes = (mesh + [C.c_void_p, C.c_void_p] + mesh + [C.c_void_p, C.c_void_p]
                                        + [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)])
         L.orc_bilinear.restype = C.c_int
-        L.orc_bilinear.argtypes = mesh + mesh + [C.POINTER(C.c_void_p)]
+        L.orc_bilinear.argtypes = mesh + mesh + [C.c_int, C.POINTER(C.c_void_p)]
         L.orc_result_nnz.restype = C.c_int64
         L.orc_result_nnz.argtypes = [C.c_void_p]
         L.orc_result_stats.argtypes = [C.c_void_p, _i64p]
@@ -212,10 +212,10 @@ class Oracle:
         order = np.lexsort((col, row))
         return Weights(w.n_src, w.n_dst, row[order], col[order], val[order], w.frac_a, w.frac_b, w.area_a, w.area_b)
 
-    def bilinear(self, src, dst) -> Weights:
+    def bilinear(self, src, dst, unmapped: int = 1) -> Weights:
         h = C.c_void_p()
         t0 = time.perf_counter()
-        rc = self.L.orc_bilinear(*_mesh_args(src), *_mesh_args(dst), C.byref(h))
+        rc = self.L.orc_bilinear(*_mesh_args(src), *_mesh_args(dst), unmapped, C.byref(h))
         dt = time.perf_counter() - t0
         if rc != 0:
             raise RuntimeError(f"oracle bilinear failed rc={rc}")

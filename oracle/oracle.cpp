@@ -679,6 +679,179 @@ static bool conservative_rect(const Mesh &S, const Mesh &D, const GridInfo &sg, 
     return true;
 }
 
+// Non-uniform rectilinear conservative fast path:
+// generate_conservative_rect_nonuniform
+// (src/solver/weight_generator_conservative_rect_nonuniform.cpp:52-311). Cell
+// c is (c % ni, c / ni) on the tolerance-unique sorted node coordinates; the
+// source range is found by binary search (:140-156); entries with overlap
+// > 1e-12 and a positive source area are kept. The destination box is shifted
+// by whole turns onto a global source (:106-111) and source cells past the
+// last column carry +360 (:170-174); the areas inside the loop use those
+// shifted coordinates, the reported areas the unshifted ones (:251-300).
+static void conservative_rect_nu(const Mesh &S, const Mesh &D, const GridInfo &sg, const GridInfo &dg, int norm_type,
+                                 orc_result *res) {
+    const i64 n_src = S.n_cells, n_dst = D.n_cells;
+    const i64 sni = sg.ni, snj = sg.nj, dni = dg.ni, dnj = dg.nj;
+    const std::vector<double> &sl = sg.ulon, &st = sg.ulat, &dl = dg.ulon, &dt = dg.ulat;
+    const double s_lon_min = sl[0], s_lon_max = sl[sni];
+    const bool src_global = (s_lon_max - s_lon_min) > 350.0;
+    constexpr double d2r = 3.14159265358979323846 / 180.0;
+    auto band = [&](double lo_x, double hi_x, double lo_y, double hi_y) {
+        double dlon = hi_x - lo_x;
+        dlon *= d2r;
+        return dlon * (std::sin(hi_y * d2r) - std::sin(lo_y * d2r));
+    };
+    std::vector<i64> rows, cols;
+    std::vector<double> w;
+    std::vector<double> fa(n_src, 0.0), fb(n_dst, 0.0);
+    for (i64 jd = 0; jd < dnj; ++jd)
+        for (i64 id = 0; id < dni; ++id) {
+            const i64 j = id + jd * dni;
+            if (D.mask && D.mask[j] == 0) continue;
+            const double d_lo_x = dl[id], d_hi_x = dl[id + 1], d_lo_y = dt[jd], d_hi_y = dt[jd + 1];
+            double dlx = d_lo_x, dhx = d_hi_x;
+            if (src_global) {
+                const double shift = 360.0 * std::floor((d_lo_x - s_lon_min) / 360.0);
+                dlx = d_lo_x - shift;
+                dhx = d_hi_x - shift;
+            }
+            const double area_dst = D.areas ? D.areas[j] : band(dlx, dhx, d_lo_y, d_hi_y);
+            if (area_dst <= 0.0) continue;
+            int is0 = static_cast<int>(std::lower_bound(sl.begin(), sl.end(), dlx) - sl.begin()) - 1;
+            int is1 = static_cast<int>(std::upper_bound(sl.begin(), sl.end(), dhx) - sl.begin());
+            is0 = std::max(0, is0);
+            if (!src_global || dhx <= s_lon_max) is1 = std::min(static_cast<int>(sni) - 1, is1);
+            int js0 = static_cast<int>(std::lower_bound(st.begin(), st.end(), d_lo_y) - st.begin()) - 1;
+            int js1 = static_cast<int>(std::upper_bound(st.begin(), st.end(), d_hi_y) - st.begin());
+            js0 = std::max(0, js0);
+            js1 = std::min(static_cast<int>(snj) - 1, js1);
+            for (int js = js0; js <= js1; ++js)
+                for (int is = is0; is <= is1; ++is) {
+                    int ia = is;
+                    if (src_global) ia = ((is % static_cast<int>(sni)) + static_cast<int>(sni)) % static_cast<int>(sni);
+                    const i64 c = ia + static_cast<i64>(js) * sni;
+                    if (S.mask && S.mask[c] == 0) continue;
+                    double s_lo_x = sl[ia], s_hi_x = sl[ia + 1];
+                    if (src_global && is >= static_cast<int>(sni)) {
+                        s_lo_x += 360.0;
+                        s_hi_x += 360.0;
+                    }
+                    const double s_lo_y = st[js], s_hi_y = st[js + 1];
+                    const double dx = std::fmax(0.0, std::fmin(s_hi_x, dhx) - std::fmax(s_lo_x, dlx));
+                    const double lo_y = std::fmax(s_lo_y, d_lo_y), hi_y = std::fmin(s_hi_y, d_hi_y);
+                    double ov = 0.0;
+                    if (!(hi_y <= lo_y || dx <= 0.0)) ov = (dx * d2r) * (std::sin(hi_y * d2r) - std::sin(lo_y * d2r));
+                    if (!(ov > 1e-12)) continue;
+                    const double area_src = S.areas ? S.areas[c] : band(s_lo_x, s_hi_x, s_lo_y, s_hi_y);
+                    if (area_src <= 0.0) continue;
+                    w.push_back(ov / area_dst);
+                    rows.push_back(j);
+                    cols.push_back(c);
+                    fa[c] += ov / area_src;
+                    fb[j] += ov / area_dst;
+                }
+        }
+    if (norm_type == 1)
+        for (size_t k = 0; k < w.size(); ++k)
+            if (fb[rows[k]] > 0.0) w[k] /= fb[rows[k]];
+    std::vector<double> sa(n_src), da(n_dst);
+    for (i64 i = 0; i < n_src; ++i) {
+        const i64 ci = i % sni, cj = i / sni;
+        sa[i] = S.areas ? S.areas[i] : band(sl[ci], sl[ci + 1], st[cj], st[cj + 1]);
+        fa[i] = std::min(fa[i], 1.0);
+    }
+    for (i64 j = 0; j < n_dst; ++j) {
+        const i64 ci = j % dni, cj = j / dni;
+        da[j] = D.areas ? D.areas[j] : band(dl[ci], dl[ci + 1], dt[cj], dt[cj + 1]);
+        fb[j] = std::min(fb[j], 1.0);
+    }
+    std::vector<size_t> perm(w.size());
+    std::iota(perm.begin(), perm.end(), 0);
+    std::sort(perm.begin(), perm.end(), [&](size_t a, size_t b) {
+        return rows[a] != rows[b] ? rows[a] < rows[b] : cols[a] < cols[b];
+    });
+    res->n_src = n_src;
+    res->n_dst = n_dst;
+    for (size_t q : perm) {
+        res->row.push_back(rows[q]);
+        res->col.push_back(cols[q]);
+        res->w.push_back(w[q]);
+    }
+    res->frac_a = fa;
+    res->frac_b = fb;
+    res->area_a = sa;
+    res->area_b = da;
+}
+
+// Regular x regular bilinear fast path: generate_bilinear_rect
+// (src/solver/weight_generator_bilinear_rect.cpp:31-320). The destination
+// point is the plain mean of its vertices' (lon, lat) in degrees; on a
+// periodic source it is first brought into [lon_min, lon_min + 360). The
+// fractional cell-centre index (fi, fj) is tested against the bounds with a
+// 1e-9 slack, floored and clamped (wrapped in longitude when periodic), and
+// the four weights (1-tx)(1-ty), tx(1-ty), (1-tx)ty, tx ty go to (i,j),
+// (i1,j), (i,j1), (i1,j1). Rows are stored column-ascending (to_csr), ties
+// in emission order. frac_a = 1, frac_b = 1 on mapped rows, areas 0.
+// Returns false on an unmapped destination under Error.
+static bool bilinear_regular(const Mesh &S, const Mesh &D, const GridInfo &sg, int unmapped, orc_result *res) {
+    const i64 n_src = S.n_cells, n_dst = D.n_cells;
+    const int ni = static_cast<int>(sg.ni), nj = static_cast<int>(sg.nj);
+    const double lon_min = sg.lon_min, lat_min = sg.lat_min, dlon = sg.dlon, dlat = sg.dlat;
+    const bool periodic = std::abs((sg.lon_max - sg.lon_min) - 360.0) < 1.0e-10 * dlon;
+    res->n_src = n_src;
+    res->n_dst = n_dst;
+    res->frac_a.assign(n_src, 1.0);
+    res->frac_b.assign(n_dst, 0.0);
+    res->area_a.assign(n_src, 0.0);
+    res->area_b.assign(n_dst, 0.0);
+    for (i64 c = 0; c < n_dst; ++c) {
+        double ls = 0.0, ts = 0.0;
+        for (i64 q = D.off[c]; q < D.off[c + 1]; ++q) {
+            ls += D.lon(D.idx[q]);
+            ts += D.lat(D.idx[q]);
+        }
+        double ld = ls / static_cast<double>(D.off[c + 1] - D.off[c]);
+        const double td = ts / static_cast<double>(D.off[c + 1] - D.off[c]);
+        if (periodic) {
+            double off = ld - lon_min;
+            off = off - std::floor(off / 360.0) * 360.0;
+            ld = lon_min + off;
+        }
+        const double fi = (ld - lon_min) / dlon - 0.5, fj = (td - lat_min) / dlat - 0.5;
+        const double tol = 1.0e-9;
+        bool inside = fj >= -0.5 - tol && fj <= static_cast<double>(nj) - 0.5 + tol;
+        if (!periodic) inside = inside && fi >= -0.5 - tol && fi <= static_cast<double>(ni) - 0.5 + tol;
+        if (!inside) {
+            if (unmapped == 0) return false;
+            continue;
+        }
+        int i = static_cast<int>(std::floor(fi)), j = static_cast<int>(std::floor(fj));
+        j = std::max(0, std::min(j, nj - 2));
+        if (periodic) {
+            i = ((i % ni) + ni) % ni;
+        } else {
+            i = std::max(0, std::min(i, ni - 2));
+        }
+        const double tx = std::min(1.0, std::max(0.0, fi - static_cast<double>(i)));
+        const double ty = std::min(1.0, std::max(0.0, fj - static_cast<double>(j)));
+        int i1 = i + 1;
+        if (i1 >= ni) i1 = periodic ? 0 : ni - 1;
+        const int j1 = std::min(j + 1, nj - 1);
+        const i64 src[4] = {static_cast<i64>(j) * ni + i, static_cast<i64>(j) * ni + i1, static_cast<i64>(j1) * ni + i,
+                            static_cast<i64>(j1) * ni + i1};
+        const double w[4] = {(1.0 - tx) * (1.0 - ty), tx * (1.0 - ty), (1.0 - tx) * ty, tx * ty};
+        int ordk[4] = {0, 1, 2, 3};
+        std::stable_sort(ordk, ordk + 4, [&](int a, int b) { return src[a] < src[b]; });
+        for (int k = 0; k < 4; ++k) {
+            res->row.push_back(c);
+            res->col.push_back(src[ordk[k]]);
+            res->w.push_back(w[ordk[k]]);
+        }
+        res->frac_b[c] = 1.0;
+    }
+    return true;
+}
+
 extern "C" {
 
 int orc_num_threads() {
@@ -779,8 +952,7 @@ int orc_morton_order(i64 n_nodes, const double *lonlat, i64 n_cells, const i64 *
 // norm_type: 0 DstArea, 1 FracArea. unmapped: 0 Error, 1 Ignore.
 // faithful = 1 runs the clip loop serially in Morton order as the reference
 // does; 0 runs it with OpenMP and merges in the same order (identical output).
-// Returns 0 ok, -2 both meshes regular/rectilinear (fast paths not restated),
-// -7 unmapped destination under Error.
+// Returns 0 ok, -7 unmapped destination under Error.
 int orc_conservative(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *soff, const i64 *sidx,
                      const double *sareas, const int *smask, i64 dn_nodes, const double *dlonlat, i64 dn_cells,
                      const i64 *doff, const i64 *didx, const double *dareas, const int *dmask, int norm_type,
@@ -795,9 +967,16 @@ int orc_conservative(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i6
             *out = res;
             return 0;
         }
-        delete res;  // declined: the general path below
-    } else if (sg.rectilinear && dg.rectilinear) {
-        return -2;  // the non-uniform rectilinear fast path is not restated
+        delete res;  // declined: the non-uniform rectilinear path, then the general path
+    }
+    if (sg.rectilinear && dg.rectilinear) {
+        auto *res = new orc_result;
+        conservative_rect_nu(S, D, sg, dg, norm_type, res);
+        if (D.n_cells > 0 && (unmapped != 0 || !res->w.empty())) {
+            *out = res;
+            return 0;
+        }
+        delete res;
     }
 
     auto sxyz = node_xyz(S), dxyz = node_xyz(D);
@@ -930,15 +1109,26 @@ int orc_conservative(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i6
 
 // Rectilinear-source bilinear weights: generate_bilinear_rect_nonuniform
 // (src/solver/weight_generator_bilinear_rect_nonuniform.cpp:22-149) behind
-// the dispatch of generate_bilinear (src/solver/weight_generator.cpp:2306-2345).
-// Returns -2 when both meshes are regular (the regular fast path is not
-// restated) and -3 when the source is not rectilinear.
+// the dispatch of generate_bilinear (src/solver/weight_generator.cpp:2306-2345),
+// which sends regular x regular pairs to bilinear_regular first.
+// unmapped: 0 Error, 1 Ignore (only the regular path leaves rows unmapped).
+// Returns -3 when the source is not rectilinear, -7 for an unmapped
+// destination under Error.
 int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *soff, const i64 *sidx, i64 dn_nodes,
-                 const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, orc_result **out) {
+                 const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, int unmapped,
+                 orc_result **out) {
     Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, nullptr, nullptr};
     Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, nullptr, nullptr};
     GridInfo sg = detect(S), dg = detect(D);
-    if (sg.regular && dg.regular) return -2;
+    if (sg.regular && dg.regular && dn_cells > 0) {
+        auto *res = new orc_result;
+        if (!bilinear_regular(S, D, sg, unmapped, res)) {
+            delete res;
+            return -7;
+        }
+        *out = res;
+        return 0;
+    }
     if (!sg.rectilinear) return -3;
     i64 ni = sg.ni, nj = sg.nj;
     std::vector<double> cl(ni), ct(nj);

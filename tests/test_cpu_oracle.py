@@ -238,3 +238,51 @@ def test_coastal_postpass_oracle(oracle):
     assert len(dry) > 0 and np.all(counts[dry] == 1)
     none = oracle.coastal(w, src, dst, mask, nearest_wet=False)
     assert set(np.unique(none.row)) == set(np.unique(w.row))
+
+
+def test_conservative_rectilinear_oracle(oracle):
+    """Non-uniform rectilinear fast path (weight_generator_conservative_rect_
+    nonuniform.cpp): on two global grids every row sums to 1 and every source
+    cell is fully used (frac 1, area-weighted column sums = source areas)."""
+    src = grids.equal_area_latlon(72, 36, stretch=0.4)
+    dst = grids.equal_area_latlon(50, 28, lon_start=-180.0, stretch=0.3)
+    w = oracle.conservative(src, dst)
+    rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
+    assert np.all(np.abs(rs - 1.0) < 1e-12)
+    assert np.all(np.abs(w.frac_a - 1.0) < 1e-12) and np.all(np.abs(w.frac_b - 1.0) < 1e-12)
+    cs = np.bincount(w.col, weights=w.w * w.area_b[w.row], minlength=w.n_src)
+    assert np.all(np.abs(cs - w.area_a) < 1e-12 * w.area_a.max())
+    # equal-area bands: every source band has the same area per unit longitude
+    band = w.area_a.reshape(36, 72).sum(axis=1)
+    assert np.all(np.abs(band - band[0]) < 1e-12 * band[0])
+
+
+def test_conservative_declined_regular_takes_rectilinear_path(oracle):
+    """Two non-global regular grids whose longitudes do not fit are declined
+    by the regular fast path and handled by the rectilinear one: band-overlap
+    weights, rows inside the source sum to 1, rows outside stay empty."""
+    src = grids.regular_latlon(40, 30, 20.0, -10.0, 1.0, 1.0)  # lon 20..60, lat -10..20
+    dst = grids.regular_latlon(20, 20, 10.0, -20.0, 2.0, 2.0)  # lon 10..50, lat -20..20
+    w = oracle.conservative(src, dst)
+    rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
+    counts = np.bincount(w.row, minlength=w.n_dst)
+    assert np.all(rs <= 1.0 + 1e-12)
+    inside = 5 * 20 + 5  # lon 20..22, lat -10..-8: four source cells
+    assert counts[inside] == 4 and abs(rs[inside] - 1.0) < 1e-12
+    assert counts[5 * 20 + 4] == 0  # lon 18..20 only touches the source edge
+    assert counts[4 * 20 + 5] == 0  # lat -12..-10 likewise
+
+
+def test_bilinear_regular_known_answer(oracle):
+    """Regular bilinear fast path: 10 deg cells onto 20 deg cells put every
+    destination centre on the corner of four source cells (weights 1/4); a
+    field linear in latitude is reproduced exactly away from the poles."""
+    src, dst = grids.latlon_deg(10.0), grids.latlon_deg(20.0)
+    w = oracle.bilinear(src, dst)
+    assert w.nnz == 4 * dst.n_cells
+    assert np.all(w.w == 0.25)
+    assert np.all(np.bincount(w.row, minlength=w.n_dst) == 4)
+    lat_s = np.repeat(-85.0 + 10.0 * np.arange(18), 36)
+    y = np.bincount(w.row, weights=w.w * lat_s[w.col], minlength=w.n_dst)
+    lat_d = np.repeat(-80.0 + 20.0 * np.arange(9), 18)
+    assert np.allclose(y, lat_d, rtol=0, atol=1e-12)

@@ -104,8 +104,9 @@ def test_bilinear_parity(gpu, oracle):
 def test_unsupported_and_unmapped(gpu, oracle):
     a = gpu.make_regular_mesh(36, 18, 0.0, -90.0, 10.0, 10.0)
     b = gpu.make_regular_mesh(18, 9, 0.0, -90.0, 20.0, 20.0)
-    with pytest.raises(gpu.Unsupported):  # regular x regular bilinear fast path not provided
-        gpu.generate_weights(a, b, {"method": "bilinear"})
+    cs = gpu.Mesh.from_grid(grids.cubed_sphere(4))
+    with pytest.raises(gpu.Unsupported):  # bilinear from a non-rectilinear source (BVH bilinear) not provided
+        gpu.generate_weights(cs, b, {"method": "bilinear"})
     with pytest.raises(gpu.Unsupported):
         gpu.generate_weights(a, b, {"method": "patch"})
     # a regional source leaves most of a global destination unmapped
@@ -515,3 +516,73 @@ def test_coastal_postpass_parity(gpu, oracle, name, make):
         M = gpu.generate_weights(ms, md, {"method": "conservative", "extrap_method": extrap})
         ref = oracle.coastal(wo, src, dst, mask, nearest_wet=nearest)
         _check_weights(M, ref)
+
+
+RECT_PAIRS = [
+    ("equal-area stretched->2deg", lambda: (grids.equal_area_latlon(72, 36, stretch=0.4), grids.latlon_deg(2.0))),
+    ("1deg->shifted equal-area", lambda: (grids.latlon_deg(1.0),
+                                          grids.equal_area_latlon(96, 48, lon_start=-180.0, stretch=0.3))),
+    ("equal-area->equal-area", lambda: (grids.equal_area_latlon(180, 90, stretch=0.2),
+                                        grids.equal_area_latlon(50, 28, lon_start=-90.0, stretch=0.5))),
+    ("declined regular pair", lambda: (grids.regular_latlon(40, 30, 20.0, -10.0, 1.0, 1.0),
+                                       grids.regular_latlon(20, 20, 10.0, -20.0, 2.0, 2.0))),
+]
+
+
+@pytest.mark.parametrize("name,make", RECT_PAIRS)
+def test_conservative_rectilinear_fast_path(gpu, oracle, name, make):
+    """Rectilinear x rectilinear conservative weights (the non-uniform fast
+    path, which also takes regular pairs the regular path declines) against
+    the oracle: index set bit-exact, values within 1e-12, DstArea and
+    FracArea."""
+    src, dst = make()
+    ms, md = gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst)
+    _check_weights(gpu.generate_weights(ms, md, {"method": "conservative"}), oracle.conservative(src, dst))
+    _check_weights(gpu.generate_weights(ms, md, {"method": "conservative", "norm_type": "FracArea"}),
+                   oracle.conservative(src, dst, norm_type=1))
+
+
+def test_fast_paths_return_partial_coverage_under_error(gpu, oracle):
+    """The fast paths return their matrix as it is under UnmappedAction::Error
+    when some rows are empty but not all: a regional source on a global
+    destination raises nothing and matches the oracle."""
+    src, dst = grids.regular_latlon(40, 30, 20.0, -10.0, 1.0, 1.0), grids.latlon_deg(2.0)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst),
+                             {"method": "conservative", "unmapped": "Error"})
+    _check_weights(M, oracle.conservative(src, dst, unmapped=0))
+    src = grids.equal_area_latlon(36, 18, stretch=0.3)
+    dst = grids.rectilinear([0.0, 5.0, 12.0, 30.0], [-10.0, 0.0, 7.5])
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst),
+                             {"method": "conservative", "unmapped": "Error"})
+    _check_weights(M, oracle.conservative(src, dst, unmapped=0))
+
+
+BILINEAR_REGULAR_PAIRS = [
+    ("10deg->20deg", lambda: (grids.latlon_deg(10.0), grids.latlon_deg(20.0))),
+    ("1deg->0.75deg", lambda: (grids.latlon_deg(1.0), grids.latlon_deg(0.75))),
+    ("1deg->shifted 2deg", lambda: (grids.latlon_deg(1.0), grids.regular_latlon(180, 90, -180.0, -90.0, 2.0, 2.0))),
+    ("regional->global", lambda: (grids.regular_latlon(40, 30, 20.0, -10.0, 1.0, 1.0), grids.latlon_deg(2.0))),
+]
+
+
+@pytest.mark.parametrize("name,make", BILINEAR_REGULAR_PAIRS)
+def test_bilinear_regular_fast_path(gpu, oracle, name, make):
+    """Regular x regular bilinear (weight_generator_bilinear_rect.cpp) against
+    the oracle, bit for bit: index arithmetic and four products per row. A
+    regional source leaves rows unmapped: empty under Ignore, an error under
+    Error, on both sides."""
+    src, dst = make()
+    ms, md = gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst)
+    M = gpu.generate_weights(ms, md, {"method": "bilinear"})
+    wo = oracle.bilinear(src, dst)
+    csr = _check_weights(M, wo)
+    assert np.array_equal(csr["val"], wo.w)
+    if name == "regional->global":
+        assert wo.nnz < 4 * dst.n_cells
+        with pytest.raises(gpu.AxgbError) as e:
+            gpu.generate_weights(ms, md, {"method": "bilinear", "unmapped": "Error"})
+        assert e.value.code == gpu.ERR_UNMAPPED
+        with pytest.raises(RuntimeError):
+            oracle.bilinear(src, dst, unmapped=0)
+    else:
+        assert wo.nnz == 4 * dst.n_cells
