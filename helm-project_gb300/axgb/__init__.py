@@ -45,7 +45,8 @@ _SYMBOLS = [
     "axgb_batch_create", "axgb_batch_apply", "axgb_destroy_batch", "axgb_conservation_f64",
     "axgb_conservation_f32", "axgb_matrix_device_status", "axgb_conservation_f64_noalloc",
     "axgb_set_kernel_choice", "axgb_get_kernel_choice", "axgb_nan_batch_apply_f64", "axgb_apply_masked_f64",
-    "axgb_nan_batch_apply_host", "axgb_matrix_serialize", "axgb_matrix_deserialize",
+    "axgb_nan_batch_apply_host", "axgb_matrix_serialize", "axgb_matrix_deserialize", "axgb_esmf_write",
+    "axgb_esmf_read", "axgb_matrix_write_esmf", "axgb_matrix_read_esmf",
 ]
 
 
@@ -120,6 +121,10 @@ def lib():
     L.axgb_nan_batch_apply_host.argtypes = [C.c_int, vp, C.c_int64, vp, C.c_int64, C.c_int64, C.c_double]
     L.axgb_matrix_serialize.argtypes = [C.c_int, vp, C.c_int64, vp]
     L.axgb_matrix_deserialize.argtypes = [vp, C.c_int64, vp]
+    L.axgb_esmf_write.argtypes = [C.c_char_p, C.c_int64, C.c_int64, C.c_int64, vp, vp, vp]
+    L.axgb_esmf_read.argtypes = [C.c_char_p, vp, vp, vp, vp, vp, vp, C.c_int64]
+    L.axgb_matrix_write_esmf.argtypes = [C.c_int, C.c_char_p]
+    L.axgb_matrix_read_esmf.argtypes = [C.c_char_p, vp]
     L.axgb_get_kernel_choice.argtypes = [C.c_int, C.c_int64, vp, vp]
     _L = L
     return L
@@ -334,6 +339,20 @@ class Matrix:
         _ensure_init()
         h = C.c_int()
         _check(lib().axgb_matrix_deserialize(C.c_char_p(blob), len(blob), C.byref(h)))
+        return cls(h.value)
+
+    def write_esmf(self, path) -> None:
+        """ESMF weight file (EsmfWeightIO::write_esmf, src/io/esmf_weight_io.cpp:66-113),
+        as NetCDF-3 64-bit offset."""
+        _check(lib().axgb_matrix_write_esmf(self.handle, os.fsencode(path)))
+
+    @classmethod
+    def read_esmf(cls, path):
+        """EsmfWeightIO::read_esmf (esmf_weight_io.cpp:115-183): NetCDF-3 files;
+        frac and area arrays come back zero."""
+        _ensure_init()
+        h = C.c_int()
+        _check(lib().axgb_matrix_read_esmf(os.fsencode(path), C.byref(h)))
         return cls(h.value)
 
     @classmethod
@@ -555,3 +574,27 @@ class Batch:
         except Exception:
             pass
         self.handle = 0
+
+
+def esmf_write(path, n_a: int, n_b: int, S, col_idx, row_idx) -> None:
+    """Host-only ESMF weight file writer (no device needed): S float64, 1-based
+    int32 col_idx / row_idx, global attributes n_a / n_b."""
+    w = np.ascontiguousarray(S, np.float64)
+    c = np.ascontiguousarray(col_idx, np.int32)
+    r = np.ascontiguousarray(row_idx, np.int32)
+    if not (w.shape == c.shape == r.shape and w.ndim == 1):
+        raise InvalidArgument(ERR_INVALID, "esmf_write: S, col_idx, row_idx must be 1-D of one length")
+    _check(lib().axgb_esmf_write(os.fsencode(path), int(n_a), int(n_b), w.size, _ptr(w), _ptr(c), _ptr(r)))
+
+
+def esmf_read(path) -> dict:
+    """Host-only ESMF weight file reader: dict of n_a, n_b, S, col_idx, row_idx
+    (1-based, as stored)."""
+    na, nb, nz = C.c_int64(), C.c_int64(), C.c_int64()
+    p = os.fsencode(path)
+    _check(lib().axgb_esmf_read(p, C.byref(na), C.byref(nb), C.byref(nz), None, None, None, 0))
+    S = np.zeros(nz.value)
+    c = np.zeros(nz.value, np.int32)
+    r = np.zeros(nz.value, np.int32)
+    _check(lib().axgb_esmf_read(p, C.byref(na), C.byref(nb), C.byref(nz), _ptr(S), _ptr(c), _ptr(r), S.size))
+    return {"n_a": na.value, "n_b": nb.value, "S": S, "col_idx": c, "row_idx": r}

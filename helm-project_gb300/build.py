@@ -2,9 +2,9 @@
 
 CUDA translation units are compiled by nvcc with one -gencode
 (compute_103a -> sm_103a); the geometry units (prep.cu, weights.cu) with
---fmad=false so double expressions round as written. The host C++ unit
-(api.cpp) is compiled by g++ with -ffp-contract=off and OpenMP (parallel
-sort in the grid detector). Units compile in parallel; the link uses nvcc.
+--fmad=false so double expressions round as written. The host C++ units
+(api.cpp, esmf_io.cpp) are compiled by g++ with -ffp-contract=off and OpenMP
+(parallel sort in the grid detector). Units compile in parallel; the link uses nvcc.
 """
 
 from __future__ import annotations
@@ -31,6 +31,7 @@ UNITS = [
     ("scan_sort.cu", []),
     ("coastal.cu", []),
 ]
+HOST_UNITS = ["api.cpp", "esmf_io.cpp"]  # host C++ (g++)
 HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", os.path.join("..", "..", "include", "axgb.h")]
 
 
@@ -69,12 +70,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)
-    api = os.path.join(CSRC, "api.cpp")
-    api_o = os.path.join(OBJDIR, "api.cpp.o")
-    objs.append(api_o)
-    if force or _stale(api_o, [api, *hdrs, __file__]):
-        jobs.append(["g++", "-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp",
-                     "-I", os.path.join(CUDA_HOME, "include"), "-c", api, "-o", api_o])
+    for src in HOST_UNITS:
+        srcp = os.path.join(CSRC, src)
+        obj = os.path.join(OBJDIR, src + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [srcp, *hdrs, __file__]):
+            jobs.append(["g++", "-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp",
+                         "-I", os.path.join(CUDA_HOME, "include"), "-c", srcp, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
         outs = list(ex.map(_compile, jobs))
     if verbose:

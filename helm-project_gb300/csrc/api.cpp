@@ -653,6 +653,27 @@ inline uint8_t native_endian() {
 inline int64_t cache_size(int64_t ns, int64_t nd, int64_t nnz) { return kCacheHeader + 24 * nnz + 16 * ns + 16 * nd; }
 }  // namespace
 
+// COO triplets (any order) -> CSR, stable by row, then axgb_matrix_import_csr
+// (which sorts each row by column, as to_csr).
+static int import_coo(int64_t ns, int64_t nd, int64_t nz, const int64_t *rows, const int64_t *cols, const double *vals,
+                      const double *fa, const double *fb, const double *aa, const double *ab, int *h, const char *who) {
+    std::vector<int64_t> rp(nd + 1, 0);
+    for (int64_t k = 0; k < nz; ++k) {
+        AXGB_REQUIRE(rows[k] >= 0 && rows[k] < nd, std::string(who) + ": row out of range");
+        AXGB_REQUIRE(cols[k] >= 0 && cols[k] < ns, std::string(who) + ": column out of range");
+        rp[rows[k] + 1]++;
+    }
+    for (int64_t j = 0; j < nd; ++j) rp[j + 1] += rp[j];
+    std::vector<int64_t> pos(rp.begin(), rp.end() - 1), cc(nz);
+    std::vector<double> vv(nz);
+    for (int64_t k = 0; k < nz; ++k) {
+        const int64_t at = pos[rows[k]]++;
+        cc[at] = cols[k];
+        vv[at] = vals[k];
+    }
+    return axgb_matrix_import_csr(ns, nd, nz, rp.data(), cc.data(), vv.data(), fa, fb, aa, ab, h);
+}
+
 int axgb_matrix_serialize(int h, void *buf, int64_t buf_size, int64_t *written) {
     AXGB_TRY({
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
@@ -725,22 +746,74 @@ int axgb_matrix_deserialize(const void *buf, int64_t buf_size, int *h) {
         std::memcpy(fb.data(), q + 8 * ns, 8 * nd);
         std::memcpy(aa.data(), q + 8 * ns + 8 * nd, 8 * ns);
         std::memcpy(ab.data(), q + 16 * ns + 8 * nd, 8 * nd);
-        // COO -> CSR, stable by row (to_csr order: rows ascending, then columns)
-        std::vector<int64_t> rp(nd + 1, 0);
-        for (uint64_t k = 0; k < nz; ++k) {
-            AXGB_REQUIRE(rows[k] >= 0 && static_cast<uint64_t>(rows[k]) < nd, "matrix_deserialize: row out of range");
-            rp[rows[k] + 1]++;
+        return import_coo(static_cast<int64_t>(ns), static_cast<int64_t>(nd), static_cast<int64_t>(nz), rows.data(),
+                          cols.data(), vals.data(), fa.data(), fb.data(), aa.data(), ab.data(), h,
+                          "matrix_deserialize");
+    });
+}
+
+int axgb_esmf_write(const char *path, int64_t n_a, int64_t n_b, int64_t nnz, const double *S, const int32_t *col_idx,
+                    const int32_t *row_idx) {
+    AXGB_TRY({
+        AXGB_REQUIRE(path, "esmf_write: NULL path");
+        esmf_write(path, n_a, n_b, nnz, S, col_idx, row_idx);
+    });
+}
+
+int axgb_esmf_read(const char *path, int64_t *n_a, int64_t *n_b, int64_t *nnz, double *S, int32_t *col_idx,
+                   int32_t *row_idx, int64_t capacity) {
+    AXGB_TRY({
+        AXGB_REQUIRE(path && n_a && n_b && nnz, "esmf_read: NULL argument");
+        EsmfWeights w = esmf_read(path);
+        *n_a = w.n_a;
+        *n_b = w.n_b;
+        *nnz = static_cast<int64_t>(w.S.size());
+        if (!S) return AXGB_SUCCESS;  // size query
+        AXGB_REQUIRE(col_idx && row_idx, "esmf_read: NULL index arrays");
+        AXGB_REQUIRE(capacity >= *nnz, "esmf_read: capacity (" + std::to_string(capacity) + ") < nnz (" +
+                                           std::to_string(*nnz) + ")");
+        std::copy(w.S.begin(), w.S.end(), S);
+        std::copy(w.col1.begin(), w.col1.end(), col_idx);
+        std::copy(w.row1.begin(), w.row1.end(), row_idx);
+    });
+}
+
+int axgb_matrix_write_esmf(int h, const char *path) {
+    AXGB_TRY({
+        AXGB_REQUIRE(path, "matrix_write_esmf: NULL path");
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        std::vector<int> rp(m->n_dst + 1), c(m->nnz);
+        std::vector<double> v(m->nnz);
+        m->row_ptr.download(rp.data(), rp.size());
+        m->col.download(c.data(), c.size());
+        m->val.download(v.data(), v.size());
+        AXGB_CUDA(cudaDeviceSynchronize());
+        // 0-based -> 1-based (esmf_weight_io.cpp:82-90), in CSR order
+        std::vector<int32_t> col1(m->nnz), row1(m->nnz);
+        for (int64_t j = 0; j < m->n_dst; ++j)
+            for (int k = rp[j]; k < rp[j + 1]; ++k) {
+                row1[k] = static_cast<int32_t>(j + 1);
+                col1[k] = c[k] + 1;
+            }
+        esmf_write(path, m->n_src, m->n_dst, m->nnz, v.data(), col1.data(), row1.data());
+    });
+}
+
+int axgb_matrix_read_esmf(const char *path, int *h) {
+    AXGB_TRY({
+        AXGB_REQUIRE(path && h, "matrix_read_esmf: NULL argument");
+        EsmfWeights w = esmf_read(path);
+        AXGB_REQUIRE(w.n_a >= 0 && w.n_b >= 0, "matrix_read_esmf: negative n_a / n_b");
+        const int64_t nz = static_cast<int64_t>(w.S.size());
+        std::vector<int64_t> rows(nz), cols(nz);
+        for (int64_t k = 0; k < nz; ++k) {  // 1-based -> 0-based (esmf_weight_io.cpp:163-167)
+            rows[k] = static_cast<int64_t>(w.row1[k]) - 1;
+            cols[k] = static_cast<int64_t>(w.col1[k]) - 1;
         }
-        for (uint64_t j = 0; j < nd; ++j) rp[j + 1] += rp[j];
-        std::vector<int64_t> pos(rp.begin(), rp.end() - 1), cc(nz);
-        std::vector<double> vv(nz);
-        for (uint64_t k = 0; k < nz; ++k) {
-            const int64_t at = pos[rows[k]]++;
-            cc[at] = cols[k];
-            vv[at] = vals[k];
-        }
-        return axgb_matrix_import_csr(static_cast<int64_t>(ns), static_cast<int64_t>(nd), static_cast<int64_t>(nz),
-                                      rp.data(), cc.data(), vv.data(), fa.data(), fb.data(), aa.data(), ab.data(), h);
+        // frac and area arrays are zero, as the reference's read_esmf leaves them
+        std::vector<double> za(w.n_a, 0.0), zb(w.n_b, 0.0);
+        return import_coo(w.n_a, w.n_b, nz, rows.data(), cols.data(), w.S.data(), za.data(), zb.data(), za.data(),
+                          zb.data(), h, "matrix_read_esmf");
     });
 }
 

@@ -243,6 +243,15 @@ bool generate_conservative_regular(Mesh &src, Mesh &dst, const axgb_regrid_confi
 // rectilinear x rectilinear fast path (non-uniform edges); false = an empty
 // matrix under UnmappedAction::Error (use generate_conservative)
 bool generate_conservative_rectilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
+// esmf_io.cpp: ESMF weight files (NetCDF-3); col1/row1 are 1-based
+struct EsmfWeights {
+    std::int64_t n_a = 0, n_b = 0;
+    std::vector<double> S;
+    std::vector<std::int32_t> col1, row1;
+};
+void esmf_write(const std::string &path, std::int64_t n_a, std::int64_t n_b, std::int64_t nnz, const double *S,
+                const std::int32_t *col1, const std::int32_t *row1);
+EsmfWeights esmf_read(const std::string &path);
 // regular x regular bilinear fast path; false = no destination cells (fall through)
 bool generate_bilinear_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);

@@ -175,6 +175,26 @@ int axgb_matrix_export_csr(int matrix_handle, int64_t *row_ptr, int64_t *col_idx
 int axgb_matrix_serialize(int matrix_handle, void *buf, int64_t buf_size, int64_t *written);
 int axgb_matrix_deserialize(const void *buf, int64_t buf_size, int *matrix_handle);
 
+/* ESMF weight files: EsmfWeightIO::write_esmf / read_esmf
+ * (src/io/esmf_weight_io.cpp:66-183). The file holds dimension num_wgts,
+ * variables S (double), col_idx and row_idx (int, 1-based) and global int
+ * attributes n_a, n_b (source / destination cell counts). It is written in
+ * the NetCDF-3 64-bit-offset format, which libnetcdf (and so the reference's
+ * read_esmf) opens. Reading takes NetCDF-3 classic and 64-bit-offset files;
+ * a NETCDF4 (HDF5) file, the format the reference writes, or a CDF-5 file is
+ * AXGB_ERR_UNSUPPORTED. A missing attribute or variable is AXGB_ERR_INVALID.
+ * axgb_esmf_write / axgb_esmf_read work on host arrays and need no device;
+ * axgb_esmf_read with S NULL only returns the sizes. axgb_matrix_write_esmf
+ * writes a matrix's entries in CSR order; axgb_matrix_read_esmf builds a
+ * matrix from a file with frac and area arrays zero, as the reference's
+ * reader leaves them. */
+int axgb_esmf_write(const char *path, int64_t n_a, int64_t n_b, int64_t nnz, const double *S, const int32_t *col_idx,
+                    const int32_t *row_idx);
+int axgb_esmf_read(const char *path, int64_t *n_a, int64_t *n_b, int64_t *nnz, double *S, int32_t *col_idx,
+                   int32_t *row_idx, int64_t capacity);
+int axgb_matrix_write_esmf(int matrix_handle, const char *path);
+int axgb_matrix_read_esmf(const char *path, int *matrix_handle);
+
 int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int64_t *row_ptr, const int64_t *col_idx,
                            const double *values, const double *frac_a, const double *frac_b, const double *area_a,
                            const double *area_b, int *matrix_handle);

@@ -586,3 +586,41 @@ def test_bilinear_regular_fast_path(gpu, oracle, name, make):
             oracle.bilinear(src, dst, unmapped=0)
     else:
         assert wo.nnz == 4 * dst.n_cells
+
+
+def test_esmf_weight_file_round_trip(gpu, oracle, tmp_path):
+    """ESMF weight file of a generated matrix: scipy's NetCDF-3 reader sees S,
+    1-based col_idx / row_idx in CSR order and n_a / n_b; read_esmf rebuilds
+    the CSR bit for bit with frac and area arrays zero (as the reference's
+    read_esmf leaves them); a shuffled file gives the same matrix."""
+    import torch
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    src, dst = grids.latlon_deg(5.0), grids.cubed_sphere(8)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    csr = M.to_csr()
+    p = tmp_path / "w.nc"
+    M.write_esmf(p)
+    f = netcdf(str(p), "r", mmap=False)
+    try:
+        assert (int(f.n_a), int(f.n_b)) == (M.n_src, M.n_dst)
+        rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
+        assert np.array_equal(f.variables["row_idx"][:], rows + 1)
+        assert np.array_equal(f.variables["col_idx"][:], csr["col"] + 1)
+        assert np.array_equal(f.variables["S"][:], csr["val"])
+    finally:
+        f.close()
+    M2 = gpu.Matrix.read_esmf(p)
+    csr2 = M2.to_csr()
+    for k in ("row_ptr", "col", "val"):
+        assert np.array_equal(csr[k], csr2[k]), k
+    for k in ("frac_a", "frac_b", "area_a", "area_b"):
+        assert not np.any(csr2[k]), k
+    x = torch.tensor(np.random.default_rng(2).standard_normal(M.n_src), device="cuda")
+    assert torch.equal(gpu.apply_f64(M, x), gpu.apply_f64(M2, x))
+    w = gpu.esmf_read(p)
+    perm = np.random.default_rng(4).permutation(w["S"].size)
+    q = tmp_path / "shuffled.nc"
+    gpu.esmf_write(q, w["n_a"], w["n_b"], w["S"][perm], w["col_idx"][perm], w["row_idx"][perm])
+    csr3 = gpu.Matrix.read_esmf(q).to_csr()
+    for k in ("row_ptr", "col", "val"):
+        assert np.array_equal(csr[k], csr3[k]), k
