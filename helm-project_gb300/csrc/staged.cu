@@ -36,6 +36,11 @@ constexpr int kRows = 128;       // rows per block (4 warps)
 constexpr int kMaxUS = 3072;     // staging floats per field a block may use
 constexpr int kMaxL = 32;        // longest row handled by the blocked kernels
 constexpr int kPool = 4;         // streams the class launches are spread over
+// Entries are skipped past the warp's longest row in groups of kGroup: the
+// group's straight-line code lets the scheduler overlap the compensated
+// steps of neighbouring entries; entries past a row's end are zero (weight
+// 0 on the zero slot) and leave the sums unchanged.
+constexpr int kGroup = 4;
 const int kUsBuckets[] = {1024, 3072};  // staging strides compiled into the chunk kernel
 
 inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
@@ -145,21 +150,24 @@ __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, c
             cn[q] = pk(0.f, 0.f);
         }
 #pragma unroll
-        for (int k = 0; k < L; ++k) {
-            if (k < wl) {  // warp-uniform
-                const F2 hp = pk(h[k], h[k]), hn = pk(-h[k], -h[k]), ln = pk(-lw[k], -lw[k]);
-                const float *p0 = cur + li[k];
+        for (int k0 = 0; k0 < L; k0 += kGroup) {
+            if (k0 < wl) {  // warp-uniform
 #pragma unroll
-                for (int q = 0; q < T / 2; ++q) {
-                    const F2 xv = pk(p0[(2 * q) * US], p0[(2 * q + 1) * US]);
-                    const F2 p = mul2(hp, xv);
-                    const F2 pen = fma2(hn, xv, p);  // p - h*x, exact
-                    const F2 t = add2(sa[q], p);
-                    const F2 bp = sub2(t, sa[q]);
-                    const F2 e = add2(sub2(sa[q], sub2(t, bp)), sub2(p, bp));
-                    const F2 u1 = fma2(ln, xv, pen);  // -(lo*x + product error)
-                    cn[q] = add2(cn[q], sub2(u1, e));
-                    sa[q] = t;
+                for (int k = k0; k < k0 + kGroup && k < L; ++k) {
+                    const F2 hp = pk(h[k], h[k]), hn = pk(-h[k], -h[k]), ln = pk(-lw[k], -lw[k]);
+                    const float *p0 = cur + li[k];
+#pragma unroll
+                    for (int q = 0; q < T / 2; ++q) {
+                        const F2 xv = pk(p0[(2 * q) * US], p0[(2 * q + 1) * US]);
+                        const F2 p = mul2(hp, xv);
+                        const F2 pen = fma2(hn, xv, p);  // p - h*x, exact
+                        const F2 t = add2(sa[q], p);
+                        const F2 bp = sub2(t, sa[q]);
+                        const F2 e = add2(sub2(sa[q], sub2(t, bp)), sub2(p, bp));
+                        const F2 u1 = fma2(ln, xv, pen);  // -(lo*x + product error)
+                        cn[q] = add2(cn[q], sub2(u1, e));
+                        sa[q] = t;
+                    }
                 }
             }
         }
