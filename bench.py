@@ -208,11 +208,21 @@ def main():
     ap.add_argument("--apply-only", action="store_true",
                     help="time only the split apply (no FP64 apply, oracle parity, e2e, weight generation "
                          "or CPU baseline reports); for profiler captures")
+    ap.add_argument("--weightgen-only", action="store_true",
+                    help="only generate the 0.25 deg -> C384 conservative weights (three times) and print their "
+                         "timing; for profiler captures of the weight-generation kernels")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return reference_arm(args)
+    if args.weightgen_only:
+        import axgb
+        from axgb import grids
+        axgb.init(0)
+        md = axgb.Mesh.from_grid(grids.latlon_deg(0.25))
+        print(json.dumps({"weightgen_0p25_to_c384": weightgen_c384(md, None)}))
+        return 0
     if args.workload == "voronoi":
         return voronoi_main(args)
 

@@ -120,6 +120,7 @@ struct MeshView {
     // per-cell products of the prep kernel
     double *area;
     DCap *cap;           // centroid xyz + angular radius
+    float4 *capf;           // the same rounded to float (the search's cap prefilter)
     float *box;             // reference float AABB [n_cells*6]
     unsigned char *flags;   // bit0 degenerate, bit1 masked, bit2 area<=0; class in bits 4..5
 };
@@ -134,6 +135,7 @@ struct Mesh {
     DBuf<int> d_off, d_idx, d_mask;
     DBuf<double> d_xyz, d_lonlat, d_trig, d_user_area, d_area;
     DBuf<DCap> d_cap;
+    DBuf<float4> d_capf;
     DBuf<float> d_box;
     DBuf<unsigned char> d_flags;
     bool prepped = false;

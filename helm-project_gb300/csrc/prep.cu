@@ -22,6 +22,7 @@ MeshView Mesh::view() const {
     v.mask = has_mask ? d_mask.p : nullptr;
     v.area = d_area.p;
     v.cap = d_cap.p;
+    v.capf = d_capf.p;
     v.box = d_box.p;
     v.flags = d_flags.p;
     return v;
@@ -99,6 +100,8 @@ __global__ void k_cell_prep(MeshView m) {
     f |= static_cast<unsigned char>(cls << 4);
     m.area[c] = area;
     m.cap[c] = cap;
+    m.capf[c] = make_float4(__double2float_rn(cap.x), __double2float_rn(cap.y), __double2float_rn(cap.z),
+                            __double2float_rn(cap.r));
     m.flags[c] = f;
 }
 
@@ -109,6 +112,7 @@ void mesh_prepare(Mesh &m, cudaStream_t s) {
     if (m.prepped) return;
     m.d_area.alloc(m.n_cells);
     m.d_cap.alloc(m.n_cells);
+    m.d_capf.alloc(m.n_cells);
     m.d_box.alloc(6 * m.n_cells);
     m.d_flags.alloc(m.n_cells);
     if (m.n_cells > 0) {

@@ -188,10 +188,32 @@ __device__ __forceinline__ bool fbox_meet(const float *a, const float *b) {
     return true;
 }
 
+// The cap test acos(clamp(dot(c_s, c_d))) > r_s + r_d is taken in FP64 as
+// the reference takes it (spherical_cap_filter.hpp:190-197), but most pairs
+// are decided in FP32 first. On unit vectors the angle exceeds R exactly
+// when the chord |c_s - c_d| exceeds 2 sin(R/2) (for R below pi, where
+// both sides are monotone). From the float copies of the centroids and
+// radii (rounding 6e-8 relative each) the float chord lies within 1.1e-6
+// of the chord of the double centroids, and 2 sinf(R/2) within 0.6e-6 of
+// its double value; the FP64 acos and sum differ from the exact angle and
+// sum by less than 2e-8. So when the float sides differ by more than
+// kCapMargin, the FP64 test returns the same answer. Nearer pairs, and sums
+// above 3, take the FP64 test.
+constexpr float kCapMargin = 4.0e-6f;
+
 // Exact reference gates for a pair that the LBVH admitted.
-__device__ __forceinline__ bool gate(const MeshView &S, int i, const float *dbox, const DCap &dc) {
+__device__ __forceinline__ bool gate(const MeshView &S, int i, const float *dbox, const DCap &dc, const float4 &dcf) {
     if (S.flags[i] & kExcluded) return false;
     if (!fbox_meet(S.box + 6 * static_cast<i64>(i), dbox)) return false;
+    const float4 sf = S.capf[i];
+    const float rs = sf.w + dcf.w;
+    if (rs < 3.0f) {
+        const float ex = sf.x - dcf.x, ey = sf.y - dcf.y, ez = sf.z - dcf.z;
+        const float ch = sqrtf(ex * ex + ey * ey + ez * ez);
+        const float t = 2.0f * sinf(0.5f * rs);
+        if (ch > t + kCapMargin) return false;
+        if (ch < t - kCapMargin) return true;
+    }
     DCap sc = S.cap[i];
     double cd = sc.x * dc.x + sc.y * dc.y + sc.z * dc.z;  // dot(centroid_s, centroid_d)
     cd = fmin(1.0, fmax(-1.0, cd));
@@ -208,6 +230,7 @@ __global__ void k_search(MeshView S, MeshView D, const float4 *__restrict__ nlo,
         int cnt = 0;
         if (!(D.flags[j] & kExcluded) && root >= 0) {
             DCap dc = D.cap[j];
+            const float4 dcf = D.capf[j];
             float dbox[6];
 #pragma unroll
             for (int d = 0; d < 6; ++d) dbox[d] = D.box[6 * j + d];
@@ -234,7 +257,7 @@ __global__ void k_search(MeshView S, MeshView D, const float4 *__restrict__ nlo,
                     if (node >= n_leaf_base) {
                         int cell = __float_as_int(lo.w);
                         ++hits;
-                        if (gate(S, cell, dbox, dc)) {
+                        if (gate(S, cell, dbox, dc, dcf)) {
                             if (FILL) out_src[wbase + cnt] = cell;
                             ++cnt;
                         }
