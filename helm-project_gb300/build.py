@@ -1,8 +1,9 @@
 """Build libaxgb.so for sm_103a, in tree (helm-project_gb300/axgb/lib/).
 
 CUDA translation units are compiled by nvcc with one -gencode
-(compute_103a -> sm_103a); the geometry units (prep.cu, weights.cu) with
---fmad=false so double expressions round as written. The host C++ units
+(compute_103a -> sm_103a); the geometry units (prep.cu, weights.cu,
+coastal.cu, nearest.cu) with --fmad=false so double expressions, and the
+float distances of the nearest searches, round as written. The host C++ units
 (api.cpp, esmf_io.cpp) are compiled by g++ with -ffp-contract=off and OpenMP
 (parallel sort in the grid detector). Units compile in parallel; the link uses nvcc.
 """
@@ -29,7 +30,8 @@ UNITS = [
     ("apply.cu", []),
     ("staged.cu", []),
     ("scan_sort.cu", []),
-    ("coastal.cu", []),
+    ("coastal.cu", ["--fmad=false"]),
+    ("nearest.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["api.cpp", "esmf_io.cpp"]  # host C++ (g++)
 HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", os.path.join("..", "..", "include", "axgb.h")]

@@ -559,9 +559,12 @@ int axgb_generate_weights(int src, int dst, const axgb_regrid_config *cfg_in, in
                     throw Error(AXGB_ERR_UNSUPPORTED, "bilinear: source is not rectilinear (BVH bilinear not provided)");
                 generate_bilinear(*S, *D, cfg, *M);
             }
+        } else if (cfg.method == AXGB_NEAREST_NEIGHBOR) {
+            generate_nearest(*S, *D, cfg, *M);  // generate_nearest (weight_generator.cpp:2097-2118)
         } else {
             throw Error(AXGB_ERR_UNSUPPORTED, "generate_weights: method " + std::to_string(cfg.method) +
-                                                  " not provided (Conservative1stOrder and Bilinear are)");
+                                                  " not provided (Conservative1stOrder, Bilinear and "
+                                                  "NearestNeighbor are)");
         }
         // generate() applies the coastal post-pass to every method (weight_generator.cpp:2014)
         coastal_postpass(*S, *D, cfg, *M);

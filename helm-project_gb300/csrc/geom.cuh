@@ -75,10 +75,10 @@ __device__ double d_poly_area(const DPoly<CAP> &p) {
     return fabs(total);
 }
 
-// Arc (v1 -> v2) against great circle (ea, eb), midpoint fallback
-// (spherical_clipper.hpp:265-295).
-__device__ __forceinline__ DV3 d_arc_cross(const DV3 &v1, const DV3 &v2, const DV3 &ea, const DV3 &eb) {
-    DV3 n1 = d_cross(ea, eb);
+// Arc (v1 -> v2) against the great circle of normal n1 = ea x eb, midpoint
+// fallback (spherical_clipper.hpp:265-295; the caller passes the edge
+// normal it already formed, the same product).
+__device__ __forceinline__ DV3 d_arc_cross(const DV3 &v1, const DV3 &v2, const DV3 &n1) {
     DV3 n2 = d_cross(v1, v2);
     DV3 d = d_cross(n1, n2);
     double dl = d_lensq(d);
@@ -93,6 +93,8 @@ __device__ __forceinline__ DV3 d_arc_cross(const DV3 &v1, const DV3 &v2, const D
 // circles, inclusive eps = -1e-14, edges with |a x b|^2 < 1e-30 skipped;
 // spherical_clipper.hpp:181-229 and :301-335). Returns the overlap area;
 // sets *over when a polygon exceeded CAP.
+// The previous vertex's side test is the value the loop formed one step
+// earlier (the same dot product), and the two buffers swap roles per edge.
 template <int CAP>
 __device__ double d_overlap_area(const DPoly<CAP> &subject, const DPoly<CAP> &clip, DPoly<CAP> &bufa,
                                  DPoly<CAP> &bufb, bool *over) {
@@ -105,38 +107,38 @@ __device__ double d_overlap_area(const DPoly<CAP> &subject, const DPoly<CAP> &cl
         bufa.y[i] = subject.y[i];
         bufa.z[i] = subject.z[i];
     }
+    DPoly<CAP> *in = &bufa, *out = &bufb;
     constexpr double eps = -1.0e-14;
     for (int ci = 0; ci < clip.n; ++ci) {
         DV3 ea = clip.at(ci);
         DV3 eb = clip.at(ci + 1 == clip.n ? 0 : ci + 1);
         DV3 nrm = d_cross(ea, eb);
         if (d_lensq(nrm) < 1.0e-30) continue;
-        bufb.clear();
-        const int nin = bufa.n;
+        out->clear();
+        const int nin = in->n;
+        DV3 prv = in->at(nin - 1);
+        double dp = d_dot(nrm, prv);
         for (int i = 0; i < nin; ++i) {
-            int pi = (i + nin - 1) % nin;
-            DV3 cur = bufa.at(i), prv = bufa.at(pi);
+            DV3 cur = in->at(i);
             double dc = d_dot(nrm, cur);
-            double dp = d_dot(nrm, prv);
             bool cin = dc >= eps;
             bool pin = dp >= eps;
             if (cin) {
-                if (!pin) bufb.push(d_arc_cross(prv, cur, ea, eb));
-                bufb.push(cur);
+                if (!pin) out->push(d_arc_cross(prv, cur, nrm));
+                out->push(cur);
             } else if (pin) {
-                bufb.push(d_arc_cross(prv, cur, ea, eb));
+                out->push(d_arc_cross(prv, cur, nrm));
             }
+            prv = cur;
+            dp = dc;
         }
-        if (bufb.over) *over = true;
-        bufa.n = bufb.n;
-        for (int i = 0; i < bufb.n; ++i) {
-            bufa.x[i] = bufb.x[i];
-            bufa.y[i] = bufb.y[i];
-            bufa.z[i] = bufb.z[i];
-        }
-        if (bufa.n < 3) return 0.0;
+        if (out->over) *over = true;
+        DPoly<CAP> *t = in;
+        in = out;
+        out = t;
+        if (in->n < 3) return 0.0;
     }
-    return d_poly_area(bufa);
+    return d_poly_area(*in);
 }
 
 // Degenerate classification (degenerate_cell_handler.hpp:115-142, 259-367):

@@ -254,6 +254,9 @@ struct EsmfWeights {
 void esmf_write(const std::string &path, std::int64_t n_a, std::int64_t n_b, std::int64_t nnz, const double *S,
                 const std::int32_t *col1, const std::int32_t *row1);
 EsmfWeights esmf_read(const std::string &path);
+// nearest.cu: nearest-neighbour weights (index rounding for two regular
+// grids, else an exact float nearest query over centroid points)
+void generate_nearest(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 // regular x regular bilinear fast path; false = no destination cells (fall through)
 bool generate_bilinear_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);

@@ -1,0 +1,229 @@
+// Nearest-neighbour weights: WeightGenerator::generate_nearest
+// (src/solver/weight_generator.cpp:2097-2118). Each destination cell takes
+// weight 1 from one source cell.
+//   * Two regular grids: generate_nearest_rect (:2025-2080). The
+//     destination cell's lower-left corner (lon_min + i*dlon, lat_min +
+//     j*dlat) is rounded to the nearest source index, wrapped in longitude
+//     and clamped in latitude; frac and area arrays stay zero.
+//   * Otherwise generate_nearest_impl<3> (:2132-2260): cell centroids as
+//     compute_cell_centroids_xy (:75-138), turned into float unit vectors
+//     (cos/sin of the degree values times pi/180, in double, then rounded),
+//     and for each destination point the source point at the least float
+//     squared Euclidean distance. The reference asks ArborX v2.1 for
+//     nearest(point, 1), which this checkout does not vendor; here exact
+//     ties go to the lower source index. frac arrays are 1 and the areas
+//     are the cells' own (mesh areas or spherical polygon areas). Masks play
+//     no part (the coastal post-pass handles a masked source afterwards).
+// The search is exact: source points are bucketed in a uniform g^3 grid over
+// [-1, 1]^3 and each query scans shells of cells around its own until no
+// unseen point can be nearer (with a 1e-5 margin over float rounding).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.hpp"
+
+namespace axgb {
+namespace {
+
+inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
+
+struct NnGrid {
+    int g;
+    float h;  // cell edge, 2 / g
+};
+
+__device__ __forceinline__ int nn_cell(float v, const NnGrid &G) {
+    const int c = static_cast<int>(floorf((v + 1.0f) / G.h));
+    return min(G.g - 1, max(0, c));
+}
+
+// Float unit vector of a cell's centroid (compute_cell_centroids_xy, then
+// the point construction of generate_nearest_impl<3>).
+__global__ void k_nn_points(MeshView m, float4 *pts) {
+    const i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const double pi = 3.14159265358979323846;
+    const int b = m.off[c], e = m.off[c + 1], nv = e - b;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int k = b; k < e; ++k) {
+        const double lon = m.lonlat[m.idx[k]] * pi / 180.0, lat = m.lonlat[m.idx[k] + m.n_nodes] * pi / 180.0;
+        sx += cos(lat) * cos(lon);
+        sy += cos(lat) * sin(lon);
+        sz += sin(lat);
+    }
+    const double inv = nv > 0 ? 1.0 / static_cast<double>(nv) : 0.0;
+    double lat_avg = asin(sz * inv), lon_avg = atan2(sy * inv, sx * inv);
+    if (lon_avg < 0.0) lon_avg += 2.0 * pi;
+    lon_avg = lon_avg * 180.0 / pi;
+    lat_avg = lat_avg * 180.0 / pi;
+    const double lon = lon_avg * pi / 180.0, lat = lat_avg * pi / 180.0;
+    pts[c] = make_float4(static_cast<float>(cos(lat) * cos(lon)), static_cast<float>(cos(lat) * sin(lon)),
+                         static_cast<float>(sin(lat)), 0.0f);
+}
+
+__global__ void k_nn_keys(const float4 *pts, i64 n, NnGrid G, std::uint64_t *key, int *val, int *cnt) {
+    const i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pts[i];
+    const int cell = (nn_cell(p.x, G) * G.g + nn_cell(p.y, G)) * G.g + nn_cell(p.z, G);
+    key[i] = static_cast<std::uint64_t>(cell);
+    val[i] = static_cast<int>(i);
+    atomicAdd(&cnt[cell], 1);
+}
+
+__device__ __forceinline__ float nn_d2(const float4 &a, const float4 &q) {
+    const float dx = a.x - q.x, dy = a.y - q.y, dz = a.z - q.z;
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// One thread per destination point: shells r = 0, 1, ... of cells around the
+// point's cell. Points outside the shells seen so far are at least r*h away;
+// the search ends once the best distance is below r*h - 1e-5.
+__global__ void k_nn_query(const float4 *__restrict__ sp, const int *__restrict__ order,
+                           const int *__restrict__ start, NnGrid G, const float4 *__restrict__ dp, i64 n_dst,
+                           int *col) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n_dst) return;
+    const float4 q = dp[j];
+    const int cx = nn_cell(q.x, G), cy = nn_cell(q.y, G), cz = nn_cell(q.z, G);
+    float best = INFINITY;
+    int bi = -1;
+    for (int r = 0; r <= G.g; ++r) {
+        for (int ix = max(0, cx - r); ix <= min(G.g - 1, cx + r); ++ix)
+            for (int iy = max(0, cy - r); iy <= min(G.g - 1, cy + r); ++iy) {
+                const bool face = abs(ix - cx) == r || abs(iy - cy) == r;
+                // on the shell: every z of the column when x or y is on its face,
+                // else only the two z faces
+                const int zs = face ? 1 : 2 * r;
+                for (int iz = cz - r; iz <= cz + r; iz += max(1, zs)) {
+                    if (iz < 0 || iz >= G.g) continue;
+                    const int cell = (ix * G.g + iy) * G.g + iz;
+                    for (int k = start[cell]; k < start[cell + 1]; ++k) {
+                        const int s = order[k];
+                        const float d2 = nn_d2(sp[s], q);
+                        if (d2 < best || (d2 == best && s < bi)) {
+                            best = d2;
+                            bi = s;
+                        }
+                    }
+                }
+            }
+        const float reach = static_cast<float>(r) * G.h - 1.0e-5f;
+        if (bi >= 0 && reach > 0.0f && best < reach * reach) break;
+    }
+    col[j] = bi;
+}
+
+struct RectNN {
+    i64 s_ni, s_nj, d_ni;
+    double s_lon, s_lat, s_dlon, s_dlat, d_lon, d_lat, d_dlon, d_dlat;
+};
+
+// generate_nearest_rect (:2050-2077).
+__global__ void k_nn_rect(RectNN a, i64 n_dst, int *col) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n_dst) return;
+    const i64 di = j % a.d_ni, dj = j / a.d_ni;
+    const double lon = a.d_lon + static_cast<double>(di) * a.d_dlon;
+    const double lat = a.d_lat + static_cast<double>(dj) * a.d_dlat;
+    i64 si = static_cast<i64>(round((lon - a.s_lon) / a.s_dlon));
+    si = si % a.s_ni;
+    if (si < 0) si += a.s_ni;
+    i64 sj = static_cast<i64>(round((lat - a.s_lat) / a.s_dlat));
+    if (sj < 0) sj = 0;
+    if (sj >= a.s_nj) sj = a.s_nj - 1;
+    col[j] = static_cast<int>(sj * a.s_ni + si);
+}
+
+__global__ void k_nn_csr(const int *col_all, i64 n_dst, int *cnt) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j < n_dst) cnt[j] = col_all[j] >= 0 ? 1 : 0;
+}
+
+__global__ void k_nn_pack(const int *col_all, const int *row_ptr, i64 n_dst, int *col, double *val) {
+    const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n_dst || col_all[j] < 0) return;
+    col[row_ptr[j]] = col_all[j];
+    val[row_ptr[j]] = 1.0;
+}
+
+__global__ void k_nn_fill(double *a, i64 n, double v) {
+    const i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+}  // namespace
+
+void generate_nearest(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {
+    cudaStream_t s = 0;
+    const i64 n_src = src.n_cells, n_dst = dst.n_cells;
+    AXGB_REQUIRE(n_src < (i64(1) << 31) - 1 && n_dst < (i64(1) << 31) - 1, "meshes above 2^31 cells");
+    mesh_prepare(src, s);
+    mesh_prepare(dst, s);
+    out.n_src = n_src;
+    out.n_dst = n_dst;
+    DBuf<int> col_all(n_dst);
+    const bool rect = src.grid.regular && dst.grid.regular;
+    if (rect) {
+        const GridInfo &sg = src.grid, &dg = dst.grid;
+        RectNN a{sg.ni, sg.nj, dg.ni, sg.lon_min, sg.lat_min, sg.dlon, sg.dlat, dg.lon_min, dg.lat_min, dg.dlon, dg.dlat};
+        if (n_dst) k_nn_rect<<<nblk(n_dst, 256), 256, 0, s>>>(a, n_dst, col_all.p);
+        AXGB_CUDA(cudaGetLastError());
+    } else if (n_src == 0) {
+        if (n_dst) AXGB_CUDA(cudaMemsetAsync(col_all.p, 0xff, sizeof(int) * n_dst, s));
+        if (n_dst && cfg.unmapped == AXGB_UNMAPPED_ERROR)
+            throw Error(AXGB_ERR_UNMAPPED, "generate_nearest: unmapped destination cell 0 (no source cells)");
+    } else {
+        DBuf<float4> sp(n_src), dp(n_dst);
+        k_nn_points<<<nblk(n_src, 128), 128, 0, s>>>(src.view(), sp.p);
+        if (n_dst) k_nn_points<<<nblk(n_dst, 128), 128, 0, s>>>(dst.view(), dp.p);
+        AXGB_CUDA(cudaGetLastError());
+        // about 8 source points per occupied cell: the sphere meets ~4.7 g^2 of the g^3 cells
+        const int g = static_cast<int>(std::clamp(std::lround(std::sqrt(static_cast<double>(n_src) / 37.6)), 1L, 384L));
+        const NnGrid G{g, 2.0f / static_cast<float>(g)};
+        const i64 ncell = static_cast<i64>(g) * g * g;
+        DBuf<std::uint64_t> key(n_src);
+        DBuf<int> order(n_src), cnt(ncell), start(ncell + 1);
+        cnt.zero(s);
+        k_nn_keys<<<nblk(n_src, 256), 256, 0, s>>>(sp.p, n_src, G, key.p, order.p, cnt.p);
+        AXGB_CUDA(cudaGetLastError());
+        int bits = 1;
+        while ((i64(1) << bits) < ncell) ++bits;
+        radix_sort_pairs_u64(key.p, order.p, n_src, bits, s);  // stable: ascending index within a cell
+        scan_exclusive_i32(cnt.p, start.p, ncell, s);
+        if (n_dst) k_nn_query<<<nblk(n_dst, 128), 128, 0, s>>>(sp.p, order.p, start.p, G, dp.p, n_dst, col_all.p);
+        AXGB_CUDA(cudaGetLastError());
+    }
+    DBuf<int> cnt(n_dst);
+    out.row_ptr.alloc(n_dst + 1);
+    if (n_dst) k_nn_csr<<<nblk(n_dst, 256), 256, 0, s>>>(col_all.p, n_dst, cnt.p);
+    scan_exclusive_i32(cnt.p, out.row_ptr.p, n_dst, s);
+    int nnz = 0;
+    AXGB_CUDA(cudaMemcpy(&nnz, out.row_ptr.p + n_dst, sizeof(int), cudaMemcpyDeviceToHost));
+    out.nnz = nnz;
+    out.col.alloc(std::max(1, nnz));
+    out.val.alloc(std::max(1, nnz));
+    if (n_dst) k_nn_pack<<<nblk(n_dst, 256), 256, 0, s>>>(col_all.p, out.row_ptr.p, n_dst, out.col.p, out.val.p);
+    out.frac_a.alloc(n_src);
+    out.frac_b.alloc(n_dst);
+    out.area_a.alloc(n_src);
+    out.area_b.alloc(n_dst);
+    if (rect) {  // default-initialised views in generate_nearest_rect
+        out.frac_a.zero(s);
+        out.frac_b.zero(s);
+        out.area_a.zero(s);
+        out.area_b.zero(s);
+    } else {
+        if (n_src) k_nn_fill<<<nblk(n_src, 256), 256, 0, s>>>(out.frac_a.p, n_src, 1.0);
+        if (n_dst) k_nn_fill<<<nblk(n_dst, 256), 256, 0, s>>>(out.frac_b.p, n_dst, 1.0);
+        if (n_src) AXGB_CUDA(cudaMemcpyAsync(out.area_a.p, src.d_area.p, sizeof(double) * n_src, cudaMemcpyDeviceToDevice, s));
+        if (n_dst) AXGB_CUDA(cudaMemcpyAsync(out.area_b.p, dst.d_area.p, sizeof(double) * n_dst, cudaMemcpyDeviceToDevice, s));
+    }
+    AXGB_CUDA(cudaGetLastError());
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    out.stats[3] = nnz;
+    slice_centroids(dst.view(), out, s);
+}
+
+}  // namespace axgb

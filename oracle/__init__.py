@@ -97,6 +97,8 @@ class Oracle:
                                        + [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)])
         L.orc_bilinear.restype = C.c_int
         L.orc_bilinear.argtypes = mesh + mesh + [C.c_int, C.POINTER(C.c_void_p)]
+        L.orc_nearest.restype = C.c_int
+        L.orc_nearest.argtypes = mesh + mesh + [C.c_int, C.POINTER(C.c_void_p)]
         L.orc_result_nnz.restype = C.c_int64
         L.orc_result_nnz.argtypes = [C.c_void_p]
         L.orc_result_stats.argtypes = [C.c_void_p, _i64p]
@@ -219,6 +221,15 @@ class Oracle:
         dt = time.perf_counter() - t0
         if rc != 0:
             raise RuntimeError(f"oracle bilinear failed rc={rc}")
+        return self._collect(h, src.n_cells, dst.n_cells, dt)
+
+    def nearest(self, src, dst, unmapped: int = 1) -> Weights:
+        h = C.c_void_p()
+        t0 = time.perf_counter()
+        rc = self.L.orc_nearest(*_mesh_args(src), *_mesh_args(dst), unmapped, C.byref(h))
+        dt = time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError(f"oracle nearest failed rc={rc}")
         return self._collect(h, src.n_cells, dst.n_cells, dt)
 
     def _collect(self, h, n_src, n_dst, dt):

@@ -852,6 +852,100 @@ static bool bilinear_regular(const Mesh &S, const Mesh &D, const GridInfo &sg, i
     return true;
 }
 
+// Nearest-neighbour weights: WeightGenerator::generate_nearest
+// (src/solver/weight_generator.cpp:2097-2118). Two regular grids take
+// generate_nearest_rect (:2025-2080): the destination cell's lower-left
+// corner rounded to a source index, wrapped in longitude, clamped in
+// latitude, frac/area zero. Otherwise generate_nearest_impl<3>
+// (:2132-2260): float unit vectors of the compute_cell_centroids_xy
+// centroids (:75-138) and, per destination point, the source point at the
+// least float squared distance (dx*dx + dy*dy + dz*dz, no contraction);
+// ArborX v2.1's nearest(point, 1) is not in the checkout, so exact ties go
+// to the lower source index. frac = 1, areas = the cells' areas.
+// Brute force over all source points. unmapped: 0 Error, 1 Ignore; returns
+// false when there is no source cell under Error.
+static bool nearest(const Mesh &S, const Mesh &D, int unmapped, orc_result *res) {
+    const i64 n_src = S.n_cells, n_dst = D.n_cells;
+    res->n_src = n_src;
+    res->n_dst = n_dst;
+    GridInfo sg = detect(S), dg = detect(D);
+    if (sg.regular && dg.regular) {
+        for (i64 j = 0; j < n_dst; ++j) {
+            const i64 di = j % dg.ni, dj = j / dg.ni;
+            const double lon = dg.lon_min + static_cast<double>(di) * dg.dlon;
+            const double lat = dg.lat_min + static_cast<double>(dj) * dg.dlat;
+            i64 si = static_cast<i64>(std::round((lon - sg.lon_min) / sg.dlon));
+            si = si % sg.ni;
+            if (si < 0) si += sg.ni;
+            i64 sj = static_cast<i64>(std::round((lat - sg.lat_min) / sg.dlat));
+            sj = std::max<i64>(0, std::min<i64>(sj, sg.nj - 1));
+            res->row.push_back(j);
+            res->col.push_back(sj * sg.ni + si);
+            res->w.push_back(1.0);
+        }
+        res->frac_a.assign(n_src, 0.0);
+        res->frac_b.assign(n_dst, 0.0);
+        res->area_a.assign(n_src, 0.0);
+        res->area_b.assign(n_dst, 0.0);
+        return true;
+    }
+    if (n_src == 0 && n_dst > 0 && unmapped == 0) return false;
+    auto points = [](const Mesh &m) {
+        std::vector<float> p(3 * m.n_cells);
+        for (i64 c = 0; c < m.n_cells; ++c) {
+            double sx = 0, sy = 0, sz = 0;
+            const i64 b = m.off[c], e = m.off[c + 1];
+            for (i64 q = b; q < e; ++q) {
+                const double lo = m.lon(m.idx[q]) * kPi / 180.0, la = m.lat(m.idx[q]) * kPi / 180.0;
+                sx += std::cos(la) * std::cos(lo);
+                sy += std::cos(la) * std::sin(lo);
+                sz += std::sin(la);
+            }
+            const double inv = (e - b > 0) ? 1.0 / static_cast<double>(e - b) : 0.0;
+            double lat = std::asin(sz * inv), lon = std::atan2(sy * inv, sx * inv);
+            if (lon < 0.0) lon += 2.0 * kPi;
+            lon = lon * 180.0 / kPi;
+            lat = lat * 180.0 / kPi;
+            const double lr = lon * kPi / 180.0, tr = lat * kPi / 180.0;
+            p[3 * c] = static_cast<float>(std::cos(tr) * std::cos(lr));
+            p[3 * c + 1] = static_cast<float>(std::cos(tr) * std::sin(lr));
+            p[3 * c + 2] = static_cast<float>(std::sin(tr));
+        }
+        return p;
+    };
+    const std::vector<float> sp = points(S), dp = points(D);
+    std::vector<i64> best(n_dst, -1);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (i64 j = 0; j < n_dst; ++j) {
+        float bd = std::numeric_limits<float>::infinity();
+        i64 bi = -1;
+        for (i64 i = 0; i < n_src; ++i) {
+            const float dx = sp[3 * i] - dp[3 * j], dy = sp[3 * i + 1] - dp[3 * j + 1], dz = sp[3 * i + 2] - dp[3 * j + 2];
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < bd) {  // ascending i: the first of equal distances is kept
+                bd = d2;
+                bi = i;
+            }
+        }
+        best[j] = bi;
+    }
+    std::vector<double> sa(n_src), da(n_dst);
+    auto sx = node_xyz(S), dx = node_xyz(D);
+    for (i64 c = 0; c < n_src; ++c) sa[c] = S.areas ? S.areas[c] : poly_area(cell_poly(S, sx, c));
+    for (i64 c = 0; c < n_dst; ++c) da[c] = D.areas ? D.areas[c] : poly_area(cell_poly(D, dx, c));
+    for (i64 j = 0; j < n_dst; ++j)
+        if (best[j] >= 0) {
+            res->row.push_back(j);
+            res->col.push_back(best[j]);
+            res->w.push_back(1.0);
+        }
+    res->frac_a.assign(n_src, 1.0);
+    res->frac_b.assign(n_dst, 1.0);
+    res->area_a = sa;
+    res->area_b = da;
+    return true;
+}
+
 extern "C" {
 
 int orc_num_threads() {
@@ -1178,6 +1272,21 @@ int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *s
     res->frac_b.assign(dn_cells, 1.0);
     res->area_a.assign(sn_cells, 0.0);
     res->area_b.assign(dn_cells, 0.0);
+    *out = res;
+    return 0;
+}
+
+// Nearest-neighbour weights (see nearest above). Returns 0 ok, -7 when
+// there is no source cell under Error.
+int orc_nearest(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *soff, const i64 *sidx, i64 dn_nodes,
+                const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, int unmapped, orc_result **out) {
+    Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, nullptr, nullptr};
+    Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, nullptr, nullptr};
+    auto *res = new orc_result;
+    if (!nearest(S, D, unmapped, res)) {
+        delete res;
+        return -7;
+    }
     *out = res;
     return 0;
 }

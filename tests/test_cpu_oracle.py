@@ -286,3 +286,39 @@ def test_bilinear_regular_known_answer(oracle):
     y = np.bincount(w.row, weights=w.w * lat_s[w.col], minlength=w.n_dst)
     lat_d = np.repeat(-80.0 + 20.0 * np.arange(9), 18)
     assert np.allclose(y, lat_d, rtol=0, atol=1e-12)
+
+
+def test_nearest_regular_known_answer(oracle):
+    """generate_nearest_rect: a 20 deg cell's lower-left corner (20i, -90+20j)
+    rounds to the 10 deg source cell (2i, 2j); weights 1, frac and areas 0."""
+    src, dst = grids.latlon_deg(10.0), grids.latlon_deg(20.0)
+    w = oracle.nearest(src, dst)
+    assert w.nnz == dst.n_cells and np.all(w.w == 1.0)
+    j = np.arange(dst.n_cells)
+    di, dj = j % 18, j // 18
+    assert np.array_equal(w.row, j)
+    assert np.array_equal(w.col, (2 * dj) * 36 + 2 * di)
+    assert not np.any(w.frac_a) and not np.any(w.area_b)
+
+
+def test_nearest_unstructured_is_nearest(oracle):
+    """generate_nearest_impl<3>: one weight-1 entry per destination, at a
+    source centroid as near as any (to float rounding of the points)."""
+    src, dst = grids.cubed_sphere(8), grids.latlon_deg(10.0)
+    w = oracle.nearest(src, dst)
+    assert w.nnz == dst.n_cells and np.array_equal(w.row, np.arange(dst.n_cells)) and np.all(w.w == 1.0)
+
+    def unit(m):
+        # compute_cell_centroids_xy: lat = asin of the unnormalised mean z,
+        # lon = atan2 of the mean y, x; then the unit vector of (lon, lat)
+        ll = np.radians(m.node_lonlat[m.conn_indices])
+        v = np.stack([np.cos(ll[:, 1]) * np.cos(ll[:, 0]), np.cos(ll[:, 1]) * np.sin(ll[:, 0]), np.sin(ll[:, 1])], 1)
+        nv = np.diff(m.conn_offsets)
+        mean = np.add.reduceat(v, m.conn_offsets[:-1], axis=0) / nv[:, None]
+        lat, lon = np.arcsin(mean[:, 2]), np.arctan2(mean[:, 1], mean[:, 0])
+        return np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], 1)
+    s, d = unit(src), unit(dst)
+    dist = np.linalg.norm(d[:, None, :] - s[None, :, :], axis=2)
+    chosen = dist[np.arange(dst.n_cells), w.col]
+    assert np.all(chosen <= dist.min(axis=1) + 1e-6)
+    assert np.all(w.frac_a == 1.0) and np.all(w.area_a > 0)

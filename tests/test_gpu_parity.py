@@ -624,3 +624,36 @@ def test_esmf_weight_file_round_trip(gpu, oracle, tmp_path):
     csr3 = gpu.Matrix.read_esmf(q).to_csr()
     for k in ("row_ptr", "col", "val"):
         assert np.array_equal(csr[k], csr3[k]), k
+
+
+NEAREST_PAIRS = [
+    ("1deg->C48", lambda: (grids.latlon_deg(1.0), grids.cubed_sphere(48))),
+    ("C48->1deg", lambda: (grids.cubed_sphere(48), grids.latlon_deg(1.0))),
+    ("C12->C8", lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8))),
+    ("voronoi40962->2deg", lambda: (grids.voronoi(40962, seed=5), grids.latlon_deg(2.0))),
+    ("2deg->1deg (regular)", lambda: (grids.latlon_deg(2.0), grids.latlon_deg(1.0))),
+    ("1deg->shifted 3deg (regular)", lambda: (grids.latlon_deg(1.0),
+                                              grids.regular_latlon(120, 60, -180.0, -90.0, 3.0, 3.0))),
+]
+
+
+@pytest.mark.parametrize("name,make", NEAREST_PAIRS)
+def test_nearest_neighbor_parity(gpu, oracle, name, make):
+    """Nearest-neighbour weights (generate_nearest: index rounding for two
+    regular grids, else the exact float nearest centroid) against the oracle:
+    every (dst, src) pair identical, weights, fractions and areas as well."""
+    src, dst = make()
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "nearest_neighbor"})
+    wo = oracle.nearest(src, dst)
+    csr = _check_weights(M, wo)
+    assert np.array_equal(csr["val"], wo.w)
+
+
+def test_nearest_neighbor_masked_source(gpu, oracle):
+    """A masked source: the nearest-neighbour matrix goes through the coastal
+    post-pass like every method's (generate(), weight_generator.cpp:2014)."""
+    src, dst = grids.latlon_deg(5.0), grids.cubed_sphere(8)
+    mask = _land_mask(src)
+    ms = gpu.Mesh.from_arrays(src.node_lonlat, src.conn_offsets, src.conn_indices, mask=mask)
+    M = gpu.generate_weights(ms, gpu.Mesh.from_grid(dst), {"method": "nearest_neighbor"})
+    _check_weights(M, oracle.coastal(oracle.nearest(src, dst), src, dst, mask))
