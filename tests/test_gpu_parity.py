@@ -657,3 +657,66 @@ def test_nearest_neighbor_masked_source(gpu, oracle):
     ms = gpu.Mesh.from_arrays(src.node_lonlat, src.conn_offsets, src.conn_indices, mask=mask)
     M = gpu.generate_weights(ms, gpu.Mesh.from_grid(dst), {"method": "nearest_neighbor"})
     _check_weights(M, oracle.coastal(oracle.nearest(src, dst), src, dst, mask))
+
+
+PROPERTY_PAIRS = PAIRS[:5] + REGULAR_PAIRS[:3] + RECT_PAIRS[:3]
+
+
+@pytest.mark.parametrize("name,make", PROPERTY_PAIRS)
+def test_weight_properties(gpu, name, make):
+    """prop_conservative_nonneg.cpp / prop_grid_combinations.cpp /
+    prop_csr_format.cpp: weights >= 0, indices in range, row sums <= 1 + 1e-9,
+    row_ptr monotone from 0 to nnz, columns strictly ascending in each row."""
+    src, dst = make()
+    csr = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"}).to_csr()
+    rp, col, val = csr["row_ptr"], csr["col"], csr["val"]
+    assert rp[0] == 0 and rp[-1] == val.size and np.all(np.diff(rp) >= 0)
+    assert np.all(val >= 0.0)
+    assert np.all((col >= 0) & (col < src.n_cells))
+    rows = np.repeat(np.arange(dst.n_cells), np.diff(rp))
+    same_row = rows[1:] == rows[:-1]
+    assert np.all(col[1:][same_row] > col[:-1][same_row])
+    rs = np.bincount(rows, weights=val, minlength=dst.n_cells)
+    assert rs.max() <= 1.0 + 1e-9
+
+
+@pytest.mark.parametrize("direction", ["C96->1deg", "1deg->C96"])
+def test_constant_field_c96(gpu, direction):
+    """test_c96_benchmarks.py:60-104: a constant field regrids to 1 within
+    1e-12 (FP64 apply, DstArea and FracArea, great circles); the split-FP32
+    apply within 1e-6."""
+    import torch
+    a, b = grids.cubed_sphere(96), grids.latlon_deg(1.0)
+    src, dst = (a, b) if direction == "C96->1deg" else (b, a)
+    ms, md = gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst)
+    for norm in ("DstArea", "FracArea"):
+        M = gpu.generate_weights(ms, md, {"method": "conservative", "norm_type": norm})
+        y = gpu.apply_weights(M, np.ones(src.n_cells))
+        assert np.abs(y - 1.0).max() < 1e-12, (norm, np.abs(y - 1.0).max())
+        x32 = torch.ones((4, src.n_cells), dtype=torch.float32, device="cuda")
+        y32 = gpu.apply_f32split(M, x32).cpu().numpy()
+        assert np.abs(y32 - 1.0).max() < 1e-6
+
+
+@pytest.mark.parametrize("method,budget", [("bilinear", 0.250), ("nearest_neighbor", 0.350),
+                                           ("conservative", 0.400)])
+def test_performance_budgets(gpu, method, budget):
+    """test_axis_performance.py:47-110: 360 x 180 cells to 720 x 360 cells,
+    weight generation within the reference's per-method budget and the apply
+    of one field (host arrays in and out) within 80 ms."""
+    import time
+    src, dst = grids.latlon_deg(1.0), grids.latlon_deg(0.5)
+    warm = gpu.generate_weights(gpu.Mesh.from_grid(grids.latlon_deg(30.0)), gpu.Mesh.from_grid(grids.latlon_deg(20.0)),
+                                {"method": method})
+    gpu.apply_weights(warm, np.ones(warm.n_src))
+    ms, md = gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst)
+    t0 = time.perf_counter()
+    M = gpu.generate_weights(ms, md, {"method": method})
+    gen = time.perf_counter() - t0
+    field = grids.cell_centroids_xyz(src)[:, 0]  # cos(lat) cos(lon), the reference test's field
+    t0 = time.perf_counter()
+    y = gpu.apply_weights(M, field)
+    app = time.perf_counter() - t0
+    assert gen < budget, gen
+    assert app < 0.080, app
+    assert y.shape == (dst.n_cells,) and np.all(np.isfinite(y))
