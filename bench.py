@@ -208,6 +208,9 @@ def main():
     ap.add_argument("--apply-only", action="store_true",
                     help="time only the split apply (no FP64 apply, oracle parity, e2e, weight generation "
                          "or CPU baseline reports); for profiler captures")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only run the 17-pair persistent batch (weights, graph-captured batch apply, per-pair "
+                         "calls) and print its report; for profiler captures of the batch kernels")
     ap.add_argument("--weightgen-only", action="store_true",
                     help="only generate the 0.25 deg -> C384 conservative weights (three times) and print their "
                          "timing; for profiler captures of the weight-generation kernels")
@@ -216,6 +219,11 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return reference_arm(args)
+    if args.batch_only:
+        import axgb
+        axgb.init(0)
+        print(json.dumps({"batch_17_pairs": batch_pairs(args)}))
+        return 0
     if args.weightgen_only:
         import axgb
         from axgb import grids
