@@ -34,7 +34,7 @@ UNITS = [
     ("nearest.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["api.cpp", "esmf_io.cpp"]  # host C++ (g++)
-HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", os.path.join("..", "..", "include", "axgb.h")]
+HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", "lbvh.cuh", os.path.join("..", "..", "include", "axgb.h")]
 
 
 def _nvcc():

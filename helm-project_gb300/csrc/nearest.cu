@@ -14,29 +14,24 @@
 //     ties go to the lower source index. frac arrays are 1 and the areas
 //     are the cells' own (mesh areas or spherical polygon areas). Masks play
 //     no part (the coastal post-pass handles a masked source afterwards).
-// The search is exact: source points are bucketed in a uniform g^3 grid over
-// [-1, 1]^3 and each query scans shells of cells around its own until no
-// unseen point can be nearer (with a 1e-5 margin over float rounding).
+// The search is exact and logarithmic, as the reference's BVH query: an
+// LBVH over the source points (lbvh.cuh) and, per destination point, a
+// stackless walk that skips every node whose box is farther than the best
+// point so far, seeded with the points next to the query in Morton order.
+// A box's float distance never exceeds that of a point inside it (the same
+// clamped differences, summed in the same order, no contraction), so no
+// nearer point is ever skipped.
 #include <algorithm>
 #include <cmath>
 #include <vector>
 
 #include "internal.hpp"
+#include "lbvh.cuh"
 
 namespace axgb {
 namespace {
 
 inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
-
-struct NnGrid {
-    int g;
-    float h;  // cell edge, 2 / g
-};
-
-__device__ __forceinline__ int nn_cell(float v, const NnGrid &G) {
-    const int c = static_cast<int>(floorf((v + 1.0f) / G.h));
-    return min(G.g - 1, max(0, c));
-}
 
 // Float unit vector of a cell's centroid (compute_cell_centroids_xy, then
 // the point construction of generate_nearest_impl<3>).
@@ -62,14 +57,21 @@ __global__ void k_nn_points(MeshView m, float4 *pts) {
                          static_cast<float>(sin(lat)), 0.0f);
 }
 
-__global__ void k_nn_keys(const float4 *pts, i64 n, NnGrid G, std::uint64_t *key, int *val, int *cnt) {
+__global__ void k_pt_keys(const float4 *pts, i64 n, unsigned *keys, int *vals) {
     const i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = pts[i];
-    const int cell = (nn_cell(p.x, G) * G.g + nn_cell(p.y, G)) * G.g + nn_cell(p.z, G);
-    key[i] = static_cast<std::uint64_t>(cell);
-    val[i] = static_cast<int>(i);
-    atomicAdd(&cnt[cell], 1);
+    keys[i] = morton30(p.x, p.y, p.z);
+    vals[i] = static_cast<int>(i);
+}
+
+__global__ void k_pt_leaves(Bvh t, const float4 *pts, const int *vals) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= t.n) return;
+    const int s = vals[q];
+    const float4 p = pts[s];
+    t.lo[t.n - 1 + q] = make_float4(p.x, p.y, p.z, __int_as_float(s));
+    t.hi[t.n - 1 + q] = make_float4(p.x, p.y, p.z, __int_as_float(-1));
 }
 
 __device__ __forceinline__ float nn_d2(const float4 &a, const float4 &q) {
@@ -77,40 +79,55 @@ __device__ __forceinline__ float nn_d2(const float4 &a, const float4 &q) {
     return dx * dx + dy * dy + dz * dz;
 }
 
-// One thread per destination point: shells r = 0, 1, ... of cells around the
-// point's cell. Points outside the shells seen so far are at least r*h away;
-// the search ends once the best distance is below r*h - 1e-5.
-__global__ void k_nn_query(const float4 *__restrict__ sp, const int *__restrict__ order,
-                           const int *__restrict__ start, NnGrid G, const float4 *__restrict__ dp, i64 n_dst,
-                           int *col) {
+// One thread per destination point. Ties go to the lower source index:
+// nodes at exactly the best distance are still entered.
+__global__ void k_nn_query(const float4 *__restrict__ nlo, const float4 *__restrict__ nhi, int root, int n_leaf_base,
+                           const unsigned *__restrict__ keys, const int *__restrict__ vals, int n_src,
+                           const float4 *__restrict__ sp, const float4 *__restrict__ dp, i64 n_dst, int *col,
+                           int *err) {
     const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n_dst) return;
     const float4 q = dp[j];
-    const int cx = nn_cell(q.x, G), cy = nn_cell(q.y, G), cz = nn_cell(q.z, G);
     float best = INFINITY;
     int bi = -1;
-    for (int r = 0; r <= G.g; ++r) {
-        for (int ix = max(0, cx - r); ix <= min(G.g - 1, cx + r); ++ix)
-            for (int iy = max(0, cy - r); iy <= min(G.g - 1, cy + r); ++iy) {
-                const bool face = abs(ix - cx) == r || abs(iy - cy) == r;
-                // on the shell: every z of the column when x or y is on its face,
-                // else only the two z faces
-                const int zs = face ? 1 : 2 * r;
-                for (int iz = cz - r; iz <= cz + r; iz += max(1, zs)) {
-                    if (iz < 0 || iz >= G.g) continue;
-                    const int cell = (ix * G.g + iy) * G.g + iz;
-                    for (int k = start[cell]; k < start[cell + 1]; ++k) {
-                        const int s = order[k];
-                        const float d2 = nn_d2(sp[s], q);
-                        if (d2 < best || (d2 == best && s < bi)) {
-                            best = d2;
-                            bi = s;
-                        }
-                    }
-                }
+    auto take = [&](int s) {
+        const float d2 = nn_d2(sp[s], q);
+        if (d2 < best || (d2 == best && s < bi)) {
+            best = d2;
+            bi = s;
+        }
+    };
+    // seed: the source points on either side of the query in Morton order
+    const unsigned code = morton30(q.x, q.y, q.z);
+    int lo_i = 0, hi_i = n_src;
+    while (lo_i < hi_i) {
+        const int mid = (lo_i + hi_i) >> 1;
+        if (keys[mid] < code) lo_i = mid + 1;
+        else hi_i = mid;
+    }
+    for (int k = max(0, lo_i - 1); k <= min(n_src - 1, lo_i); ++k) take(vals[k]);
+    // ropes visit every node at most once; a longer walk means a malformed tree
+    const int max_steps = 2 * (2 * n_leaf_base + 1) + 8;
+    int steps = 0, node = root;
+    while (node >= 0) {
+        if (++steps > max_steps) {
+            atomicOr(err, 1);
+            break;
+        }
+        const float4 lo = nlo[node], hi = nhi[node];
+        const float dx = fmaxf(fmaxf(lo.x - q.x, 0.f), q.x - hi.x);
+        const float dy = fmaxf(fmaxf(lo.y - q.y, 0.f), q.y - hi.y);
+        const float dz = fmaxf(fmaxf(lo.z - q.z, 0.f), q.z - hi.z);
+        if (dx * dx + dy * dy + dz * dz <= best) {
+            if (node >= n_leaf_base) {
+                take(__float_as_int(lo.w));
+                node = __float_as_int(hi.w);
+            } else {
+                node = __float_as_int(lo.w);
             }
-        const float reach = static_cast<float>(r) * G.h - 1.0e-5f;
-        if (bi >= 0 && reach > 0.0f && best < reach * reach) break;
+        } else {
+            node = __float_as_int(hi.w);
+        }
     }
     col[j] = bi;
 }
@@ -179,20 +196,32 @@ void generate_nearest(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matri
         k_nn_points<<<nblk(n_src, 128), 128, 0, s>>>(src.view(), sp.p);
         if (n_dst) k_nn_points<<<nblk(n_dst, 128), 128, 0, s>>>(dst.view(), dp.p);
         AXGB_CUDA(cudaGetLastError());
-        // about 8 source points per occupied cell: the sphere meets ~4.7 g^2 of the g^3 cells
-        const int g = static_cast<int>(std::clamp(std::lround(std::sqrt(static_cast<double>(n_src) / 37.6)), 1L, 384L));
-        const NnGrid G{g, 2.0f / static_cast<float>(g)};
-        const i64 ncell = static_cast<i64>(g) * g * g;
-        DBuf<std::uint64_t> key(n_src);
-        DBuf<int> order(n_src), cnt(ncell), start(ncell + 1);
-        cnt.zero(s);
-        k_nn_keys<<<nblk(n_src, 256), 256, 0, s>>>(sp.p, n_src, G, key.p, order.p, cnt.p);
+        // LBVH over the source points (the construction of the candidate search)
+        const int n = static_cast<int>(n_src);
+        DBuf<float4> nlo(2 * n - 1), nhi(2 * n - 1);
+        DBuf<int> parent(2 * n - 1), right(n > 1 ? n - 1 : 1), flag(n > 1 ? n - 1 : 1), vals(n), err(1);
+        DBuf<unsigned> keys(n);
+        k_pt_keys<<<nblk(n, 256), 256, 0, s>>>(sp.p, n, keys.p, vals.p);
         AXGB_CUDA(cudaGetLastError());
-        int bits = 1;
-        while ((i64(1) << bits) < ncell) ++bits;
-        radix_sort_pairs_u64(key.p, order.p, n_src, bits, s);  // stable: ascending index within a cell
-        scan_exclusive_i32(cnt.p, start.p, ncell, s);
-        if (n_dst) k_nn_query<<<nblk(n_dst, 128), 128, 0, s>>>(sp.p, order.p, start.p, G, dp.p, n_dst, col_all.p);
+        radix_sort_pairs_u32(keys.p, vals.p, n, 30, s);
+        Bvh t{n, 0, nlo.p, nhi.p, parent.p, right.p, flag.p, keys.p};  // root: internal node 0, or the single leaf
+        AXGB_CUDA(cudaMemsetAsync(parent.p, 0xff, sizeof(int) * (2 * n - 1), s));
+        flag.zero(s);
+        err.zero(s);
+        k_pt_leaves<<<nblk(n, 256), 256, 0, s>>>(t, sp.p, vals.p);
+        if (n > 1) {
+            k_internal<<<nblk(n - 1, 256), 256, 0, s>>>(t);
+            k_refit<<<nblk(n, 256), 256, 0, s>>>(t);
+        }
+        k_ropes<<<nblk(2 * n - 1, 256), 256, 0, s>>>(t);
+        if (n_dst)
+            k_nn_query<<<nblk(n_dst, 128), 128, 0, s>>>(nlo.p, nhi.p, 0, n - 1, keys.p, vals.p, n, sp.p, dp.p, n_dst,
+                                                        col_all.p, err.p);
+        AXGB_CUDA(cudaGetLastError());
+        int h_err = 0;
+        AXGB_CUDA(cudaMemcpyAsync(&h_err, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        AXGB_CUDA(cudaStreamSynchronize(s));
+        if (h_err) throw Error(AXGB_ERROR, "generate_nearest: LBVH walk exceeded its step bound (malformed tree)");
         AXGB_CUDA(cudaGetLastError());
     }
     DBuf<int> cnt(n_dst);

@@ -631,6 +631,8 @@ NEAREST_PAIRS = [
     ("C48->1deg", lambda: (grids.cubed_sphere(48), grids.latlon_deg(1.0))),
     ("C12->C8", lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8))),
     ("voronoi40962->2deg", lambda: (grids.voronoi(40962, seed=5), grids.latlon_deg(2.0))),
+    ("regional 1deg->C24 (far queries)", lambda: (grids.regular_latlon(40, 30, 20.0, -10.0, 1.0, 1.0),
+                                                  grids.cubed_sphere(24))),
     ("2deg->1deg (regular)", lambda: (grids.latlon_deg(2.0), grids.latlon_deg(1.0))),
     ("1deg->shifted 3deg (regular)", lambda: (grids.latlon_deg(1.0),
                                               grids.regular_latlon(120, 60, -180.0, -90.0, 3.0, 3.0))),
