@@ -57,79 +57,9 @@ __global__ void k_nn_points(MeshView m, float4 *pts) {
                          static_cast<float>(sin(lat)), 0.0f);
 }
 
-__global__ void k_pt_keys(const float4 *pts, i64 n, unsigned *keys, int *vals) {
-    const i64 i = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 p = pts[i];
-    keys[i] = morton30(p.x, p.y, p.z);
-    vals[i] = static_cast<int>(i);
-}
-
-__global__ void k_pt_leaves(Bvh t, const float4 *pts, const int *vals) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= t.n) return;
-    const int s = vals[q];
-    const float4 p = pts[s];
-    t.lo[t.n - 1 + q] = make_float4(p.x, p.y, p.z, __int_as_float(s));
-    t.hi[t.n - 1 + q] = make_float4(p.x, p.y, p.z, __int_as_float(-1));
-}
-
-__device__ __forceinline__ float nn_d2(const float4 &a, const float4 &q) {
-    const float dx = a.x - q.x, dy = a.y - q.y, dz = a.z - q.z;
-    return dx * dx + dy * dy + dz * dz;
-}
-
-// One thread per destination point. Ties go to the lower source index:
-// nodes at exactly the best distance are still entered.
-__global__ void k_nn_query(const float4 *__restrict__ nlo, const float4 *__restrict__ nhi, int root, int n_leaf_base,
-                           const unsigned *__restrict__ keys, const int *__restrict__ vals, int n_src,
-                           const float4 *__restrict__ sp, const float4 *__restrict__ dp, i64 n_dst, int *col,
-                           int *err) {
+__global__ void k_nn_query(PtTreeView T, const float4 *__restrict__ dp, i64 n_dst, int *col, int *err) {
     const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (j >= n_dst) return;
-    const float4 q = dp[j];
-    float best = INFINITY;
-    int bi = -1;
-    auto take = [&](int s) {
-        const float d2 = nn_d2(sp[s], q);
-        if (d2 < best || (d2 == best && s < bi)) {
-            best = d2;
-            bi = s;
-        }
-    };
-    // seed: the source points on either side of the query in Morton order
-    const unsigned code = morton30(q.x, q.y, q.z);
-    int lo_i = 0, hi_i = n_src;
-    while (lo_i < hi_i) {
-        const int mid = (lo_i + hi_i) >> 1;
-        if (keys[mid] < code) lo_i = mid + 1;
-        else hi_i = mid;
-    }
-    for (int k = max(0, lo_i - 1); k <= min(n_src - 1, lo_i); ++k) take(vals[k]);
-    // ropes visit every node at most once; a longer walk means a malformed tree
-    const int max_steps = 2 * (2 * n_leaf_base + 1) + 8;
-    int steps = 0, node = root;
-    while (node >= 0) {
-        if (++steps > max_steps) {
-            atomicOr(err, 1);
-            break;
-        }
-        const float4 lo = nlo[node], hi = nhi[node];
-        const float dx = fmaxf(fmaxf(lo.x - q.x, 0.f), q.x - hi.x);
-        const float dy = fmaxf(fmaxf(lo.y - q.y, 0.f), q.y - hi.y);
-        const float dz = fmaxf(fmaxf(lo.z - q.z, 0.f), q.z - hi.z);
-        if (dx * dx + dy * dy + dz * dz <= best) {
-            if (node >= n_leaf_base) {
-                take(__float_as_int(lo.w));
-                node = __float_as_int(hi.w);
-            } else {
-                node = __float_as_int(lo.w);
-            }
-        } else {
-            node = __float_as_int(hi.w);
-        }
-    }
-    col[j] = bi;
+    if (j < n_dst) col[j] = pt_nearest(T, dp[j], err);
 }
 
 struct RectNN {
@@ -197,26 +127,11 @@ void generate_nearest(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matri
         if (n_dst) k_nn_points<<<nblk(n_dst, 128), 128, 0, s>>>(dst.view(), dp.p);
         AXGB_CUDA(cudaGetLastError());
         // LBVH over the source points (the construction of the candidate search)
-        const int n = static_cast<int>(n_src);
-        DBuf<float4> nlo(2 * n - 1), nhi(2 * n - 1);
-        DBuf<int> parent(2 * n - 1), right(n > 1 ? n - 1 : 1), flag(n > 1 ? n - 1 : 1), vals(n), err(1);
-        DBuf<unsigned> keys(n);
-        k_pt_keys<<<nblk(n, 256), 256, 0, s>>>(sp.p, n, keys.p, vals.p);
-        AXGB_CUDA(cudaGetLastError());
-        radix_sort_pairs_u32(keys.p, vals.p, n, 30, s);
-        Bvh t{n, 0, nlo.p, nhi.p, parent.p, right.p, flag.p, keys.p};  // root: internal node 0, or the single leaf
-        AXGB_CUDA(cudaMemsetAsync(parent.p, 0xff, sizeof(int) * (2 * n - 1), s));
-        flag.zero(s);
+        PtTree T;
+        build_pt_tree(T, sp.p, nullptr, static_cast<int>(n_src), PtMap{1.0, 0.0, 0.0, 0.0}, s);
+        DBuf<int> err(1);
         err.zero(s);
-        k_pt_leaves<<<nblk(n, 256), 256, 0, s>>>(t, sp.p, vals.p);
-        if (n > 1) {
-            k_internal<<<nblk(n - 1, 256), 256, 0, s>>>(t);
-            k_refit<<<nblk(n, 256), 256, 0, s>>>(t);
-        }
-        k_ropes<<<nblk(2 * n - 1, 256), 256, 0, s>>>(t);
-        if (n_dst)
-            k_nn_query<<<nblk(n_dst, 128), 128, 0, s>>>(nlo.p, nhi.p, 0, n - 1, keys.p, vals.p, n, sp.p, dp.p, n_dst,
-                                                        col_all.p, err.p);
+        if (n_dst) k_nn_query<<<nblk(n_dst, 128), 128, 0, s>>>(T.view(sp.p), dp.p, n_dst, col_all.p, err.p);
         AXGB_CUDA(cudaGetLastError());
         int h_err = 0;
         AXGB_CUDA(cudaMemcpyAsync(&h_err, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
