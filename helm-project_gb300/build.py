@@ -2,7 +2,7 @@
 
 CUDA translation units are compiled by nvcc with one -gencode
 (compute_103a -> sm_103a); the geometry units (prep.cu, weights.cu,
-coastal.cu, nearest.cu) with --fmad=false so double expressions, and the
+coastal.cu, nearest.cu, bilinear.cu) with --fmad=false so double expressions, and the
 float distances of the nearest searches, round as written. The host C++ units
 (api.cpp, esmf_io.cpp) are compiled by g++ with -ffp-contract=off and OpenMP
 (parallel sort in the grid detector). Units compile in parallel; the link uses nvcc.
@@ -32,6 +32,7 @@ UNITS = [
     ("scan_sort.cu", []),
     ("coastal.cu", ["--fmad=false"]),
     ("nearest.cu", ["--fmad=false"]),
+    ("bilinear.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["api.cpp", "esmf_io.cpp"]  # host C++ (g++)
 HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", "lbvh.cuh", os.path.join("..", "..", "include", "axgb.h")]

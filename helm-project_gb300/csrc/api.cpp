@@ -555,9 +555,10 @@ int axgb_generate_weights(int src, int dst, const axgb_regrid_config *cfg_in, in
             bool done = false;
             if (S->grid.regular && D->grid.regular) done = generate_bilinear_regular(*S, *D, cfg, *M);
             if (!done) {
-                if (!S->grid.rectilinear)
-                    throw Error(AXGB_ERR_UNSUPPORTED, "bilinear: source is not rectilinear (BVH bilinear not provided)");
-                generate_bilinear(*S, *D, cfg, *M);
+                if (S->grid.rectilinear)
+                    generate_bilinear(*S, *D, cfg, *M);
+                else
+                    generate_bilinear_general(*S, *D, cfg, *M);  // point location (weight_generator.cpp:2346-2667)
             }
         } else if (cfg.method == AXGB_NEAREST_NEIGHBOR) {
             generate_nearest(*S, *D, cfg, *M);  // generate_nearest (weight_generator.cpp:2097-2118)

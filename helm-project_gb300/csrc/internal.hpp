@@ -257,6 +257,9 @@ EsmfWeights esmf_read(const std::string &path);
 // nearest.cu: nearest-neighbour weights (index rounding for two regular
 // grids, else an exact float nearest query over centroid points)
 void generate_nearest(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
+// bilinear.cu: bilinear weights from a non-rectilinear source (nearest
+// centroids, quad / triangle / inverse-distance stencils)
+void generate_bilinear_general(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 // regular x regular bilinear fast path; false = no destination cells (fall through)
 bool generate_bilinear_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);
 void generate_bilinear(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out);

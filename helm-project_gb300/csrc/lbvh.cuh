@@ -221,6 +221,67 @@ __device__ int pt_nearest(const PtTreeView &T, const float4 &q, int *err) {
     return bi;
 }
 
+// The K nearest points to q in ascending (distance, index) order; returns
+// how many were found (min(K, n)). Nodes at the K-th distance are entered,
+// so ties resolve to the lower indices.
+template <int K>
+__device__ int pt_knearest(const PtTreeView &T, const float4 &q, int *out, float *outd, int *err) {
+    int cnt = 0;
+    float bd[K];
+    int bi[K];
+    auto take = [&](int s) {
+        const float d2 = pt_d2(T.pts[s], q);
+        if (cnt == K && !(d2 < bd[K - 1] || (d2 == bd[K - 1] && s < bi[K - 1]))) return;
+        for (int k = 0; k < cnt; ++k)
+            if (bi[k] == s) return;  // seeded already
+        int at = cnt < K ? cnt++ : K - 1;
+        while (at > 0 && (d2 < bd[at - 1] || (d2 == bd[at - 1] && s < bi[at - 1]))) {
+            bd[at] = bd[at - 1];
+            bi[at] = bi[at - 1];
+            --at;
+        }
+        bd[at] = d2;
+        bi[at] = s;
+    };
+    if (T.n <= 0) return 0;
+    const unsigned code = pt_code(q, T.m);
+    int lo_i = 0, hi_i = T.n;
+    while (lo_i < hi_i) {
+        const int mid = (lo_i + hi_i) >> 1;
+        if (T.keys[mid] < code) lo_i = mid + 1;
+        else hi_i = mid;
+    }
+    for (int k = max(0, lo_i - K / 2); k < min(T.n, lo_i + K / 2); ++k) take(T.vals[k]);
+    const int n_leaf_base = T.n - 1;
+    const int max_steps = 2 * (2 * n_leaf_base + 1) + 8;
+    int steps = 0, node = 0;
+    while (node >= 0) {
+        if (++steps > max_steps) {
+            atomicOr(err, 1);
+            break;
+        }
+        const float4 lo = T.lo[node], hi = T.hi[node];
+        const float dx = fmaxf(fmaxf(lo.x - q.x, 0.f), q.x - hi.x);
+        const float dy = fmaxf(fmaxf(lo.y - q.y, 0.f), q.y - hi.y);
+        const float dz = fmaxf(fmaxf(lo.z - q.z, 0.f), q.z - hi.z);
+        if (cnt < K || dx * dx + dy * dy + dz * dz <= bd[K - 1]) {
+            if (node >= n_leaf_base) {
+                take(__float_as_int(lo.w));
+                node = __float_as_int(hi.w);
+            } else {
+                node = __float_as_int(lo.w);
+            }
+        } else {
+            node = __float_as_int(hi.w);
+        }
+    }
+    for (int k = 0; k < cnt; ++k) {
+        out[k] = bi[k];
+        outd[k] = bd[k];
+    }
+    return cnt;
+}
+
 // Owner of a point tree's device arrays.
 struct PtTree {
     DBuf<float4> lo, hi;

@@ -852,6 +852,206 @@ static bool bilinear_regular(const Mesh &S, const Mesh &D, const GridInfo &sg, i
     return true;
 }
 
+// Bilinear from a non-rectilinear source: the general path of
+// generate_bilinear (src/solver/weight_generator.cpp:2346-2667). Candidates:
+// the min(8, n_src) source centroids (compute_cell_centroids_xy, as float
+// lon/lat) nearest the destination centroid by float squared distance,
+// ascending (distance, index) (ArborX's nearest(point, k) is not in the
+// checkout). Phase A: first 4-combination passing map_to_reference_quad
+// (:596-666) on the gnomonic projections (:584-590); Phase B: first
+// triangle passing barycentric_triangle (:670-684); Phase C: inverse chord
+// distances to the first four. Brute force over all sources.
+namespace bil {
+struct V2 {
+    double x, y;
+};
+V2 gnomonic(double lon0, double lat0, double lon, double lat) {
+    double cos_c = std::sin(lat0) * std::sin(lat) + std::cos(lat0) * std::cos(lat) * std::cos(lon - lon0);
+    if (cos_c <= 0.0) cos_c = 1e-15;
+    return {(std::cos(lat) * std::sin(lon - lon0)) / cos_c,
+            (std::sin(lat) * std::cos(lat0) - std::cos(lat) * std::sin(lat0) * std::cos(lon - lon0)) / cos_c};
+}
+bool ref_quad(double px, double py, const V2 &v0, const V2 &v1, const V2 &v2, const V2 &v3, double &xo, double &eo) {
+    double xi = 0.0, eta = 0.0;
+    const double tol = 1e-12;
+    for (int iter = 0; iter < 20; ++iter) {
+        double N0 = 0.25 * (1.0 - xi) * (1.0 - eta);
+        double N1 = 0.25 * (1.0 + xi) * (1.0 - eta);
+        double N2 = 0.25 * (1.0 + xi) * (1.0 + eta);
+        double N3 = 0.25 * (1.0 - xi) * (1.0 + eta);
+        double x_cur = N0 * v0.x + N1 * v1.x + N2 * v2.x + N3 * v3.x;
+        double y_cur = N0 * v0.y + N1 * v1.y + N2 * v2.y + N3 * v3.y;
+        double rx = px - x_cur, ry = py - y_cur;
+        if (std::abs(rx) < tol && std::abs(ry) < tol) {
+            xo = xi;
+            eo = eta;
+            return true;
+        }
+        double a0 = -0.25 * (1.0 - eta), a1 = 0.25 * (1.0 - eta), a2 = 0.25 * (1.0 + eta), a3 = -0.25 * (1.0 + eta);
+        double b0 = -0.25 * (1.0 - xi), b1 = -0.25 * (1.0 + xi), b2 = 0.25 * (1.0 + xi), b3 = 0.25 * (1.0 - xi);
+        double dx_dxi = a0 * v0.x + a1 * v1.x + a2 * v2.x + a3 * v3.x;
+        double dy_dxi = a0 * v0.y + a1 * v1.y + a2 * v2.y + a3 * v3.y;
+        double dx_deta = b0 * v0.x + b1 * v1.x + b2 * v2.x + b3 * v3.x;
+        double dy_deta = b0 * v0.y + b1 * v1.y + b2 * v2.y + b3 * v3.y;
+        double det = dx_dxi * dy_deta - dx_deta * dy_dxi;
+        if (std::abs(det) < 1e-30) return false;
+        double inv_det = 1.0 / det;
+        double dxi = inv_det * (dy_deta * rx - dx_deta * ry);
+        double deta = inv_det * (-dy_dxi * rx + dx_dxi * ry);
+        xi += dxi;
+        eta += deta;
+        xi = std::max(-2.0, std::min(2.0, xi));
+        eta = std::max(-2.0, std::min(2.0, eta));
+    }
+    xo = xi;
+    eo = eta;
+    return (std::abs(xi) <= 1.0 + 1e-6 && std::abs(eta) <= 1.0 + 1e-6);
+}
+bool bary(double px, double py, const V2 &v0, const V2 &v1, const V2 &v2, double &l0, double &l1, double &l2) {
+    double denom = (v1.y - v2.y) * (v0.x - v2.x) + (v2.x - v1.x) * (v0.y - v2.y);
+    if (std::abs(denom) < 1e-30) {
+        l0 = l1 = l2 = 1.0 / 3.0;
+        return false;
+    }
+    double inv = 1.0 / denom;
+    l0 = ((v1.y - v2.y) * (px - v2.x) + (v2.x - v1.x) * (py - v2.y)) * inv;
+    l1 = ((v2.y - v0.y) * (px - v2.x) + (v0.x - v2.x) * (py - v2.y)) * inv;
+    l2 = 1.0 - l0 - l1;
+    const double eps = -1e-10;
+    return (l0 >= eps && l1 >= eps && l2 >= eps);
+}
+void centroids(const Mesh &m, std::vector<double> &cx, std::vector<double> &cy) {
+    cx.resize(m.n_cells);
+    cy.resize(m.n_cells);
+    for (i64 c = 0; c < m.n_cells; ++c) {
+        double sx = 0, sy = 0, sz = 0;
+        const i64 b = m.off[c], e = m.off[c + 1];
+        for (i64 q = b; q < e; ++q) {
+            const double lo = m.lon(m.idx[q]) * kPi / 180.0, la = m.lat(m.idx[q]) * kPi / 180.0;
+            sx += std::cos(la) * std::cos(lo);
+            sy += std::cos(la) * std::sin(lo);
+            sz += std::sin(la);
+        }
+        const double inv = (e - b > 0) ? 1.0 / static_cast<double>(e - b) : 0.0;
+        double lat = std::asin(sz * inv), lon = std::atan2(sy * inv, sx * inv);
+        if (lon < 0.0) lon += 2.0 * kPi;
+        cx[c] = lon * 180.0 / kPi;
+        cy[c] = lat * 180.0 / kPi;
+    }
+}
+}  // namespace bil
+
+static void bilinear_general(const Mesh &S, const Mesh &D, orc_result *res) {
+    using bil::V2;
+    const i64 n_src = S.n_cells, n_dst = D.n_cells;
+    std::vector<double> scx, scy, dcx, dcy;
+    bil::centroids(S, scx, scy);
+    bil::centroids(D, dcx, dcy);
+    std::vector<float> sfx(n_src), sfy(n_src);
+    for (i64 i = 0; i < n_src; ++i) {
+        sfx[i] = static_cast<float>(scx[i]);
+        sfy[i] = static_cast<float>(scy[i]);
+    }
+    const int k_query = static_cast<int>(std::min<i64>(8, n_src));
+    std::vector<std::vector<std::pair<i64, double>>> rows(n_dst);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (i64 j = 0; j < n_dst; ++j) {
+        const float qx = static_cast<float>(dcx[j]), qy = static_cast<float>(dcy[j]), qz = 0.0f;
+        std::vector<std::pair<float, i64>> all(n_src);
+        for (i64 i = 0; i < n_src; ++i) {
+            const float dx = sfx[i] - qx, dy = sfy[i] - qy, dz = 0.0f - qz;
+            all[i] = {dx * dx + dy * dy + dz * dz, i};
+        }
+        std::partial_sort(all.begin(), all.begin() + k_query, all.end());
+        std::vector<i64> cand(k_query);
+        for (int k = 0; k < k_query; ++k) cand[k] = all[k].second;
+        const int n_avail = k_query;
+        auto &out = rows[j];
+        if (n_avail == 0) continue;
+        const double lon0 = dcx[j] * kPi / 180.0, lat0 = dcy[j] * kPi / 180.0;
+        std::vector<V2> q(n_avail);
+        for (int a = 0; a < n_avail; ++a)
+            q[a] = bil::gnomonic(lon0, lat0, scx[cand[a]] * kPi / 180.0, scy[cand[a]] * kPi / 180.0);
+        bool done = false;
+        for (int a = 0; a < n_avail - 3 && !done; ++a)
+            for (int b = a + 1; b < n_avail - 2 && !done; ++b)
+                for (int c = b + 1; c < n_avail - 1 && !done; ++c)
+                    for (int d = c + 1; d < n_avail && !done; ++d) {
+                        double xi = 0.0, eta = 0.0;
+                        if (bil::ref_quad(0.0, 0.0, q[a], q[b], q[c], q[d], xi, eta)) {
+                            xi = std::max(-1.0, std::min(1.0, xi));
+                            eta = std::max(-1.0, std::min(1.0, eta));
+                            out = {{cand[a], 0.25 * (1.0 - xi) * (1.0 - eta)},
+                                   {cand[b], 0.25 * (1.0 + xi) * (1.0 - eta)},
+                                   {cand[c], 0.25 * (1.0 + xi) * (1.0 + eta)},
+                                   {cand[d], 0.25 * (1.0 - xi) * (1.0 + eta)}};
+                            done = true;
+                        }
+                    }
+        for (int a = 0; a < n_avail - 2 && !done; ++a)
+            for (int b = a + 1; b < n_avail - 1 && !done; ++b)
+                for (int c = b + 1; c < n_avail && !done; ++c) {
+                    double l0 = 0.0, l1 = 0.0, l2 = 0.0;
+                    if (bil::bary(0.0, 0.0, q[a], q[b], q[c], l0, l1, l2)) {
+                        l0 = std::max(0.0, l0);
+                        l1 = std::max(0.0, l1);
+                        l2 = std::max(0.0, l2);
+                        const double sum = l0 + l1 + l2;
+                        if (sum > 0.0) {
+                            l0 /= sum;
+                            l1 /= sum;
+                            l2 /= sum;
+                        } else {
+                            l0 = l1 = l2 = 1.0 / 3.0;
+                        }
+                        out = {{cand[a], l0}, {cand[b], l1}, {cand[c], l2}};
+                        done = true;
+                    }
+                }
+        if (!done) {
+            const int n_idw = std::min(4, n_avail);
+            std::vector<double> dist(n_idw);
+            double sum_inv = 0.0;
+            int zero = -1;
+            for (int k = 0; k < n_idw; ++k) {
+                const double lon_s = scx[cand[k]] * kPi / 180.0, lat_s = scy[cand[k]] * kPi / 180.0;
+                const double lon_d = dcx[j] * kPi / 180.0, lat_d = dcy[j] * kPi / 180.0;
+                const double sx = std::cos(lat_s) * std::cos(lon_s), sy = std::cos(lat_s) * std::sin(lon_s),
+                             sz = std::sin(lat_s);
+                const double dx = std::cos(lat_d) * std::cos(lon_d) - sx, dy = std::cos(lat_d) * std::sin(lon_d) - sy,
+                             dz = std::sin(lat_d) - sz;
+                const double dd = std::sqrt(dx * dx + dy * dy + dz * dz);
+                if (dd <= 0.0) {
+                    zero = k;
+                    break;
+                }
+                dist[k] = dd;
+                sum_inv += 1.0 / dd;
+            }
+            if (zero >= 0) {
+                out = {{cand[zero], 1.0}};
+            } else {
+                for (int k = 0; k < n_idw; ++k) out.push_back({cand[k], (1.0 / dist[k]) / sum_inv});
+            }
+        }
+        std::stable_sort(out.begin(), out.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+    }
+    res->n_src = n_src;
+    res->n_dst = n_dst;
+    for (i64 j = 0; j < n_dst; ++j)
+        for (auto &e : rows[j]) {
+            res->row.push_back(j);
+            res->col.push_back(e.first);
+            res->w.push_back(e.second);
+        }
+    auto dxyz = node_xyz(D);
+    res->frac_a.assign(n_src, 1.0);
+    res->frac_b.assign(n_dst, 1.0);
+    res->area_a.assign(n_src, 0.0);
+    res->area_b.resize(n_dst);
+    for (i64 c = 0; c < n_dst; ++c) res->area_b[c] = D.areas ? D.areas[c] : poly_area(cell_poly(D, dxyz, c));
+}
+
 // Nearest-neighbour weights: WeightGenerator::generate_nearest
 // (src/solver/weight_generator.cpp:2097-2118). Two regular grids take
 // generate_nearest_rect (:2025-2080): the destination cell's lower-left
@@ -1206,8 +1406,8 @@ int orc_conservative(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i6
 // the dispatch of generate_bilinear (src/solver/weight_generator.cpp:2306-2345),
 // which sends regular x regular pairs to bilinear_regular first.
 // unmapped: 0 Error, 1 Ignore (only the regular path leaves rows unmapped).
-// Returns -3 when the source is not rectilinear, -7 for an unmapped
-// destination under Error.
+// A source that is not rectilinear takes bilinear_general. Returns -7 for an
+// unmapped destination under Error.
 int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *soff, const i64 *sidx, i64 dn_nodes,
                  const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, int unmapped,
                  orc_result **out) {
@@ -1223,7 +1423,13 @@ int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *s
         *out = res;
         return 0;
     }
-    if (!sg.rectilinear) return -3;
+    if (!sg.rectilinear) {
+        if (dn_cells > 0 && sn_cells == 0 && unmapped == 0) return -7;
+        auto *res = new orc_result;
+        bilinear_general(S, D, res);
+        *out = res;
+        return 0;
+    }
     i64 ni = sg.ni, nj = sg.nj;
     std::vector<double> cl(ni), ct(nj);
     for (i64 i = 0; i < ni; ++i) cl[i] = 0.5 * (sg.ulon[i] + sg.ulon[i + 1]);

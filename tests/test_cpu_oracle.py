@@ -322,3 +322,17 @@ def test_nearest_unstructured_is_nearest(oracle):
     chosen = dist[np.arange(dst.n_cells), w.col]
     assert np.all(chosen <= dist.min(axis=1) + 1e-6)
     assert np.all(w.frac_a == 1.0) and np.all(w.area_a > 0)
+
+
+def test_bilinear_general_oracle(oracle):
+    """Bilinear from a cubed sphere (the point-location path): 3 or 4
+    non-negative weights per row (quad, triangle or inverse distance) summing
+    to 1, each row's sources among its eight nearest centroids."""
+    src, dst = grids.cubed_sphere(12), grids.latlon_deg(10.0)
+    w = oracle.bilinear(src, dst)
+    counts = np.bincount(w.row, minlength=w.n_dst)
+    assert np.all((counts >= 1) & (counts <= 4))
+    assert np.all(w.w >= 0.0)
+    rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
+    assert np.abs(rs - 1.0).max() < 1e-12
+    assert np.all(w.area_a == 0.0) and np.all(w.area_b > 0.0)

@@ -104,9 +104,8 @@ def test_bilinear_parity(gpu, oracle):
 def test_unsupported_and_unmapped(gpu, oracle):
     a = gpu.make_regular_mesh(36, 18, 0.0, -90.0, 10.0, 10.0)
     b = gpu.make_regular_mesh(18, 9, 0.0, -90.0, 20.0, 20.0)
-    cs = gpu.Mesh.from_grid(grids.cubed_sphere(4))
-    with pytest.raises(gpu.Unsupported):  # bilinear from a non-rectilinear source (BVH bilinear) not provided
-        gpu.generate_weights(cs, b, {"method": "bilinear"})
+    with pytest.raises(gpu.Unsupported):
+        gpu.generate_weights(a, b, {"method": "bicubic"})
     with pytest.raises(gpu.Unsupported):
         gpu.generate_weights(a, b, {"method": "patch"})
     # a regional source leaves most of a global destination unmapped
@@ -722,3 +721,25 @@ def test_performance_budgets(gpu, method, budget):
     assert gen < budget, gen
     assert app < 0.080, app
     assert y.shape == (dst.n_cells,) and np.all(np.isfinite(y))
+
+
+BILINEAR_GENERAL_PAIRS = [
+    ("C24->5deg", lambda: (grids.cubed_sphere(24), grids.latlon_deg(5.0))),
+    ("C48->1deg", lambda: (grids.cubed_sphere(48), grids.latlon_deg(1.0))),
+    ("C12->C8", lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8))),
+    ("voronoi40962->2deg", lambda: (grids.voronoi(40962, seed=5), grids.latlon_deg(2.0))),
+    ("tripole360x270->1deg", lambda: (grids.tripole(360, 270, seed=4), grids.latlon_deg(1.0))),
+]
+
+
+@pytest.mark.parametrize("name,make", BILINEAR_GENERAL_PAIRS)
+def test_bilinear_general_parity(gpu, oracle, name, make):
+    """Bilinear from a non-rectilinear source (nearest centroids, then the
+    reference's quad / triangle / inverse-distance stencils) against the
+    oracle: every (dst, src) pair and every weight identical."""
+    src, dst = make()
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "bilinear"})
+    wo = oracle.bilinear(src, dst)
+    csr = _check_weights(M, wo)
+    # host-libm inputs and IEEE double stencils on the device: bit for bit
+    assert np.array_equal(csr["val"], wo.w)
