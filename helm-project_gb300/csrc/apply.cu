@@ -142,11 +142,10 @@ __global__ void __launch_bounds__(256) k_split(SellArgs a, const float *__restri
         }
         i64 f = f0;
         if constexpr (U >= 2) {
-            F2 hp[L], hn[L], lp[L];
+            F2 hp[L], lp[L];
 #pragma unroll
             for (int k = 0; k < L; ++k) {
                 hp[k] = pk(h[k], h[k]);
-                hn[k] = pk(-h[k], -h[k]);
                 lp[k] = pk(lw[k], lw[k]);
             }
             for (; f + U <= f1; f += U) {
@@ -164,7 +163,7 @@ __global__ void __launch_bounds__(256) k_split(SellArgs a, const float *__restri
                         for (int u = 0; u < U / 2; ++u) {
                             float xa = ldg_f(xf + (2 * u) * ldx + c[k]);
                             float xb = ldg_f(xf + (2 * u + 1) * ldx + c[k]);
-                            csum2(s[u], cc[u], hp[k], hn[k], lp[k], pk(xa, xb));
+                            csum2(s[u], cc[u], h[k], hp[k], lp[k], xa, xb);
                         }
                     }
                 }

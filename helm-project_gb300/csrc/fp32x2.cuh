@@ -35,70 +35,49 @@ __device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
 }
 
 // One compensated step for one field: s + c accumulates (hi + lo) * x.
+// TwoSum of s and p = fl(h*x) gives t and the error (s - a) + (p - b), with
+// b = t - s and a = t - b. The second part is formed together with the
+// product error as fma(h, x, -b) = fl(h*x - b): one rounding at the scale
+// of the error term instead of a separate exact product error. Here
+// bn = s - t is -b exactly (rounding is sign-symmetric), so a = t + bn. The
+// low weight enters as c = fma(lo, x, c), then c += e. Nine operations.
 __device__ __forceinline__ void csum1(float &s, float &c, float h, float l, float x) {
-    float p = __fmul_rn(h, x);
-    float pe = __fmaf_rn(h, x, -p);
-    float q = __fmaf_rn(l, x, pe);
-    float t = __fadd_rn(s, p);
-    float bp = __fsub_rn(t, s);
-    float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-    s = t;
-    c = __fadd_rn(c, __fadd_rn(e, q));
-}
-
-// Same for two fields at once; hn = -hi (so mul gives -p exactly).
-__device__ __forceinline__ void csum2(F2 &s, F2 &c, F2 h, F2 hn, F2 l, F2 x) {
-    F2 pn = mul2(hn, x);
-    F2 pe = fma2(h, x, pn);
-    F2 q = fma2(l, x, pe);
-    F2 t = sub2(s, pn);
-    F2 bp = sub2(t, s);
-    F2 a2 = sub2(s, sub2(t, bp));
-    F2 a3 = add2(pn, bp);
-    F2 e = sub2(a2, a3);
-    s = t;
-    c = add2(c, add2(e, q));
-}
-
-// Same arithmetic as csum2 (bitwise identical results) but without a
-// negated-weight register pair: the product error is formed with -x and
-// the compensation is carried negated (cn = -c); the row value is s - cn.
-__device__ __forceinline__ void cstep2(F2 &s, F2 &cn, F2 h, F2 l, F2 x, F2 mone) {
-    F2 nx = mul2(x, mone);
-    F2 p = mul2(h, x);
-    F2 pen = fma2(h, nx, p);  // p - h*x = -(product error), exact
-    F2 t = add2(s, p);
-    F2 bp = sub2(t, s);
-    F2 a2 = sub2(s, sub2(t, bp));
-    F2 a3 = sub2(p, bp);
-    F2 e = add2(a2, a3);      // TwoSum error
-    F2 u1 = fma2(l, nx, pen); // -(lo*x + product error)
-    cn = add2(cn, sub2(u1, e));
+    const float p = __fmul_rn(h, x);
+    const float t = __fadd_rn(s, p);
+    const float bn = __fsub_rn(s, t);
+    const float a = __fadd_rn(t, bn);
+    const float e = __fadd_rn(__fsub_rn(s, a), __fmaf_rn(h, x, bn));
+    c = __fadd_rn(__fmaf_rn(l, x, c), e);
     s = t;
 }
 
-
-// Bitwise negation of both halves on the integer pipe (keeps the FMA pipe
-// for the arithmetic).
-__device__ __forceinline__ F2 neg2(F2 a) {
-    F2 r;
-    r.v = a.v ^ 0x8000000080000000ull;
-    return r;
+// The same step for two fields at once (each half bitwise csum1). The two
+// products are formed by scalar multiplies with explicit rounding: a packed
+// multiply whose only use is the next packed add gets fused with it into
+// one packed fma by the code generator (t = fl(s + h*x) instead of
+// fl(s + fl(h*x))), which breaks the error-free sum.
+__device__ __forceinline__ void csum2(F2 &s, F2 &c, float h, F2 hp, F2 lp, float xa, float xb) {
+    const F2 x = pk(xa, xb);
+    const F2 p = pk(__fmul_rn(h, xa), __fmul_rn(h, xb));
+    const F2 t = add2(s, p);
+    const F2 bn = sub2(s, t);
+    const F2 a = add2(t, bn);
+    const F2 e = add2(sub2(s, a), fma2(hp, x, bn));
+    c = add2(fma2(lp, x, c), e);
+    s = t;
 }
 
-// cstep2 with the negation on the integer pipe: 11 FMA-pipe operations per
-// entry for two fields; results bitwise identical to csum1 on each field.
-__device__ __forceinline__ void cstep2i(F2 &s, F2 &cn, F2 h, F2 l, F2 x) {
-    F2 nx = neg2(x);
-    F2 p = mul2(h, x);
-    F2 pen = fma2(h, nx, p);
-    F2 t = add2(s, p);
-    F2 bp = sub2(t, s);
-    F2 a2 = sub2(s, sub2(t, bp));
-    F2 a3 = sub2(p, bp);
-    F2 e = add2(a2, a3);
-    F2 u1 = fma2(l, nx, pen);
-    cn = add2(cn, sub2(u1, e));
+// The same step with the compensation carried negated (cn = -c, ln = -lo):
+// fma(-lo, x, -c) = -fma(lo, x, c) and -c - e = -(c + e) exactly, so the row
+// value s - cn is bitwise that of csum1.
+__device__ __forceinline__ void cstepn(F2 &s, F2 &cn, float h, F2 hp, F2 ln, float xa, float xb) {
+    const F2 x = pk(xa, xb);
+    const F2 p = pk(__fmul_rn(h, xa), __fmul_rn(h, xb));  // not fusable (see csum2)
+    const F2 t = add2(s, p);
+    const F2 bn = sub2(s, t);
+    const F2 a = add2(t, bn);
+    const F2 e = add2(sub2(s, a), fma2(hp, x, bn));
+    cn = sub2(fma2(ln, x, cn), e);
     s = t;
 }
 

@@ -137,8 +137,8 @@ __device__ __forceinline__ int item_setup(const BlkArgs &a, const float *__restr
 }
 
 // Row reduction of one staged tile of T fields (field stride US floats in
-// shared memory). Per entry the packed weights (h, -h, -lo) are formed once
-// for the T/2 field pairs; per pair the compensated step is 11 FMA-pipe ops.
+// shared memory). Per entry the packed weights (h, -lo) are formed once for
+// the T/2 field pairs; per pair the compensated step is 9 FMA-pipe ops.
 template <int L, int T, int US>
 __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, const float *h, const float *lw, int wl,
                                               i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy) {
@@ -154,20 +154,11 @@ __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, c
             if (k0 < wl) {  // warp-uniform
 #pragma unroll
                 for (int k = k0; k < k0 + kGroup && k < L; ++k) {
-                    const F2 hp = pk(h[k], h[k]), hn = pk(-h[k], -h[k]), ln = pk(-lw[k], -lw[k]);
+                    const F2 hp = pk(h[k], h[k]), ln = pk(-lw[k], -lw[k]);
                     const float *p0 = cur + li[k];
 #pragma unroll
-                    for (int q = 0; q < T / 2; ++q) {
-                        const F2 xv = pk(p0[(2 * q) * US], p0[(2 * q + 1) * US]);
-                        const F2 p = mul2(hp, xv);
-                        const F2 pen = fma2(hn, xv, p);  // p - h*x, exact
-                        const F2 t = add2(sa[q], p);
-                        const F2 bp = sub2(t, sa[q]);
-                        const F2 e = add2(sub2(sa[q], sub2(t, bp)), sub2(p, bp));
-                        const F2 u1 = fma2(ln, xv, pen);  // -(lo*x + product error)
-                        cn[q] = add2(cn[q], sub2(u1, e));
-                        sa[q] = t;
-                    }
+                    for (int q = 0; q < T / 2; ++q)
+                        cstepn(sa[q], cn[q], h[k], hp, ln, p0[(2 * q) * US], p0[(2 * q + 1) * US]);
                 }
             }
         }
@@ -207,10 +198,10 @@ __device__ __forceinline__ void reduce_tile(const float *cur, int us, const int 
 #pragma unroll
         for (int k = 0; k < L; ++k) {
             if (k < wl) {
-                const F2 h2 = pk(h[k], h[k]), l2 = pk(lw[k], lw[k]);
+                const F2 h2 = pk(h[k], h[k]), l2 = pk(-lw[k], -lw[k]);
                 const float *p0 = cur + li[k];
 #pragma unroll
-                for (int q = 0; q < T / 2; ++q) cstep2i(sa[q], cn[q], h2, l2, pk(p0[(2 * q) * us], p0[(2 * q + 1) * us]));
+                for (int q = 0; q < T / 2; ++q) cstepn(sa[q], cn[q], h[k], h2, l2, p0[(2 * q) * us], p0[(2 * q + 1) * us]);
             }
         }
         if (row >= 0) {
