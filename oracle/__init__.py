@@ -167,13 +167,20 @@ class Oracle:
         return nnz, st
 
     def conservative(self, src, dst, norm_type: int = 0, unmapped: int = 1, faithful: bool = False,
-                     src_mask=None, dst_mask=None) -> Weights:
+                     src_mask=None, dst_mask=None, src_areas=None, dst_areas=None) -> Weights:
+        """Conservative weights; masks (int32, 0 = masked) and cell areas
+        (float64, replacing the computed ones) as the meshes may carry them."""
         h = C.c_void_p()
         t0 = time.perf_counter()
-        sm = None if src_mask is None else np.ascontiguousarray(src_mask, np.int32)
-        dm = None if dst_mask is None else np.ascontiguousarray(dst_mask, np.int32)
-        rc = self.L.orc_conservative(*_mesh_args(src), None, None if sm is None else sm.ctypes.data_as(C.c_void_p),
-                                     *_mesh_args(dst), None, None if dm is None else dm.ctypes.data_as(C.c_void_p),
+
+        def opt(a, dt):
+            return None if a is None else np.ascontiguousarray(a, dt)
+        sm, dm = opt(src_mask, np.int32), opt(dst_mask, np.int32)
+        sa, da = opt(src_areas, np.float64), opt(dst_areas, np.float64)
+
+        def ptr(a):
+            return None if a is None else a.ctypes.data_as(C.c_void_p)
+        rc = self.L.orc_conservative(*_mesh_args(src), ptr(sa), ptr(sm), *_mesh_args(dst), ptr(da), ptr(dm),
                                      norm_type, unmapped, int(faithful), C.byref(h))
         dt = time.perf_counter() - t0
         if rc != 0:

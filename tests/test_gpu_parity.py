@@ -743,3 +743,48 @@ def test_bilinear_general_parity(gpu, oracle, name, make):
     csr = _check_weights(M, wo)
     # host-libm inputs and IEEE double stencils on the device: bit for bit
     assert np.array_equal(csr["val"], wo.w)
+
+
+def _with(g, gpu, mask=None, areas=None):
+    return gpu.Mesh.from_arrays(g.node_lonlat, g.conn_offsets, g.conn_indices, areas=areas, mask=mask)
+
+
+MASK_PAIRS = [
+    ("clipper C24->2deg", lambda: (grids.cubed_sphere(24), grids.latlon_deg(2.0))),
+    ("regular 1deg->2deg", lambda: (grids.latlon_deg(1.0), grids.latlon_deg(2.0))),
+    ("rectilinear", lambda: (grids.equal_area_latlon(72, 36, stretch=0.4), grids.latlon_deg(3.0))),
+]
+
+
+@pytest.mark.parametrize("name,make", MASK_PAIRS)
+def test_destination_mask_and_user_areas(gpu, oracle, name, make):
+    """Masked destination cells get no entries (every generation path), and
+    cell areas given with the mesh replace the computed ones in weights,
+    fractions and the reported areas; against the oracle on the same
+    inputs."""
+    src, dst = make()
+    rng = np.random.default_rng(21)
+    dmask = (rng.random(dst.n_cells) > 0.2).astype(np.int32)
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), _with(dst, gpu, mask=dmask), {"method": "conservative"})
+    wo = oracle.conservative(src, dst, dst_mask=dmask)
+    _check_weights(M, wo)
+    assert not np.isin(np.nonzero(dmask == 0)[0], wo.row).any()
+    # user areas: the cells' own areas scaled by a seeded factor near 1
+    sa = M.to_csr()["area_a"] * (1.0 + 0.01 * rng.random(src.n_cells))
+    da = M.to_csr()["area_b"] * (1.0 + 0.01 * rng.random(dst.n_cells))
+    da[da == 0.0] = 1.0
+    Ma = gpu.generate_weights(_with(src, gpu, areas=sa), _with(dst, gpu, areas=da), {"method": "conservative"})
+    _check_weights(Ma, oracle.conservative(src, dst, src_areas=sa, dst_areas=da))
+
+
+@pytest.mark.parametrize("name,make", MASK_PAIRS)
+def test_both_masks_with_coastal(gpu, oracle, name, make):
+    """Source and destination masks together: the generator drops both, then
+    the coastal post-pass renormalises and extrapolates the unmasked rows."""
+    src, dst = make()
+    smask = _land_mask(src)
+    rng = np.random.default_rng(22)
+    dmask = (rng.random(dst.n_cells) > 0.1).astype(np.int32)
+    M = gpu.generate_weights(_with(src, gpu, mask=smask), _with(dst, gpu, mask=dmask), {"method": "conservative"})
+    wo = oracle.conservative(src, dst, src_mask=smask, dst_mask=dmask)
+    _check_weights(M, oracle.coastal(wo, src, dst, smask))
