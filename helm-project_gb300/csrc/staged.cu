@@ -32,8 +32,14 @@
 namespace axgb {
 namespace {
 
-constexpr int kRows = 128;       // rows per block (4 warps)
-constexpr int kMaxUS = 3072;     // staging floats per field a block may use
+constexpr int kWarps = 4;        // warps (32-row slices) per block
+constexpr int kRows = 32 * kWarps;  // rows per block
+// Staging strides (floats per field) compiled into the staged kernels: a
+// block takes the smaller one that holds its chunks; blocks needing more than
+// the larger one go to the direct kernels.
+constexpr int kUsSmall = 256 * kWarps;
+constexpr int kUsLarge = 768 * kWarps;
+constexpr int kMaxUS = kUsLarge;  // staging floats per field a block may use
 constexpr int kMaxL = 32;        // longest row handled by the blocked kernels
 constexpr int kPool = 4;         // streams the class launches are spread over
 // Entries are skipped past the warp's longest row in groups of kGroup: the
@@ -41,7 +47,7 @@ constexpr int kPool = 4;         // streams the class launches are spread over
 // steps of neighbouring entries; entries past a row's end are zero (weight
 // 0 on the zero slot) and leave the sums unchanged.
 constexpr int kGroup = 4;
-const int kUsBuckets[] = {1024, 3072};  // staging strides compiled into the chunk kernel
+const int kUsBuckets[] = {kUsSmall, kUsLarge};
 
 inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
 
@@ -231,8 +237,8 @@ __device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, 
                                              i64 &row) {
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     row = a.brow[static_cast<i64>(b) * kRows + tid];
-    wl = a.wlen[b * 4 + w];
-    const int base = a.wbase[b * 4 + w];
+    wl = a.wlen[b * kWarps + w];
+    const int base = a.wbase[b * kWarps + w];
 #pragma unroll
     for (int k = 0; k < L; ++k) {
         if (k < wl) {
@@ -444,12 +450,13 @@ inline unsigned spread10h(unsigned v) {
 
 // Groups of up to 4 slices: Morton visit order, each group completed with
 // the nearest unused slices among the next kWindow candidates.
-std::vector<std::array<int, 4>> group_slices(i64 nsl, const std::vector<float> &xyz) {
-    std::vector<std::array<int, 4>> groups;
+std::vector<std::array<int, kWarps>> group_slices(i64 nsl, const std::vector<float> &xyz) {
+    std::vector<std::array<int, kWarps>> groups;
     if (xyz.size() != static_cast<size_t>(3 * nsl)) {
-        for (i64 q = 0; q < nsl; q += 4) {
-            std::array<int, 4> g{-1, -1, -1, -1};
-            for (int w = 0; w < 4 && q + w < nsl; ++w) g[w] = static_cast<int>(q + w);
+        for (i64 q = 0; q < nsl; q += kWarps) {
+            std::array<int, kWarps> g;
+            g.fill(-1);
+            for (int w = 0; w < kWarps && q + w < nsl; ++w) g[w] = static_cast<int>(q + w);
             groups.push_back(g);
         }
         return groups;
@@ -469,17 +476,19 @@ std::vector<std::array<int, 4>> group_slices(i64 nsl, const std::vector<float> &
         int s = order[q];
         if (used[s]) continue;
         used[s] = 1;
-        std::array<int, 4> g{s, -1, -1, -1};
-        // nearest 3 among the next kWindow unused slices in Morton order
+        std::array<int, kWarps> g;
+        g.fill(-1);
+        g[0] = s;
+        // nearest kWarps - 1 among the next kWindow unused slices in Morton order
         std::vector<std::pair<float, int>> cand;
-        for (i64 r = q + 1; r < nsl && static_cast<int>(cand.size()) < kWindow; ++r) {
+        for (i64 r = q + 1; r < nsl && kWarps > 1 && static_cast<int>(cand.size()) < kWindow; ++r) {
             int c = order[r];
             if (used[c]) continue;
             float dx = xyz[3 * c] - xyz[3 * s], dy = xyz[3 * c + 1] - xyz[3 * s + 1], dz = xyz[3 * c + 2] - xyz[3 * s + 2];
             cand.push_back({dx * dx + dy * dy + dz * dz, c});
         }
-        std::partial_sort(cand.begin(), cand.begin() + std::min<size_t>(3, cand.size()), cand.end());
-        for (int w = 0; w < 3 && w < static_cast<int>(cand.size()); ++w) {
+        std::partial_sort(cand.begin(), cand.begin() + std::min<size_t>(kWarps - 1, cand.size()), cand.end());
+        for (int w = 0; w < kWarps - 1 && w < static_cast<int>(cand.size()); ++w) {
             g[w + 1] = cand[w].second;
             used[cand[w].second] = 1;
         }
@@ -490,14 +499,14 @@ std::vector<std::array<int, 4>> group_slices(i64 nsl, const std::vector<float> &
 
 struct HostBlock {
     int rows[kRows];
-    int wlen[4];
+    int wlen[kWarps];
     int L;                     // row-length class (multiple of 4)
     int us;                    // 4 * chunks + 4
     std::vector<int> ccol;     // chunk start columns
     std::vector<int4> runs;    // (col, chunks, staging offset, 0)
     std::vector<unsigned short> lidx;  // k-major per warp, concatenated warps
     std::vector<float> hi, lo;
-    int wbase_rel[4];
+    int wbase_rel[kWarps];
 };
 
 struct OrderScratch {
@@ -515,7 +524,7 @@ struct OrderScratch {
 void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::vector<int> &col,
                    const std::vector<int> &cols, std::vector<int> &perm, OrderScratch &S) {
     const int zero = 4 * static_cast<int>(cols.size());
-    for (int w = 0; w < 4; ++w) {
+    for (int w = 0; w < kWarps; ++w) {
         int r_of[32], n_of[32], left[32];
         for (int lane = 0; lane < 32; ++lane) {
             const int r = H.rows[32 * w + lane];
@@ -678,7 +687,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
                 j = j1;
             }
             int maxlen = 0;
-            for (int w = 0; w < 4; ++w) {
+            for (int w = 0; w < kWarps; ++w) {
                 int mx = 0;
                 for (int t = 32 * w; t < 32 * w + 32; ++t)
                     if (H.rows[t] >= 0) mx = std::max(mx, rp[H.rows[t] + 1] - rp[H.rows[t]]);
@@ -691,7 +700,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
             H.hi.clear();
             H.lo.clear();
             int off = 0;
-            for (int w = 0; w < 4; ++w) {
+            for (int w = 0; w < kWarps; ++w) {
                 H.wbase_rel[w] = off;
                 for (int k = 0; k < H.wlen[w]; ++k)
                     for (int lane = 0; lane < 32; ++lane) {
@@ -715,7 +724,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
         }
     });
     // classes and flattening
-    std::vector<int> brow(nb * kRows), wbase(nb * 4), wlen(nb * 4), cstart(nb + 1, 0), rstart(nb + 1, 0);
+    std::vector<int> brow(nb * kRows), wbase(nb * kWarps), wlen(nb * kWarps), cstart(nb + 1, 0), rstart(nb + 1, 0);
     std::vector<int> ccol;
     std::vector<int4> runs;
     std::vector<unsigned short> lidx;
@@ -726,9 +735,9 @@ void build_blocked(Matrix &m, cudaStream_t s) {
         HostBlock &H = hb[b];
         const int ebase = static_cast<int>(lidx.size());
         for (int t = 0; t < kRows; ++t) brow[b * kRows + t] = H.rows[t];
-        for (int w = 0; w < 4; ++w) {
-            wbase[b * 4 + w] = ebase + H.wbase_rel[w];
-            wlen[b * 4 + w] = H.wlen[w];
+        for (int w = 0; w < kWarps; ++w) {
+            wbase[b * kWarps + w] = ebase + H.wbase_rel[w];
+            wlen[b * kWarps + w] = H.wlen[w];
         }
         cstart[b] = static_cast<int>(ccol.size());
         ccol.insert(ccol.end(), H.ccol.begin(), H.ccol.end());
@@ -737,7 +746,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
         lidx.insert(lidx.end(), H.lidx.begin(), H.lidx.end());
         hi.insert(hi.end(), H.hi.begin(), H.hi.end());
         lo.insert(lo.end(), H.lo.begin(), H.lo.end());
-        int maxlen = std::max({H.wlen[0], H.wlen[1], H.wlen[2], H.wlen[3]});
+        int maxlen = *std::max_element(H.wlen, H.wlen + kWarps);
         if (maxlen <= kMaxL && H.us <= kMaxUS) {
             int ub = 0;
             while (kUsBuckets[ub] < H.us) ++ub;
@@ -812,17 +821,17 @@ void launch_chunk_us(const BlkArgs &a, i64 grid, const float *x, i64 ldx, float 
     k_blk_chunk<L, T, NS, US><<<static_cast<unsigned>(grid), kRows, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
 }
 
-// Staging stride buckets compiled in: 1024 and 3072 floats per field.
+// Staging stride buckets compiled in: kUsSmall and kUsLarge floats per field.
 template <int L, int T>
 void launch_chunk(const BlkArgs &a, int us, int ns, i64 grid, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs,
                   cudaStream_t s) {
-    if (us <= 1024) {
+    if (us <= kUsSmall) {
         if (ns >= 3)
-            launch_chunk_us<L, T, 3, 1024>(a, grid, x, ldx, y, ldy, nrhs, s);
+            launch_chunk_us<L, T, 3, kUsSmall>(a, grid, x, ldx, y, ldy, nrhs, s);
         else
-            launch_chunk_us<L, T, 2, 1024>(a, grid, x, ldx, y, ldy, nrhs, s);
+            launch_chunk_us<L, T, 2, kUsSmall>(a, grid, x, ldx, y, ldy, nrhs, s);
     } else {
-        launch_chunk_us<L, (T > 4 ? 4 : T), 2, 3072>(a, grid, x, ldx, y, ldy, nrhs, s);
+        launch_chunk_us<L, (T > 4 ? 4 : T), 2, kUsLarge>(a, grid, x, ldx, y, ldy, nrhs, s);
     }
 }
 
@@ -1023,10 +1032,10 @@ void blk_batch_launch(BlkBatch &bb, cudaStream_t s) {
     for (auto &g : bb.groups) {
         if (g.total == 0) continue;
         AXGB_CUDA(cudaMemsetAsync(g.counter.p, 0, sizeof(unsigned long long), s));
-        if (g.us <= 1024)
-            persist_dispatch<1024>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
+        if (g.us <= kUsSmall)
+            persist_dispatch<kUsSmall>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
         else
-            persist_dispatch<3072>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
+            persist_dispatch<kUsLarge>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
     }
     AXGB_CUDA(cudaGetLastError());
 }
