@@ -373,3 +373,38 @@ class RefLib:
         if n > cap:
             raise RuntimeError("reference result larger than buffer")
         return Weights(src.n_cells, dst.n_cells, row[:n], col[:n], w[:n], fa, fb, aa, ab)
+
+
+class RefFastLib:
+    """The reference's regular / rectilinear fast-path sources compiled
+    through the shim (oracle/_ref/libaxisref_fast.so, oracle/ref_fast.cpp).
+    run(kind, src, dst): kind 0 generate_conservative_rect, 1
+    generate_conservative_rect_nonuniform, 2 generate_bilinear_rect, 3
+    generate_bilinear_rect_nonuniform; returns Weights in to_csr order."""
+
+    CONS_REGULAR, CONS_RECTILINEAR, BIL_REGULAR, BIL_RECTILINEAR = 0, 1, 2, 3
+
+    def __init__(self, path: str | None = None):
+        if path is None:
+            path = os.path.join(HERE, "_ref", "libaxisref_fast.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = C.CDLL(path)
+        mesh = [C.c_int64, _f64p, C.c_int64, _i64p, _i64p]
+        L.ref_fast.argtypes = ([C.c_int] + mesh + mesh + [C.c_int, C.c_int, C.c_int64, C.POINTER(C.c_int64), _i64p,
+                                                          _i64p, _f64p, _f64p, _f64p, _f64p, _f64p])
+        L.ref_fast.restype = C.c_int
+        self.L = L
+
+    def run(self, kind: int, src, dst, norm_type: int = 0, unmapped: int = 1) -> Weights:
+        cap = 64 * dst.n_cells + 64
+        nnz = C.c_int64(0)
+        row, col, w = np.zeros(cap, np.int64), np.zeros(cap, np.int64), np.zeros(cap)
+        fa, fb = np.zeros(src.n_cells), np.zeros(dst.n_cells)
+        aa, ab = np.zeros(src.n_cells), np.zeros(dst.n_cells)
+        rc = self.L.ref_fast(kind, *_mesh_args(src), *_mesh_args(dst), norm_type, unmapped, cap, C.byref(nnz), row,
+                             col, w, fa, fb, aa, ab)
+        if rc != 0 or nnz.value > cap:
+            raise RuntimeError(f"reference fast path failed rc={rc}")
+        n = nnz.value
+        return Weights(src.n_cells, dst.n_cells, row[:n].copy(), col[:n].copy(), w[:n].copy(), fa, fb, aa, ab)

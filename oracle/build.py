@@ -5,6 +5,9 @@
   compiled unchanged from the reference checkout through the host shim in
   ``oracle/ref_shim`` plus the glue in ``ref_driver.cpp``; built only when the
   reference checkout exists (never on machines without it).
+* ``oracle/_ref/libaxisref_fast.so`` the reference's regular/rectilinear
+  fast-path sources (four files of src/solver/) compiled unchanged the same
+  way, with ``ref_fast.cpp``; also only where the checkout exists.
 
 Both use ``-O2 -ffp-contract=off`` so double expressions are evaluated as
 written, like the reference's host build.
@@ -51,7 +54,30 @@ def build_ref(force: bool = False) -> str | None:
     return out
 
 
+REF_SRC = "/root/reference/libs/axis/src/solver"
+FAST_SOURCES = ["weight_generator_conservative_rect.cpp", "weight_generator_conservative_rect_nonuniform.cpp",
+                "weight_generator_bilinear_rect.cpp", "weight_generator_bilinear_rect_nonuniform.cpp"]
+
+
+def build_ref_fast(force: bool = False) -> str | None:
+    """oracle/_ref/libaxisref_fast.so: the reference's regular/rectilinear
+    fast-path sources compiled unchanged where they lie, with ref_fast.cpp."""
+    if not os.path.isdir(REF_SRC):
+        return None
+    shim = os.path.join(HERE, "ref_shim")
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libaxisref_fast.so")
+    srcs = [os.path.join(HERE, "ref_fast.cpp")] + [os.path.join(REF_SRC, f) for f in FAST_SOURCES]
+    deps = srcs + [os.path.join(shim, f) for f in ("Kokkos_Core.hpp", "KokkosSparse_CrsMatrix.hpp")]
+    if force or _needs(out, deps):
+        subprocess.check_call(["g++", *[f for f in FLAGS if f != "-fopenmp"], "-I", shim, "-I", REF_INCLUDE, *srcs,
+                               "-o", out])
+    return out
+
+
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref(force))
+    print(build_ref_fast(force))

@@ -1,7 +1,8 @@
 // Minimal host-only stand-in for the part of the Kokkos API that the AXIS
-// geometry headers use (View, RangePolicy, parallel_for/reduce, math
-// wrappers, mirror/deep_copy). It lets oracle/ref_driver.cpp compile the
-// reference's header-only geometry code unchanged, serially, on the host.
+// geometry headers and the regular/rectilinear fast-path sources use (View,
+// RangePolicy, parallel_for/reduce, math wrappers, mirror/deep_copy, Device).
+// It lets oracle/ref_driver.cpp and oracle/ref_fast.cpp compile the
+// reference's code unchanged, serially, on the host.
 // Test infrastructure: used only to build oracle/_ref/libaxisref.so.
 #pragma once
 
@@ -29,6 +30,11 @@ struct HostSpace {
     using memory_space = HostSpace;
 };
 using DefaultHostExecutionSpace = Serial;
+template <class ExecSpace, class MemSpace>
+struct Device {
+    using execution_space = ExecSpace;
+    using memory_space = MemSpace;
+};
 using DefaultExecutionSpace = Serial;
 struct LayoutLeft {};
 struct LayoutRight {};
@@ -51,6 +57,7 @@ inline double asin(double x) { return std::asin(x); }
 inline double cos(double x) { return std::cos(x); }
 inline double sin(double x) { return std::sin(x); }
 inline double abs(double x) { return std::fabs(x); }
+inline double floor(double x) { return std::floor(x); }
 inline bool isnan(double x) { return std::isnan(x); }
 inline bool isinf(double x) { return std::isinf(x); }
 inline double nan(const char *s) { return std::nan(s); }
