@@ -17,7 +17,13 @@ nor the grid generators to reproduce the inputs:
 * ``clip.npz``: 200 random spherical polygon pairs and the reference
   clipper's overlap area and output polygon;
 * ``cellprep_<grid>.npz``: a mesh and the reference's cell areas, bounding
-  caps, float AABBs and degenerate flags.
+  caps, float AABBs and degenerate flags;
+* ``fastpath_<case>.npz``: src/dst meshes, the method ("conservative" or
+  "bilinear"), the normalisation and the reference's own regular /
+  rectilinear fast-path output (row, col, w, frac and area arrays). These
+  come from ``oracle/_ref/libaxisref_fast.so``: the reference's
+  weight_generator_{conservative,bilinear}_rect{,_nonuniform}.cpp compiled
+  unchanged through the same shim, with its grid detection and to_csr.
 """
 
 from __future__ import annotations
@@ -34,7 +40,7 @@ for p in (ROOT, os.path.join(ROOT, "helm-project_gb300")):
         sys.path.insert(0, p)
 
 from axgb import grids  # noqa: E402
-from oracle import RefLib  # noqa: E402
+from oracle import RefFastLib, RefLib  # noqa: E402
 from oracle import build as obuild  # noqa: E402
 
 CONSERVATIVE = {
@@ -47,6 +53,25 @@ CELLPREP = {
     "C8": lambda: grids.cubed_sphere(8),
     "5deg": lambda: grids.latlon_deg(5.0),
     "tripole48x36": lambda: grids.tripole(48, 36, seed=4, jitter=0.1),
+}
+
+# name -> (make, reference fast-path kind, method, norm_type). Each pair is
+# one the reference's dispatch sends to that fast path.
+FASTPATH = {
+    "cons_regular_5deg_to_10deg": (lambda: (grids.latlon_deg(5.0), grids.latlon_deg(10.0)),
+                                   RefFastLib.CONS_REGULAR, "conservative", 0),
+    "cons_regular_10deg_to_7p5deg_fracarea": (lambda: (grids.latlon_deg(10.0), grids.latlon_deg(7.5)),
+                                              RefFastLib.CONS_REGULAR, "conservative", 1),
+    "cons_rectilinear_ea36x18_to_10deg": (lambda: (grids.equal_area_latlon(36, 18, stretch=0.4),
+                                                   grids.latlon_deg(10.0)),
+                                          RefFastLib.CONS_RECTILINEAR, "conservative", 0),
+    "cons_rectilinear_declined_regional": (lambda: (grids.regular_latlon(20, 15, 20.0, -10.0, 2.0, 2.0),
+                                                    grids.regular_latlon(10, 10, 10.0, -20.0, 4.0, 4.0)),
+                                           RefFastLib.CONS_RECTILINEAR, "conservative", 1),
+    "bil_regular_5deg_to_12deg": (lambda: (grids.latlon_deg(5.0), grids.latlon_deg(12.0)),
+                                  RefFastLib.BIL_REGULAR, "bilinear", 0),
+    "bil_rectilinear_ea36x18_to_C6": (lambda: (grids.equal_area_latlon(36, 18, stretch=0.4), grids.cubed_sphere(6)),
+                                    RefFastLib.BIL_RECTILINEAR, "bilinear", 0),
 }
 
 
@@ -82,6 +107,16 @@ def main():
         c = ref.cell_prep(m)
         np.savez_compressed(os.path.join(HERE, f"cellprep_{name}.npz"), **mesh_dict("mesh", m), **c)
         print("cellprep", name, m.n_cells)
+    if obuild.build_ref_fast() is None:
+        raise SystemExit("the reference checkout is needed to generate the fast-path fixtures")
+    fast = RefFastLib()
+    for name, (make, kind, method, norm) in FASTPATH.items():
+        src, dst = make()
+        w = fast.run(kind, src, dst, norm)
+        np.savez_compressed(os.path.join(HERE, f"fastpath_{name}.npz"), **mesh_dict("src", src),
+                            **mesh_dict("dst", dst), method=method, norm_type=norm, row=w.row, col=w.col, w=w.w,
+                            frac_a=w.frac_a, frac_b=w.frac_b, area_a=w.area_a, area_b=w.area_b)
+        print("fastpath", name, "nnz", w.nnz)
     rng = np.random.default_rng(20240)
     subj, clipp, nsub, ncl, area, nout, outp = [], [], [], [], [], [], []
     for _ in range(200):

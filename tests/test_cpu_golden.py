@@ -7,10 +7,11 @@ from golden_io import cases, load, mesh
 
 CONS = cases("conservative")
 CELL = cases("cellprep")
+FAST = cases("fastpath")
 
 
 def test_fixtures_present():
-    assert len(CONS) >= 4 and len(CELL) >= 3
+    assert len(CONS) >= 4 and len(CELL) >= 3 and len(FAST) >= 6
 
 
 @pytest.mark.parametrize("name", CONS)
@@ -37,3 +38,19 @@ def test_oracle_clip_golden(oracle):
         area, poly = oracle.clip(a, b)
         assert area == z["area"][i]
         assert np.array_equal(poly, z["out"][i, : z["n_out"][i]])
+
+
+@pytest.mark.parametrize("name", FAST)
+def test_oracle_fastpath_golden(oracle, name):
+    """The oracle's dispatch (regular, then rectilinear, then the clipper for
+    conservative; regular, then rectilinear source for bilinear) against the
+    reference's own fast-path sources on the same pair: every array bit for
+    bit."""
+    z = load("fastpath", name)
+    src, dst = mesh(z, "src"), mesh(z, "dst")
+    if str(z["method"]) == "conservative":
+        w = oracle.conservative(src, dst, norm_type=int(z["norm_type"]))
+    else:
+        w = oracle.bilinear(src, dst)
+    for k in ("row", "col", "w", "frac_a", "frac_b", "area_a", "area_b"):
+        assert np.array_equal(getattr(w, k), z[k]), k

@@ -1,6 +1,7 @@
 """GPU weights and cell geometry against the golden vectors produced by the
 reference's own geometry code (tests/golden): the (dst, src) index set
-bit-exact, weights, fractions and areas within 1e-12 relative."""
+bit-exact, weights, fractions and areas within 1e-12 relative (bilinear
+weights bit for bit)."""
 import numpy as np
 import pytest
 
@@ -24,6 +25,27 @@ def test_gpu_conservative_golden(gpu, name):
     for k in ("frac_a", "frac_b", "area_a", "area_b"):
         ref = z[k]
         assert np.max(np.abs(csr[k] - ref) / np.maximum(np.abs(ref), 1e-300)) < W_RTOL, k
+
+
+@pytest.mark.parametrize("name", cases("fastpath"))
+def test_gpu_fastpath_golden(gpu, name):
+    """Regular and rectilinear fast paths against the reference's own
+    weight_generator_{conservative,bilinear}_rect{,_nonuniform}.cpp output."""
+    z = load("fastpath", name)
+    method = str(z["method"])
+    cfg = {"method": method, "norm_type": ("DstArea", "FracArea")[int(z["norm_type"])], "unmapped": "Ignore"}
+    M = gpu.generate_weights(gpu.Mesh.from_grid(mesh(z, "src")), gpu.Mesh.from_grid(mesh(z, "dst")), cfg)
+    csr = M.to_csr()
+    rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
+    assert M.nnz == len(z["w"])
+    assert np.array_equal(rows, z["row"]) and np.array_equal(csr["col"], z["col"])
+    if method == "bilinear":
+        assert np.array_equal(csr["val"], z["w"])
+    else:
+        assert np.max(np.abs(csr["val"] - z["w"]) / np.abs(z["w"])) < W_RTOL
+    for k in ("frac_a", "frac_b", "area_a", "area_b"):
+        ref = z[k]
+        assert np.max(np.abs(csr[k] - ref) / np.maximum(np.abs(ref), 1e-300), initial=0.0) < W_RTOL, k
 
 
 @pytest.mark.parametrize("name", cases("cellprep"))
