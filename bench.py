@@ -148,6 +148,20 @@ def cpu_apply_rate(oracle, wo, X_cpu):
     return X_cpu.shape[0] * wo.n_dst / dt, dt
 
 
+def cpu_coo_rate(oracle, wo, X_cpu, budget_s=5.0):
+    """dst-vals/s of the COO scatter-add with OpenMP atomics (the path the
+    reference's Python batch_apply takes, include/axis/solver/apply.hpp:315-330),
+    repeated for about budget_s seconds."""
+    oracle.apply_coo_atomic(wo, X_cpu[:1])
+    reps, total = 0, 0.0
+    while total < budget_s and reps < 100:
+        t0 = time.perf_counter()
+        oracle.apply_coo_atomic(wo, X_cpu)
+        total += time.perf_counter() - t0
+        reps += 1
+    return reps * X_cpu.shape[0] * wo.n_dst / total, reps, total
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -176,6 +190,7 @@ def reference_arm(args):
         times.append(dt)
     ms = 1e3 * statistics.mean(times)
     value = sample * wo.n_dst / (ms / 1e3)
+    coo, coo_reps, coo_s = cpu_coo_rate(o, wo, X[:16])
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -183,7 +198,10 @@ def reference_arm(args):
                       "nrhs_sampled": sample, "parallelism": "host threads"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                             "sample": f"{sample} of {NRHS} RHS per step, FP64 CSR row loop (OpenMP), "
-                                      f"oracle weights generated in {gen_s:.1f} s"},
+                                      f"oracle weights generated in {gen_s:.1f} s",
+                            "coo_atomic_value": coo,
+                            "coo_atomic_sample": f"16 RHS x {coo_reps} repeats, FP64 COO scatter-add with OpenMP "
+                                                 f"atomics, {coo_s:.1f} s"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     return 0
@@ -405,9 +423,13 @@ def main():
                 reps += 1
                 total += dt
             rate = reps * ns * wo.n_dst / total
+            coo, coo_reps, coo_s = cpu_coo_rate(o, wo, xs[:16])
             result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                       "sample": f"{ns} of {nrhs} RHS x {reps} repeats, FP64 CSR row loop "
-                                                f"(OpenMP, oracle port), {total:.1f} s"}
+                                                f"(OpenMP, oracle port), {total:.1f} s",
+                                      "coo_atomic_value": coo,
+                                      "coo_atomic_sample": f"{min(16, ns)} RHS x {coo_reps} repeats, FP64 COO "
+                                                           f"scatter-add with OpenMP atomics, {coo_s:.1f} s"}
         print(json.dumps(result), flush=True)
     replicas.finalize()
     return 0
