@@ -42,10 +42,11 @@ constexpr int kUsLarge = 768 * kWarps;
 constexpr int kMaxUS = kUsLarge;  // staging floats per field a block may use
 constexpr int kMaxL = 32;        // longest row handled by the blocked kernels
 constexpr int kPool = 4;         // streams the class launches are spread over
-// Entries are skipped past the warp's longest row in groups of kGroup: the
-// group's straight-line code lets the scheduler overlap the compensated
-// steps of neighbouring entries; entries past a row's end are zero (weight
-// 0 on the zero slot) and leave the sums unchanged.
+// A warp steps through its entries in whole groups of kGroup (straight-line
+// code, so the scheduler overlaps the compensated steps of neighbouring
+// entries) and then through the 1 .. kGroup-1 entries left up to its longest
+// row; entries past a row's end are zero (weight 0 on the zero slot) and
+// leave the sums unchanged.
 constexpr int kGroup = 4;
 const int kUsBuckets[] = {kUsSmall, kUsLarge};
 
@@ -155,17 +156,21 @@ __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, c
             sa[q] = pk(0.f, 0.f);
             cn[q] = pk(0.f, 0.f);
         }
+        auto step = [&](int k) {
+            const F2 hp = pk(h[k], h[k]), ln = pk(-lw[k], -lw[k]);
+            const float *p0 = cur + li[k];
+#pragma unroll
+            for (int q = 0; q < T / 2; ++q) cstepn(sa[q], cn[q], h[k], hp, ln, p0[(2 * q) * US], p0[(2 * q + 1) * US]);
+        };
 #pragma unroll
         for (int k0 = 0; k0 < L; k0 += kGroup) {
-            if (k0 < wl) {  // warp-uniform
+            if (k0 + kGroup <= wl) {  // warp-uniform: a whole group
 #pragma unroll
-                for (int k = k0; k < k0 + kGroup && k < L; ++k) {
-                    const F2 hp = pk(h[k], h[k]), ln = pk(-lw[k], -lw[k]);
-                    const float *p0 = cur + li[k];
+                for (int k = k0; k < k0 + kGroup && k < L; ++k) step(k);
+            } else if (k0 < wl) {  // the warp's last 1 .. kGroup-1 entries
 #pragma unroll
-                    for (int q = 0; q < T / 2; ++q)
-                        cstepn(sa[q], cn[q], h[k], hp, ln, p0[(2 * q) * US], p0[(2 * q + 1) * US]);
-                }
+                for (int k = k0; k < k0 + kGroup - 1 && k < L; ++k)
+                    if (k < wl) step(k);
             }
         }
         if (row >= 0) {
