@@ -23,7 +23,7 @@
 // those values in the reference's operation order (--fmad=false), so every
 // weight is bitwise the reference's arithmetic. Entries of a row are stored
 // column-ascending (to_csr). frac = 1, area_a = 0, area_b the destination
-// cells' areas.
+// cells' get_cell_areas (mesh areas, else planar shoelace areas in degrees).
 #include <algorithm>
 #include <cmath>
 #include <thread>
@@ -394,7 +394,7 @@ void generate_bilinear_general(Mesh &src, Mesh &dst, const axgb_regrid_config &c
     if (n_src) k_bil_fill<<<nblk(n_src, 256), 256, 0, s>>>(out.frac_a.p, n_src, 1.0);
     if (n_dst) k_bil_fill<<<nblk(n_dst, 256), 256, 0, s>>>(out.frac_b.p, n_dst, 1.0);
     out.area_a.zero(s);  // the ESMF convention for bilinear (:2646-2650)
-    if (n_dst) AXGB_CUDA(cudaMemcpyAsync(out.area_b.p, dst.d_area.p, sizeof(double) * n_dst, cudaMemcpyDeviceToDevice, s));
+    planar_cell_areas(dst.view(), out.area_b.p, s);  // get_cell_areas(dst_mesh) (:2652-2655)
     AXGB_CUDA(cudaGetLastError());
     AXGB_CUDA(cudaStreamSynchronize(s));
     out.stats[3] = nnz;

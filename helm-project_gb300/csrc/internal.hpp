@@ -297,6 +297,9 @@ void blk_batch_set_fields(BlkBatch &bb, const float *const *x, const i64 *ldx, f
                           cudaStream_t s);
 void blk_batch_launch(BlkBatch &bb, cudaStream_t s);
 void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s);
+// get_cell_areas of src/solver/weight_generator.cpp:297-312: the mesh's own
+// areas where it has them, else planar shoelace areas in degrees (nearest.cu).
+void planar_cell_areas(const MeshView &m, double *out, cudaStream_t s);
 
 // scan_sort.cu: device primitives (own implementations)
 // out[0..n] = exclusive prefix sum of in[0..n-1], out[n] = total.

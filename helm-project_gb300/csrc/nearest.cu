@@ -12,8 +12,10 @@
 //     squared Euclidean distance. The reference asks ArborX v2.1 for
 //     nearest(point, 1), which this checkout does not vendor; here exact
 //     ties go to the lower source index. frac arrays are 1 and the areas
-//     are the cells' own (mesh areas or spherical polygon areas). Masks play
-//     no part (the coastal post-pass handles a masked source afterwards).
+//     are get_cell_areas (:297-312): the mesh's own areas where it has them,
+//     else the planar shoelace area of the cell's (lon, lat) degree corners
+//     (compute_single_cell_area, :266-293). Masks play no part (the coastal
+//     post-pass handles a masked source afterwards).
 // The search is exact and logarithmic, as the reference's BVH query: an
 // LBVH over the source points (lbvh.cuh) and, per destination point, a
 // stackless walk that skips every node whose box is farther than the best
@@ -100,7 +102,37 @@ __global__ void k_nn_fill(double *a, i64 n, double v) {
     if (i < n) a[i] = v;
 }
 
+// get_cell_areas (:297-312) with compute_single_cell_area (:266-293): the
+// shoelace sum of lon0*lat1 - lon1*lat0 over the cell's edges in degrees,
+// halved in magnitude; 0 below three corners. Built without contraction.
+__global__ void k_planar_area(MeshView m, double *out) {
+    const i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= m.n_cells) return;
+    if (m.user_area) {
+        out[c] = m.user_area[c];
+        return;
+    }
+    const int b = m.off[c], n = m.off[c + 1] - b;
+    if (n < 3) {
+        out[c] = 0.0;
+        return;
+    }
+    double a = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const int p = m.idx[b + i], q = m.idx[b + (i + 1) % n];
+        const double x0 = m.lonlat[p], y0 = m.lonlat[p + m.n_nodes];
+        const double x1 = m.lonlat[q], y1 = m.lonlat[q + m.n_nodes];
+        a += x0 * y1 - x1 * y0;
+    }
+    out[c] = fabs(a) * 0.5;
+}
+
 }  // namespace
+
+void planar_cell_areas(const MeshView &m, double *out, cudaStream_t s) {
+    if (m.n_cells) k_planar_area<<<nblk(m.n_cells, 256), 256, 0, s>>>(m, out);
+    AXGB_CUDA(cudaGetLastError());
+}
 
 void generate_nearest(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &out) {
     cudaStream_t s = 0;
@@ -161,8 +193,8 @@ void generate_nearest(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matri
     } else {
         if (n_src) k_nn_fill<<<nblk(n_src, 256), 256, 0, s>>>(out.frac_a.p, n_src, 1.0);
         if (n_dst) k_nn_fill<<<nblk(n_dst, 256), 256, 0, s>>>(out.frac_b.p, n_dst, 1.0);
-        if (n_src) AXGB_CUDA(cudaMemcpyAsync(out.area_a.p, src.d_area.p, sizeof(double) * n_src, cudaMemcpyDeviceToDevice, s));
-        if (n_dst) AXGB_CUDA(cudaMemcpyAsync(out.area_b.p, dst.d_area.p, sizeof(double) * n_dst, cudaMemcpyDeviceToDevice, s));
+        planar_cell_areas(src.view(), out.area_a.p, s);
+        planar_cell_areas(dst.view(), out.area_b.p, s);
     }
     AXGB_CUDA(cudaGetLastError());
     AXGB_CUDA(cudaStreamSynchronize(s));

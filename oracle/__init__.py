@@ -39,6 +39,9 @@ class Weights:
         self.frac_a, self.frac_b, self.area_a, self.area_b = frac_a, frac_b, area_a, area_b
         self.stats = stats or {}
         self.seconds = seconds
+        # per entry, its place in its row's generation order where that is
+        # not column order (general bilinear), else None
+        self.gen = None
 
     @property
     def nnz(self):
@@ -104,6 +107,8 @@ class Oracle:
         L.orc_result_stats.argtypes = [C.c_void_p, _i64p]
         L.orc_result_copy.argtypes = [C.c_void_p, _i64p, _i64p, _f64p, _f64p, _f64p, _f64p, _f64p]
         L.orc_result_free.argtypes = [C.c_void_p]
+        L.orc_result_gen.restype = C.c_int
+        L.orc_result_gen.argtypes = [C.c_void_p, _i64p]
         L.orc_nan_batch_apply.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_int64, _f64p, C.c_int64,
                                           C.c_int64, C.c_double]
         L.orc_apply_masked.argtypes = [C.c_int64, _i64p, _i64p, _f64p, _f64p, C.c_void_p, _f64p]
@@ -190,15 +195,21 @@ class Oracle:
     def coastal(self, w: Weights, src, dst, src_mask, nearest_wet: bool = True) -> Weights:
         """coastal_renormalize_and_extrapolate (src/solver/weight_generator.cpp:
         1736-1881) on CSR-ordered weights: wet entries (mask > 0) kept, a row
-        whose wet weights sum to s in (0, 1) divided by s (sums in CSR order),
-        and with NearestWet every row left empty given the wet source (mask != 0)
-        whose float (lon, lat) centroid (compute_cell_centroids_xy, :75-138) is
-        nearest, weight 1, ties to the lower index. Brute-force search."""
+        whose wet weights sum to s in (0, 1) divided by s, and with NearestWet
+        every row left empty given the wet source (mask != 0) whose float
+        (lon, lat) centroid (compute_cell_centroids_xy, :75-138) is nearest,
+        weight 1, ties to the lower index. Brute-force search. The row sums
+        run in the order the generator emitted the entries (w.gen where the
+        weights carry it, else column order), as the reference's COO loop."""
         mask = np.asarray(src_mask)
         keep = mask[w.col] > 0
         s = np.zeros(w.n_dst)
-        for k in np.nonzero(keep)[0]:  # in CSR order, as the device pass sums
-            s[w.row[k]] += w.w[k]
+        seq = np.arange(w.nnz)
+        if w.gen is not None:  # within each row, generation order
+            seq = np.lexsort((w.gen, w.row))
+        for k in seq:
+            if keep[k]:
+                s[w.row[k]] += w.w[k]
         row, col, val = w.row[keep], w.col[keep], w.w[keep].copy()
         ren = (s[row] > 0.0) & (s[row] < 1.0)
         val[ren] = val[ren] / s[row][ren]
@@ -251,9 +262,13 @@ class Oracle:
         aa = np.zeros(n_src)
         ab = np.zeros(n_dst)
         self.L.orc_result_copy(h, row, col, w, fa, fb, aa, ab)
+        gen = np.zeros(nnz, np.int64)
+        has_gen = self.L.orc_result_gen(h, gen)
         self.L.orc_result_free(h)
-        return Weights(n_src, n_dst, row, col, w, fa, fb, aa, ab,
-                       stats=dict(box_pairs=int(st[0]), cap_pass=int(st[1]), clipped=int(st[2])), seconds=dt)
+        out = Weights(n_src, n_dst, row, col, w, fa, fb, aa, ab,
+                      stats=dict(box_pairs=int(st[0]), cap_pass=int(st[1]), clipped=int(st[2])), seconds=dt)
+        out.gen = gen if has_gen else None
+        return out
 
     def apply_csr(self, wts: Weights, x, compensated: bool = True):
         """x: [nrhs, n_src] float64 (row-major = one field per row)."""
@@ -406,5 +421,56 @@ class RefFastLib:
                              col, w, fa, fb, aa, ab)
         if rc != 0 or nnz.value > cap:
             raise RuntimeError(f"reference fast path failed rc={rc}")
+        n = nnz.value
+        return Weights(src.n_cells, dst.n_cells, row[:n].copy(), col[:n].copy(), w[:n].copy(), fa, fb, aa, ab)
+
+
+class RefGenLib:
+    """The reference's whole WeightGenerator::generate (weight_generator.cpp
+    and the sources it calls) compiled through the shims, ArborX's queries by
+    exhaustive search (oracle/_ref/libaxisref_gen.so, oracle/ref_generate.cpp).
+    generate(method, src, dst, ...) returns Weights in to_csr order or raises
+    RuntimeError with the reference's message. Quadratic searches: small
+    grids only."""
+
+    METHODS = {"bilinear": 0, "nearest_neighbor": 1, "conservative": 4}
+
+    def __init__(self, path: str | None = None):
+        if path is None:
+            path = os.path.join(HERE, "_ref", "libaxisref_gen.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = C.CDLL(path)
+        mesh = [C.c_int64, _f64p, C.c_int64, _i64p, _i64p, C.c_void_p, C.c_void_p]
+        L.ref_generate.argtypes = ([C.c_int] + mesh + mesh + [C.c_int] * 4 + [C.c_int64, C.POINTER(C.c_int64), _i64p,
+                                                                               _i64p, _f64p, _f64p, _f64p, _f64p, _f64p])
+        L.ref_generate.restype = C.c_int
+        L.ref_generate_error.restype = C.c_char_p
+        self.L = L
+
+    def generate(self, method, src, dst, norm_type=0, line_type=1, unmapped=1, extrap=1, src_mask=None,
+                 dst_mask=None, src_areas=None, dst_areas=None) -> Weights:
+        m = self.METHODS[method] if isinstance(method, str) else int(method)
+        keep = []
+
+        def opt(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dt)
+            keep.append(a)
+            return a.ctypes.data_as(C.c_void_p)
+
+        cap = 64 * dst.n_cells + 64
+        nnz = C.c_int64(0)
+        row, col, w = np.zeros(cap, np.int64), np.zeros(cap, np.int64), np.zeros(cap)
+        fa, fb = np.zeros(src.n_cells), np.zeros(dst.n_cells)
+        aa, ab = np.zeros(src.n_cells), np.zeros(dst.n_cells)
+        rc = self.L.ref_generate(m, *_mesh_args(src), opt(src_mask, np.int32), opt(src_areas, np.float64),
+                                 *_mesh_args(dst), opt(dst_mask, np.int32), opt(dst_areas, np.float64), norm_type,
+                                 line_type, unmapped, extrap, cap, C.byref(nnz), row, col, w, fa, fb, aa, ab)
+        if rc != 0:
+            raise RuntimeError(self.L.ref_generate_error().decode())
+        if nnz.value > cap:
+            raise RuntimeError("reference generate: output above capacity")
         n = nnz.value
         return Weights(src.n_cells, dst.n_cells, row[:n].copy(), col[:n].copy(), w[:n].copy(), fa, fb, aa, ab)

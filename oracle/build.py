@@ -8,6 +8,11 @@
 * ``oracle/_ref/libaxisref_fast.so`` the reference's regular/rectilinear
   fast-path sources (four files of src/solver/) compiled unchanged the same
   way, with ``ref_fast.cpp``; also only where the checkout exists.
+* ``oracle/_ref/libaxisref_gen.so`` the reference's whole weight generator
+  (src/solver/weight_generator.cpp and the solver sources it calls) compiled
+  unchanged the same way, ArborX replaced by the exhaustive search of
+  ``ref_shim/ArborX.hpp``, with ``ref_generate.cpp``; also only where the
+  checkout exists.
 
 Both use ``-O2 -ffp-contract=off`` so double expressions are evaluated as
 written, like the reference's host build.
@@ -76,8 +81,31 @@ def build_ref_fast(force: bool = False) -> str | None:
     return out
 
 
+GEN_SOURCES = ["weight_generator.cpp", *FAST_SOURCES, "gradient_reconstructor.cpp", "halo_pattern.cpp",
+               "interpolation_matrix.cpp"]
+SHIM_HEADERS = ["Kokkos_Core.hpp", "KokkosSparse_CrsMatrix.hpp", "Kokkos_UnorderedMap.hpp", "ArborX.hpp"]
+
+
+def build_ref_gen(force: bool = False) -> str | None:
+    """oracle/_ref/libaxisref_gen.so: WeightGenerator::generate of the
+    reference, compiled unchanged where its sources lie, with ref_generate.cpp."""
+    if not os.path.isdir(REF_SRC):
+        return None
+    shim = os.path.join(HERE, "ref_shim")
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libaxisref_gen.so")
+    srcs = [os.path.join(HERE, "ref_generate.cpp")] + [os.path.join(REF_SRC, f) for f in GEN_SOURCES]
+    deps = srcs + [os.path.join(shim, f) for f in SHIM_HEADERS]
+    if force or _needs(out, deps):
+        subprocess.check_call(["g++", *[f for f in FLAGS if f != "-fopenmp"], "-Wl,--no-undefined", "-I", shim,
+                               "-I", REF_INCLUDE, *srcs, "-o", out])
+    return out
+
+
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref(force))
     print(build_ref_fast(force))
+    print(build_ref_gen(force))

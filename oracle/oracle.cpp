@@ -178,6 +178,22 @@ Poly cell_poly(const Mesh &m, const std::vector<V3> &xyz, i64 c) {
     return p;
 }
 
+// get_cell_areas (src/solver/weight_generator.cpp:297-312): the mesh's own
+// areas where it has them, else compute_single_cell_area (:266-293), the
+// planar shoelace area of the cell's (lon, lat) corners in degrees. The
+// nearest-neighbour and general bilinear paths report these.
+double planar_area(const Mesh &m, i64 c) {
+    if (m.areas) return m.areas[c];
+    const i64 b = m.off[c], n = m.off[c + 1] - b;
+    if (n < 3) return 0.0;
+    double a = 0.0;
+    for (i64 i = 0; i < n; ++i) {
+        const i64 p = m.idx[b + i], q = m.idx[b + (i + 1) % n];
+        a += m.lon(p) * m.lat(q) - m.lon(q) * m.lat(p);
+    }
+    return std::fabs(a) * 0.5;
+}
+
 // ─── Regular / rectilinear detection (include/axis/detail/regular_grid_detector.hpp:64-299)
 
 struct GridInfo {
@@ -571,6 +587,9 @@ std::vector<i64> morton_order(const Mesh &m) {
 struct orc_result {
     i64 n_src = 0, n_dst = 0;
     std::vector<i64> row, col;  // CSR order: sorted by (row, col)
+    // Per CSR entry, its place in its row's generation (COO) order where
+    // that differs from column order (general bilinear); empty otherwise.
+    std::vector<i64> gen;
     std::vector<double> w, frac_a, frac_b, area_a, area_b;
     i64 n_box_pairs = 0, n_cap_pass = 0, n_clipped = 0;
     double seconds = 0.0;
@@ -954,6 +973,7 @@ static void bilinear_general(const Mesh &S, const Mesh &D, orc_result *res) {
     }
     const int k_query = static_cast<int>(std::min<i64>(8, n_src));
     std::vector<std::vector<std::pair<i64, double>>> rows(n_dst);
+    std::vector<std::vector<i64>> ranks(n_dst);  // each CSR entry's place in the row's generation order
 #pragma omp parallel for schedule(dynamic, 64)
     for (i64 j = 0; j < n_dst; ++j) {
         const float qx = static_cast<float>(dcx[j]), qy = static_cast<float>(dcy[j]), qz = 0.0f;
@@ -1034,22 +1054,31 @@ static void bilinear_general(const Mesh &S, const Mesh &D, orc_result *res) {
                 for (int k = 0; k < n_idw; ++k) out.push_back({cand[k], (1.0 / dist[k]) / sum_inv});
             }
         }
-        std::stable_sort(out.begin(), out.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+        // to_csr order (columns ascending, stable), remembering the order the
+        // entries were generated in: the coastal post-pass sums a row's wet
+        // weights in that order (:1769-1777)
+        std::vector<i64> ord(out.size());
+        for (std::size_t k = 0; k < ord.size(); ++k) ord[k] = static_cast<i64>(k);
+        std::stable_sort(ord.begin(), ord.end(), [&](i64 x, i64 y) { return out[x].first < out[y].first; });
+        std::vector<std::pair<i64, double>> sorted(out.size());
+        for (std::size_t k = 0; k < ord.size(); ++k) sorted[k] = out[ord[k]];
+        out.swap(sorted);
+        ranks[j] = std::move(ord);
     }
     res->n_src = n_src;
     res->n_dst = n_dst;
     for (i64 j = 0; j < n_dst; ++j)
-        for (auto &e : rows[j]) {
+        for (std::size_t k = 0; k < rows[j].size(); ++k) {
             res->row.push_back(j);
-            res->col.push_back(e.first);
-            res->w.push_back(e.second);
+            res->col.push_back(rows[j][k].first);
+            res->w.push_back(rows[j][k].second);
+            res->gen.push_back(ranks[j][k]);
         }
-    auto dxyz = node_xyz(D);
     res->frac_a.assign(n_src, 1.0);
     res->frac_b.assign(n_dst, 1.0);
-    res->area_a.assign(n_src, 0.0);
+    res->area_a.assign(n_src, 0.0);  // :2646-2650
     res->area_b.resize(n_dst);
-    for (i64 c = 0; c < n_dst; ++c) res->area_b[c] = D.areas ? D.areas[c] : poly_area(cell_poly(D, dxyz, c));
+    for (i64 c = 0; c < n_dst; ++c) res->area_b[c] = planar_area(D, c);  // :2652-2655
 }
 
 // Nearest-neighbour weights: WeightGenerator::generate_nearest
@@ -1061,7 +1090,7 @@ static void bilinear_general(const Mesh &S, const Mesh &D, orc_result *res) {
 // centroids (:75-138) and, per destination point, the source point at the
 // least float squared distance (dx*dx + dy*dy + dz*dz, no contraction);
 // ArborX v2.1's nearest(point, 1) is not in the checkout, so exact ties go
-// to the lower source index. frac = 1, areas = the cells' areas.
+// to the lower source index. frac = 1, areas = get_cell_areas (planar_area).
 // Brute force over all source points. unmapped: 0 Error, 1 Ignore; returns
 // false when there is no source cell under Error.
 static bool nearest(const Mesh &S, const Mesh &D, int unmapped, orc_result *res) {
@@ -1129,10 +1158,9 @@ static bool nearest(const Mesh &S, const Mesh &D, int unmapped, orc_result *res)
         }
         best[j] = bi;
     }
-    std::vector<double> sa(n_src), da(n_dst);
-    auto sx = node_xyz(S), dx = node_xyz(D);
-    for (i64 c = 0; c < n_src; ++c) sa[c] = S.areas ? S.areas[c] : poly_area(cell_poly(S, sx, c));
-    for (i64 c = 0; c < n_dst; ++c) da[c] = D.areas ? D.areas[c] : poly_area(cell_poly(D, dx, c));
+    std::vector<double> sa(n_src), da(n_dst);  // get_cell_areas (:2249-2258)
+    for (i64 c = 0; c < n_src; ++c) sa[c] = planar_area(S, c);
+    for (i64 c = 0; c < n_dst; ++c) da[c] = planar_area(D, c);
     for (i64 j = 0; j < n_dst; ++j)
         if (best[j] >= 0) {
             res->row.push_back(j);
@@ -1514,6 +1542,14 @@ void orc_result_copy(const orc_result *r, i64 *row, i64 *col, double *w, double 
     std::copy(r->frac_b.begin(), r->frac_b.end(), fb);
     std::copy(r->area_a.begin(), r->area_a.end(), aa);
     std::copy(r->area_b.begin(), r->area_b.end(), ab);
+}
+
+// Generation ranks (see orc_result::gen): copies them and returns 1, or
+// returns 0 when the rows were generated in column order.
+int orc_result_gen(const orc_result *r, i64 *gen) {
+    if (r->gen.empty()) return 0;
+    std::copy(r->gen.begin(), r->gen.end(), gen);
+    return 1;
 }
 
 void orc_result_free(orc_result *r) { delete r; }

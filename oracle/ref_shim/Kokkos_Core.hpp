@@ -1,8 +1,9 @@
 // Minimal host-only stand-in for the part of the Kokkos API that the AXIS
-// geometry headers and the regular/rectilinear fast-path sources use (View,
-// RangePolicy, parallel_for/reduce, math wrappers, mirror/deep_copy, Device).
-// It lets oracle/ref_driver.cpp and oracle/ref_fast.cpp compile the
-// reference's code unchanged, serially, on the host.
+// geometry headers, the regular/rectilinear fast-path sources and the weight
+// generator use (View of rank 0 to 2, RangePolicy, parallel_for/reduce,
+// atomics, math wrappers, mirror/deep_copy, Device). It lets
+// oracle/ref_driver.cpp, oracle/ref_fast.cpp and oracle/ref_generate.cpp
+// compile the reference's code unchanged, serially, on the host.
 // Test infrastructure: used only to build oracle/_ref/libaxisref.so.
 #pragma once
 
@@ -58,24 +59,38 @@ inline double cos(double x) { return std::cos(x); }
 inline double sin(double x) { return std::sin(x); }
 inline double abs(double x) { return std::fabs(x); }
 inline double floor(double x) { return std::floor(x); }
+inline double round(double x) { return std::round(x); }
+inline double atan(double x) { return std::atan(x); }
 inline bool isnan(double x) { return std::isnan(x); }
 inline bool isinf(double x) { return std::isinf(x); }
 inline double nan(const char *s) { return std::nan(s); }
 
 template <class T>
-struct view_traits;
+struct view_traits {  // rank 0
+    using value = T;
+    static constexpr int rank = 0;
+    static constexpr std::size_t e1 = 1;
+};
 template <class U>
 struct view_traits<U *> {
     using value = U;
     static constexpr int rank = 1;
+    static constexpr std::size_t e1 = 1;
 };
 template <class U>
 struct view_traits<U **> {
     using value = U;
     static constexpr int rank = 2;
+    static constexpr std::size_t e1 = 0;  // run-time extent
+};
+template <class U, std::size_t N>
+struct view_traits<U *[N]> {
+    using value = U;
+    static constexpr int rank = 2;
+    static constexpr std::size_t e1 = N;
 };
 
-// Rank-1 or rank-2 (column-major) host array with shared ownership.
+// Rank-0, rank-1 or rank-2 (column-major) host array with shared ownership.
 template <class DataType, class... Props>
 class View {
    public:
@@ -89,12 +104,17 @@ class View {
     std::size_t e0 = 0, e1 = 1;
 
     View() = default;
+    explicit View(const std::string &) : store(new nc_value[1]()), ptr(store.get()), e0(1), e1(1) {}
     View(const std::string &, std::size_t n0, std::size_t n1 = 1)
-        : store(new nc_value[n0 * n1 > 0 ? n0 * n1 : 1]()), ptr(store.get()), e0(n0), e1(Rank > 1 ? n1 : 1) {}
+        : store(new nc_value[n0 * ext1(n1) > 0 ? n0 * ext1(n1) : 1]()), ptr(store.get()), e0(n0), e1(ext1(n1)) {}
     View(value_type *p, std::size_t n0, std::size_t n1 = 1) : ptr(const_cast<nc_value *>(p)), e0(n0), e1(Rank > 1 ? n1 : 1) {}
     template <class D2, class... P2>
     View(const View<D2, P2...> &o) : store(o.store), ptr(o.ptr), e0(o.e0), e1(o.e1) {}
 
+    static constexpr std::size_t ext1(std::size_t n1) {
+        return Rank < 2 ? 1 : (view_traits<DataType>::e1 ? view_traits<DataType>::e1 : n1);
+    }
+    value_type &operator()() const { return ptr[0]; }
     value_type &operator()(std::size_t i) const { return ptr[i]; }
     value_type &operator()(std::size_t i, std::size_t j) const { return ptr[i + j * e0]; }
     value_type &operator[](std::size_t i) const { return ptr[i]; }
@@ -161,6 +181,17 @@ std::enable_if_t<std::is_arithmetic_v<T>> parallel_reduce(const std::string &, c
     T s{};
     for (std::size_t i = p.b; i < p.e; ++i) f(i, s);
     result = s;
+}
+
+template <class T, class U>
+void atomic_add(T *p, U v) {
+    *p += v;
+}
+template <class T, class U>
+T atomic_fetch_add(T *p, U v) {
+    const T old = *p;
+    *p += v;
+    return old;
 }
 
 inline void fence() {}
