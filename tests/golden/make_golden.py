@@ -23,7 +23,13 @@ nor the grid generators to reproduce the inputs:
   rectilinear fast-path output (row, col, w, frac and area arrays). These
   come from ``oracle/_ref/libaxisref_fast.so``: the reference's
   weight_generator_{conservative,bilinear}_rect{,_nonuniform}.cpp compiled
-  unchanged through the same shim, with its grid detection and to_csr.
+  unchanged through the same shim, with its grid detection and to_csr;
+* ``generate_<case>.npz``: src/dst meshes, source/destination masks where
+  the case has them, the method and extrapolation, and the output of the
+  reference's whole WeightGenerator::generate (``oracle/_ref/
+  libaxisref_gen.so``: weight_generator.cpp and the solver sources it calls,
+  compiled unchanged, ArborX's queries by exhaustive search) for the
+  nearest-neighbour, general bilinear and masked / coastal paths.
 """
 
 from __future__ import annotations
@@ -40,7 +46,7 @@ for p in (ROOT, os.path.join(ROOT, "helm-project_gb300")):
         sys.path.insert(0, p)
 
 from axgb import grids  # noqa: E402
-from oracle import RefFastLib, RefLib  # noqa: E402
+from oracle import RefFastLib, RefGenLib, RefLib  # noqa: E402
 from oracle import build as obuild  # noqa: E402
 
 CONSERVATIVE = {
@@ -72,6 +78,40 @@ FASTPATH = {
                                   RefFastLib.BIL_REGULAR, "bilinear", 0),
     "bil_rectilinear_ea36x18_to_C6": (lambda: (grids.equal_area_latlon(36, 18, stretch=0.4), grids.cubed_sphere(6)),
                                     RefFastLib.BIL_RECTILINEAR, "bilinear", 0),
+}
+
+
+
+def land_mask(src):
+    """1 = wet: every cell whose centroid lies outside a 30S-40N, 20E-110E box."""
+    c = grids.cell_centroids_xyz(src)
+    lat = np.degrees(np.arcsin(c[:, 2]))
+    lon = np.degrees(np.arctan2(c[:, 1], c[:, 0])) % 360
+    return (~((lat > -30) & (lat < 40) & (lon > 20) & (lon < 110))).astype(np.int32)
+
+
+def dst_mask(dst, seed=22, dry=0.1):
+    return (np.random.default_rng(seed).random(dst.n_cells) > dry).astype(np.int32)
+
+
+# name -> (make, method, source mask?, destination mask?, extrapolation 0 None / 1 NearestWet)
+GENERATE = {
+    "nearest_C12_to_C8": (lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8)), "nearest_neighbor", False, False, 1),
+    "nearest_voronoi642_to_10deg": (lambda: (grids.voronoi(642, seed=5), grids.latlon_deg(10.0)), "nearest_neighbor",
+                                    False, False, 1),
+    "bilinear_C12_to_C8": (lambda: (grids.cubed_sphere(12), grids.cubed_sphere(8)), "bilinear", False, False, 1),
+    "bilinear_tripole48x36_to_10deg": (lambda: (grids.tripole(48, 36, seed=4, jitter=0.1), grids.latlon_deg(10.0)),
+                                       "bilinear", False, False, 1),
+    "cons_5deg_to_C8_srcmask_nearestwet": (lambda: (grids.latlon_deg(5.0), grids.cubed_sphere(8)), "conservative",
+                                           True, False, 1),
+    "cons_C8_to_10deg_srcmask_none": (lambda: (grids.cubed_sphere(8), grids.latlon_deg(10.0)), "conservative",
+                                      True, False, 0),
+    "cons_C8_to_10deg_both_masks": (lambda: (grids.cubed_sphere(8), grids.latlon_deg(10.0)), "conservative", True,
+                                    True, 1),
+    "nearest_5deg_to_C8_srcmask": (lambda: (grids.latlon_deg(5.0), grids.cubed_sphere(8)), "nearest_neighbor", True,
+                                   False, 1),
+    "bilinear_C8_to_10deg_srcmask": (lambda: (grids.cubed_sphere(8), grids.latlon_deg(10.0)), "bilinear", True,
+                                     False, 1),
 }
 
 
@@ -117,6 +157,23 @@ def main():
                             **mesh_dict("dst", dst), method=method, norm_type=norm, row=w.row, col=w.col, w=w.w,
                             frac_a=w.frac_a, frac_b=w.frac_b, area_a=w.area_a, area_b=w.area_b)
         print("fastpath", name, "nnz", w.nnz)
+    if obuild.build_ref_gen() is None:
+        raise SystemExit("the reference checkout is needed to generate the generate() fixtures")
+    gen = RefGenLib()
+    for name, (make, method, smask, dmask, extrap) in GENERATE.items():
+        src, dst = make()
+        sm = land_mask(src) if smask else None
+        dm = dst_mask(dst) if dmask else None
+        w = gen.generate(method, src, dst, extrap=extrap, src_mask=sm, dst_mask=dm)
+        extra = {}
+        if sm is not None:
+            extra["src_mask"] = sm
+        if dm is not None:
+            extra["dst_mask"] = dm
+        np.savez_compressed(os.path.join(HERE, f"generate_{name}.npz"), **mesh_dict("src", src),
+                            **mesh_dict("dst", dst), **extra, method=method, extrap=extrap, row=w.row, col=w.col,
+                            w=w.w, frac_a=w.frac_a, frac_b=w.frac_b, area_a=w.area_a, area_b=w.area_b)
+        print("generate", name, "nnz", w.nnz)
     rng = np.random.default_rng(20240)
     subj, clipp, nsub, ncl, area, nout, outp = [], [], [], [], [], [], []
     for _ in range(200):

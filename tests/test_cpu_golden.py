@@ -8,10 +8,11 @@ from golden_io import cases, load, mesh
 CONS = cases("conservative")
 CELL = cases("cellprep")
 FAST = cases("fastpath")
+GEN = cases("generate")
 
 
 def test_fixtures_present():
-    assert len(CONS) >= 4 and len(CELL) >= 3 and len(FAST) >= 6
+    assert len(CONS) >= 4 and len(CELL) >= 3 and len(FAST) >= 6 and len(GEN) >= 9
 
 
 @pytest.mark.parametrize("name", CONS)
@@ -52,5 +53,33 @@ def test_oracle_fastpath_golden(oracle, name):
         w = oracle.conservative(src, dst, norm_type=int(z["norm_type"]))
     else:
         w = oracle.bilinear(src, dst)
+    for k in ("row", "col", "w", "frac_a", "frac_b", "area_a", "area_b"):
+        assert np.array_equal(getattr(w, k), z[k]), k
+
+
+def oracle_generate(oracle, z, src, dst):
+    """The oracle's composition of one generate() fixture: the method's
+    weights (masked destination rows dropped), then the coastal post-pass
+    when the source has a mask."""
+    method = str(z["method"])
+    sm = np.asarray(z["src_mask"]) if "src_mask" in z else None
+    dm = np.asarray(z["dst_mask"]) if "dst_mask" in z else None
+    if method == "conservative":
+        w = oracle.conservative(src, dst, src_mask=sm, dst_mask=dm)
+    elif method == "bilinear":
+        w = oracle.bilinear(src, dst)
+    else:
+        w = oracle.nearest(src, dst)
+    if sm is not None:
+        w = oracle.coastal(w, src, dst, sm, nearest_wet=bool(int(z["extrap"])))
+    return w
+
+
+@pytest.mark.parametrize("name", GEN)
+def test_oracle_generate_golden(oracle, name):
+    """Nearest-neighbour, general bilinear and masked / coastal weights
+    against the reference's whole WeightGenerator::generate: bit for bit."""
+    z = load("generate", name)
+    w = oracle_generate(oracle, z, mesh(z, "src"), mesh(z, "dst"))
     for k in ("row", "col", "w", "frac_a", "frac_b", "area_a", "area_b"):
         assert np.array_equal(getattr(w, k), z[k]), k

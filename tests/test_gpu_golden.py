@@ -48,6 +48,27 @@ def test_gpu_fastpath_golden(gpu, name):
         assert np.max(np.abs(csr[k] - ref) / np.maximum(np.abs(ref), 1e-300), initial=0.0) < W_RTOL, k
 
 
+@pytest.mark.parametrize("name", cases("generate"))
+def test_gpu_generate_golden(gpu, name):
+    """Nearest-neighbour, general bilinear and masked / coastal weights
+    against the reference's whole WeightGenerator::generate (masks on the
+    meshes, the coastal post-pass inside generate_weights)."""
+    z = load("generate", name)
+    src, dst = mesh(z, "src"), mesh(z, "dst")
+    ms = gpu.Mesh.from_arrays(src.node_lonlat, src.conn_offsets, src.conn_indices,
+                              mask=np.asarray(z["src_mask"]) if "src_mask" in z else None)
+    md = gpu.Mesh.from_arrays(dst.node_lonlat, dst.conn_offsets, dst.conn_indices,
+                              mask=np.asarray(z["dst_mask"]) if "dst_mask" in z else None)
+    cfg = {"method": str(z["method"]), "extrap_method": ("none", "nearest_wet")[int(z["extrap"])]}
+    csr = gpu.generate_weights(ms, md, cfg).to_csr()
+    rows = np.repeat(np.arange(len(csr["row_ptr"]) - 1), np.diff(csr["row_ptr"]))
+    assert np.array_equal(rows, z["row"]) and np.array_equal(csr["col"], z["col"])
+    assert np.max(np.abs(csr["val"] - z["w"]) / np.abs(z["w"]), initial=0.0) < W_RTOL
+    for k in ("frac_a", "frac_b", "area_a", "area_b"):
+        ref = z[k]
+        assert np.max(np.abs(csr[k] - ref) / np.maximum(np.abs(ref), 1e-300), initial=0.0) < W_RTOL, k
+
+
 @pytest.mark.parametrize("name", cases("cellprep"))
 def test_gpu_cellprep_golden(gpu, name):
     z = load("cellprep", name)
