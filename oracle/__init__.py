@@ -474,3 +474,43 @@ class RefGenLib:
             raise RuntimeError("reference generate: output above capacity")
         n = nnz.value
         return Weights(src.n_cells, dst.n_cells, row[:n].copy(), col[:n].copy(), w[:n].copy(), fa, fb, aa, ab)
+
+
+class RefApplyLib:
+    """The reference's NaN-aware batch apply and masked apply
+    (include/axis/solver/apply.hpp, team-policy CSR paths) compiled through
+    the shims (oracle/_ref/libaxisref_apply.so, oracle/ref_apply.cpp). Same
+    calling conventions as Oracle.nan_batch_apply / Oracle.apply_masked."""
+
+    def __init__(self, path: str | None = None):
+        if path is None:
+            path = os.path.join(HERE, "_ref", "libaxisref_apply.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = C.CDLL(path)
+        csr = [C.c_int64, C.c_int64, C.c_int64, _i64p, _i64p, _f64p]
+        L.ref_nan_batch_apply.argtypes = csr + [_f64p, _f64p, C.c_int64, C.c_double]
+        L.ref_nan_batch_apply.restype = C.c_int
+        L.ref_apply_masked.argtypes = csr + [_f64p, _f64p, C.c_void_p]
+        L.ref_apply_masked.restype = C.c_int
+        self.L = L
+
+    def _csr(self, wts: Weights):
+        return (wts.n_src, wts.n_dst, wts.nnz, np.ascontiguousarray(wts.row), np.ascontiguousarray(wts.col),
+                np.ascontiguousarray(wts.w))
+
+    def nan_batch_apply(self, wts: Weights, x, na_thres: float):
+        """x: [nrhs, n_src] (each field contiguous = LayoutLeft [n_src, nrhs]); returns [nrhs, n_dst]."""
+        x = np.ascontiguousarray(np.atleast_2d(x), np.float64)
+        y = np.zeros((x.shape[0], wts.n_dst))
+        if self.L.ref_nan_batch_apply(*self._csr(wts), x.reshape(-1), y.reshape(-1), x.shape[0], float(na_thres)):
+            raise RuntimeError("reference nan_batch_apply threw")
+        return y
+
+    def apply_masked(self, wts: Weights, x, mask, y0):
+        y = np.array(y0, np.float64, copy=True)
+        m = np.ascontiguousarray(mask, np.int32)
+        if self.L.ref_apply_masked(*self._csr(wts), np.ascontiguousarray(x, np.float64), y,
+                                   m.ctypes.data_as(C.c_void_p)):
+            raise RuntimeError("reference masked apply threw")
+        return y

@@ -13,6 +13,9 @@
   unchanged the same way, ArborX replaced by the exhaustive search of
   ``ref_shim/ArborX.hpp``, with ``ref_generate.cpp``; also only where the
   checkout exists.
+* ``oracle/_ref/libaxisref_apply.so`` the reference's NaN-aware and masked
+  applies (include/axis/solver/apply.hpp, header-only) compiled unchanged the
+  same way, with ``ref_apply.cpp``; also only where the checkout exists.
 
 Both use ``-O2 -ffp-contract=off`` so double expressions are evaluated as
 written, like the reference's host build.
@@ -83,7 +86,8 @@ def build_ref_fast(force: bool = False) -> str | None:
 
 GEN_SOURCES = ["weight_generator.cpp", *FAST_SOURCES, "gradient_reconstructor.cpp", "halo_pattern.cpp",
                "interpolation_matrix.cpp"]
-SHIM_HEADERS = ["Kokkos_Core.hpp", "KokkosSparse_CrsMatrix.hpp", "Kokkos_UnorderedMap.hpp", "ArborX.hpp"]
+SHIM_HEADERS = ["Kokkos_Core.hpp", "KokkosSparse_CrsMatrix.hpp", "KokkosSparse_spmv.hpp", "Kokkos_UnorderedMap.hpp",
+                "ArborX.hpp"]
 
 
 def build_ref_gen(force: bool = False) -> str | None:
@@ -103,9 +107,29 @@ def build_ref_gen(force: bool = False) -> str | None:
     return out
 
 
+def build_ref_apply(force: bool = False) -> str | None:
+    """oracle/_ref/libaxisref_apply.so: nan_batch_apply and the masked apply
+    of the reference's apply.hpp, with ref_apply.cpp."""
+    if not os.path.isdir(REF_SRC):
+        return None
+    shim = os.path.join(HERE, "ref_shim")
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libaxisref_apply.so")
+    srcs = [os.path.join(HERE, "ref_apply.cpp")] + [os.path.join(REF_SRC, f) for f in
+                                                     ("halo_pattern.cpp", "interpolation_matrix.cpp")]
+    deps = srcs + [os.path.join(shim, f) for f in SHIM_HEADERS] + [os.path.join(REF_INCLUDE, "axis", "solver",
+                                                                               "apply.hpp")]
+    if force or _needs(out, deps):
+        subprocess.check_call(["g++", *[f for f in FLAGS if f != "-fopenmp"], "-Wl,--no-undefined", "-I", shim,
+                               "-I", REF_INCLUDE, *srcs, "-o", out])
+    return out
+
+
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref(force))
     print(build_ref_fast(force))
     print(build_ref_gen(force))
+    print(build_ref_apply(force))

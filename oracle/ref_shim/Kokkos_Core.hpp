@@ -183,6 +183,58 @@ std::enable_if_t<std::is_arithmetic_v<T>> parallel_reduce(const std::string &, c
     result = s;
 }
 
+// Hierarchical parallelism as a host backend runs it: one thread per team,
+// vector length 1, so every nested range runs in order.
+constexpr int AUTO = -1;
+struct TeamMember {
+    int rank;
+    int league_rank() const { return rank; }
+    int team_rank() const { return 0; }
+    int team_size() const { return 1; }
+};
+template <class ExecSpace = Serial>
+struct TeamPolicy {
+    using member_type = TeamMember;
+    int league;
+    TeamPolicy(int league_size, int) : league(league_size) {}
+};
+template <class I>
+struct NestedRange {
+    I b, e;
+};
+template <class I>
+NestedRange<I> ThreadVectorRange(const TeamMember &, I n) {
+    return {I(0), n};
+}
+template <class I>
+NestedRange<I> TeamThreadRange(const TeamMember &, I n) {
+    return {I(0), n};
+}
+template <class I, class J>
+NestedRange<std::common_type_t<I, J>> TeamVectorRange(const TeamMember &, I b, J e) {
+    return {static_cast<std::common_type_t<I, J>>(b), static_cast<std::common_type_t<I, J>>(e)};
+}
+template <class E, class F>
+void parallel_for(const std::string &, const TeamPolicy<E> &p, F f) {
+    for (int t = 0; t < p.league; ++t) f(TeamMember{t});
+}
+template <class I, class F>
+void parallel_for(const NestedRange<I> &r, F f) {
+    for (I i = r.b; i < r.e; ++i) f(i);
+}
+template <class I, class F, class T>
+void parallel_reduce(const NestedRange<I> &r, F f, T &result) {
+    T s{};
+    for (I i = r.b; i < r.e; ++i) f(i, s);
+    result = s;
+}
+struct PerTeamTag {};
+inline PerTeamTag PerTeam(const TeamMember &) { return {}; }
+template <class F>
+void single(PerTeamTag, F f) {
+    f();
+}
+
 template <class T, class U>
 void atomic_add(T *p, U v) {
     *p += v;

@@ -29,7 +29,11 @@ nor the grid generators to reproduce the inputs:
   reference's whole WeightGenerator::generate (``oracle/_ref/
   libaxisref_gen.so``: weight_generator.cpp and the solver sources it calls,
   compiled unchanged, ArborX's queries by exhaustive search) for the
-  nearest-neighbour, general bilinear and masked / coastal paths.
+  nearest-neighbour, general bilinear and masked / coastal paths;
+* ``apply_nan_masked.npz``: a CSR matrix (the 5 deg -> C8 conservative
+  fixture's), fields with NaNs and the reference's own nan_batch_apply at
+  four thresholds, and a masked apply (``oracle/_ref/libaxisref_apply.so``:
+  include/axis/solver/apply.hpp compiled unchanged through the shim).
 """
 
 from __future__ import annotations
@@ -46,7 +50,7 @@ for p in (ROOT, os.path.join(ROOT, "helm-project_gb300")):
         sys.path.insert(0, p)
 
 from axgb import grids  # noqa: E402
-from oracle import RefFastLib, RefGenLib, RefLib  # noqa: E402
+from oracle import RefApplyLib, RefFastLib, RefGenLib, RefLib, Weights  # noqa: E402
 from oracle import build as obuild  # noqa: E402
 
 CONSERVATIVE = {
@@ -174,6 +178,26 @@ def main():
                             **mesh_dict("dst", dst), **extra, method=method, extrap=extrap, row=w.row, col=w.col,
                             w=w.w, frac_a=w.frac_a, frac_b=w.frac_b, area_a=w.area_a, area_b=w.area_b)
         print("generate", name, "nnz", w.nnz)
+    if obuild.build_ref_apply() is None:
+        raise SystemExit("the reference checkout is needed to generate the apply fixture")
+    app = RefApplyLib()
+    z = np.load(os.path.join(HERE, "conservative_5deg_to_C8.npz"))
+    n_src, n_dst = len(z["frac_a"]), len(z["frac_b"])
+    w = Weights(n_src, n_dst, z["row"], z["col"], z["w"], z["frac_a"], z["frac_b"], z["area_a"], z["area_b"])
+    rng = np.random.default_rng(31)
+    x = rng.standard_normal((6, n_src)) + 280.0
+    for v, p in enumerate((0.0, 0.05, 0.3, 0.6, 0.9, 1.0)):
+        x[v, rng.uniform(size=n_src) < p] = np.nan
+    thres = np.array([0.0, 0.25, 0.5, 1.0])
+    y_nan = np.stack([app.nan_batch_apply(w, x, t) for t in thres])
+    xm = rng.standard_normal(n_src) + 280.0
+    mask = (np.arange(n_dst) % 5 != 1).astype(np.int32)
+    y0 = np.full(n_dst, -3.0)
+    y_masked = app.apply_masked(w, xm, mask, y0)
+    np.savez_compressed(os.path.join(HERE, "apply_nan_masked.npz"), n_src=n_src, n_dst=n_dst,
+                        row_ptr=w.row_ptr(), col=w.col, val=w.w, x=x, thres=thres, y_nan=y_nan, x_masked=xm,
+                        mask=mask, y0=y0, y_masked=y_masked)
+    print("apply fixture: NaN outputs", int(np.isnan(y_nan).sum()))
     rng = np.random.default_rng(20240)
     subj, clipp, nsub, ncl, area, nout, outp = [], [], [], [], [], [], []
     for _ in range(200):

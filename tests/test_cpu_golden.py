@@ -83,3 +83,17 @@ def test_oracle_generate_golden(oracle, name):
     w = oracle_generate(oracle, z, mesh(z, "src"), mesh(z, "dst"))
     for k in ("row", "col", "w", "frac_a", "frac_b", "area_a", "area_b"):
         assert np.array_equal(getattr(w, k), z[k]), k
+
+
+def test_oracle_apply_golden(oracle):
+    """NaN-aware batch apply and masked apply against the reference's own
+    apply.hpp loops on the same CSR matrix: bit for bit, NaN positions
+    included."""
+    from oracle import Weights
+    z = load("apply_nan_masked")
+    n_src, n_dst = int(z["n_src"]), int(z["n_dst"])
+    row = np.repeat(np.arange(n_dst), np.diff(z["row_ptr"]))
+    w = Weights(n_src, n_dst, row, z["col"], z["val"], None, None, None, None)
+    for t, ref in zip(z["thres"], z["y_nan"]):
+        np.testing.assert_array_equal(oracle.nan_batch_apply(w, z["x"], float(t)), ref)
+    np.testing.assert_array_equal(oracle.apply_masked(w, z["x_masked"], z["mask"], z["y0"]), z["y_masked"])

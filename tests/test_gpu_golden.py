@@ -70,6 +70,24 @@ def test_gpu_generate_golden(gpu, name):
         assert np.max(np.abs(csr[k] - ref) / np.maximum(np.abs(ref), 1e-300), initial=0.0) < W_RTOL, k
 
 
+def test_gpu_apply_golden(gpu):
+    """NaN-aware batch apply (device and host entry points) and masked apply
+    against the reference's own apply.hpp loops on the same CSR matrix: bit
+    for bit, NaN positions included."""
+    import torch
+    z = load("apply_nan_masked")
+    M = gpu.Matrix.from_csr(int(z["n_src"]), int(z["n_dst"]), z["row_ptr"], z["col"], z["val"])
+    X = np.asarray(z["x"])
+    for t, ref in zip(z["thres"], z["y_nan"]):
+        got = gpu.nan_apply_f64(M, torch.tensor(X, device="cuda"), float(t)).cpu().numpy()
+        np.testing.assert_array_equal(got, ref)
+        np.testing.assert_array_equal(gpu.nan_batch_apply(M, X.T, float(t)), ref.T)
+    y = torch.tensor(np.asarray(z["y0"]), device="cuda")
+    gpu.apply_masked(M, torch.tensor(np.asarray(z["x_masked"]), device="cuda"), y,
+                     torch.tensor(np.asarray(z["mask"]), device="cuda"))
+    np.testing.assert_array_equal(y.cpu().numpy(), z["y_masked"])
+
+
 @pytest.mark.parametrize("name", cases("cellprep"))
 def test_gpu_cellprep_golden(gpu, name):
     z = load("cellprep", name)
