@@ -514,3 +514,22 @@ class RefApplyLib:
                                    m.ctypes.data_as(C.c_void_p)):
             raise RuntimeError("reference masked apply threw")
         return y
+
+
+def ref_cache_blob(lib: RefApplyLib, n_src, n_dst, row, col, val, frac_a, frac_b, area_a, area_b) -> bytes:
+    """The reference's WeightCache::serialize blob of a COO matrix (entries in
+    the given order) with its frac/area arrays."""
+    L = lib.L
+    L.ref_cache_serialize.argtypes = [C.c_int64, C.c_int64, C.c_int64, _i64p, _i64p, _f64p, _f64p, _f64p, _f64p,
+                                      _f64p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
+    L.ref_cache_serialize.restype = C.c_int
+    arrs = [np.ascontiguousarray(a, dt) for a, dt in ((row, np.int64), (col, np.int64), (val, np.float64),
+                                                      (frac_a, np.float64), (frac_b, np.float64),
+                                                      (area_a, np.float64), (area_b, np.float64))]
+    size = C.c_int64(0)
+    if L.ref_cache_serialize(n_src, n_dst, len(arrs[2]), *arrs, None, 0, C.byref(size)):
+        raise RuntimeError("reference serialize failed")
+    buf = C.create_string_buffer(size.value)
+    if L.ref_cache_serialize(n_src, n_dst, len(arrs[2]), *arrs, buf, size.value, C.byref(size)):
+        raise RuntimeError("reference serialize failed")
+    return buf.raw

@@ -1,8 +1,11 @@
-// Driver that runs the reference's OWN NaN-aware batch apply and masked
-// apply (AXIS include/axis/solver/apply.hpp:349-413 and :441-520, the CSR
-// team-policy paths, compiled unchanged through the host shims in ref_shim/)
-// on a CSR matrix built by the reference's InterpolationMatrix::to_csr, so
-// that the oracle's restatements of those loops are pinned bit for bit.
+// Driver that runs the reference's OWN header-only solver code, compiled
+// unchanged through the host shims in ref_shim/: the NaN-aware batch apply
+// and masked apply (AXIS include/axis/solver/apply.hpp:349-413 and
+// :441-520, the CSR team-policy paths) on a CSR matrix built by the
+// reference's InterpolationMatrix::to_csr, so that the oracle's restatements
+// of those loops are pinned bit for bit; and WeightCache::serialize
+// (include/axis/solver/weight_cache.hpp:76-139), whose blob pins the device
+// library's weight-cache writer and reader byte for byte.
 //
 // TEST INFRASTRUCTURE ONLY: built by oracle/build.py into
 // oracle/_ref/libaxisref_apply.so when the reference checkout exists, and
@@ -11,6 +14,7 @@
 #include <Kokkos_Core.hpp>
 #include <axis/solver/apply.hpp>
 #include <axis/solver/interpolation_matrix.hpp>
+#include <axis/solver/weight_cache.hpp>
 #include <cstdint>
 #include <stdexcept>
 
@@ -20,7 +24,8 @@ using i64 = std::int64_t;
 
 namespace {
 
-IM make_matrix(i64 n_src, i64 n_dst, i64 nnz, const i64 *row, const i64 *col, const double *val) {
+IM make_coo(i64 n_src, i64 n_dst, i64 nnz, const i64 *row, const i64 *col, const double *val, const double *pfa,
+             const double *pfb, const double *paa, const double *pab) {
     Kokkos::View<double *, HS> w("w", nnz), fa("fa", n_src), fb("fb", n_dst), aa("aa", n_src), ab("ab", n_dst);
     Kokkos::View<axis::index_t *, HS> r("r", nnz), c("c", nnz);
     for (i64 k = 0; k < nnz; ++k) {
@@ -28,7 +33,19 @@ IM make_matrix(i64 n_src, i64 n_dst, i64 nnz, const i64 *row, const i64 *col, co
         r(k) = row[k];
         c(k) = col[k];
     }
-    IM m(w, r, c, fa, fb, aa, ab, static_cast<std::size_t>(n_src), static_cast<std::size_t>(n_dst));
+    for (i64 i = 0; i < n_src; ++i) {
+        fa(i) = pfa ? pfa[i] : 0.0;
+        aa(i) = paa ? paa[i] : 0.0;
+    }
+    for (i64 j = 0; j < n_dst; ++j) {
+        fb(j) = pfb ? pfb[j] : 0.0;
+        ab(j) = pab ? pab[j] : 0.0;
+    }
+    return IM(w, r, c, fa, fb, aa, ab, static_cast<std::size_t>(n_src), static_cast<std::size_t>(n_dst));
+}
+
+IM make_matrix(i64 n_src, i64 n_dst, i64 nnz, const i64 *row, const i64 *col, const double *val) {
+    IM m = make_coo(n_src, n_dst, nnz, row, col, val, nullptr, nullptr, nullptr, nullptr);
     m.to_csr();
     return m;
 }
@@ -62,6 +79,21 @@ int ref_apply_masked(i64 n_src, i64 n_dst, i64 nnz, const i64 *row, const i64 *c
         axis::field_view<double, 1> dst(y, static_cast<std::size_t>(n_dst));
         axis::field_view<const int, 1> msk(mask, static_cast<std::size_t>(n_dst));
         axis::solver::apply<HS>(m, src, dst, msk);
+    } catch (const std::exception &) {
+        return -3;
+    }
+    return 0;
+}
+
+// WeightCache::serialize of the COO matrix (row, col, val in the given
+// order) with its frac/area arrays. Query with buf = null: *size receives
+// the blob size. Returns 0, or -3 when it threw (buffer too small).
+int ref_cache_serialize(i64 n_src, i64 n_dst, i64 nnz, const i64 *row, const i64 *col, const double *val,
+                        const double *fa, const double *fb, const double *aa, const double *ab, unsigned char *buf,
+                        i64 cap, i64 *size) {
+    try {
+        IM m = make_coo(n_src, n_dst, nnz, row, col, val, fa, fb, aa, ab);
+        *size = static_cast<i64>(axis::solver::WeightCache::serialize(m, buf, static_cast<std::size_t>(cap)));
     } catch (const std::exception &) {
         return -3;
     }

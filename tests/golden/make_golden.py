@@ -33,7 +33,10 @@ nor the grid generators to reproduce the inputs:
 * ``apply_nan_masked.npz``: a CSR matrix (the 5 deg -> C8 conservative
   fixture's), fields with NaNs and the reference's own nan_batch_apply at
   four thresholds, and a masked apply (``oracle/_ref/libaxisref_apply.so``:
-  include/axis/solver/apply.hpp compiled unchanged through the shim).
+  include/axis/solver/apply.hpp compiled unchanged through the shim);
+* ``weight_cache_5deg_to_C8.npz``: the reference's own WeightCache::serialize
+  blob (as bytes) (include/axis/solver/weight_cache.hpp, same library) of the 5 deg ->
+  C8 conservative fixture's matrix, entries in CSR order.
 """
 
 from __future__ import annotations
@@ -50,7 +53,7 @@ for p in (ROOT, os.path.join(ROOT, "helm-project_gb300")):
         sys.path.insert(0, p)
 
 from axgb import grids  # noqa: E402
-from oracle import RefApplyLib, RefFastLib, RefGenLib, RefLib, Weights  # noqa: E402
+from oracle import RefApplyLib, RefFastLib, RefGenLib, RefLib, Weights, ref_cache_blob  # noqa: E402
 from oracle import build as obuild  # noqa: E402
 
 CONSERVATIVE = {
@@ -198,6 +201,10 @@ def main():
                         row_ptr=w.row_ptr(), col=w.col, val=w.w, x=x, thres=thres, y_nan=y_nan, x_masked=xm,
                         mask=mask, y0=y0, y_masked=y_masked)
     print("apply fixture: NaN outputs", int(np.isnan(y_nan).sum()))
+    blob = ref_cache_blob(app, n_src, n_dst, z["row"], z["col"], z["w"], z["frac_a"], z["frac_b"], z["area_a"],
+                          z["area_b"])
+    np.savez_compressed(os.path.join(HERE, "weight_cache_5deg_to_C8.npz"), blob=np.frombuffer(blob, np.uint8))
+    print("weight cache blob", len(blob), "bytes")
     rng = np.random.default_rng(20240)
     subj, clipp, nsub, ncl, area, nout, outp = [], [], [], [], [], [], []
     for _ in range(200):

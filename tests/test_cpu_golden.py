@@ -97,3 +97,31 @@ def test_oracle_apply_golden(oracle):
     for t, ref in zip(z["thres"], z["y_nan"]):
         np.testing.assert_array_equal(oracle.nan_batch_apply(w, z["x"], float(t)), ref)
     np.testing.assert_array_equal(oracle.apply_masked(w, z["x_masked"], z["mask"], z["y0"]), z["y_masked"])
+
+
+def test_weight_cache_blob_golden():
+    """The reference's WeightCache blob of the 5 deg -> C8 matrix read with
+    the layout of weight_cache.hpp:14-26 (40-byte header, then w, row, col,
+    frac_a, frac_b, area_a, area_b): the same arrays as the weight fixture.
+    Where the reference checkout exists, its serializer re-makes the blob
+    byte for byte."""
+    import struct
+    blob = load("weight_cache", "5deg_to_C8")["blob"].tobytes()
+    z = load("conservative", "5deg_to_C8")
+    magic, version, endian = struct.unpack_from("<IIB", blob, 0)
+    assert (magic, version, endian) == (0x43574841, 1, 1) and blob[9:16] == bytes(7)
+    ns, nd, nz = struct.unpack_from("<QQQ", blob, 16)
+    assert (ns, nd, nz) == (len(z["frac_a"]), len(z["frac_b"]), len(z["w"]))
+    off = 40
+    for name, n, dt in (("w", nz, "<f8"), ("row", nz, "<i8"), ("col", nz, "<i8"), ("frac_a", ns, "<f8"),
+                        ("frac_b", nd, "<f8"), ("area_a", ns, "<f8"), ("area_b", nd, "<f8")):
+        assert np.array_equal(np.frombuffer(blob, dtype=dt, count=n, offset=off), z[name]), name
+        off += 8 * n
+    assert off == len(blob)
+    try:
+        from oracle import RefApplyLib, ref_cache_blob
+        lib = RefApplyLib()
+    except FileNotFoundError:
+        return
+    assert ref_cache_blob(lib, ns, nd, z["row"], z["col"], z["w"], z["frac_a"], z["frac_b"], z["area_a"],
+                          z["area_b"]) == blob

@@ -88,6 +88,23 @@ def test_gpu_apply_golden(gpu):
     np.testing.assert_array_equal(y.cpu().numpy(), z["y_masked"])
 
 
+def test_gpu_weight_cache_golden(gpu):
+    """The reference's own WeightCache blob: the device library reads it into
+    the fixture's CSR arrays, and writes the same matrix back byte for byte."""
+    blob = load("weight_cache", "5deg_to_C8")["blob"].tobytes()
+    z = load("conservative", "5deg_to_C8")
+    n_src, n_dst = len(z["frac_a"]), len(z["frac_b"])
+    csr = gpu.Matrix.deserialize(blob).to_csr()
+    rows = np.repeat(np.arange(n_dst), np.diff(csr["row_ptr"]))
+    assert np.array_equal(rows, z["row"]) and np.array_equal(csr["col"], z["col"])
+    assert np.array_equal(csr["val"], z["w"])
+    for k in ("frac_a", "frac_b", "area_a", "area_b"):
+        assert np.array_equal(csr[k], z[k]), k
+    rp = np.concatenate([[0], np.cumsum(np.bincount(z["row"], minlength=n_dst))])
+    M = gpu.Matrix.from_csr(n_src, n_dst, rp, z["col"], z["w"], z["frac_a"], z["frac_b"], z["area_a"], z["area_b"])
+    assert M.serialize() == blob
+
+
 @pytest.mark.parametrize("name", cases("cellprep"))
 def test_gpu_cellprep_golden(gpu, name):
     z = load("cellprep", name)
