@@ -507,6 +507,19 @@ class RefApplyLib:
             raise RuntimeError("reference nan_batch_apply threw")
         return y
 
+    def conservation(self, wts: Weights, src, dst, norm_type: int = 0):
+        """check_conservation (src/solver/conservation.cpp); same keys as
+        Oracle.conservation."""
+        L = self.L
+        L.ref_conservation.argtypes = [C.c_int64, _f64p, _f64p, _f64p, C.c_int64, _f64p, _f64p, _f64p, C.c_int,
+                                       _f64p]
+        L.ref_conservation.restype = C.c_int
+        out = np.zeros(4)
+        f = [np.ascontiguousarray(a, np.float64) for a in (src, wts.area_a, wts.frac_a, dst, wts.area_b, wts.frac_b)]
+        if L.ref_conservation(wts.n_src, f[0], f[1], f[2], wts.n_dst, f[3], f[4], f[5], norm_type, out):
+            raise RuntimeError("reference check_conservation threw")
+        return dict(src_integral=out[0], dst_integral=out[1], absolute_error=out[2], relative_error=out[3])
+
     def apply_masked(self, wts: Weights, x, mask, y0):
         y = np.array(y0, np.float64, copy=True)
         m = np.ascontiguousarray(mask, np.int32)

@@ -14,9 +14,10 @@
   ``ref_shim/ArborX.hpp``, with ``ref_generate.cpp``; also only where the
   checkout exists.
 * ``oracle/_ref/libaxisref_apply.so`` the reference's NaN-aware and masked
-  applies (include/axis/solver/apply.hpp) and weight-cache serializer
-  (weight_cache.hpp), header-only, compiled unchanged the same way, with
-  ``ref_apply.cpp``; also only where the checkout exists.
+  applies (include/axis/solver/apply.hpp), weight-cache serializer
+  (weight_cache.hpp) and conservation report (src/solver/conservation.cpp),
+  compiled unchanged the same way, with ``ref_apply.cpp``; also only where
+  the checkout exists.
 
 Both use ``-O2 -ffp-contract=off`` so double expressions are evaluated as
 written, like the reference's host build.
@@ -110,8 +111,8 @@ def build_ref_gen(force: bool = False) -> str | None:
 
 def build_ref_apply(force: bool = False) -> str | None:
     """oracle/_ref/libaxisref_apply.so: nan_batch_apply and the masked apply
-    of the reference's apply.hpp and its WeightCache::serialize, with
-    ref_apply.cpp."""
+    of the reference's apply.hpp, its WeightCache::serialize and
+    check_conservation (conservation.cpp), with ref_apply.cpp."""
     if not os.path.isdir(REF_SRC):
         return None
     shim = os.path.join(HERE, "ref_shim")
@@ -119,7 +120,8 @@ def build_ref_apply(force: bool = False) -> str | None:
     os.makedirs(outdir, exist_ok=True)
     out = os.path.join(outdir, "libaxisref_apply.so")
     srcs = [os.path.join(HERE, "ref_apply.cpp")] + [os.path.join(REF_SRC, f) for f in
-                                                     ("halo_pattern.cpp", "interpolation_matrix.cpp")]
+                                                     ("halo_pattern.cpp", "interpolation_matrix.cpp",
+                                                      "conservation.cpp")]
     solver_inc = os.path.join(REF_INCLUDE, "axis", "solver")
     deps = (srcs + [os.path.join(shim, f) for f in SHIM_HEADERS] +
             [os.path.join(solver_inc, f) for f in ("apply.hpp", "weight_cache.hpp")])

@@ -3,9 +3,11 @@
 // and masked apply (AXIS include/axis/solver/apply.hpp:349-413 and
 // :441-520, the CSR team-policy paths) on a CSR matrix built by the
 // reference's InterpolationMatrix::to_csr, so that the oracle's restatements
-// of those loops are pinned bit for bit; and WeightCache::serialize
+// of those loops are pinned bit for bit; WeightCache::serialize
 // (include/axis/solver/weight_cache.hpp:76-139), whose blob pins the device
-// library's weight-cache writer and reader byte for byte.
+// library's weight-cache writer and reader byte for byte; and
+// check_conservation (src/solver/conservation.cpp, its reductions run in
+// index order by the shim).
 //
 // TEST INFRASTRUCTURE ONLY: built by oracle/build.py into
 // oracle/_ref/libaxisref_apply.so when the reference checkout exists, and
@@ -13,6 +15,7 @@
 
 #include <Kokkos_Core.hpp>
 #include <axis/solver/apply.hpp>
+#include <axis/solver/conservation.hpp>
 #include <axis/solver/interpolation_matrix.hpp>
 #include <axis/solver/weight_cache.hpp>
 #include <cstdint>
@@ -79,6 +82,29 @@ int ref_apply_masked(i64 n_src, i64 n_dst, i64 nnz, const i64 *row, const i64 *c
         axis::field_view<double, 1> dst(y, static_cast<std::size_t>(n_dst));
         axis::field_view<const int, 1> msk(mask, static_cast<std::size_t>(n_dst));
         axis::solver::apply<HS>(m, src, dst, msk);
+    } catch (const std::exception &) {
+        return -3;
+    }
+    return 0;
+}
+
+// check_conservation (src/solver/conservation.cpp) for a matrix's frac/area
+// arrays and one source and destination field; norm_type 0 DstArea,
+// 1 FracArea. out = (src_integral, dst_integral, absolute_error,
+// relative_error). Returns 0, or -3 when it threw.
+int ref_conservation(i64 n_src, const double *src, const double *area_a, const double *frac_a, i64 n_dst,
+                     const double *dst, const double *area_b, const double *frac_b, int norm_type, double *out) {
+    try {
+        const i64 zero = 0;
+        IM m = make_coo(n_src, n_dst, 0, &zero, &zero, nullptr, frac_a, frac_b, area_a, area_b);
+        axis::field_view<const double, 1> s(src, static_cast<std::size_t>(n_src));
+        axis::field_view<const double, 1> d(dst, static_cast<std::size_t>(n_dst));
+        auto r = axis::solver::check_conservation<HS>(
+            s, d, m, norm_type ? axis::solver::NormType::FracArea : axis::solver::NormType::DstArea);
+        out[0] = r.src_integral;
+        out[1] = r.dst_integral;
+        out[2] = r.absolute_error;
+        out[3] = r.relative_error;
     } catch (const std::exception &) {
         return -3;
     }

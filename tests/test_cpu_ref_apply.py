@@ -1,9 +1,9 @@
-"""Pins the oracle's NaN-aware batch apply and masked apply against the
-reference's own loops (include/axis/solver/apply.hpp, the team-policy CSR
-paths of nan_batch_apply and the masked apply), compiled unchanged by
-oracle/build.py into oracle/_ref/libaxisref_apply.so. Bit for bit, NaN
-positions included. Skipped where the reference checkout (and so that
-library) is absent."""
+"""Pins the oracle's NaN-aware batch apply, masked apply and conservation
+report against the reference's own code (include/axis/solver/apply.hpp, the
+team-policy CSR paths of nan_batch_apply and the masked apply, and
+src/solver/conservation.cpp), compiled unchanged by oracle/build.py into
+oracle/_ref/libaxisref_apply.so. Bit for bit, NaN positions included.
+Skipped where the reference checkout (and so that library) is absent."""
 import numpy as np
 import pytest
 
@@ -44,3 +44,13 @@ def test_masked_apply_pinned(ref, oracle, i):
     for mask in ((rng.random(w.n_dst) > 0.3).astype(np.int32), np.ones(w.n_dst, np.int32),
                  np.zeros(w.n_dst, np.int32)):
         np.testing.assert_array_equal(ref.apply_masked(w, x, mask, y0), oracle.apply_masked(w, x, mask, y0))
+
+
+@pytest.mark.parametrize("i", range(len(PAIRS)))
+@pytest.mark.parametrize("norm", [0, 1])
+def test_conservation_report_pinned(ref, oracle, i, norm):
+    w = oracle.conservative(*PAIRS[i], norm_type=norm)
+    rng = np.random.default_rng(60 + i)
+    x = rng.standard_normal(w.n_src) * 50.0 + 280.0
+    y = oracle.apply_csr(w, x, compensated=False)[0]
+    assert ref.conservation(w, x, y, norm) == oracle.conservation(w, x, y, norm)
