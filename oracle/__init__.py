@@ -40,7 +40,7 @@ class Weights:
         self.stats = stats or {}
         self.seconds = seconds
         # per entry, its place in its row's generation order where that is
-        # not column order (general bilinear), else None
+        # not column order (fast paths, general bilinear), else None
         self.gen = None
 
     @property

@@ -587,8 +587,9 @@ std::vector<i64> morton_order(const Mesh &m) {
 struct orc_result {
     i64 n_src = 0, n_dst = 0;
     std::vector<i64> row, col;  // CSR order: sorted by (row, col)
-    // Per CSR entry, its place in its row's generation (COO) order where
-    // that differs from column order (general bilinear); empty otherwise.
+    // Per CSR entry, its place in its row's generation (COO) order (the
+    // fast paths and general bilinear, whose rows are not emitted in column
+    // order); empty where the order is the column order (the clipper path).
     std::vector<i64> gen;
     std::vector<double> w, frac_a, frac_b, area_a, area_b;
     i64 n_box_pairs = 0, n_cap_pass = 0, n_clipped = 0;
@@ -686,10 +687,11 @@ static bool conservative_rect(const Mesh &S, const Mesh &D, const GridInfo &sg, 
     });
     res->n_src = n_src;
     res->n_dst = n_dst;
-    for (size_t q : perm) {
+    for (size_t q : perm) {  // q: the entry's place in generation order
         res->row.push_back(rows[q]);
         res->col.push_back(cols[q]);
         res->w.push_back(w[q]);
+        res->gen.push_back(static_cast<i64>(q));
     }
     res->frac_a = fa;
     res->frac_b = fb;
@@ -791,10 +793,11 @@ static void conservative_rect_nu(const Mesh &S, const Mesh &D, const GridInfo &s
     });
     res->n_src = n_src;
     res->n_dst = n_dst;
-    for (size_t q : perm) {
+    for (size_t q : perm) {  // q: the entry's place in generation order
         res->row.push_back(rows[q]);
         res->col.push_back(cols[q]);
         res->w.push_back(w[q]);
+        res->gen.push_back(static_cast<i64>(q));
     }
     res->frac_a = fa;
     res->frac_b = fb;
@@ -865,6 +868,7 @@ static bool bilinear_regular(const Mesh &S, const Mesh &D, const GridInfo &sg, i
             res->row.push_back(c);
             res->col.push_back(src[ordk[k]]);
             res->w.push_back(w[ordk[k]]);
+            res->gen.push_back(ordk[k]);  // the corner's place in the emission order
         }
         res->frac_b[c] = 1.0;
     }
@@ -1468,6 +1472,7 @@ int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *s
     res->row.resize(4 * dn_cells);
     res->col.resize(4 * dn_cells);
     res->w.resize(4 * dn_cells);
+    res->gen.resize(4 * dn_cells);
 #pragma omp parallel for schedule(static)
     for (i64 c = 0; c < dn_cells; ++c) {
         i64 b = D.off[c], e = D.off[c + 1];
@@ -1500,6 +1505,7 @@ int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *s
             res->row[4 * c + k] = c;
             res->col[4 * c + k] = src[ordk[k]];
             res->w[4 * c + k] = w[ordk[k]];
+            res->gen[4 * c + k] = ordk[k];
         }
     }
     res->frac_a.assign(sn_cells, 1.0);

@@ -20,6 +20,12 @@ PAIRS = {
     "equal-area->10deg": lambda: (grids.equal_area_latlon(36, 18, stretch=0.4), grids.latlon_deg(10.0)),
     "voronoi->10deg": lambda: (grids.voronoi(642, seed=5), grids.latlon_deg(10.0)),
     "C8->voronoi": lambda: (grids.cubed_sphere(8), grids.voronoi(642, seed=5)),
+    "regional->C8": lambda: (grids.regular_latlon(20, 15, 20.0, -10.0, 2.0, 2.0), grids.cubed_sphere(8)),
+    "C8->regional": lambda: (grids.cubed_sphere(8), grids.regular_latlon(20, 15, 20.0, -10.0, 2.0, 2.0)),
+    "shifted 5deg->C6": lambda: (grids.regular_latlon(72, 36, -180.0, -90.0, 5.0, 5.0), grids.cubed_sphere(6)),
+    "equal-area->equal-area": lambda: (grids.equal_area_latlon(36, 18, stretch=0.4),
+                                       grids.equal_area_latlon(24, 12, lon_start=-90.0, stretch=0.2)),
+    "tripole->voronoi": lambda: (grids.tripole(24, 18, seed=2, jitter=0.1), grids.voronoi(162, seed=3)),
 }
 CASES = ["cons", "cons_fracarea", "nearest", "bilinear", "cons_srcmask_nearestwet", "cons_srcmask_none",
          "cons_dstmask", "cons_both_masks", "nearest_srcmask", "bilinear_srcmask", "cons_user_areas"]
@@ -44,6 +50,8 @@ def land_mask(src):
 def run_case(case, ref, oracle, s, d):
     """(reference output, oracle output) of one scenario."""
     m = land_mask(s)
+    if m.min() == m.max():  # a regional grid wholly inside or outside the land box
+        m[::3] = 1 - m[::3]
     rng = np.random.default_rng(22)
     dm = (rng.random(d.n_cells) > 0.1).astype(np.int32)
     if case == "cons":
