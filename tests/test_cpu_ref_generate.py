@@ -104,3 +104,50 @@ def test_reference_generate_unmapped_error(ref, oracle):
         ref.generate("conservative", s, d, unmapped=0)
     with pytest.raises(RuntimeError):
         oracle.conservative(s, d, unmapped=0)
+
+
+def degenerate(m, seed):
+    """A tenth of the cells with a repeated vertex and three cells collapsed
+    to a point: the degenerate-cell scan's cases."""
+    from axgb.grids import MeshArrays
+    rng = np.random.default_rng(seed)
+    idx, off = m.conn_indices.copy(), m.conn_offsets
+    for c in rng.choice(m.n_cells, m.n_cells // 10, replace=False):
+        if off[c + 1] - off[c] >= 4:
+            idx[off[c] + 1] = idx[off[c]]
+    for c in rng.choice(m.n_cells, 3, replace=False):
+        idx[off[c]:off[c + 1]] = idx[off[c]]
+    return MeshArrays(m.node_lonlat, off, idx, name="degenerate")
+
+
+def triangulated(m):
+    """Every quadrilateral split into two triangles."""
+    from axgb.grids import MeshArrays
+    off, idx = [0], []
+    for c in range(m.n_cells):
+        v = list(m.conn_indices[m.conn_offsets[c]:m.conn_offsets[c + 1]])
+        parts = [[v[0], v[1], v[2]], [v[0], v[2], v[3]]] if len(v) == 4 else [v]
+        for p in parts:
+            idx += p
+            off.append(len(idx))
+    return MeshArrays(m.node_lonlat, np.array(off, np.int64), np.array(idx, np.int64), name="triangulated")
+
+
+ODD = {
+    "degenerate C8->10deg": lambda: (degenerate(grids.cubed_sphere(8), 1), grids.latlon_deg(10.0)),
+    "5deg->degenerate C8": lambda: (grids.latlon_deg(5.0), degenerate(grids.cubed_sphere(8), 2)),
+    "triangulated C6->10deg": lambda: (triangulated(grids.cubed_sphere(6)), grids.latlon_deg(10.0)),
+    "10deg->triangulated C6": lambda: (grids.latlon_deg(10.0), triangulated(grids.cubed_sphere(6))),
+    "triangulated C6->C5": lambda: (triangulated(grids.cubed_sphere(6)), grids.cubed_sphere(5)),
+}
+
+
+@pytest.mark.parametrize("case", ["cons", "cons_fracarea", "nearest", "bilinear"])
+@pytest.mark.parametrize("pair", list(ODD))
+def test_oracle_matches_reference_generate_odd_cells(ref, oracle, pair, case):
+    """Degenerate cells (repeated vertices, cells collapsed to a point) and
+    triangle meshes, on either side."""
+    s, d = ODD[pair]()
+    r, o = run_case(case, ref, oracle, s, d)
+    for k in ("row", "col", "w", "frac_a", "frac_b", "area_a", "area_b"):
+        assert np.array_equal(getattr(r, k), getattr(o, k)), k
