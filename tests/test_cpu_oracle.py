@@ -336,3 +336,24 @@ def test_bilinear_general_oracle(oracle):
     rs = np.bincount(w.row, weights=w.w, minlength=w.n_dst)
     assert np.abs(rs - 1.0).max() < 1e-12
     assert np.all(w.area_a == 0.0) and np.all(w.area_b > 0.0)
+
+
+@pytest.mark.parametrize("make", [lambda: grids.cubed_sphere(12), lambda: grids.tripole(48, 36, seed=4, jitter=0.1),
+                                  lambda: grids.voronoi(642, seed=5), lambda: grids.latlon_deg(5.0)])
+def test_cap_radius_soundness(oracle, make):
+    """prop_spherical_cap_filter.cpp: every vertex of a cell lies inside its
+    bounding cap (angle from the centre <= radius + 1e-14), and the cap test
+    never rejects a pair the clipper finds overlapping (every kept pair of a
+    conservative weight set passes acos(c1.c2) <= r1 + r2)."""
+    m = make()
+    c = oracle.cell_prep(m)
+    ll = np.radians(np.asarray(m.node_lonlat, np.float64))
+    nodes = np.stack([np.cos(ll[:, 1]) * np.cos(ll[:, 0]), np.cos(ll[:, 1]) * np.sin(ll[:, 0]), np.sin(ll[:, 1])], 1)
+    cell_of = np.repeat(np.arange(m.n_cells), np.diff(m.conn_offsets))
+    dots = np.einsum("ij,ij->i", nodes[m.conn_indices], c["cap_c"][cell_of])
+    ang = np.arccos(np.clip(dots, -1.0, 1.0))
+    assert np.all(ang <= c["cap_r"][cell_of] + 1e-12)  # numpy's trig here, so 1e-12 not 1e-14
+    w = oracle.conservative(m, grids.latlon_deg(10.0))
+    d = oracle.cell_prep(grids.latlon_deg(10.0))
+    cosang = np.einsum("ij,ij->i", c["cap_c"][w.col], d["cap_c"][w.row])
+    assert np.all(np.arccos(np.clip(cosang, -1.0, 1.0)) <= c["cap_r"][w.col] + d["cap_r"][w.row] + 1e-14)
