@@ -342,7 +342,7 @@ def test_bilinear_general_oracle(oracle):
                                   lambda: grids.voronoi(642, seed=5), lambda: grids.latlon_deg(5.0)])
 def test_cap_radius_soundness(oracle, make):
     """prop_spherical_cap_filter.cpp: every vertex of a cell lies inside its
-    bounding cap (angle from the centre <= radius + 1e-14), and the cap test
+    bounding cap (angle from the centre <= radius, to 1e-12 with numpy trig), and the cap test
     never rejects a pair the clipper finds overlapping (every kept pair of a
     conservative weight set passes acos(c1.c2) <= r1 + r2)."""
     m = make()
@@ -352,7 +352,7 @@ def test_cap_radius_soundness(oracle, make):
     cell_of = np.repeat(np.arange(m.n_cells), np.diff(m.conn_offsets))
     dots = np.einsum("ij,ij->i", nodes[m.conn_indices], c["cap_c"][cell_of])
     ang = np.arccos(np.clip(dots, -1.0, 1.0))
-    assert np.all(ang <= c["cap_r"][cell_of] + 1e-12)  # numpy's trig here, so 1e-12 not 1e-14
+    assert np.all(ang <= c["cap_r"][cell_of] + 1e-12)
     w = oracle.conservative(m, grids.latlon_deg(10.0))
     d = oracle.cell_prep(grids.latlon_deg(10.0))
     cosang = np.einsum("ij,ij->i", c["cap_c"][w.col], d["cap_c"][w.row])
