@@ -104,7 +104,9 @@ class View {
     std::size_t e0 = 0, e1 = 1;
 
     View() = default;
-    explicit View(const std::string &) : store(new nc_value[1]()), ptr(store.get()), e0(1), e1(1) {}
+    // label only: one element for rank 0, an empty array otherwise
+    explicit View(const std::string &)
+        : store(new nc_value[1]()), ptr(store.get()), e0(Rank == 0 ? 1 : 0), e1(Rank > 1 ? ext1(0) : 1) {}
     View(const std::string &, std::size_t n0, std::size_t n1 = 1)
         : store(new nc_value[n0 * ext1(n1) > 0 ? n0 * ext1(n1) : 1]()), ptr(store.get()), e0(n0), e1(ext1(n1)) {}
     View(value_type *p, std::size_t n0, std::size_t n1 = 1) : ptr(const_cast<nc_value *>(p)), e0(n0), e1(Rank > 1 ? n1 : 1) {}
