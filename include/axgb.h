@@ -1,7 +1,8 @@
 /*
  * axgb.h — C ABI of the GB300 (sm_103a) implementation of the AXIS
- * regridding hot path: first-order conservative and rectilinear bilinear
- * weight generation, and the sparse weight apply.
+ * regridding hot path: first-order conservative, bilinear and
+ * nearest-neighbour weight generation (with the reference's fast paths,
+ * masks and coastal post-pass), and the sparse weight apply.
  *
  * Conventions (those of the AXIS Fortran/C interop layer,
  * libs/axis/src/fortran/axis_c_interop.cpp:36-62):
@@ -123,11 +124,18 @@ int axgb_destroy_mesh(int mesh_handle);
 /* ─── Weight generation ──────────────────────────────────────────────────
  * Replaces WeightGenerator::generate (solver/weight_generator.hpp:60-62,
  * weight_generator.cpp:1887-2019) and python generate_weights
- * (axis_py.cpp:633-652). Supported: Conservative1stOrder with GreatCircle
- * lines through the general (BVH + spherical clipper) path, and Bilinear
- * with a rectilinear source. Other dispatch branches return
- * AXGB_ERR_UNSUPPORTED. The matrix lives on the device in CSR form with its
- * frac_a/frac_b/area_a/area_b arrays. Synchronous. */
+ * (axis_py.cpp:633-652), in the reference's dispatch order:
+ *   - Conservative1stOrder: regular x regular (analytic, may decline), then
+ *     rectilinear x rectilinear, then the general BVH + spherical clipper
+ *     path (GreatCircle lines only);
+ *   - Bilinear: regular x regular, else a rectilinear source, else the
+ *     point-location path for any source mesh;
+ *   - NearestNeighbor: regular index rounding, else an exact nearest search.
+ * Cell masks and user areas of the meshes are honoured, and a masked source
+ * goes through the coastal post-pass (renormalisation, NearestWet). Other
+ * methods (Bicubic, Patch, Conservative2ndOrder) and Cartesian lines on the
+ * clipper path return AXGB_ERR_UNSUPPORTED. The matrix lives on the device
+ * in CSR form with its frac_a/frac_b/area_a/area_b arrays. Synchronous. */
 int axgb_generate_weights(int src_mesh, int dst_mesh, const axgb_regrid_config *cfg, int *matrix_handle);
 
 /* Replaces axis_generate_weights_c (axis_c_interop.cpp:117-145): method code
