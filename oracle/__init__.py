@@ -99,9 +99,9 @@ class Oracle:
         L.orc_conservative.argtypes = (mesh + [C.c_void_p, C.c_void_p] + mesh + [C.c_void_p, C.c_void_p]
                                        + [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)])
         L.orc_bilinear.restype = C.c_int
-        L.orc_bilinear.argtypes = mesh + mesh + [C.c_int, C.POINTER(C.c_void_p)]
+        L.orc_bilinear.argtypes = mesh + mesh + [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
         L.orc_nearest.restype = C.c_int
-        L.orc_nearest.argtypes = mesh + mesh + [C.c_int, C.POINTER(C.c_void_p)]
+        L.orc_nearest.argtypes = mesh + mesh + [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
         L.orc_result_nnz.restype = C.c_int64
         L.orc_result_nnz.argtypes = [C.c_void_p]
         L.orc_result_stats.argtypes = [C.c_void_p, _i64p]
@@ -232,19 +232,37 @@ class Oracle:
         order = np.lexsort((col, row))
         return Weights(w.n_src, w.n_dst, row[order], col[order], val[order], w.frac_a, w.frac_b, w.area_a, w.area_b)
 
-    def bilinear(self, src, dst, unmapped: int = 1) -> Weights:
+    @staticmethod
+    def _areas(a, n):
+        """(keep-alive array, pointer) of optional per-cell areas."""
+        if a is None:
+            return None, None
+        a = np.ascontiguousarray(a, np.float64)
+        assert a.shape == (n,)
+        return a, a.ctypes.data_as(C.c_void_p)
+
+    def bilinear(self, src, dst, unmapped: int = 1, src_areas=None, dst_areas=None) -> Weights:
+        """Bilinear weights; cell areas given with the meshes replace the
+        computed ones where the path reports areas (get_cell_areas)."""
         h = C.c_void_p()
+        sa, sp = self._areas(src_areas, src.n_cells)
+        da, dp = self._areas(dst_areas, dst.n_cells)
         t0 = time.perf_counter()
-        rc = self.L.orc_bilinear(*_mesh_args(src), *_mesh_args(dst), unmapped, C.byref(h))
+        rc = self.L.orc_bilinear(*_mesh_args(src), *_mesh_args(dst), sp, dp, unmapped, C.byref(h))
+        del sa, da
         dt = time.perf_counter() - t0
         if rc != 0:
             raise RuntimeError(f"oracle bilinear failed rc={rc}")
         return self._collect(h, src.n_cells, dst.n_cells, dt)
 
-    def nearest(self, src, dst, unmapped: int = 1) -> Weights:
+    def nearest(self, src, dst, unmapped: int = 1, src_areas=None, dst_areas=None) -> Weights:
+        """Nearest-neighbour weights; areas as for bilinear."""
         h = C.c_void_p()
+        sa, sp = self._areas(src_areas, src.n_cells)
+        da, dp = self._areas(dst_areas, dst.n_cells)
         t0 = time.perf_counter()
-        rc = self.L.orc_nearest(*_mesh_args(src), *_mesh_args(dst), unmapped, C.byref(h))
+        rc = self.L.orc_nearest(*_mesh_args(src), *_mesh_args(dst), sp, dp, unmapped, C.byref(h))
+        del sa, da
         dt = time.perf_counter() - t0
         if rc != 0:
             raise RuntimeError(f"oracle nearest failed rc={rc}")

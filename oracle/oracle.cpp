@@ -1441,10 +1441,10 @@ int orc_conservative(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i6
 // A source that is not rectilinear takes bilinear_general. Returns -7 for an
 // unmapped destination under Error.
 int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *soff, const i64 *sidx, i64 dn_nodes,
-                 const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, int unmapped,
-                 orc_result **out) {
-    Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, nullptr, nullptr};
-    Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, nullptr, nullptr};
+                 const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, const double *sareas,
+                 const double *dareas, int unmapped, orc_result **out) {
+    Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, sareas, nullptr};
+    Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, dareas, nullptr};
     GridInfo sg = detect(S), dg = detect(D);
     if (sg.regular && dg.regular && dn_cells > 0) {
         auto *res = new orc_result;
@@ -1519,9 +1519,10 @@ int orc_bilinear(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *s
 // Nearest-neighbour weights (see nearest above). Returns 0 ok, -7 when
 // there is no source cell under Error.
 int orc_nearest(i64 sn_nodes, const double *slonlat, i64 sn_cells, const i64 *soff, const i64 *sidx, i64 dn_nodes,
-                const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, int unmapped, orc_result **out) {
-    Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, nullptr, nullptr};
-    Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, nullptr, nullptr};
+                const double *dlonlat, i64 dn_cells, const i64 *doff, const i64 *didx, const double *sareas,
+                const double *dareas, int unmapped, orc_result **out) {
+    Mesh S{sn_nodes, sn_cells, slonlat, soff, sidx, sareas, nullptr};
+    Mesh D{dn_nodes, dn_cells, dlonlat, doff, didx, dareas, nullptr};
     auto *res = new orc_result;
     if (!nearest(S, D, unmapped, res)) {
         delete res;

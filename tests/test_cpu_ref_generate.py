@@ -3,8 +3,9 @@
 unchanged by oracle/build.py into oracle/_ref/libaxisref_gen.so, with
 ArborX's queries replaced by an exhaustive search (oracle/ref_shim/ArborX.hpp).
 Covers the dispatch of every method, the nearest-neighbour and general
-bilinear paths, source and destination masks, the coastal post-pass with and
-without NearestWet, and user cell areas. Every array bit for bit. Skipped
+bilinear paths, source and destination masks (which nearest-neighbour and
+bilinear do not read), the coastal post-pass with and without NearestWet,
+and user cell areas. Every array bit for bit. Skipped
 where the reference checkout (and so that library) is absent."""
 import numpy as np
 import pytest
@@ -28,7 +29,8 @@ PAIRS = {
     "tripole->voronoi": lambda: (grids.tripole(24, 18, seed=2, jitter=0.1), grids.voronoi(162, seed=3)),
 }
 CASES = ["cons", "cons_fracarea", "nearest", "bilinear", "cons_srcmask_nearestwet", "cons_srcmask_none",
-         "cons_dstmask", "cons_both_masks", "nearest_srcmask", "bilinear_srcmask", "cons_user_areas"]
+         "cons_dstmask", "cons_both_masks", "nearest_srcmask", "bilinear_srcmask", "cons_user_areas",
+         "nearest_user_areas", "bilinear_user_areas", "nearest_dstmask_ignored", "bilinear_dstmask_ignored"]
 
 
 @pytest.fixture(scope="module")
@@ -84,6 +86,17 @@ def run_case(case, ref, oracle, s, d):
         da[da == 0.0] = 1.0
         return (ref.generate("conservative", s, d, src_areas=sa, dst_areas=da),
                 oracle.conservative(s, d, src_areas=sa, dst_areas=da))
+    if case in ("nearest_user_areas", "bilinear_user_areas"):
+        sa = np.linspace(1.0, 2.0, s.n_cells)
+        da = np.linspace(3.0, 4.0, d.n_cells)
+        fn = oracle.nearest if case.startswith("nearest") else oracle.bilinear
+        meth = "nearest_neighbor" if case.startswith("nearest") else "bilinear"
+        return ref.generate(meth, s, d, src_areas=sa, dst_areas=da), fn(s, d, src_areas=sa, dst_areas=da)
+    if case in ("nearest_dstmask_ignored", "bilinear_dstmask_ignored"):
+        # these methods do not read destination masks
+        fn = oracle.nearest if case.startswith("nearest") else oracle.bilinear
+        meth = "nearest_neighbor" if case.startswith("nearest") else "bilinear"
+        return ref.generate(meth, s, d, dst_mask=dm), fn(s, d)
     raise ValueError(case)
 
 
