@@ -64,3 +64,29 @@ def test_weight_cache_header_checks_without_device():
         rc = L.axgb_matrix_deserialize(ctypes.c_char_p(blob), len(blob), ctypes.byref(h))
         assert rc == axgb.ERR_INVALID, msg
         assert axgb.last_error()
+
+
+def test_config_names_match_the_python_binding():
+    """Every spelling parse_regrid_config of python/axis_py.cpp:144-221
+    accepts maps to the RegridConfig enum value (regrid_config.hpp:24-72);
+    integers pass through; an unknown name raises ValueError naming it."""
+    import pytest
+
+    import axgb
+    names = {
+        "method": {"bilinear": 0, "Bilinear": 0, "nearest_neighbor": 1, "NearestNeighbor": 1, "bicubic": 2,
+                   "Bicubic": 2, "patch": 3, "Patch": 3, "conservative": 4, "Conservative1stOrder": 4,
+                   "conservative2nd": 5, "Conservative2ndOrder": 5},
+        "norm_type": {"dstarea": 0, "DstArea": 0, "fracarea": 1, "FracArea": 1},
+        "unmapped": {"error": 0, "Error": 0, "ignore": 1, "Ignore": 1},
+        "line_type": {"cartesian": 0, "Cartesian": 0, "great_circle": 1, "GreatCircle": 1},
+    }
+    for key, table in names.items():
+        for text, value in table.items():
+            assert getattr(axgb.parse_regrid_config({key: text}), key) == value, (key, text)
+            assert getattr(axgb.parse_regrid_config({key: value}), key) == value
+        with pytest.raises(ValueError, match="Unknown"):
+            axgb.parse_regrid_config({key: "no_such_name"})
+    assert axgb.parse_regrid_config({"use_limiter": True}).use_limiter == 1
+    assert axgb.parse_regrid_config({}).extrap_method == 1  # NearestWet by default
+    assert axgb.parse_regrid_config({"extrap_method": "none"}).extrap_method == 0
