@@ -46,7 +46,7 @@ _SYMBOLS = [
     "axgb_conservation_f32", "axgb_matrix_device_status", "axgb_conservation_f64_noalloc",
     "axgb_set_kernel_choice", "axgb_get_kernel_choice", "axgb_nan_batch_apply_f64", "axgb_apply_masked_f64",
     "axgb_nan_batch_apply_host", "axgb_matrix_serialize", "axgb_matrix_deserialize", "axgb_esmf_write",
-    "axgb_esmf_read", "axgb_matrix_write_esmf", "axgb_matrix_read_esmf",
+    "axgb_esmf_read", "axgb_matrix_write_esmf", "axgb_matrix_read_esmf", "axgb_apply_f32split_hilo",
 ]
 
 
@@ -104,6 +104,7 @@ def lib():
     L.axgb_apply_f64.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp]
     L.axgb_apply_f32split.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp]
     L.axgb_apply_f32split_tuned.argtypes = [C.c_int, vp, i64, vp, i64, i64, C.c_int, C.c_int, C.c_int, vp]
+    L.axgb_apply_f32split_hilo.argtypes = [C.c_int, vp, i64, vp, i64, vp, i64, i64, vp]
     L.axgb_autotune_f32split.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp, vp]
     L.axgb_set_autotune.argtypes = [C.c_int]
     L.axgb_apply_c.argtypes = [C.c_int, vp, vp, C.c_int, C.c_int]
@@ -449,6 +450,25 @@ def apply_f32split(matrix: Matrix, x, y=None, stream=None, fields_per_pass=None,
         _check(lib().axgb_apply_f32split_tuned(matrix.handle, _ptr(x), x.stride(0), _ptr(y), y.stride(0), x.shape[0],
                                                v, int(fields_per_pass or 0), u, s))
     return y
+
+
+def apply_f32split_hilo(matrix: Matrix, x, y=None, y_lo=None, stream=None):
+    """Split-FP32 apply with a low-part output: y is bitwise apply_f32split's
+    result and y + y_lo (summed in FP64) carries each compensated row sum to
+    about 2^-48 relative. Returns (y, y_lo), CUDA float32 [nrhs, n_dst]."""
+    import torch
+    if x.dim() == 1:
+        x = x.view(1, -1)
+    nrhs = x.shape[0]
+    if y is None:
+        y = torch.empty((nrhs, matrix.n_dst), dtype=torch.float32, device=x.device)
+    if y_lo is None:
+        y_lo = torch.empty((nrhs, matrix.n_dst), dtype=torch.float32, device=x.device)
+    y2, l2 = (y.view(1, -1) if y.dim() == 1 else y), (y_lo.view(1, -1) if y_lo.dim() == 1 else y_lo)
+    _check(lib().axgb_apply_f32split_hilo(matrix.handle, _ptr(x), x.stride(0), _ptr(y2), y2.stride(0), _ptr(l2),
+                                          l2.stride(0), nrhs,
+                                          _stream(stream if stream is not None else torch.cuda.current_stream())))
+    return y, y_lo
 
 
 def autotune_f32split(matrix: Matrix, x, y, stream=None):

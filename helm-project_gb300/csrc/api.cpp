@@ -255,6 +255,26 @@ void check_apply(const Matrix &m, const void *x, i64 ldx, const void *y, i64 ldy
     AXGB_REQUIRE(m.n_dst == 0 || y != nullptr, "apply: y is NULL");
 }
 
+// Valid kernel choices: variant 0 (direct; unroll 1, 2 or 4), 1 (blocked,
+// cp.async staging; 2 or 3 buffers), 2 (blocked, bulk copies; 2 buffers),
+// 1 and 2 with 2, 4 or 8 fields per stage, 3 (blocked, producer warp and
+// mbarrier ring of 2 or 3 slots, 4 fields per stage); 4 (one fused launch
+// for few fields; the other knobs unused).
+void check_split_params(const SplitParams &p, const char *who) {
+    const std::string w(who);
+    AXGB_REQUIRE(p.variant >= 0 && p.variant <= 4, w + ": variant must be 0 to 4");
+    AXGB_REQUIRE(p.fields_per_pass >= 0, w + ": fields_per_pass must be >= 0");
+    if (p.variant == 4) return;
+    if (p.variant == 0) {
+        AXGB_REQUIRE(p.unroll == 1 || p.unroll == 2 || p.unroll == 4, w + ": direct unroll must be 1, 2 or 4");
+        return;
+    }
+    AXGB_REQUIRE(p.unroll == 2 || p.unroll == 4 || p.unroll == 8, w + ": staged fields per stage must be 2, 4 or 8");
+    AXGB_REQUIRE(p.variant != 3 || p.unroll == 4, w + ": variant 3 stages 4 fields at a time");
+    AXGB_REQUIRE(p.stages == 2 || (p.stages == 3 && p.variant != 2),
+                 w + ": staging buffers must be 2 (variant 2) or 2-3 (variants 1 and 3)");
+}
+
 SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
     std::vector<SplitParams> cands;
     for (int t : {4, 8})
@@ -262,6 +282,8 @@ SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i6
             for (int fc : {0, 128, 64, 32, 16, 8})
                 if (t <= std::max<i64>(2, nrhs) && (fc == 0 || fc < nrhs)) cands.push_back({1, fc, t, ns});
     cands.push_back({2, 64, 4, 2});
+    for (int fc : {128, 64, 0})
+        if (nrhs >= 8 && (fc == 0 || fc < nrhs)) cands.push_back({3, fc, 4, 3});
     std::vector<i64> tiles = {nrhs};
     for (i64 t : {32, 8})
         if (t < nrhs) tiles.push_back(t);
@@ -269,6 +291,7 @@ SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i6
         for (int u : {2, 4})
             if (u <= std::max<i64>(1, nrhs)) cands.push_back({0, static_cast<int>(t), u});
     if (nrhs == 1) cands.push_back({0, 1, 1});
+    if (nrhs <= 8) cands.push_back({4, 0, 1, 2});
     cudaEvent_t e0, e1;
     AXGB_CUDA(cudaEventCreate(&e0));
     AXGB_CUDA(cudaEventCreate(&e1));
@@ -345,6 +368,13 @@ SplitParams pick_params(Matrix &m, i64 nrhs) {
 
 SplitParams default_split_params(i64 nrhs) {
     SplitParams p;
+    if (nrhs <= 2) {  // one fused launch
+        p.variant = 4;
+        p.fields_per_pass = 0;
+        p.unroll = 1;
+        p.stages = 2;
+        return p;
+    }
     p.variant = 1;
     p.fields_per_pass = 64;
     p.stages = 2;
@@ -908,13 +938,8 @@ int axgb_apply_f32split_tuned(int h, const float *x, int64_t ldx, float *y, int6
     AXGB_TRY({
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         check_apply(*m, x, ldx, y, ldy, nrhs);
-        AXGB_REQUIRE(variant >= 0 && variant <= 2, "apply: variant must be 0 (direct), 1 or 2 (blocked)");
-        if (variant == 0) {
-            AXGB_REQUIRE(unroll == 1 || unroll == 2 || unroll == 4, "apply: direct unroll must be 1, 2 or 4");
-        } else {
-            AXGB_REQUIRE(unroll == 2 || unroll == 4 || unroll == 8, "apply: staged fields per stage must be 2, 4 or 8");
-        }
-        SplitParams p{variant, fields_per_pass, unroll, 2};
+        SplitParams p{variant, fields_per_pass, unroll, variant == 3 ? 3 : 2};
+        check_split_params(p, "apply");
         if (nrhs > 0) apply_split(*m, x, ldx, y, ldy, nrhs, p, static_cast<cudaStream_t>(stream));
     });
 }
@@ -949,16 +974,7 @@ int axgb_set_kernel_choice(int h, int64_t nrhs, const int32_t *choice) {
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         AXGB_REQUIRE(choice && nrhs > 0, "set_kernel_choice: NULL choice or nrhs <= 0");
         SplitParams p{choice[0], choice[1], choice[2], choice[3]};
-        AXGB_REQUIRE(p.variant >= 0 && p.variant <= 2, "set_kernel_choice: variant must be 0, 1 or 2");
-        AXGB_REQUIRE(p.fields_per_pass >= 0, "set_kernel_choice: fields_per_pass must be >= 0");
-        if (p.variant == 0) {
-            AXGB_REQUIRE(p.unroll == 1 || p.unroll == 2 || p.unroll == 4, "set_kernel_choice: direct unroll must be 1, 2 or 4");
-        } else {
-            AXGB_REQUIRE(p.unroll == 2 || p.unroll == 4 || p.unroll == 8,
-                         "set_kernel_choice: staged fields per stage must be 2, 4 or 8");
-        }
-        AXGB_REQUIRE(p.stages == 2 || (p.stages == 3 && p.variant == 1),
-                     "set_kernel_choice: stages must be 2 (or 3 with variant 1)");
+        check_split_params(p, "set_kernel_choice");
         std::lock_guard<std::mutex> lk(m->mu);
         m->tuned[nrhs] = p;
     });
@@ -1012,6 +1028,18 @@ int axgb_apply_f32split(int h, const float *x, int64_t ldx, float *y, int64_t ld
             if (!have) p = default_split_params(nrhs);
             apply_split(*m, x, ldx, y, ldy, nrhs, p, s);
         }
+    });
+}
+
+int axgb_apply_f32split_hilo(int h, const float *x, int64_t ldx, float *y, int64_t ldy, float *y_lo, int64_t ld_lo,
+                             int64_t nrhs, axgb_stream_t stream) {
+    AXGB_TRY({
+        auto m = Registry::get().find(Registry::get().mats, h, "matrix");
+        check_apply(*m, x, ldx, y, ldy, nrhs);
+        AXGB_REQUIRE(nrhs == 0 || m->n_dst == 0 || y_lo != nullptr, "apply_hilo: y_lo is NULL");
+        AXGB_REQUIRE(nrhs == 0 || ld_lo >= m->n_dst, "apply_hilo: ld_lo < n_dst");
+        if (nrhs > 0) apply_split(*m, x, ldx, y, ldy, nrhs, pick_params(*m, nrhs), static_cast<cudaStream_t>(stream),
+                                  y_lo, ld_lo);
     });
 }
 

@@ -82,12 +82,19 @@ struct Batch {
     // graph per stream, replayed while descriptors are updated in place
     std::map<cudaStream_t, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
     std::vector<const void *> last_ptrs;
+    // Every graph shares the work counters, descriptors and gather scratch
+    // above, so a call on another stream than the previous call's first waits
+    // for the previous call's work (event `done`, recorded after each launch).
+    cudaEvent_t done = nullptr;
+    cudaStream_t last_stream = nullptr;
+    bool launched = false;
     std::mutex mu;
     ~Batch() {
         for (auto &g : graphs) {
             cudaGraphExecDestroy(g.second.second);
             cudaGraphDestroy(g.second.first);
         }
+        if (done) cudaEventDestroy(done);
     }
 };
 
@@ -102,6 +109,8 @@ struct SellArgs {
     const float *hi, *lo;
     const double *w64;
     i64 n_rows;
+    float *ylo;  // split kernels: low parts of the outputs (hi+lo form), or null
+    i64 ldylo;
 };
 
 __device__ __forceinline__ float ldg_f(const float *p) { return __ldg(p); }
@@ -175,6 +184,13 @@ __global__ void __launch_bounds__(256) k_split(SellArgs a, const float *__restri
                         upk(r, ra, rb);
                         y[(f + 2 * u) * ldy + row] = ra;
                         y[(f + 2 * u + 1) * ldy + row] = rb;
+                        if (a.ylo) {
+                            float sa, sb, ca, cb;
+                            upk(s[u], sa, sb);
+                            upk(cc[u], ca, cb);
+                            a.ylo[(f + 2 * u) * a.ldylo + row] = sum_err(sa, ca, ra);
+                            a.ylo[(f + 2 * u + 1) * a.ldylo + row] = sum_err(sb, cb, rb);
+                        }
                     }
                 }
             }
@@ -185,7 +201,11 @@ __global__ void __launch_bounds__(256) k_split(SellArgs a, const float *__restri
 #pragma unroll
             for (int k = 0; k < L; ++k)
                 if (k < rl) csum1(s, cc, h[k], lw[k], ldg_f(xf + c[k]));
-            if (store) y[f * ldy + row] = __fadd_rn(s, cc);
+            if (store) {
+                const float r = __fadd_rn(s, cc);
+                y[f * ldy + row] = r;
+                if (a.ylo) a.ylo[f * a.ldylo + row] = sum_err(s, cc, r);
+            }
         }
     }
 }
@@ -289,7 +309,9 @@ __global__ void __launch_bounds__(256) k_split_rows(SellArgs a, const float *__r
         const int e = e0 + 32 * k;
         csum1(s, c, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
     }
-    y[f * ldy + row] = __fadd_rn(s, c);
+    const float r = __fadd_rn(s, c);
+    y[f * ldy + row] = r;
+    if (a.ylo) a.ylo[f * a.ldylo + row] = sum_err(s, c, r);
 }
 
 __global__ void __launch_bounds__(256) k_f64_rows(SellArgs a, const double *__restrict__ x, i64 ldx,
@@ -309,11 +331,15 @@ __global__ void __launch_bounds__(256) k_f64_rows(SellArgs a, const double *__re
     y[f * ldy + row] = s;
 }
 
+constexpr i64 kFusedMaxF64 = 2;  // FP64 applies of at most this many fields take the fused kernel
+
 struct LongRows {
     const int *row, *ptr, *col;
     const float *hi, *lo;
     const double *w64;
     i64 n;
+    float *ylo;  // split: low parts of the outputs (hi+lo form), or null
+    i64 ldylo;
 };
 constexpr int kLongF = 8;  // fields per warp in the long-row kernels
 
@@ -351,7 +377,11 @@ __device__ __forceinline__ void split_long_row(const LongRows &L, i64 w, const f
                 const float c2 = __shfl_xor_sync(0xffffffffu, c[f], off);
                 lcombine(s[f], c[f], s2, c2);
             }
-            if (lane == f) y[(f0 + f) * ldy + row] = __fadd_rn(s[f], c[f]);
+            if (lane == f) {
+                const float r = __fadd_rn(s[f], c[f]);
+                y[(f0 + f) * ldy + row] = r;
+                if (L.ylo) L.ylo[(f0 + f) * L.ldylo + row] = sum_err(s[f], c[f], r);
+            }
         }
     }
 }
@@ -363,11 +393,11 @@ __global__ void __launch_bounds__(256) k_split_long(LongRows L, const float *__r
     split_long_row(L, w, x, ldx, y, ldy, nrhs);
 }
 
-__global__ void __launch_bounds__(256) k_f64_long(LongRows L, const double *__restrict__ x, i64 ldx,
-                                                  double *__restrict__ y, i64 ldy, i64 nrhs) {
+// FP64 form of split_long_row: leaves summed with fma in entry order, then
+// the butterfly with plain additions.
+__device__ __forceinline__ void f64_long_row(const LongRows &L, i64 w, const double *x, i64 ldx, double *y,
+                                             i64 ldy, i64 nrhs) {
     const int lane = threadIdx.x & 31;
-    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (w >= L.n * ((nrhs + kLongF - 1) / kLongF)) return;
     const i64 i = w % L.n, fc = w / L.n;
     const i64 row = L.row[i];
     const int b = L.ptr[i], n = L.ptr[i + 1] - b;
@@ -391,6 +421,74 @@ __global__ void __launch_bounds__(256) k_f64_long(LongRows L, const double *__re
             if (lane == f) y[(f0 + f) * ldy + row] = s[f];
         }
     }
+}
+
+__global__ void __launch_bounds__(256) k_f64_long(LongRows L, const double *__restrict__ x, i64 ldx,
+                                                  double *__restrict__ y, i64 ldy, i64 nrhs) {
+    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (w >= L.n * ((nrhs + kLongF - 1) / kLongF)) return;
+    f64_long_row(L, w, x, ldx, y, ldy, nrhs);
+}
+
+// ─── few fields: one launch over the whole matrix ────────────────────────
+// Warps [0, n_slices): lane per row of one slice, rows of at most 32 entries,
+// each entry read from the sliced layout per field (nothing cached: with
+// one or two fields there is nothing to reuse); warps [n_slices, n_slices +
+// n_lrows): one row of more than 32 entries each, for all fields, 8 at a time
+// (split_long_row / f64_long_row). Same summation order as the class
+// kernels, so the same bits, in one launch instead of one per class.
+__global__ void __launch_bounds__(256) k_split_fused(SellArgs a, LongRows L, i64 n_slices, const float *__restrict__ x,
+                                                     i64 ldx, float *__restrict__ y, i64 ldy, i64 nrhs) {
+    const int lane = threadIdx.x & 31;
+    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (w < n_slices) {
+        const i64 row = w * 32 + lane;
+        if (row >= a.n_rows) return;
+        const int n = a.rlen[row];
+        if (n > 32) return;  // a long row: its own warp below
+        const int e0 = a.base[w] + lane;
+        for (i64 f = 0; f < nrhs; ++f) {
+            const float *xf = x + f * ldx;
+            float s = 0.f, c = 0.f;
+            for (int k = 0; k < n; ++k) {
+                const int e = e0 + 32 * k;
+                csum1(s, c, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
+            }
+            const float r = __fadd_rn(s, c);
+            y[f * ldy + row] = r;
+            if (a.ylo) a.ylo[f * a.ldylo + row] = sum_err(s, c, r);
+        }
+        return;
+    }
+    const i64 i = w - n_slices;
+    if (i >= L.n) return;
+    for (i64 fc = 0; fc * kLongF < nrhs; ++fc) split_long_row(L, fc * L.n + i, x, ldx, y, ldy, nrhs);
+}
+
+__global__ void __launch_bounds__(256) k_f64_fused(SellArgs a, LongRows L, i64 n_slices, const double *__restrict__ x,
+                                                   i64 ldx, double *__restrict__ y, i64 ldy, i64 nrhs) {
+    const int lane = threadIdx.x & 31;
+    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (w < n_slices) {
+        const i64 row = w * 32 + lane;
+        if (row >= a.n_rows) return;
+        const int n = a.rlen[row];
+        if (n > 32) return;
+        const int e0 = a.base[w] + lane;
+        for (i64 f = 0; f < nrhs; ++f) {
+            const double *xf = x + f * ldx;
+            double s = 0.0;
+            for (int k = 0; k < n; ++k) {
+                const int e = e0 + 32 * k;
+                s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
+            }
+            y[f * ldy + row] = s;
+        }
+        return;
+    }
+    const i64 i = w - n_slices;
+    if (i >= L.n) return;
+    for (i64 fc = 0; fc * kLongF < nrhs; ++fc) f64_long_row(L, fc * L.n + i, x, ldx, y, ldy, nrhs);
 }
 
 // Row-contiguous copy of the long rows' entries (in the layout's order).
@@ -558,8 +656,10 @@ void build_sell(Matrix &m, int fmt, cudaStream_t s) {
     S.built = true;
 }
 
-SellArgs sell_args(const Matrix &m, const Sell &S, int cls) {
-    SellArgs a;
+SellArgs sell_args(const Matrix &m, const Sell &S, int cls, float *ylo = nullptr, i64 ldylo = 0) {
+    SellArgs a{};
+    a.ylo = ylo;
+    a.ldylo = ldylo;
     a.ids = S.class_ids.p + S.class_begin[cls];
     a.n_ids = S.class_begin[cls + 1] - S.class_begin[cls];
     a.base = S.base.p;
@@ -588,7 +688,7 @@ void launch_split(const SellArgs &a, const float *x, i64 ldx, float *y, i64 ldy,
 }
 
 LongRows long_rows(const Sell &S) {
-    LongRows L;
+    LongRows L{};
     L.row = S.lrow.p;
     L.ptr = S.lptr.p;
     L.col = S.lcol.p;
@@ -606,10 +706,14 @@ void launch_split_rows(const SellArgs &a, const float *x, i64 ldx, float *y, i64
     const i64 warps = a.n_ids * 32 * ((nrhs + 31) / 32);
     k_split_rows<<<nblk(warps * 32, 256), 256, 0, s>>>(a, x, ldx, y, ldy, nrhs);
 }
-void launch_split_long(const Sell &S, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+void launch_split_long(const Sell &S, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s,
+                       float *ylo = nullptr, i64 ldylo = 0) {
     if (S.n_lrows == 0 || nrhs == 0) return;
     const i64 warps = S.n_lrows * ((nrhs + kLongF - 1) / kLongF);
-    k_split_long<<<nblk(warps * 32, 256), 256, 0, s>>>(long_rows(S), x, ldx, y, ldy, nrhs);
+    LongRows L = long_rows(S);
+    L.ylo = ylo;
+    L.ldylo = ldylo;
+    k_split_long<<<nblk(warps * 32, 256), 256, 0, s>>>(L, x, ldx, y, ldy, nrhs);
 }
 void launch_f64_rows(const SellArgs &a, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s) {
     if (a.n_ids == 0 || nrhs == 0) return;
@@ -620,6 +724,24 @@ void launch_f64_long(const Sell &S, const double *x, i64 ldx, double *y, i64 ldy
     if (S.n_lrows == 0 || nrhs == 0) return;
     const i64 warps = S.n_lrows * ((nrhs + kLongF - 1) / kLongF);
     k_f64_long<<<nblk(warps * 32, 256), 256, 0, s>>>(long_rows(S), x, ldx, y, ldy, nrhs);
+}
+// One launch for the whole matrix (few fields): warp per slice, then warp per long row.
+void launch_split_fused(const Matrix &m, const Sell &S, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs,
+                        cudaStream_t s, float *ylo, i64 ldylo) {
+    const i64 warps = S.n_slices + S.n_lrows;
+    if (warps == 0 || nrhs == 0) return;
+    LongRows L = long_rows(S);
+    L.ylo = ylo;
+    L.ldylo = ldylo;
+    k_split_fused<<<nblk(warps * 32, 256), 256, 0, s>>>(sell_args(m, S, 0, ylo, ldylo), L, S.n_slices, x, ldx, y, ldy,
+                                                        nrhs);
+}
+void launch_f64_fused(const Matrix &m, const Sell &S, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs,
+                      cudaStream_t s) {
+    const i64 warps = S.n_slices + S.n_lrows;
+    if (warps == 0 || nrhs == 0) return;
+    k_f64_fused<<<nblk(warps * 32, 256), 256, 0, s>>>(sell_args(m, S, 0), long_rows(S), S.n_slices, x, ldx, y, ldy,
+                                                      nrhs);
 }
 
 template <int L>
@@ -766,9 +888,11 @@ double integral(const T *f, const double *area, const double *frac, i64 n, int m
 
 // ─── conservation report without allocation ───────────────────────────────
 // For callers that cannot allocate device memory while they run (a model
-// whose memory is owned by its own pool, code between allocation-free
-// phases, or a stream that is later captured): the per-block partial sums
-// live in a fixed file-scope device array instead of cudaMalloc'd scratch.
+// whose device memory is owned by its own pool, or code between
+// allocation-free phases): the per-block partial sums live in a fixed
+// file-scope device array instead of cudaMalloc'd scratch. The call copies
+// its two results to the host and synchronises its stream, so it is made
+// before or between stream captures, never inside one.
 // Each block reduces a fixed span of 2048 cells; the partials are then
 // reduced by one block in a fixed order, so results are deterministic.
 
@@ -824,7 +948,9 @@ __global__ void k_sum_partials(const double *partial, int nb0, int nb1, double *
 }
 
 // Device address of g_noalloc_scratch for the current device, looked up
-// once per device (the host-side name is not a device address).
+// once per device (the host-side name is not a device address). The cached
+// address belongs to the device's current context: after cudaDeviceReset
+// it is stale, as is every other handle of this library on that device.
 double *noalloc_scratch() {
     static std::mutex mu;
     static double *ptr[256] = {};
@@ -859,7 +985,7 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
         const Batch::Desc &d = desc[m];
         const i64 local = static_cast<i64>(it) - d.item_begin;
         if (d.mode == 2) {  // rows of more than 32 entries
-            LongRows L;
+            LongRows L{};
             L.row = d.lrow;
             L.ptr = d.lptr;
             L.col = d.lcol;
@@ -984,53 +1110,58 @@ void gather_source(const Matrix &m, const float *x, i64 ldx, i64 nrhs, float *xr
 }
 
 void apply_split_layouts(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
-                         cudaStream_t s);
+                         cudaStream_t s, float *ylo, i64 ldylo);
 
 // A renumbered matrix first gathers the fields into stream-ordered scratch
 // (cudaMallocAsync, freed on the same stream after the apply).
 void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
-                 cudaStream_t s) {
+                 cudaStream_t s, float *ylo, i64 ldylo) {
     if (nrhs <= 0) return;
     if (!m.blocked.built) matrix_prepare(m, 2, s);
     if (!m.src_renum) {
-        apply_split_layouts(m, x, ldx, y, ldy, nrhs, p, s);
+        apply_split_layouts(m, x, ldx, y, ldy, nrhs, p, s, ylo, ldylo);
         return;
     }
     const i64 ldr = renum_ld(m);
     float *xr = nullptr;
     AXGB_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&xr), sizeof(float) * static_cast<size_t>(ldr * nrhs), s));
     gather_source(m, x, ldx, nrhs, xr, s);
-    apply_split_layouts(m, xr, ldr, y, ldy, nrhs, p, s);
+    apply_split_layouts(m, xr, ldr, y, ldy, nrhs, p, s, ylo, ldylo);
     AXGB_CUDA(cudaFreeAsync(xr, s));
 }
 
 void apply_split_layouts(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
-                         cudaStream_t s) {
+                         cudaStream_t s, float *ylo, i64 ldylo) {
     if (nrhs <= 0) return;
-    if (p.variant >= 1 && blocked_eligible(m, x, ldx, p.variant == 2)) {
+    if (p.variant >= 1 && p.variant <= 3 && blocked_eligible(m, x, ldx, p.variant == 2)) {
         if (!m.blocked.built) matrix_prepare(m, 2, s);
-        apply_blocked(m, x, ldx, y, ldy, nrhs, p.variant == 2, p.unroll, p.stages, p.fields_per_pass, s);
+        apply_blocked(m, x, ldx, y, ldy, nrhs, p.variant, p.unroll, p.stages, p.fields_per_pass, s, ylo, ldylo);
         const Blocked &B = m.blocked;
         if (B.n_fallback > 0) {
-            SellArgs a = sell_args(m, m.sell32, 4);
+            SellArgs a = sell_args(m, m.sell32, 4, ylo, ldylo);
             a.ids = B.fallback_slices.p;
             a.n_ids = B.n_fallback;
             launch_split_rows(a, x, ldx, y, ldy, nrhs, s);
         }
-        launch_split_long(m.sell32, x, ldx, y, ldy, nrhs, s);
+        launch_split_long(m.sell32, x, ldx, y, ldy, nrhs, s, ylo, ldylo);
         AXGB_CUDA(cudaGetLastError());
         return;
     }
     if (!m.sell32.built) matrix_prepare(m, 1, s);
     const Sell &S = m.sell32;
+    if (p.variant == 4) {  // one launch for the whole matrix (few fields)
+        launch_split_fused(m, S, x, ldx, y, ldy, nrhs, s, ylo, ldylo);
+        AXGB_CUDA(cudaGetLastError());
+        return;
+    }
     i64 tile = (p.fields_per_pass <= 0 || p.fields_per_pass > nrhs) ? nrhs : p.fields_per_pass;
     const int unroll = p.variant == 0 ? p.unroll : 4;
-    launch_split<8>(sell_args(m, S, 0), x, ldx, y, ldy, nrhs, tile, unroll, s);
-    launch_split<16>(sell_args(m, S, 1), x, ldx, y, ldy, nrhs, tile, unroll, s);
-    launch_split<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, unroll, s);
-    launch_split_rows(sell_args(m, S, 3), x, ldx, y, ldy, nrhs, s);
-    launch_split_rows(sell_args(m, S, 4), x, ldx, y, ldy, nrhs, s);
-    launch_split_long(S, x, ldx, y, ldy, nrhs, s);
+    launch_split<8>(sell_args(m, S, 0, ylo, ldylo), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    launch_split<16>(sell_args(m, S, 1, ylo, ldylo), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    launch_split<32>(sell_args(m, S, 2, ylo, ldylo), x, ldx, y, ldy, nrhs, tile, unroll, s);
+    launch_split_rows(sell_args(m, S, 3, ylo, ldylo), x, ldx, y, ldy, nrhs, s);
+    launch_split_rows(sell_args(m, S, 4, ylo, ldylo), x, ldx, y, ldy, nrhs, s);
+    launch_split_long(S, x, ldx, y, ldy, nrhs, s, ylo, ldylo);
     AXGB_CUDA(cudaGetLastError());
 }
 
@@ -1039,6 +1170,11 @@ void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs
     const Sell &S = m.sell64;
     i64 tile = nrhs;
     if (tile <= 0) return;
+    if (nrhs <= kFusedMaxF64) {  // one launch; same bits as the class kernels
+        launch_f64_fused(m, S, x, ldx, y, ldy, nrhs, s);
+        AXGB_CUDA(cudaGetLastError());
+        return;
+    }
     launch_f64<8>(sell_args(m, S, 0), x, ldx, y, ldy, nrhs, tile, s);
     launch_f64<16>(sell_args(m, S, 1), x, ldx, y, ldy, nrhs, tile, s);
     launch_f64<32>(sell_args(m, S, 2), x, ldx, y, ldy, nrhs, tile, s);
@@ -1198,12 +1334,32 @@ void drop_graphs(Batch &b) {
 
 }  // namespace
 
+// Ends a stream capture that an exception left open (dropping the partial
+// graph) and destroys the private capture stream when there is one.
+struct CaptureGuard {
+    cudaStream_t st;
+    bool own;
+    bool open = true;
+    ~CaptureGuard() {
+        if (open) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(st, &g);
+            if (g) cudaGraphDestroy(g);
+        }
+        if (own) cudaStreamDestroy(st);
+    }
+};
+
 // Stream-ordered. The first call (and a call whose fields change which
 // matrices can use the staged kernels) plans the work and captures a CUDA
 // graph per stream; later calls update the field pointers in the device
-// descriptors the graph reads and replay it.
+// descriptors the graph reads and replay it. Calls on different streams are
+// ordered after one another on the GPU (they share the batch's device
+// buffers).
 void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *y, const i64 *ldy, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(b.mu);
+    if (!b.done) AXGB_CUDA(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming));
+    if (b.launched && b.last_stream != s) AXGB_CUDA(cudaStreamWaitEvent(s, b.done, 0));
     const size_t nm = b.mats.size();
     std::vector<const void *> ptrs;
     std::vector<char> use(nm, 0);
@@ -1273,6 +1429,7 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
             AXGB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
             own = true;
         }
+        CaptureGuard guard{cap, own};
         cudaGraph_t g;
         cudaGraphExec_t ge;
         AXGB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
@@ -1287,12 +1444,19 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
             k_batch<<<b.blocks, 256, 0, cap>>>(b.d_desc.p, static_cast<int>(b.desc.size()), b.total_items,
                                                 b.counter.p);
         }
+        guard.open = false;
         AXGB_CUDA(cudaStreamEndCapture(cap, &g));
-        AXGB_CUDA(cudaGraphInstantiate(&ge, g, 0));
-        if (own) AXGB_CUDA(cudaStreamDestroy(cap));
+        cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            AXGB_CUDA(e);
+        }
         it = b.graphs.emplace(s, std::make_pair(g, ge)).first;
     }
     AXGB_CUDA(cudaGraphLaunch(it->second.second, s));
+    AXGB_CUDA(cudaEventRecord(b.done, s));
+    b.last_stream = s;
+    b.launched = true;
 }
 
 }  // namespace axgb

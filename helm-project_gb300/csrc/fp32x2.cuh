@@ -81,6 +81,16 @@ __device__ __forceinline__ void cstepn(F2 &s, F2 &cn, float h, F2 hp, F2 ln, flo
     s = t;
 }
 
+// Low part of a row value. The stored value is r = fl(s + c); the exact
+// rounding error of that sum (Knuth's TwoSum, exact for any operand order)
+// is returned, so r + lo represents s + c to within FP32 round-off of c's
+// own error term. Used by the hi+lo output form of the split apply.
+__device__ __forceinline__ float sum_err(float s, float c, float r) {
+    const float bp = __fsub_rn(r, s);
+    const float ap = __fsub_rn(r, bp);
+    return __fadd_rn(__fsub_rn(s, ap), __fsub_rn(c, bp));
+}
+
 // ─── rows longer than 32 entries ──────────────────────────────────────────
 // Order for a row of n > 32 entries: leaf j (j = 0..31) sums entries j,
 // j+32, j+64, ... in order with csum1; the 32 leaves are combined by an

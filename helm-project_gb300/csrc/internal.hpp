@@ -202,10 +202,11 @@ struct Blocked {
 // Kernel choice for the split-FP32 apply.
 struct SplitParams {
     int variant = 1;          // 0 direct gathers, 1 blocked + cp.async chunk staging,
-                              // 2 blocked + bulk-copy (TMA) staging
+                              // 2 blocked + bulk-copy (TMA) staging, 3 blocked + producer
+                              // warp and mbarrier ring, 4 one fused launch (few fields)
     int fields_per_pass = 0;  // direct: RHS tile width; blocked: fields per work item (0 = all)
     int unroll = 4;           // direct: fields per thread iteration; staged: fields per stage
-    int stages = 2;           // blocked chunk variant: staging buffers (2 or 3)
+    int stages = 2;           // blocked: staging buffers (variants 1 and 3: 2-3, 2: 2)
 };
 
 struct Matrix {
@@ -271,8 +272,10 @@ void coastal_postpass(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matri
 // apply.cu
 void matrix_prepare(Matrix &m, int format, cudaStream_t s);
 void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, cudaStream_t s);
+// ylo (optional): low parts of the outputs, so that y + ylo carries each row
+// value s + c to about 2^-48 relative (y's bits are unchanged).
 void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
-                 cudaStream_t s);
+                 cudaStream_t s, float *ylo = nullptr, i64 ldylo = 0);
 void conservation(Matrix &m, const void *src, const void *dst, bool f32, int norm_type, double *out, cudaStream_t s);
 void nan_batch_apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, double na_thres,
                          cudaStream_t s);
@@ -285,8 +288,8 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
 // staged.cu
 void build_blocked(Matrix &m, cudaStream_t s);
 bool blocked_eligible(const Matrix &m, const void *x, i64 ldx, bool bulk);
-void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, int ns,
-                   i64 fchunk, cudaStream_t s);
+void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, int kind, int T, int ns,
+                   i64 fchunk, cudaStream_t s, float *ylo = nullptr, i64 ldylo = 0);
 int blocked_launches(const Matrix &m);
 // persistent staged kernels over the blocked layouts of several matrices
 // (batches); use[q] selects the matrices whose fields allow the staged kernels

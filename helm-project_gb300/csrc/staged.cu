@@ -112,6 +112,23 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
     return t;
 }
+__device__ __forceinline__ void mbar_arrive(std::uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Arrive on bar once every cp.async this thread issued so far has landed (the
+// barrier's expected count includes this arrival).
+__device__ __forceinline__ void cp_async_mbar_arrive(std::uint64_t *bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Wait for the phase of the given parity to complete, for at most about one
+// second; false when the bound ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t *bar, unsigned parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (globaltimer_ns() - t0 > 1000000000ull) return false;
+    return true;
+}
 
 struct BlkArgs {
     const int *blocks;  // block ids of this launch
@@ -126,12 +143,14 @@ struct BlkArgs {
     i64 nbl;                   // blocks in this launch
     i64 fchunk;                // fields per work item (multiple of the stage width)
     i64 n_src;                 // source cells: the last chunk may be partial
+    float *ylo;                // low parts of the outputs (hi+lo form), or null
+    i64 ldylo;
 };
 
 // Work item of this CTA: (field chunk, block), chunk-major so that all CTAs
 // sweep the same fields at about the same time.
 __device__ __forceinline__ int item_setup(const BlkArgs &a, const float *__restrict__ &x, i64 ldx,
-                                          float *__restrict__ &y, i64 ldy, i64 &nrhs) {
+                                          float *__restrict__ &y, i64 ldy, i64 &nrhs, float *&ylo) {
     const i64 item = blockIdx.x;
     const i64 chunk = item / a.nbl;
     const int b = a.blocks[item - chunk * a.nbl];
@@ -139,8 +158,18 @@ __device__ __forceinline__ int item_setup(const BlkArgs &a, const float *__restr
     const i64 n = nrhs - f0 < a.fchunk ? nrhs - f0 : a.fchunk;
     x += f0 * ldx;
     y += f0 * ldy;
+    ylo = a.ylo ? a.ylo + f0 * a.ldylo : nullptr;
     nrhs = n;
     return b;
+}
+
+// Low parts of two outputs of a packed pair (row value s + c, c = -cn).
+__device__ __forceinline__ void store_lo(float *ylo, i64 ldylo, i64 f, i64 row, F2 s, F2 cn, float ra, float rb) {
+    float sa, sb, ca, cb;
+    upk(s, sa, sb);
+    upk(cn, ca, cb);
+    ylo[f * ldylo + row] = sum_err(sa, -ca, ra);
+    ylo[(f + 1) * ldylo + row] = sum_err(sb, -cb, rb);
 }
 
 // Row reduction of one staged tile of T fields (field stride US floats in
@@ -148,7 +177,8 @@ __device__ __forceinline__ int item_setup(const BlkArgs &a, const float *__restr
 // the T/2 field pairs; per pair the compensated step is 9 FMA-pipe ops.
 template <int L, int T, int US>
 __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, const float *h, const float *lw, int wl,
-                                              i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy) {
+                                              i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy,
+                                              float *__restrict__ ylo, i64 ldylo) {
     if (f0 + T <= nrhs) {
         F2 sa[T / 2], cn[T / 2];
 #pragma unroll
@@ -180,6 +210,7 @@ __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, c
                 upk(sub2(sa[q], cn[q]), ra, rb);
                 y[(f0 + 2 * q) * ldy + row] = ra;
                 y[(f0 + 2 * q + 1) * ldy + row] = rb;
+                if (ylo) store_lo(ylo, ldylo, f0 + 2 * q, row, sa[q], cn[q], ra, rb);
             }
         }
     } else {
@@ -190,7 +221,11 @@ __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, c
 #pragma unroll
             for (int k = 0; k < L; ++k)
                 if (k < wl) csum1(s1, c1, h[k], lw[k], p0[li[k]]);
-            if (row >= 0) y[(f0 + f) * ldy + row] = __fadd_rn(s1, c1);
+            if (row >= 0) {
+                const float r = __fadd_rn(s1, c1);
+                y[(f0 + f) * ldy + row] = r;
+                if (ylo) ylo[(f0 + f) * ldylo + row] = sum_err(s1, c1, r);
+            }
         }
     }
 }
@@ -198,7 +233,8 @@ __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, c
 // Runtime-stride version used by the bulk-copy kernel.
 template <int L, int T>
 __device__ __forceinline__ void reduce_tile(const float *cur, int us, const int *li, const float *h, const float *lw,
-                                            int wl, i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy) {
+                                            int wl, i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy,
+                                            float *__restrict__ ylo, i64 ldylo) {
     if (f0 + T <= nrhs) {
         F2 sa[T / 2], cn[T / 2];
 #pragma unroll
@@ -222,6 +258,7 @@ __device__ __forceinline__ void reduce_tile(const float *cur, int us, const int 
                 upk(sub2(sa[q], cn[q]), ra, rb);
                 y[(f0 + 2 * q) * ldy + row] = ra;
                 y[(f0 + 2 * q + 1) * ldy + row] = rb;
+                if (ylo) store_lo(ylo, ldylo, f0 + 2 * q, row, sa[q], cn[q], ra, rb);
             }
         }
     } else {
@@ -232,7 +269,11 @@ __device__ __forceinline__ void reduce_tile(const float *cur, int us, const int 
 #pragma unroll
             for (int k = 0; k < L; ++k)
                 if (k < wl) csum1(s1, c1, h[k], lw[k], p0[li[k]]);
-            if (row >= 0) y[(f0 + f) * ldy + row] = __fadd_rn(s1, c1);
+            if (row >= 0) {
+                const float r = __fadd_rn(s1, c1);
+                y[(f0 + f) * ldy + row] = r;
+                if (ylo) ylo[(f0 + f) * ldylo + row] = sum_err(s1, c1, r);
+            }
         }
     }
 }
@@ -263,7 +304,8 @@ __device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, 
 // fields at a time through NS shared-memory buffers of US floats per field.
 template <int L, int T, int NS, int US>
 __device__ __forceinline__ void blk_item(const BlkArgs &a, int b, const float *__restrict__ x, i64 ldx,
-                                         float *__restrict__ y, i64 ldy, i64 nrhs, float *smem) {
+                                         float *__restrict__ y, i64 ldy, i64 nrhs, float *smem,
+                                         float *__restrict__ ylo) {
     static_assert(T % 2 == 0, "fields per stage must be even");
     static_assert(NS == 2 || NS == 3, "two or three staging buffers");
     float *xs = smem;                                       // [NS][T][US]
@@ -310,7 +352,7 @@ __device__ __forceinline__ void blk_item(const BlkArgs &a, int b, const float *_
         cp_async_wait<NS - 2>();  // tile t has landed (NS-2 newer groups may be pending)
         __syncthreads();          // ... for every thread, and tile t-1 is no longer read
         stage(t + NS - 1);        // refill the buffer tile t-1 used
-        reduce_tile_c<L, T, US>(xs + (t % NS) * T * US, li, h, lw, wl, t * T, nrhs, row, y, ldy);
+        reduce_tile_c<L, T, US>(xs + (t % NS) * T * US, li, h, lw, wl, t * T, nrhs, row, y, ldy, ylo, a.ldylo);
     }
     cp_async_wait<0>();
 }
@@ -319,8 +361,95 @@ template <int L, int T, int NS, int US>
 __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__restrict__ x, i64 ldx,
                                                     float *__restrict__ y, i64 ldy, i64 nrhs) {
     extern __shared__ __align__(128) float smem[];
-    const int b = item_setup(a, x, ldx, y, ldy, nrhs);
-    blk_item<L, T, NS, US>(a, b, x, ldx, y, ldy, nrhs, smem);
+    float *ylo;
+    const int b = item_setup(a, x, ldx, y, ldy, nrhs, ylo);
+    blk_item<L, T, NS, US>(a, b, x, ldx, y, ldy, nrhs, smem, ylo);
+}
+
+// Warp-specialised form of the same work item. Warps 0..kWarps-1 reduce
+// rows as in k_blk_chunk; warp kWarps is the producer: it stages tile t into
+// ring slot t % NS with cp.async and has each of its lanes arrive on the
+// slot's `full` barrier when its copies land (count 32). A row warp waits on
+// `full` only, reduces, and arrives on the slot's `empty` barrier (count
+// kWarps); the producer waits on `empty` before it refills the slot. Row
+// warps of different lengths are thus coupled only through the NS-slot ring,
+// not by a CTA-wide barrier per tile. Every wait is bounded (about 1 s); a
+// wait that runs out sets a.status and ends the item.
+template <int L, int T, int NS, int US>
+__global__ void __launch_bounds__(kRows + 32) k_blk_ws(BlkArgs a, const float *__restrict__ x, i64 ldx,
+                                                      float *__restrict__ y, i64 ldy, i64 nrhs) {
+    static_assert(T % 2 == 0, "fields per stage must be even");
+    static_assert(NS >= 2 && NS <= 3, "two or three ring slots");
+    constexpr int kThreads = kRows + 32;
+    extern __shared__ __align__(128) float smem[];
+    __shared__ __align__(8) std::uint64_t full[NS], empty[NS];
+    __shared__ volatile int abort_flag;
+    float *ylo;
+    const int b = item_setup(a, x, ldx, y, ldy, nrhs, ylo);
+    float *xs = smem;                                       // [NS][T][US]
+    int *cc = reinterpret_cast<int *>(smem + NS * T * US);  // chunk columns
+    const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
+    const int zero = 4 * nch;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int j = tid; j < nch; j += kThreads) cc[j] = a.ccol[c0 + j];
+    for (int q = tid; q < NS * T; q += kThreads)
+        *reinterpret_cast<float4 *>(xs + q * US + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tid == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&full[s], 32);
+            mbar_init(&empty[s], kWarps);
+        }
+        abort_flag = 0;
+    }
+    __syncthreads();
+    const i64 ntile = (nrhs + T - 1) / T;
+    if (warp == kWarps) {  // producer
+        for (i64 t = 0; t < ntile; ++t) {
+            const int s = static_cast<int>(t % NS);
+            if (t >= NS && !mbar_wait_bounded(&empty[s], static_cast<unsigned>((t / NS - 1) & 1))) {
+                abort_flag = 1;
+                atomicExch(a.status, 1);
+                break;
+            }
+            if (abort_flag) break;
+            float *dst = xs + s * T * US;
+            const i64 fa = t * T;
+            const int nf = static_cast<int>((nrhs - fa < static_cast<i64>(T)) ? nrhs - fa : static_cast<i64>(T));
+            const float *xt = x + fa * ldx;
+            for (int j = lane; j < nch; j += 32) {
+                const float *src = xt + cc[j];
+                const i64 left = a.n_src - cc[j];  // the chunk of the last source cells may be partial
+                if (left >= 4) {
+#pragma unroll
+                    for (int f = 0; f < T; ++f)
+                        if (f < nf) cp_async16(dst + f * US + 4 * j, src + f * ldx);
+                } else {
+#pragma unroll
+                    for (int f = 0; f < T; ++f)
+                        if (f < nf) cp_async16_part(dst + f * US + 4 * j, src + f * ldx, static_cast<int>(4 * left));
+                }
+            }
+            cp_async_mbar_arrive(&full[s]);
+        }
+        cp_async_wait<0>();
+        return;
+    }
+    int li[L];
+    float h[L], lw[L];
+    int wl;
+    i64 row;
+    load_entries<L>(a, b, zero, li, h, lw, wl, row);
+    for (i64 t = 0; t < ntile; ++t) {
+        const int s = static_cast<int>(t % NS);
+        if (!mbar_wait_bounded(&full[s], static_cast<unsigned>((t / NS) & 1))) {
+            abort_flag = 1;
+            atomicExch(a.status, 1);
+            break;
+        }
+        reduce_tile_c<L, T, US>(xs + s * T * US, li, h, lw, wl, t * T, nrhs, row, y, ldy, ylo, a.ldylo);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+    }
 }
 
 // ─── persistent form for batches of matrices ───────────────────────────────
@@ -357,7 +486,7 @@ __global__ void __launch_bounds__(kRows) k_blk_persist(const BlkDesc *__restrict
         const int b = D.a.blocks[local - chunk * D.a.nbl];
         const i64 f0 = chunk * D.a.fchunk;
         const i64 n = D.nrhs - f0 < D.a.fchunk ? D.nrhs - f0 : D.a.fchunk;
-        blk_item<L, T, NS, US>(D.a, b, D.x + f0 * D.ldx, D.ldx, D.y + f0 * D.ldy, D.ldy, n, smem);
+        blk_item<L, T, NS, US>(D.a, b, D.x + f0 * D.ldx, D.ldx, D.y + f0 * D.ldy, D.ldy, n, smem, nullptr);
         __syncthreads();  // shared memory is reused by the next item
     }
 }
@@ -371,7 +500,8 @@ __global__ void __launch_bounds__(kRows) k_blk_bulk(BlkArgs a, const float *__re
     __shared__ int abort_flag;
     const int us = a.us;
     float *xs = smem;  // [2][T][us]
-    const int b = item_setup(a, x, ldx, y, ldy, nrhs);
+    float *ylo;
+    const int b = item_setup(a, x, ldx, y, ldy, nrhs, ylo);
     const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
     const int zero = 4 * nch;
     const int r0 = a.rstart[b], nr = a.rstart[b + 1] - r0;
@@ -420,7 +550,7 @@ __global__ void __launch_bounds__(kRows) k_blk_bulk(BlkArgs a, const float *__re
         }
         __syncthreads();
         if (abort_flag) break;
-        reduce_tile<L, T>(xs + buf * T * us, us, li, h, lw, wl, t * T, nrhs, row, y, ldy);
+        reduce_tile<L, T>(xs + buf * T * us, us, li, h, lw, wl, t * T, nrhs, row, y, ldy, ylo, a.ldylo);
         __syncthreads();
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -840,10 +970,34 @@ void launch_chunk(const BlkArgs &a, int us, int ns, i64 grid, const float *x, i6
     }
 }
 
+template <int L, int T, int NS, int US>
+void launch_ws_us(const BlkArgs &a, i64 grid, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
+    size_t bytes = sizeof(float) * static_cast<size_t>(US) * NS * T + sizeof(int) * static_cast<size_t>(US / 4);
+    AXGB_CUDA(cudaFuncSetAttribute(k_blk_ws<L, T, NS, US>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(bytes)));
+    k_blk_ws<L, T, NS, US><<<static_cast<unsigned>(grid), kRows + 32, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+
 template <int L, int T>
-void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, const float *x, i64 ldx, float *y,
-                i64 ldy, i64 nrhs, i64 fchunk, cudaStream_t s) {
-    BlkArgs a;
+void launch_ws(const BlkArgs &a, int us, int ns, i64 grid, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs,
+               cudaStream_t s) {
+    if (us <= kUsSmall) {
+        if (ns >= 3)
+            launch_ws_us<L, T, 3, kUsSmall>(a, grid, x, ldx, y, ldy, nrhs, s);
+        else
+            launch_ws_us<L, T, 2, kUsSmall>(a, grid, x, ldx, y, ldy, nrhs, s);
+    } else {
+        launch_ws_us<L, T, 2, kUsLarge>(a, grid, x, ldx, y, ldy, nrhs, s);
+    }
+}
+
+template <int L, int T>
+void launch_one(const Blocked &B, const Blocked::Launch &l, int kind, int ns, const float *x, i64 ldx, float *y,
+                i64 ldy, i64 nrhs, i64 fchunk, cudaStream_t s, float *ylo, i64 ldylo) {
+    const bool bulk = kind == 2;
+    BlkArgs a{};
+    a.ylo = ylo;
+    a.ldylo = ldylo;
     a.nbl = l.n;
     a.fchunk = (fchunk <= 0 || fchunk >= nrhs) ? nrhs : (fchunk + T - 1) / T * T;
     const i64 grid = l.n * ((nrhs + a.fchunk - 1) / a.fchunk);
@@ -861,7 +1015,9 @@ void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, c
     a.us = l.us;
     a.status = B.status.p;
     a.n_src = B.n_src;
-    if (bulk) {
+    if (kind == 3) {
+        if constexpr (T == 4) launch_ws<L, T>(a, l.us, ns, grid, x, ldx, y, ldy, nrhs, s);  // four fields per stage only
+    } else if (bulk) {
         size_t bytes = sizeof(float) * static_cast<size_t>(l.us) * 2 * T;
         AXGB_CUDA(cudaFuncSetAttribute(k_blk_bulk<L, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(bytes)));
@@ -872,34 +1028,34 @@ void launch_one(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, c
 }
 
 template <int T>
-void launch_class(const Blocked &B, const Blocked::Launch &l, bool bulk, int ns, const float *x, i64 ldx, float *y,
-                  i64 ldy, i64 nrhs, i64 fchunk, cudaStream_t s) {
+void launch_class(const Blocked &B, const Blocked::Launch &l, int kind, int ns, const float *x, i64 ldx, float *y,
+                  i64 ldy, i64 nrhs, i64 fchunk, cudaStream_t s, float *ylo, i64 ldylo) {
     {
         if (l.n == 0) return;
         // T = 8 staging of the largest buckets would exceed shared memory: use 4 there
         const bool big = static_cast<size_t>(l.us) * 2 * T * sizeof(float) > 200 * 1024;
         if (T == 8 && big) {
             switch (l.L) {
-                case 4: launch_one<4, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 8: launch_one<8, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 12: launch_one<12, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 16: launch_one<16, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 20: launch_one<20, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 24: launch_one<24, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                case 28: launch_one<28, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-                default: launch_one<32, 4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+                case 4: launch_one<4, 4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+                case 8: launch_one<8, 4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+                case 12: launch_one<12, 4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+                case 16: launch_one<16, 4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+                case 20: launch_one<20, 4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+                case 24: launch_one<24, 4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+                case 28: launch_one<28, 4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+                default: launch_one<32, 4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
             }
             return;
         }
         switch (l.L) {
-            case 4: launch_one<4, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 8: launch_one<8, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 12: launch_one<12, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 16: launch_one<16, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 20: launch_one<20, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 24: launch_one<24, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            case 28: launch_one<28, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
-            default: launch_one<32, T>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, s); break;
+            case 4: launch_one<4, T>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+            case 8: launch_one<8, T>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+            case 12: launch_one<12, T>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+            case 16: launch_one<16, T>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+            case 20: launch_one<20, T>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+            case 24: launch_one<24, T>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+            case 28: launch_one<28, T>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
+            default: launch_one<32, T>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, s, ylo, ldylo); break;
         }
     }
 }
@@ -1045,8 +1201,8 @@ void blk_batch_launch(BlkBatch &bb, cudaStream_t s) {
     AXGB_CUDA(cudaGetLastError());
 }
 
-void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, bool bulk, int T, int ns,
-                   i64 fchunk, cudaStream_t s) {
+void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, int kind, int T, int ns,
+                   i64 fchunk, cudaStream_t s, float *ylo, i64 ldylo) {
     Blocked &B = m.blocked;
     // Classes run concurrently on a small stream pool (fork/join through
     // events on the caller's stream, so the call stays stream-ordered and
@@ -1068,11 +1224,11 @@ void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nr
         const Blocked::Launch &l = B.launches[B.order[i]];
         cudaStream_t st = B.pool[i % kPool];
         if (T >= 8)
-            launch_class<8>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, st);
+            launch_class<8>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, st, ylo, ldylo);
         else if (T >= 4)
-            launch_class<4>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, st);
+            launch_class<4>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, st, ylo, ldylo);
         else
-            launch_class<2>(B, l, bulk, ns, x, ldx, y, ldy, nrhs, fchunk, st);
+            launch_class<2>(B, l, kind, ns, x, ldx, y, ldy, nrhs, fchunk, st, ylo, ldylo);
     }
     for (int q = 0; q < used; ++q) {
         AXGB_CUDA(cudaEventRecord(B.join[q], B.pool[q]));

@@ -235,16 +235,31 @@ int axgb_apply_f64(int matrix_handle, const double *x, int64_t ld_x, double *y, 
 int axgb_apply_f32split(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                         axgb_stream_t stream);
 
+/* axgb_apply_f32split with a second output: y is bitwise the result of
+ * axgb_apply_f32split (every split kernel gives the same bits), and
+ * y_lo[:, v] ([nrhs][ld_lo])
+ * receives the rounding error of each stored value, so that y + y_lo in
+ * FP64 carries the compensated row sum to about 2^-48 relative: the form for
+ * conservation-grade results (global integrals of y + y_lo meet the FP64
+ * apply's), at 4 more bytes per output written. Replaces no reference
+ * interface (the reference applies in FP64 only). */
+int axgb_apply_f32split_hilo(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, float *y_lo,
+                             int64_t ld_lo, int64_t nrhs, axgb_stream_t stream);
+
 /* Same, kernel choice explicit. variant 0: direct gathers from global
  * memory, fields_per_pass = RHS tile width (0 = all), unroll = fields per
- * thread iteration (1, 2 or 4). variants 1 and 2: rows in blocks of 4
+ * thread iteration (1, 2 or 4). variants 1 to 3: rows in blocks of 4
  * slices grouped by source locality; per block the source values are staged
  * in shared memory as 16-byte chunks, variant 1 with cp.async by all
  * threads (two staging buffers), variant 2 with bulk (TMA) copies completing
- * on an mbarrier; unroll = fields per stage (2, 4 or 8), fields_per_pass =
- * fields per work item of a block (0 = all). Variants 1 and 2 need x 16-byte
- * aligned and ld_x a multiple of 4 (variant 2 also n_src a multiple of 4);
- * otherwise the direct kernel runs. */
+ * on an mbarrier, variant 3 with cp.async by a producer warp into a ring of
+ * two or three slots guarded by mbarriers (4 fields per stage); unroll =
+ * fields per stage (2, 4 or 8),
+ * fields_per_pass = fields per work item of a block (0 = all). Variants 1
+ * to 3 need x 16-byte aligned and ld_x a multiple of 4 (variant 2 also n_src
+ * a multiple of 4); otherwise the direct kernel runs. variant 4: the whole
+ * matrix in one launch (for one or a few fields); the other knobs are
+ * unused. Every variant gives the same bits. */
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                               int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 
@@ -258,7 +273,8 @@ int axgb_set_autotune(int enable);
 
 /* Read or seed the cached kernel choice of (matrix, nrhs) that
  * axgb_apply_f32split uses: choice[4] = variant, fields_per_pass, unroll,
- * stages (stages 2 or 3, variant 1 only), as axgb_autotune_f32split returns
+ * stages (staging buffers: 2 or 3 with variants 1 and 3, else 2), as
+ * axgb_autotune_f32split returns
  * it. Seeding lets a caller reuse a choice tuned in an earlier process
  * without timing again. When nothing is cached for (matrix, nrhs), get
  * sets *cached = 0 and returns the default choice. */
@@ -304,8 +320,11 @@ int axgb_batch_apply_host_f32split(int matrix_handle, const float *src, int64_t 
  * A batch groups k matrices, each with its own field count. axgb_batch_apply
  * runs all of them (split-FP32) in one persistent kernel fed by a work queue
  * over (matrix, row slice, field tile) items, replayed from a CUDA graph
- * captured on first use per stream and per pointer set. No reference
- * counterpart: the reference applies one matrix per call. */
+ * captured on first use per stream and per pointer set. A batch's graphs
+ * share its work counters and descriptors: a call on another stream than
+ * the previous call's waits on the GPU for the previous call's work, so one
+ * batch never runs on two streams at once. No reference counterpart: the
+ * reference applies one matrix per call. */
 int axgb_batch_create(const int *matrix_handles, const int64_t *nrhs, int count, int *batch_handle);
 int axgb_batch_apply(int batch_handle, const float *const *x, const int64_t *ld_x, float *const *y,
                      const int64_t *ld_y, axgb_stream_t stream);

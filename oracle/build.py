@@ -30,7 +30,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_INCLUDE = "/root/reference/libs/axis/include"
+# The reference checkout: $AXGB_REFERENCE_ROOT, else a directory "reference"
+# beside the repository.
+REF_ROOT = os.environ.get("AXGB_REFERENCE_ROOT") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
+REF_INCLUDE = os.path.join(REF_ROOT, "libs", "axis", "include")
 FLAGS = ["-std=c++20", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp"]
 
 
@@ -64,7 +67,7 @@ def build_ref(force: bool = False) -> str | None:
     return out
 
 
-REF_SRC = "/root/reference/libs/axis/src/solver"
+REF_SRC = os.path.join(REF_ROOT, "libs", "axis", "src", "solver")
 FAST_SOURCES = ["weight_generator_conservative_rect.cpp", "weight_generator_conservative_rect_nonuniform.cpp",
                 "weight_generator_bilinear_rect.cpp", "weight_generator_bilinear_rect_nonuniform.cpp"]
 

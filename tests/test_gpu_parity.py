@@ -184,7 +184,7 @@ def test_apply_split_parity(gpu, oracle, cfg1):
     xs = torch.tensor(X, device="cuda")
     outs = []
     for v, fpp, u in ((0, 0, 1), (0, 0, 2), (0, 0, 4), (0, 3, 2), (0, 1, 1), (1, 0, 2), (1, 0, 4), (1, 0, 8),
-                      (2, 0, 2), (2, 0, 4), (2, 0, 8)):
+                      (2, 0, 2), (2, 0, 4), (2, 0, 8), (3, 0, 4), (3, 2, 4), (4, 0, 1)):
         y = gpu.apply_f32split(M, xs, fields_per_pass=fpp, unroll=u, variant=v).cpu().numpy()
         err = np.max(np.abs(y - ref) / np.abs(ref))
         assert err < SPLIT_RTOL, (v, fpp, u, err)
@@ -217,7 +217,7 @@ def test_autotune_and_batch(gpu, oracle, cfg1):
     X = torch.tensor(np.stack([f] * 5).astype(np.float32), device="cuda")
     Y = torch.empty((5, M.n_dst), dtype=torch.float32, device="cuda")
     best = gpu.autotune_f32split(M, X, Y)
-    assert best["variant"] in (0, 1) and best["unroll"] in (1, 2, 4, 8)
+    assert best["variant"] in (0, 1, 2, 3, 4) and best["unroll"] in (1, 2, 4, 8)
     ref = gpu.apply_f32split(M, X, fields_per_pass=0, unroll=1).cpu().numpy()
     assert np.array_equal(gpu.apply_f32split(M, X).cpu().numpy(), ref)  # tuned choice, same bits
     # persistent multi-matrix batch: same matrix twice plus a reversed pair
@@ -261,6 +261,15 @@ def test_kernel_choice_seed_and_read(gpu, oracle, cfg1):
     assert np.max(np.abs(y - ref) / np.abs(ref)) < SPLIT_RTOL
     with pytest.raises(gpu.InvalidArgument):
         gpu.set_kernel_choice(M, nrhs, variant=2, fields_per_pass=0, unroll=4, stages=3)
+    with pytest.raises(gpu.InvalidArgument):
+        gpu.set_kernel_choice(M, nrhs, variant=5, fields_per_pass=0, unroll=4, stages=2)
+    with pytest.raises(gpu.InvalidArgument):
+        gpu.set_kernel_choice(M, nrhs, variant=3, fields_per_pass=0, unroll=4, stages=4)
+    with pytest.raises(gpu.InvalidArgument):
+        gpu.set_kernel_choice(M, nrhs, variant=3, fields_per_pass=0, unroll=8, stages=3)
+    for v, ns in ((3, 2), (3, 3), (4, 2)):  # producer-warp ring, fused single launch
+        gpu.set_kernel_choice(M, nrhs, variant=v, fields_per_pass=0, unroll=4, stages=ns)
+        assert np.array_equal(gpu.apply_f32split(M, X).cpu().numpy().astype(np.float64), y)
 
 
 def test_long_rows_parity(gpu, oracle):
@@ -278,19 +287,132 @@ def test_long_rows_parity(gpu, oracle):
     ref = oracle.apply_csr(wo, X.astype(np.float64), compensated=True)
     xs = torch.tensor(X, device="cuda")
     outs = [gpu.apply_f32split(M, xs, fields_per_pass=fpp, unroll=u, variant=v).cpu().numpy()
-            for v, fpp, u in ((0, 0, 1), (0, 8, 4), (1, 0, 4), (1, 16, 8), (2, 0, 4))]
+            for v, fpp, u in ((0, 0, 1), (0, 8, 4), (1, 0, 4), (1, 16, 8), (2, 0, 4), (3, 0, 4), (4, 0, 1))]
     for y in outs[1:]:
         assert np.array_equal(y, outs[0])
     scale = np.abs(ref).max()
     assert np.max(np.abs(outs[0] - ref)) / scale < 1e-6
     y64 = gpu.apply_f64(M, xs.to(torch.float64)).cpu().numpy()
     assert np.max(np.abs(y64 - ref)) / scale < 1e-13
+    # one and two fields take the fused FP64 launch: the same bits per field
+    for k in (1, 2):
+        assert np.array_equal(gpu.apply_f64(M, xs[:k].to(torch.float64)).cpu().numpy(), y64[:k])
     B = gpu.Batch([M], [37])
     yb = torch.empty((37, M.n_dst), dtype=torch.float32, device="cuda")
     for _ in range(2):
         B.apply([xs], [yb])
         torch.cuda.synchronize()
         assert np.array_equal(yb.cpu().numpy(), outs[0])
+
+
+COND_PAIRS = [
+    ("1deg->C48", lambda: (grids.latlon_deg(1.0), grids.cubed_sphere(48))),
+    ("C48->1deg", lambda: (grids.cubed_sphere(48), grids.latlon_deg(1.0))),
+    ("0.5deg->C24", lambda: (grids.latlon_deg(0.5), grids.cubed_sphere(24))),  # rows of 50-90 entries
+    ("voronoi40962->2deg", lambda: (grids.voronoi(40962, seed=5), grids.latlon_deg(2.0))),
+]
+
+
+@pytest.mark.parametrize("name,make", COND_PAIRS)
+def test_apply_condition_bound_zero_mean(gpu, oracle, name, make):
+    """Per-output error bound scaled by each output's condition: with
+    c_i = sum_j |w_ij x_j|, the FP64 apply satisfies |y_i - y_ref_i| <=
+    1e-13 c_i and the split-FP32 apply |y_i - y_ref_i| <= 1e-6 c_i, on
+    zero-mean spherical-harmonic fields (no offset), whose outputs cross
+    zero, so a bound relative to |y_ref_i| alone would not hold there.
+    y_ref is the compensated FP64 oracle on the same (FP32-rounded) inputs."""
+    import torch
+    src, dst = make()
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    wo = oracle.conservative(src, dst)
+    xyz = grids.cell_centroids_xyz(src)
+    rng = np.random.default_rng(11)
+    base = fields.sh_fields(xyz, 32, [21, 22, 23]).numpy()
+    X = np.concatenate([base * s for s in rng.lognormal(0, 1, 3)]).astype(np.float32).astype(np.float64)
+    ref = oracle.apply_csr(wo, X, compensated=True)
+    cond = oracle.apply_csr(wo, np.abs(X), compensated=True)  # conservative weights are >= 0
+    assert np.all(wo.w >= 0)
+    assert (ref < 0).any() and (ref > 0).any()  # outputs cross zero
+    xd = torch.tensor(X, device="cuda")
+    y64 = gpu.apply_f64(M, xd).cpu().numpy()
+    r64 = np.abs(y64 - ref) / np.maximum(cond, 1e-300)
+    assert r64.max() <= F64_RTOL, r64.max()
+    ys = gpu.apply_f32split(M, xd.to(torch.float32)).cpu().numpy()
+    rs = np.abs(ys - ref) / np.maximum(cond, 1e-300)
+    assert rs.max() <= SPLIT_RTOL, rs.max()
+
+
+HILO_PAIRS = [
+    ("1deg->C48", lambda: (grids.latlon_deg(1.0), grids.cubed_sphere(48))),
+    ("0.5deg->C24", lambda: (grids.latlon_deg(0.5), grids.cubed_sphere(24))),  # long rows
+    ("voronoi40962->2deg", lambda: (grids.voronoi(40962, seed=5), grids.latlon_deg(2.0))),  # renumbered source
+]
+
+
+@pytest.mark.parametrize("name,make", HILO_PAIRS)
+def test_apply_split_hilo(gpu, oracle, name, make):
+    """hi+lo output form: y is bitwise the plain split apply's result under
+    every kernel variant; y + y_lo (summed in FP64) is within 1e-13 of the
+    compensated FP64 oracle relative to c_i = sum_j |w_ij x_j|, on zero-mean
+    fields; and the destination integral of the conservation report
+    (conservation.cpp:83-96) equals the one of the oracle's compensated apply
+    within 1e-13 of the integral of c (its condition)."""
+    import torch
+    src, dst = make()
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    wo = oracle.conservative(src, dst)
+    xyz = grids.cell_centroids_xyz(src)
+    rng = np.random.default_rng(12)
+    base = fields.sh_fields(xyz, 24, [31, 32]).numpy()
+    X = np.concatenate([base * s for s in rng.lognormal(0, 1, 4)]).astype(np.float32)
+    nrhs = X.shape[0]
+    X64 = X.astype(np.float64)
+    ref = oracle.apply_csr(wo, X64, compensated=True)
+    cond = oracle.apply_csr(wo, np.abs(X64), compensated=True)
+    xd = torch.tensor(X, device="cuda")
+    plain = gpu.apply_f32split(M, xd, fields_per_pass=0, unroll=1, variant=0).cpu().numpy()
+    for v, fpp, u, ns in ((0, 0, 2, 2), (0, 3, 4, 2), (1, 0, 4, 2), (1, 4, 8, 3), (3, 0, 4, 3)):
+        gpu.set_kernel_choice(M, nrhs, variant=v, fields_per_pass=fpp, unroll=u, stages=ns)
+        y, ylo = gpu.apply_f32split_hilo(M, xd)
+        y, ylo = y.cpu().numpy(), ylo.cpu().numpy()
+        assert np.array_equal(y, plain), (v, fpp, u)
+        hl = y.astype(np.float64) + ylo.astype(np.float64)
+        err = np.abs(hl - ref) / np.maximum(cond, 1e-300)
+        assert err.max() <= 1e-13, (v, fpp, u, err.max())
+    assert M.device_status() == 0
+    hl_d = torch.tensor(hl, device="cuda")
+    for k in range(nrhs):
+        rep = gpu.check_conservation(M, xd[k].to(torch.float64), hl_d[k])
+        ro = oracle.conservation(wo, X64[k], ref[k])
+        scale = float(np.sum(wo.area_b * cond[k]))
+        assert abs(rep["dst_integral"] - ro["dst_integral"]) <= 1e-13 * scale, (k, rep, ro)
+    with pytest.raises(gpu.InvalidArgument):
+        gpu.apply_f32split_hilo(M, xd, y_lo=torch.empty((nrhs, M.n_dst - 1), dtype=torch.float32, device="cuda"))
+
+
+def test_batch_on_two_streams(gpu, oracle, cfg1):
+    """One batch applied alternately on two streams, with different fields on
+    each: the second stream's call waits for the first's work on the GPU
+    (the batch's work counters and descriptors are shared), so both outputs
+    equal the per-call path bit for bit."""
+    import torch
+    src, dst, M, wo, f = cfg1
+    rng = np.random.default_rng(17)
+    Xa = torch.tensor(np.stack([f * s for s in rng.lognormal(0, 1, 6)]).astype(np.float32), device="cuda")
+    Xb = torch.tensor(np.stack([-f * s for s in rng.lognormal(0, 1, 6)]).astype(np.float32), device="cuda")
+    ra = gpu.apply_f32split(M, Xa, fields_per_pass=0, unroll=1).cpu().numpy()
+    rb = gpu.apply_f32split(M, Xb, fields_per_pass=0, unroll=1).cpu().numpy()
+    B = gpu.Batch([M], [6])
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    ya = torch.empty((6, M.n_dst), dtype=torch.float32, device="cuda")
+    yb = torch.empty((6, M.n_dst), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(3):
+        B.apply([Xa], [ya], stream=s1)
+        B.apply([Xb], [yb], stream=s2)
+    torch.cuda.synchronize()
+    assert np.array_equal(ya.cpu().numpy(), ra)
+    assert np.array_equal(yb.cpu().numpy(), rb)
 
 
 def test_one_dimensional_fields(gpu, oracle, cfg1):
