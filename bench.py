@@ -140,6 +140,22 @@ def rel_errors(y, ref):
             "rms_rel": float(np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean(ref ** 2)))}
 
 
+def cond_errors(y, ref, cond):
+    """Error of each output scaled by its condition c_i = sum_j |w_ij x_j|
+    (outputs that cross zero keep a meaningful bound), max over outputs."""
+    d = np.abs(y.astype(np.float64) - ref)
+    return float(np.max(d / np.maximum(cond, 1e-300)))
+
+
+def weight_parity(M, wo):
+    """Index set and weights of a GPU matrix against the oracle's."""
+    csr = M.to_csr()
+    rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
+    same = bool(M.nnz == wo.nnz and np.array_equal(rows, wo.row) and np.array_equal(csr["col"], wo.col))
+    wrel = float(np.max(np.abs(csr["val"] - wo.w) / np.maximum(np.abs(wo.w), 1e-300))) if same and M.nnz else None
+    return {"index_set_identical": same, "weights_max_rel": wrel, "nnz": int(M.nnz), "oracle_nnz": int(wo.nnz)}
+
+
 def cpu_apply_rate(oracle, wo, X_cpu):
     """dst-vals/s of the oracle's CSR FP64 apply (OpenMP rows) on X_cpu."""
     t0 = time.perf_counter()
@@ -214,6 +230,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="axgb", choices=["axgb", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-voronoi", action="store_true",
+                    help="skip the 2,621,442-cell Voronoi -> 0.1 deg case of the default run (its mesh is generated "
+                         "on the host in a background process while the headline is measured)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nrhs", type=int, default=NRHS,
                     help="fields per step (default 1016 = 8 tracers x 127 levels; smaller values make "
@@ -265,6 +284,16 @@ def main():
 
     barrier = replicas.barrier
 
+    # the Voronoi mesh of the large unstructured case takes a minute or two of
+    # host time: generate it in a spawned process while the GPU works
+    vor_job = vor_path = None
+    if rank == 0 and not args.apply_only and not args.no_voronoi:
+        import multiprocessing as mp
+        import tempfile
+        vor_path = os.path.join(tempfile.mkdtemp(prefix="axgb_vor_"), "mesh.npz")
+        vor_job = mp.get_context("spawn").Process(target=voronoi_mesh_job, args=(vor_path,), daemon=True)
+        vor_job.start()
+
     # ── weights for the headline workload ──
     t0 = time.perf_counter()
     src_g, dst_g = grids.cubed_sphere(768), grids.latlon_deg(0.25)
@@ -285,6 +314,7 @@ def main():
     nrhs = max(1, min(args.nrhs, NRHS))
     X, scales = make_fields(xyz, nrhs)
     torch.cuda.synchronize()
+    e2e_bufs = e2e_alloc(M, X) if rank == 0 and not args.apply_only and not args.no_e2e else None
     log(f"fields {time.perf_counter() - t0:.1f}s")
     Y = torch.empty((nrhs, M.n_dst), dtype=torch.float32, device=dev)
     t0 = time.perf_counter()
@@ -384,10 +414,20 @@ def main():
         sample = sorted({0, 1, min(500, nrhs - 1), nrhs - 1})
         Xs = X[sample].to(torch.float64).cpu().numpy()
         ref = o.apply_csr(wo, Xs, compensated=True)
+        cond = o.apply_csr(wo, np.abs(Xs), compensated=True)
         e_split = rel_errors(Y[sample].cpu().numpy(), ref)
         e_f64 = rel_errors(Y64[sample].cpu().numpy(), ref)
+        e_split["max_err_over_cond"] = cond_errors(Y[sample].cpu().numpy(), ref, cond)
+        e_f64["max_err_over_cond"] = cond_errors(Y64[sample].cpu().numpy(), ref, cond)
         cons_split = axgb.check_conservation(M, X[0], Y[0])
         cons_f64 = axgb.check_conservation(M, X64[0], Y64[0])
+        # hi+lo output of the split apply (y + y_lo in FP64) and the oracle's own compensated apply, same field
+        yh, yl = axgb.apply_f32split_hilo(M, X[:1])
+        hilo = yh[0].to(torch.float64) + yl[0].to(torch.float64)
+        cons_hilo = axgb.check_conservation(M, X64[0], hilo)
+        cons_exact = o.conservation(wo, Xs[0], ref[0])
+        e_hilo = cond_errors(hilo.cpu().numpy()[None], ref[:1], cond[:1])
+        del yh, yl, hilo
         # operator conservation: sum_j w_ij area_b_j = area_a_i frac_a_i
         colsum = np.bincount(csr["col"], weights=csr["val"] * csr["area_b"][rows], minlength=M.n_src)
         rhs = csr["area_a"] * csr["frac_a"]
@@ -396,23 +436,42 @@ def main():
                             "oracle_weightgen_s": t_oracle, "split": e_split, "fp64": e_f64,
                             "sampled_rhs": sample}
         result["conservation"] = {"split_field_rel": cons_split["relative_error"],
-                                  "fp64_field_rel": cons_f64["relative_error"], "operator_max_rel": op_cons}
+                                  "split_hilo_field_rel": cons_hilo["relative_error"],
+                                  "fp64_field_rel": cons_f64["relative_error"],
+                                  "oracle_exact_field_rel": cons_exact["relative_error"],
+                                  "operator_max_rel": op_cons, "split_hilo_max_err_over_cond": e_hilo,
+                                  "field": "field 0 (tracer 0, level 0)",
+                                  "note": "oracle_exact_field_rel is the compensated FP64 oracle apply of the same "
+                                          "field: the floor the reference's own weights and areas set"}
         log("parity", result["parity"])
         log("conservation", result["conservation"])
         del X64, Y64
         torch.cuda.empty_cache()
 
         # ── end to end through the host-buffer C ABI ──
-        if not args.no_e2e:
-            result["e2e"] = e2e(M, X, args)
+        if e2e_bufs is not None:
+            result["e2e"] = e2e_run(M, e2e_bufs, args)
+            del e2e_bufs
         # ── weight generation for 0.25 deg -> C384 ──
         result["weightgen_0p25_to_c384"] = weightgen_c384(md, dst_g)
         # ── single-field configurations (1 deg -> C48, 0.25 deg -> C384) ──
         result["single_field_configs"] = small_configs(o)
         log("single-field", result["single_field_configs"])
         # ── uneven batch of 17 grid pairs in one persistent launch ──
-        result["batch_17_pairs"] = batch_pairs(args)
+        result["batch_17_pairs"] = batch_pairs(args, o)
         log("batch", {k: v for k, v in result["batch_17_pairs"].items() if k not in ("pairs", "nrhs")})
+        # ── large unstructured case: Voronoi 2,621,442 cells -> 0.1 deg ──
+        if vor_job is not None:
+            vor_job.join(timeout=1200)
+            if vor_job.exitcode == 0:
+                src_v, t_mesh = load_voronoi_mesh(vor_path)
+                result["voronoi_2p6M_to_0p1deg"] = voronoi_case(args, src_v, o, t_mesh)
+                del src_v
+                log("voronoi", {k: result["voronoi_2p6M_to_0p1deg"].get(k) for k in ("ms_per_step", "parity")})
+            else:
+                if vor_job.is_alive():
+                    vor_job.terminate()
+                result["voronoi_2p6M_to_0p1deg"] = {"error": f"mesh generation exit code {vor_job.exitcode}"}
         # ── CPU baseline: oracle CSR apply on this host ──
         if not args.no_cpu:
             ns = min(64, nrhs)
@@ -460,11 +519,12 @@ def profiled_traffic():
     return None
 
 
-def e2e(M, X, args):
+def e2e_alloc(M, X):
+    """Pinned host copies of the headline fields and outputs, made before the
+    oracle and the other host work of the run allocate host memory."""
     import torch
-
-    import axgb
-    need = 4 * (M.n_src + M.n_dst) * NRHS
+    nrhs = X.shape[0]
+    need = 4 * (M.n_src + M.n_dst) * nrhs
     avail = 0
     try:
         for ln in open("/proc/meminfo"):
@@ -472,12 +532,45 @@ def e2e(M, X, args):
                 avail = int(ln.split()[1]) * 1024
     except OSError:
         pass
-    nrhs = NRHS
     if avail and need > 0.6 * avail:
-        nrhs = max(8, int(NRHS * 0.6 * avail / need))
+        nrhs = max(8, int(nrhs * 0.6 * avail / need))
     Xh = torch.empty((nrhs, M.n_src), dtype=torch.float32, pin_memory=True)
     Yh = torch.empty((nrhs, M.n_dst), dtype=torch.float32, pin_memory=True)
     Xh.copy_(X[:nrhs])
+    return Xh, Yh, nrhs
+
+
+def link_floor_ms(M, Xh, Yh, reps=3):
+    """The same bytes as one host-buffer apply moved by plain copies alone:
+    host->device chunks on one stream and device->host chunks on another,
+    concurrently (the floor the host link sets for the end-to-end step)."""
+    import torch
+    nrhs = Xh.shape[0]
+    per = max(1, (1 << 26) // (M.n_src + M.n_dst))
+    dx = torch.empty((2, per, M.n_src), dtype=torch.float32, device="cuda")
+    dy = torch.zeros((2, per, M.n_dst), dtype=torch.float32, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    best = 1e30
+    for _ in range(reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(s1):
+            for c, v0 in enumerate(range(0, nrhs, per)):
+                nv = min(per, nrhs - v0)
+                dx[c % 2, :nv].copy_(Xh[v0:v0 + nv], non_blocking=True)
+        with torch.cuda.stream(s2):
+            for c, v0 in enumerate(range(0, nrhs, per)):
+                nv = min(per, nrhs - v0)
+                Yh[v0:v0 + nv].copy_(dy[c % 2, :nv], non_blocking=True)
+        torch.cuda.synchronize()
+        best = min(best, time.perf_counter() - t0)
+    del dx, dy
+    return 1e3 * best
+
+
+def e2e_run(M, bufs, args):
+    import axgb
+    Xh, Yh, nrhs = bufs
     steps = max(3, min(args.steps, 5))
     for _ in range(1):
         axgb.batch_apply_host_f32split(M, Xh, Yh)
@@ -487,30 +580,48 @@ def e2e(M, X, args):
         axgb.batch_apply_host_f32split(M, Xh, Yh)
         t.append(time.perf_counter() - t0)
     s = statistics.mean(t)
+    floor = link_floor_ms(M, Xh, Yh)
     return {"value": M.n_dst * nrhs / s, "unit": UNIT, "h2d_bytes_per_step": 4 * M.n_src * nrhs,
             "d2h_bytes_per_step": 4 * M.n_dst * nrhs, "ms_per_step": 1e3 * s, "nrhs": nrhs,
+            "link_floor_ms": floor, "frac_of_link_floor": floor / (1e3 * s),
+            "link_floor": "the same bytes by plain chunked copies, host->device and device->host concurrently",
             "api": "axgb_batch_apply_host_f32split (pinned host buffers)"}
 
 
-def voronoi_main(args):
+VORONOI = dict(n=2621442, seed=5, jitter=0.2, lloyd=5)
+
+
+def voronoi_mesh_job(path):
+    """Generate the config-5 Voronoi mesh and save it (run in a spawned
+    process while the GPU measures the headline workload)."""
+    from axgb import grids
+    t0 = time.perf_counter()
+    g = grids.voronoi(**VORONOI)
+    np.savez(path, node=g.node_lonlat, off=g.conn_offsets, idx=g.conn_indices, seconds=time.perf_counter() - t0)
+
+
+def load_voronoi_mesh(path):
+    from axgb import grids
+    d = np.load(path)
+    return grids.MeshArrays(d["node"], d["off"], d["idx"], name=f"voronoi{VORONOI['n']}"), float(d["seconds"])
+
+
+def voronoi_case(args, src_g, o, t_mesh, timed_steps=None):
     """Large unstructured case: a 2,621,442-cell spherical Voronoi mesh
     (seeded jittered Fibonacci generators, 5 Lloyd iterations) -> 0.1 deg
     lat-lon (6,480,000 cells). Conservative weights generated on the GPU
     (pairs/s), then the split-FP32 apply of 64 FP32 fields (8 seeded
     spherical-harmonic fields with l <= 256, each at 8 seeded lognormal
     scales) against the plain FP64 apply, with the whole weight set, sampled
-    field errors and the conservation errors checked against the CPU oracle."""
+    field errors and the conservation errors checked against the CPU oracle
+    (o; None skips the oracle checks)."""
     import torch
 
     import axgb
     from axgb import fields, grids
-    axgb.init(0)
     dev = torch.device("cuda", 0)
-    t0 = time.perf_counter()
-    src_g = grids.voronoi(2621442, seed=5, jitter=0.2, lloyd=5)
+    steps = timed_steps or args.steps
     dst_g = grids.latlon_deg(0.1)
-    t_mesh = time.perf_counter() - t0
-    log(f"voronoi mesh {t_mesh:.1f}s")
     ms, md = axgb.Mesh.from_grid(src_g), axgb.Mesh.from_grid(dst_g)
     times = []
     for _ in range(3):
@@ -519,7 +630,7 @@ def voronoi_main(args):
         M = axgb.generate_weights(ms, md, {"method": "conservative"})
         times.append(time.perf_counter() - t0)
     st = M.stats()
-    log(f"weights {min(times):.3f}s nnz={M.nnz} {st}")
+    log(f"voronoi weights {min(times):.3f}s nnz={M.nnz} {st}")
     nrhs = 64
     xyz = torch.tensor(grids.cell_centroids_xyz(src_g), device=dev)
     base = fields.sh_fields(xyz, 256, [7000 + k for k in range(8)], chunk=1 << 20)
@@ -531,7 +642,7 @@ def voronoi_main(args):
     for k in range(8):
         sc = torch.tensor(scales[k], dtype=torch.float64, device=dev)
         X[8 * k:8 * k + 8] = (base[k][None, :] * sc[:, None]).to(torch.float32)
-    del base
+    del base, xyz
     Y = torch.empty((nrhs, M.n_dst), dtype=torch.float32, device=dev)
     M.prepare(2)
     if args.kernel:
@@ -540,7 +651,7 @@ def voronoi_main(args):
         axgb.set_kernel_choice(M, nrhs, **tuned)
     else:
         tuned = axgb.autotune_f32split(M, X, Y)
-    log(f"kernel: {tuned}")
+    log(f"voronoi kernel: {tuned}")
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -549,43 +660,22 @@ def voronoi_main(args):
             fn()
         torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             fn()
         e1.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / args.steps
+        return e0.elapsed_time(e1) / steps
 
     clk = ClockSampler(0)
     clk.start()
     ms_split = timed(lambda: axgb.apply_f32split(M, X, Y, stream=stream))
     clocks = clk.stop()
-    if args.apply_only:
-        log(f"split {ms_split:.3f} ms")
-        return 0
-    X64 = X.to(torch.float64)
-    Y64 = torch.empty((nrhs, M.n_dst), dtype=torch.float64, device=dev)
-    M.prepare(0)
-    ms64 = timed(lambda: axgb.apply_f64(M, X64, Y64, stream=stream))
     bytes_split = 4 * (M.n_src + M.n_dst) * nrhs + 12 * M.nnz + 4 * (M.n_dst + 1)
     peak, peak_kind = peaks()
     achieved = bytes_split / (ms_split / 1e3) / 1e9
-    log(f"split {ms_split:.3f} ms ({achieved:.0f} GB/s), fp64 {ms64:.3f} ms")
-    from oracle import Oracle
-    o = Oracle()
-    o.threads(os.cpu_count() or 1)
-    t0 = time.perf_counter()
-    wo = o.conservative(src_g, dst_g)
-    t_oracle = time.perf_counter() - t0
-    csr = M.to_csr()
-    rows = np.repeat(np.arange(M.n_dst), np.diff(csr["row_ptr"]))
-    same = M.nnz == wo.nnz and np.array_equal(rows, wo.row) and np.array_equal(csr["col"], wo.col)
-    wrel = float(np.max(np.abs(csr["val"] - wo.w) / wo.w)) if same else None
-    sample = [0, 9, 35, 63]
-    Xs = X[sample].to(torch.float64).cpu().numpy()
-    ref = o.apply_csr(wo, Xs, compensated=True)
     result = {
         "metric": "regrid apply dst-vals/s (split-FP32 SpMM, Voronoi 2.6M -> 0.1deg, 64 RHS)",
-        "value": M.n_dst * nrhs / (ms_split / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "value": M.n_dst * nrhs / (ms_split / 1e3), "unit": UNIT, "n_gpus": 1, "steps": steps,
         "warmup": args.warmup, "ms_per_step": ms_split, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "spherical Voronoi 2,621,442 cells (5 Lloyd iterations) -> 0.1deg lat-lon "
@@ -595,24 +685,62 @@ def voronoi_main(args):
                    "l2": f"inputs {4 * M.n_src * nrhs / 1e9:.2f} GB per step > L2", "parallelism": "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_kind": peak_kind, "bytes_per_step": bytes_split},
-        "fp64_apply": {"ms_per_step": ms64, "split_speedup": ms64 / ms_split},
         "clocks": clocks,
         "mesh_generation_s": t_mesh,
         "weightgen": {"seconds_best": min(times), "seconds_first": times[0], "nnz": M.nnz,
                       "pairs_per_s": M.nnz / min(times), "candidates": st["bvh_candidates"],
                       "gated": st["gated_pairs"], "fallback_clips": st["fallback_clips"],
                       "stages_ms": {k: st[k] for k in st if k.startswith("t_")}},
-        "parity": {"index_set_identical": bool(same), "weights_max_rel": wrel, "oracle_weightgen_s": t_oracle,
-                   "split": rel_errors(Y[sample].cpu().numpy(), ref),
-                   "fp64": rel_errors(Y64[sample].cpu().numpy(), ref), "sampled_rhs": sample},
-        "conservation": {"split_field_rel": axgb.check_conservation(M, X[0], Y[0])["relative_error"],
-                         "fp64_field_rel": axgb.check_conservation(M, X64[0], Y64[0])["relative_error"]},
     }
-    print(json.dumps(result), flush=True)
+    if not args.apply_only:
+        X64 = X.to(torch.float64)
+        Y64 = torch.empty((nrhs, M.n_dst), dtype=torch.float64, device=dev)
+        M.prepare(0)
+        ms64 = timed(lambda: axgb.apply_f64(M, X64, Y64, stream=stream))
+        result["fp64_apply"] = {"ms_per_step": ms64, "split_speedup": ms64 / ms_split}
+        log(f"voronoi split {ms_split:.3f} ms ({achieved:.0f} GB/s), fp64 {ms64:.3f} ms")
+        if o is not None:
+            t0 = time.perf_counter()
+            wo = o.conservative(src_g, dst_g)
+            t_oracle = time.perf_counter() - t0
+            sample = [0, 9, 35, 63]
+            Xs = X[sample].to(torch.float64).cpu().numpy()
+            ref = o.apply_csr(wo, Xs, compensated=True)
+            cond = o.apply_csr(wo, np.abs(Xs), compensated=True)
+            e_s, e_d = rel_errors(Y[sample].cpu().numpy(), ref), rel_errors(Y64[sample].cpu().numpy(), ref)
+            e_s["max_err_over_cond"] = cond_errors(Y[sample].cpu().numpy(), ref, cond)
+            e_d["max_err_over_cond"] = cond_errors(Y64[sample].cpu().numpy(), ref, cond)
+            result["parity"] = dict(weight_parity(M, wo), oracle_weightgen_s=t_oracle, split=e_s, fp64=e_d,
+                                    sampled_rhs=sample)
+            result["conservation"] = {
+                "split_field_rel": axgb.check_conservation(M, X[0], Y[0])["relative_error"],
+                "fp64_field_rel": axgb.check_conservation(M, X64[0], Y64[0])["relative_error"],
+                "oracle_exact_field_rel": o.conservation(wo, Xs[0], ref[0])["relative_error"]}
+        del X64, Y64
+    del X, Y, M
+    torch.cuda.empty_cache()
+    return result
+
+
+def voronoi_main(args):
+    """--workload voronoi: the config-5 case on its own, one JSON line."""
+    import axgb
+    from axgb import grids
+    axgb.init(0)
+    t0 = time.perf_counter()
+    src_g = grids.voronoi(**VORONOI)
+    t_mesh = time.perf_counter() - t0
+    log(f"voronoi mesh {t_mesh:.1f}s")
+    o = None
+    if not args.apply_only:
+        from oracle import Oracle
+        o = Oracle()
+        o.threads(os.cpu_count() or 1)
+    print(json.dumps(voronoi_case(args, src_g, o, t_mesh)), flush=True)
     return 0
 
 
-def batch_pairs(args):
+def batch_pairs(args, o=None):
     """Uneven batch of grid pairs in one persistent, graph-captured launch:
     every cubed-sphere (C48, C96, C192, C384) x lat-lon (2, 1, 0.5, 0.25 deg)
     combination, the direction alternating with the parity of the two grid
@@ -681,11 +809,33 @@ def batch_pairs(args):
     torch.cuda.synchronize()
     ms_p = e0.elapsed_time(e1) / args.steps
     same = all(torch.equal(a, b) for a, b in zip(ys, yp))
+    oracle_parity = None
+    if o is not None:
+        # every pair's weights against the oracle, and the batch outputs of up
+        # to two fields per pair against the compensated FP64 oracle apply
+        oracle_parity = {"pairs_index_set_identical": 0, "weights_max_rel": 0.0, "apply_max_err_over_cond": 0.0,
+                         "mismatched": []}
+        for (name, _, gs, _, gd), M, x, y in zip(pairs, mats, xs, ys):
+            wo = o.conservative(gs, gd)
+            wp = weight_parity(M, wo)
+            if wp["index_set_identical"]:
+                oracle_parity["pairs_index_set_identical"] += 1
+                oracle_parity["weights_max_rel"] = max(oracle_parity["weights_max_rel"], wp["weights_max_rel"] or 0.0)
+                k = min(2, x.shape[0])
+                xf = x[:k].to(torch.float64).cpu().numpy()
+                ref = o.apply_csr(wo, xf, compensated=True)
+                cond = o.apply_csr(wo, np.abs(xf), compensated=True)
+                oracle_parity["apply_max_err_over_cond"] = max(oracle_parity["apply_max_err_over_cond"],
+                                                               cond_errors(y[:k].cpu().numpy(), ref, cond))
+            else:
+                oracle_parity["mismatched"].append({name: wp})
+        oracle_parity["pairs"] = len(pairs)
     dst_vals = sum(k * M.n_dst for k, M in zip(nrhs, mats))
     nbytes = sum(4 * k * (M.n_src + M.n_dst) + 12 * M.nnz + 4 * (M.n_dst + 1) for k, M in zip(nrhs, mats))
     return {"pairs": [p[0] for p in pairs], "nrhs": nrhs, "nnz_total": int(sum(M.nnz for M in mats)),
             "weightgen_s": t_gen, "batch_ms": ms_b, "batch_dst_vals_per_s": dst_vals / (ms_b / 1e3),
             "batch_GBps": nbytes / ms_b / 1e6, "per_pair_calls_ms": ms_p, "bitwise_equal_to_per_pair": bool(same),
+            "oracle_parity": oracle_parity,
             "launches": "one CUDA graph per batch apply: a persistent staged kernel per row-length class "
                         "(work queue over the blocks of all pairs) and one persistent direct kernel for "
                         "the slices the staged layout leaves out and the rows of more than 32 entries"}
@@ -756,6 +906,15 @@ def small_configs(o):
     ms_d = dev_time(lambda: axgb.apply_f64(M, x64, y64))
     wo = o.conservative(src, dst)
     ref = o.apply_csr(wo, x64.cpu().numpy(), compensated=True)
+    cond = o.apply_csr(wo, np.abs(x64.cpu().numpy()), compensated=True)
+    cons_par = weight_parity(M, wo)
+    # bilinear 0.25 deg -> C384 against the oracle at full size
+    Mbil = axgb.generate_weights(axgb.Mesh.from_grid(src), axgb.Mesh.from_grid(dst), {"method": "bilinear"})
+    wb = o.bilinear(src, dst)
+    bil_par = weight_parity(Mbil, wb)
+    if bil_par["index_set_identical"]:
+        bil_par["bitwise"] = bool(np.array_equal(Mbil.to_csr()["val"], wb.w))
+    del Mbil
     # NaN-aware batched FP64 apply (skipna) on the same matrix: 16 fields, 5% NaN sources
     nf = 16
     gen = torch.Generator(device="cuda").manual_seed(77)
@@ -774,9 +933,15 @@ def small_configs(o):
         "ms": ms_nan, "GBps": nan_bytes / ms_nan / 1e6,
         "bitwise_equal_to_oracle_loop": bool(np.array_equal(yn[:2].cpu().numpy(), ref_nan, equal_nan=True)),
         "nan_outputs": int(torch.isnan(yn).sum().item())}
+    e_s, e_d = rel_errors(y32.cpu().numpy(), ref), rel_errors(y64.cpu().numpy(), ref)
+    e_s["max_err_over_cond"] = cond_errors(y32.cpu().numpy(), ref, cond)
+    e_d["max_err_over_cond"] = cond_errors(y64.cpu().numpy(), ref, cond)
+    bytes_1 = 12 * M.nnz + 4 * (M.n_dst + 1) + 4 * M.n_src + 4 * M.n_dst
     out["c2_0p25deg_to_C384_one_field"] = {
-        "nnz": M.nnz, "split_ms": ms_s, "fp64_ms": ms_d, "split_speedup": ms_d / ms_s,
-        "split": rel_errors(y32.cpu().numpy(), ref), "fp64": rel_errors(y64.cpu().numpy(), ref),
+        "nnz": M.nnz, "conservative_weights_vs_oracle": cons_par, "bilinear_weights_vs_oracle": bil_par,
+        "split_ms": ms_s, "fp64_ms": ms_d, "split_speedup": ms_d / ms_s,
+        "split_GBps": bytes_1 / ms_s / 1e6, "split_kernel": axgb.get_kernel_choice(M, 1),
+        "split": e_s, "fp64": e_d,
         "conservation_split": axgb.check_conservation(M, x32[0], y32[0])["relative_error"],
         "conservation_fp64": axgb.check_conservation(M, x64[0], y64[0])["relative_error"]}
     return out
@@ -788,6 +953,14 @@ def weightgen_c384(md_0p25, latlon_g):
     import axgb
     from axgb import grids
     c384 = grids.cubed_sphere(384)
+    # cold: both meshes ingested and prepared from host arrays, then generated once
+    ll = latlon_g if latlon_g is not None else grids.latlon_deg(0.25)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m_src, m_dst = axgb.Mesh.from_grid(ll), axgb.Mesh.from_grid(c384)
+    axgb.generate_weights(m_src, m_dst, {"method": "conservative"})
+    t_cold = time.perf_counter() - t0
+    del m_src, m_dst
     t0 = time.perf_counter()
     mc = axgb.Mesh.from_grid(c384)
     t_ingest = time.perf_counter() - t0
@@ -803,6 +976,8 @@ def weightgen_c384(md_0p25, latlon_g):
     t_bil = time.perf_counter() - tb
     best = min(times)
     return {"seconds_best": best, "seconds_first": times[0], "ingest_s": t_ingest, "nnz": Mc.nnz,
+            "seconds_cold": t_cold, "cold": "both meshes ingested from host arrays (node vectors, cell prep) "
+                                            "and one generation, timed together",
             "pairs_per_s": Mc.nnz / best, "candidates_per_s": st["gated_pairs"] / best,
             "bvh_candidates": st["bvh_candidates"], "gated": st["gated_pairs"],
             "stages_ms": {k: st[k] for k in st if k.startswith("t_")}, "bilinear_s": t_bil, "bilinear_nnz": Mb.nnz}

@@ -276,7 +276,10 @@ def _fans(p: np.ndarray, tri: np.ndarray, cc: np.ndarray):
     e1, e2 = _tangent_basis(p)
     d = cc[tid] - p[owner]
     ang = np.arctan2(np.einsum("ij,ij->i", d, e2[owner]), np.einsum("ij,ij->i", d, e1[owner]))
-    order = np.lexsort((ang, owner))
+    # one sort on owner + angle fraction in [0, 1): owner ids < 2^31 leave more
+    # than 20 bits of the angle in the float64 key
+    key = owner.astype(np.float64) + (ang + np.pi) * (0.999 / (2.0 * np.pi))
+    order = np.argsort(key, kind="stable")
     off = np.zeros(n + 1, dtype=np.int64)
     off[1:] = np.cumsum(np.bincount(owner, minlength=n))
     return off, tid[order]
