@@ -46,7 +46,7 @@ _SYMBOLS = [
     "axgb_conservation_f32", "axgb_matrix_device_status", "axgb_conservation_f64_noalloc",
     "axgb_set_kernel_choice", "axgb_get_kernel_choice", "axgb_nan_batch_apply_f64", "axgb_apply_masked_f64",
     "axgb_nan_batch_apply_host", "axgb_matrix_serialize", "axgb_matrix_deserialize", "axgb_esmf_write",
-    "axgb_esmf_read", "axgb_matrix_write_esmf", "axgb_matrix_read_esmf", "axgb_apply_f32split_hilo",
+    "axgb_esmf_read", "axgb_matrix_write_esmf", "axgb_matrix_read_esmf", "axgb_apply_f32split_hilo", "axgb_probe_fp64_fma",
 ]
 
 
@@ -105,6 +105,7 @@ def lib():
     L.axgb_apply_f32split.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp]
     L.axgb_apply_f32split_tuned.argtypes = [C.c_int, vp, i64, vp, i64, i64, C.c_int, C.c_int, C.c_int, vp]
     L.axgb_apply_f32split_hilo.argtypes = [C.c_int, vp, i64, vp, i64, vp, i64, i64, vp]
+    L.axgb_probe_fp64_fma.argtypes = [i64, vp]
     L.axgb_autotune_f32split.argtypes = [C.c_int, vp, i64, vp, i64, i64, vp, vp]
     L.axgb_set_autotune.argtypes = [C.c_int]
     L.axgb_apply_c.argtypes = [C.c_int, vp, vp, C.c_int, C.c_int]
@@ -469,6 +470,13 @@ def apply_f32split_hilo(matrix: Matrix, x, y=None, y_lo=None, stream=None):
                                           l2.stride(0), nrhs,
                                           _stream(stream if stream is not None else torch.cuda.current_stream())))
     return y, y_lo
+
+
+def probe_fp64_fma(iters: int = 1 << 16) -> float:
+    """FP64 FMA throughput of the current device, TFLOP/s."""
+    out = np.zeros(1)
+    _check(lib().axgb_probe_fp64_fma(int(iters), _ptr(out)))
+    return float(out[0])
 
 
 def autotune_f32split(matrix: Matrix, x, y, stream=None):

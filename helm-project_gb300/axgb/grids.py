@@ -328,6 +328,33 @@ def voronoi(n: int = 2621442, seed: int = 5, jitter: float = 0.2, lloyd: int = 5
     return MeshArrays(node, off, fan, name=f"voronoi{n}")
 
 
+def with_degenerate_cells(m: MeshArrays, seed: int) -> MeshArrays:
+    """A copy of m in which a tenth of the cells (with at least four
+    vertices) repeat their first vertex in place of the second, and three
+    cells are collapsed to a point: the cases of the reference's
+    degenerate-cell scan (detail/degenerate_cell_handler.hpp:115-236)."""
+    rng = np.random.default_rng(seed)
+    idx, off = m.conn_indices.copy(), m.conn_offsets
+    for c in rng.choice(m.n_cells, m.n_cells // 10, replace=False):
+        if off[c + 1] - off[c] >= 4:
+            idx[off[c] + 1] = idx[off[c]]
+    for c in rng.choice(m.n_cells, 3, replace=False):
+        idx[off[c]:off[c + 1]] = idx[off[c]]
+    return MeshArrays(m.node_lonlat, off, idx, name=f"degenerate_{m.name}")
+
+
+def triangulated(m: MeshArrays) -> MeshArrays:
+    """m with every quadrilateral split into two triangles (v0 v1 v2, v0 v2 v3)."""
+    off, idx = [0], []
+    for c in range(m.n_cells):
+        v = list(m.conn_indices[m.conn_offsets[c]:m.conn_offsets[c + 1]])
+        parts = [[v[0], v[1], v[2]], [v[0], v[2], v[3]]] if len(v) == 4 else [v]
+        for p in parts:
+            idx += p
+            off.append(len(idx))
+    return MeshArrays(m.node_lonlat, np.array(off, np.int64), np.array(idx, np.int64), name=f"triangulated_{m.name}")
+
+
 def cell_centroids_xyz(mesh: MeshArrays) -> np.ndarray:
     """Normalised mean of the unit-sphere vertex vectors of every cell: the
     cap centroid of ``compute_cell_centroid_xyz``

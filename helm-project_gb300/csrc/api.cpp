@@ -904,6 +904,13 @@ int axgb_matrix_prepare(int h, int format) {
     });
 }
 
+int axgb_probe_fp64_fma(int64_t iters, double *tflops) {
+    AXGB_TRY({
+        AXGB_REQUIRE(tflops && iters > 0 && iters <= (int64_t(1) << 24), "probe_fp64_fma: iters in [1, 2^24], tflops");
+        *tflops = fp64_fma_tflops(iters);
+    });
+}
+
 int axgb_matrix_device_status(int h, int32_t *status) {
     AXGB_TRY({
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");

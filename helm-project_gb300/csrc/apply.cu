@@ -886,6 +886,54 @@ double integral(const T *f, const double *area, const double *frac, i64 n, int m
     return acc;
 }
 
+// ─── FP64 FMA rate probe ──────────────────────────────────────────────────
+// Eight independent dependent-FMA chains per thread (enough to cover the FP64
+// pipe's latency), four resident blocks of 256 threads per SM: the FP64 FMA
+// throughput the FP64 apply and the clipper are compared against. The
+// result is written so the chains are not removed.
+__global__ void __launch_bounds__(256) k_fp64_fma(double *out, i64 iters, double b, double c) {
+    const double x = 1.0 + 1e-3 * threadIdx.x;
+    double a0 = x, a1 = x + 1, a2 = x + 2, a3 = x + 3, a4 = x + 4, a5 = x + 5, a6 = x + 6, a7 = x + 7;
+    for (i64 i = 0; i < iters; ++i) {
+        a0 = fma(a0, b, c);
+        a1 = fma(a1, b, c);
+        a2 = fma(a2, b, c);
+        a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c);
+        a5 = fma(a5, b, c);
+        a6 = fma(a6, b, c);
+        a7 = fma(a7, b, c);
+    }
+    const double r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (r == 12345.678) out[0] = r;  // never true for these inputs; keeps the chains live
+}
+
+}  // namespace
+
+double fp64_fma_tflops(i64 iters) {
+    int dev = 0, sms = 0;
+    AXGB_CUDA(cudaGetDevice(&dev));
+    AXGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DBuf<double> out(1);
+    cudaEvent_t e0, e1;
+    AXGB_CUDA(cudaEventCreate(&e0));
+    AXGB_CUDA(cudaEventCreate(&e1));
+    const unsigned blocks = static_cast<unsigned>(4 * sms);
+    k_fp64_fma<<<blocks, 256>>>(out.p, iters / 8 + 1, 0.999999, 1e-7);  // warm-up
+    AXGB_CUDA(cudaEventRecord(e0));
+    k_fp64_fma<<<blocks, 256>>>(out.p, iters, 0.999999, 1e-7);
+    AXGB_CUDA(cudaEventRecord(e1));
+    AXGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    AXGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const double flops = 2.0 * 8.0 * static_cast<double>(iters) * blocks * 256.0;
+    return flops / (static_cast<double>(ms) * 1e-3) / 1e12;
+}
+
+namespace {
+
 // ─── conservation report without allocation ───────────────────────────────
 // For callers that cannot allocate device memory while they run (a model
 // whose device memory is owned by its own pool, or code between

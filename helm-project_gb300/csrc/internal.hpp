@@ -277,6 +277,7 @@ void apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs
 void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
                  cudaStream_t s, float *ylo = nullptr, i64 ldylo = 0);
 void conservation(Matrix &m, const void *src, const void *dst, bool f32, int norm_type, double *out, cudaStream_t s);
+double fp64_fma_tflops(i64 iters);  // FP64 FMA throughput of the current device (TFLOP/s)
 void nan_batch_apply_f64(Matrix &m, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs, double na_thres,
                          cudaStream_t s);
 void apply_masked_f64(Matrix &m, const double *x, const int *mask, double *y, cudaStream_t s);

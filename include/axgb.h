@@ -218,6 +218,13 @@ int axgb_matrix_prepare(int matrix_handle, int format);
  * block rows were not written). Synchronizes the device. */
 int axgb_matrix_device_status(int matrix_handle, int32_t *status);
 
+/* Measures the FP64 FMA throughput of the current device (TFLOP/s, two flops
+ * per FMA): independent dependent-FMA chains on every SM, iters FMAs per
+ * chain (1 .. 2^24), timed with CUDA events. The roofline denominator of the
+ * FP64 apply and of the clipper, which run on the FP64 pipe. Synchronous.
+ * No reference counterpart (a measurement aid). */
+int axgb_probe_fp64_fma(int64_t iters, double *tflops);
+
 /* Replaces axis_destroy_matrix_c (axis_c_interop.cpp:247-249). */
 int axgb_destroy_matrix(int matrix_handle);
 

@@ -30,6 +30,8 @@ nor the grid generators to reproduce the inputs:
   libaxisref_gen.so``: weight_generator.cpp and the solver sources it calls,
   compiled unchanged, ArborX's queries by exhaustive search) for the
   nearest-neighbour, general bilinear and masked / coastal paths;
+  Six of them put meshes with degenerate cells (a repeated vertex, cells
+  collapsed to a point) or triangle meshes on either side;
 * ``apply_nan_masked.npz``: a CSR matrix (the 5 deg -> C8 conservative
   fixture's), fields with NaNs and the reference's own nan_batch_apply at
   four thresholds, and a masked apply (``oracle/_ref/libaxisref_apply.so``:
@@ -119,6 +121,20 @@ GENERATE = {
                                    False, 1),
     "bilinear_C8_to_10deg_srcmask": (lambda: (grids.cubed_sphere(8), grids.latlon_deg(10.0)), "bilinear", True,
                                      False, 1),
+    # degenerate cells (repeated vertices, cells collapsed to a point) and triangle meshes
+    "cons_degenerateC8_to_10deg": (lambda: (grids.with_degenerate_cells(grids.cubed_sphere(8), 1),
+                                            grids.latlon_deg(10.0)), "conservative", False, False, 1),
+    "cons_5deg_to_degenerateC8": (lambda: (grids.latlon_deg(5.0),
+                                           grids.with_degenerate_cells(grids.cubed_sphere(8), 2)),
+                                  "conservative", False, False, 1),
+    "cons_triangulatedC6_to_C5": (lambda: (grids.triangulated(grids.cubed_sphere(6)), grids.cubed_sphere(5)),
+                                  "conservative", False, False, 1),
+    "cons_10deg_to_triangulatedC6": (lambda: (grids.latlon_deg(10.0), grids.triangulated(grids.cubed_sphere(6))),
+                                     "conservative", False, False, 1),
+    "bilinear_triangulatedC6_to_10deg": (lambda: (grids.triangulated(grids.cubed_sphere(6)),
+                                                  grids.latlon_deg(10.0)), "bilinear", False, False, 1),
+    "nearest_degenerateC8_to_10deg": (lambda: (grids.with_degenerate_cells(grids.cubed_sphere(8), 1),
+                                               grids.latlon_deg(10.0)), "nearest_neighbor", False, False, 1),
 }
 
 
@@ -164,10 +180,15 @@ def main():
                             **mesh_dict("dst", dst), method=method, norm_type=norm, row=w.row, col=w.col, w=w.w,
                             frac_a=w.frac_a, frac_b=w.frac_b, area_a=w.area_a, area_b=w.area_b)
         print("fastpath", name, "nnz", w.nnz)
+    make_generate(GENERATE)
+    make_apply()
+
+
+def make_generate(cases):
     if obuild.build_ref_gen() is None:
         raise SystemExit("the reference checkout is needed to generate the generate() fixtures")
     gen = RefGenLib()
-    for name, (make, method, smask, dmask, extrap) in GENERATE.items():
+    for name, (make, method, smask, dmask, extrap) in cases.items():
         src, dst = make()
         sm = land_mask(src) if smask else None
         dm = dst_mask(dst) if dmask else None
@@ -181,6 +202,9 @@ def main():
                             **mesh_dict("dst", dst), **extra, method=method, extrap=extrap, row=w.row, col=w.col,
                             w=w.w, frac_a=w.frac_a, frac_b=w.frac_b, area_a=w.area_a, area_b=w.area_b)
         print("generate", name, "nnz", w.nnz)
+
+
+def make_apply():
     if obuild.build_ref_apply() is None:
         raise SystemExit("the reference checkout is needed to generate the apply fixture")
     app = RefApplyLib()
@@ -225,4 +249,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    # --generate NAME ...: (re)make only those generate_<NAME>.npz fixtures
+    if len(sys.argv) > 2 and sys.argv[1] == "--generate":
+        make_generate({k: GENERATE[k] for k in sys.argv[2:]})
+    else:
+        main()

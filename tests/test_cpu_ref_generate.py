@@ -119,32 +119,8 @@ def test_reference_generate_unmapped_error(ref, oracle):
         oracle.conservative(s, d, unmapped=0)
 
 
-def degenerate(m, seed):
-    """A tenth of the cells with a repeated vertex and three cells collapsed
-    to a point: the degenerate-cell scan's cases."""
-    from axgb.grids import MeshArrays
-    rng = np.random.default_rng(seed)
-    idx, off = m.conn_indices.copy(), m.conn_offsets
-    for c in rng.choice(m.n_cells, m.n_cells // 10, replace=False):
-        if off[c + 1] - off[c] >= 4:
-            idx[off[c] + 1] = idx[off[c]]
-    for c in rng.choice(m.n_cells, 3, replace=False):
-        idx[off[c]:off[c + 1]] = idx[off[c]]
-    return MeshArrays(m.node_lonlat, off, idx, name="degenerate")
-
-
-def triangulated(m):
-    """Every quadrilateral split into two triangles."""
-    from axgb.grids import MeshArrays
-    off, idx = [0], []
-    for c in range(m.n_cells):
-        v = list(m.conn_indices[m.conn_offsets[c]:m.conn_offsets[c + 1]])
-        parts = [[v[0], v[1], v[2]], [v[0], v[2], v[3]]] if len(v) == 4 else [v]
-        for p in parts:
-            idx += p
-            off.append(len(idx))
-    return MeshArrays(m.node_lonlat, np.array(off, np.int64), np.array(idx, np.int64), name="triangulated")
-
+degenerate = grids.with_degenerate_cells
+triangulated = grids.triangulated
 
 ODD = {
     "degenerate C8->10deg": lambda: (degenerate(grids.cubed_sphere(8), 1), grids.latlon_deg(10.0)),
