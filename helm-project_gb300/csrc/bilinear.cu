@@ -128,13 +128,15 @@ __global__ void k_bil_candidates(PtTreeView T, const float4 *__restrict__ dpt, i
 // unit vectors of the centroids (host libm).
 __global__ void k_bilinear_general(const int *__restrict__ cand, const int *__restrict__ navail,
                                    const double2 *__restrict__ proj, const double *__restrict__ sxyz,
-                                   const double *__restrict__ dxyz, i64 n_dst, int *cnt, int *col4, double *w4) {
+                                   const double *__restrict__ dxyz, i64 n_dst, int *cnt, int *col4, double *w4,
+                                   int *gen4) {
     const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n_dst) return;
     const int n_avail = navail[j];
     int nc = 0;
     int oc[4];
     double ow[4];
+    int ork[4] = {0, 1, 2, 3};
     if (n_avail > 0) {
         const int *cj = cand + kCand * j;
         V2 q[kCand];
@@ -222,7 +224,8 @@ __global__ void k_bilinear_general(const int *__restrict__ cand, const int *__re
                 nc = n_idw;
             }
         }
-        // column-ascending within the row (the columns are distinct)
+        // column-ascending within the row (the columns are distinct); ork
+        // keeps each entry's place in the stencil (generation) order
         for (int a = 1; a < nc; ++a)
             for (int b = a; b > 0 && oc[b - 1] > oc[b]; --b) {
                 const int tc = oc[b];
@@ -231,23 +234,28 @@ __global__ void k_bilinear_general(const int *__restrict__ cand, const int *__re
                 const double tw = ow[b];
                 ow[b] = ow[b - 1];
                 ow[b - 1] = tw;
+                const int tr = ork[b];
+                ork[b] = ork[b - 1];
+                ork[b - 1] = tr;
             }
     }
     cnt[j] = nc;
     for (int k = 0; k < nc; ++k) {
         col4[4 * j + k] = oc[k];
         w4[4 * j + k] = ow[k];
+        gen4[4 * j + k] = ork[k];
     }
 }
 
-__global__ void k_bil_pack(const int *row_ptr, const int *cnt, const int *col4, const double *w4, i64 n_dst, int *col,
-                           double *w) {
+__global__ void k_bil_pack(const int *row_ptr, const int *cnt, const int *col4, const double *w4, const int *gen4,
+                           i64 n_dst, int *col, double *w, int *gen) {
     const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n_dst) return;
     const int p = row_ptr[j];
     for (int k = 0; k < cnt[j]; ++k) {
         col[p + k] = col4[4 * j + k];
         w[p + k] = w4[4 * j + k];
+        gen[p + k] = gen4[4 * j + k];
     }
 }
 
@@ -371,11 +379,11 @@ void generate_bilinear_general(Mesh &src, Mesh &dst, const axgb_regrid_config &c
     d_proj.upload(proj.data(), proj.size(), s);
     d_sx.upload(sx.data(), sx.size(), s);
     d_dx.upload(dx.data(), dx.size(), s);
-    DBuf<int> cnt(n_dst), col4(4 * n_dst);
+    DBuf<int> cnt(n_dst), col4(4 * n_dst), gen4(4 * n_dst);
     DBuf<double> w4(4 * n_dst);
     if (n_dst)
         k_bilinear_general<<<nblk(n_dst, 64), 64, 0, s>>>(cand.p, navail.p, d_proj.p, d_sx.p, d_dx.p, n_dst, cnt.p,
-                                                          col4.p, w4.p);
+                                                          col4.p, w4.p, gen4.p);
     AXGB_CUDA(cudaGetLastError());
     out.n_src = n_src;
     out.n_dst = n_dst;
@@ -386,7 +394,10 @@ void generate_bilinear_general(Mesh &src, Mesh &dst, const axgb_regrid_config &c
     out.nnz = nnz;
     out.col.alloc(std::max(1, nnz));
     out.val.alloc(std::max(1, nnz));
-    if (n_dst) k_bil_pack<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, cnt.p, col4.p, w4.p, n_dst, out.col.p, out.val.p);
+    out.gen_rank.alloc(std::max(1, nnz));
+    if (n_dst)
+        k_bil_pack<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, cnt.p, col4.p, w4.p, gen4.p, n_dst, out.col.p,
+                                                    out.val.p, out.gen_rank.p);
     out.frac_a.alloc(n_src);
     out.frac_b.alloc(n_dst);
     out.area_a.alloc(n_src);

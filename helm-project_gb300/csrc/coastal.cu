@@ -58,18 +58,41 @@ __global__ void k_centroid_xy(const double *lonlat, i64 n_nodes, const int *off,
     pt[c] = make_float4(static_cast<float>(ox), static_cast<float>(oy), 0.0f, 0.0f);
 }
 
-// Per row: wet weight sum s (CSR order), wet count; new entry count.
-__global__ void k_wet_rows(const int *rp, const int *col, const double *val, const int *mask, i64 n_dst, int extrap,
-                           int any_wet, double *wsum, int *cnt) {
+// Per row: wet weight sum s, wet count; new entry count. The sum runs in
+// the order the generator emitted the row's entries (weight_generator.cpp:
+// 1769-1777): gen (one key per CSR entry, distinct within a row) orders
+// them; without gen, or where gen already ascends, that is CSR order. Rows
+// out of order are walked by repeated selection of the next key.
+__global__ void k_wet_rows(const int *rp, const int *col, const double *val, const int *gen, const int *mask,
+                           i64 n_dst, int extrap, int any_wet, double *wsum, int *cnt) {
     const i64 j = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n_dst) return;
+    const int b = rp[j], e = rp[j + 1];
+    bool in_order = true;
+    if (gen)
+        for (int k = b + 1; k < e; ++k)
+            if (gen[k] < gen[k - 1]) in_order = false;
     double s = 0.0;
     int n = 0;
-    for (int k = rp[j]; k < rp[j + 1]; ++k)
-        if (mask[col[k]] > 0) {
-            s += val[k];
-            ++n;
+    if (in_order) {
+        for (int k = b; k < e; ++k)
+            if (mask[col[k]] > 0) {
+                s += val[k];
+                ++n;
+            }
+    } else {
+        long long prev = -1;  // keys are non-negative
+        for (int t = b; t < e; ++t) {
+            int at = -1;
+            for (int k = b; k < e; ++k)
+                if (gen[k] > prev && (at < 0 || gen[k] < gen[at])) at = k;
+            prev = gen[at];
+            if (mask[col[at]] > 0) {
+                s += val[at];
+                ++n;
+            }
         }
+    }
     wsum[j] = s;
     cnt[j] = n > 0 ? n : (extrap && any_wet ? 1 : 0);
 }
@@ -102,7 +125,10 @@ __global__ void k_coastal_fill(const int *rp, const int *col, const double *val,
 }  // namespace
 
 void coastal_postpass(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matrix &m) {
-    if (!src.has_mask) return;
+    if (!src.has_mask) {
+        m.gen_rank.release();
+        return;
+    }
     cudaStream_t s = 0;
     mesh_prepare(src, s);
     mesh_prepare(dst, s);
@@ -117,8 +143,9 @@ void coastal_postpass(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matri
     const int any_wet = wet.empty() ? 0 : 1;
     DBuf<double> wsum(n_dst);
     DBuf<int> cnt(n_dst), nrp(n_dst + 1);
-    if (n_dst) k_wet_rows<<<nblk(n_dst, 256), 256, 0, s>>>(m.row_ptr.p, m.col.p, m.val.p, src.d_mask.p, n_dst, extrap,
-                                                            any_wet, wsum.p, cnt.p);
+    if (n_dst)
+        k_wet_rows<<<nblk(n_dst, 256), 256, 0, s>>>(m.row_ptr.p, m.col.p, m.val.p, m.nnz > 0 ? m.gen_rank.p : nullptr,
+                                                    src.d_mask.p, n_dst, extrap, any_wet, wsum.p, cnt.p);
     AXGB_CUDA(cudaGetLastError());
     scan_exclusive_i32(cnt.p, nrp.p, n_dst, s);
     int nnz = 0;
@@ -150,6 +177,7 @@ void coastal_postpass(Mesh &src, Mesh &dst, const axgb_regrid_config &cfg, Matri
     m.row_ptr = std::move(nrp);
     m.col = std::move(ncol);
     m.val = std::move(nval);
+    m.gen_rank.release();
     m.nnz = nnz;
     m.stats[3] = nnz;
 }

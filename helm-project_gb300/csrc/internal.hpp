@@ -229,6 +229,13 @@ struct Matrix {
     // apply first gathers the fields into the new order.
     bool src_renum = false;
     DBuf<int> split_col, src_inv;
+    // Per CSR entry, a key of its place in its row's generation order, for
+    // the paths whose rows are not generated in column order (regular and
+    // rectilinear conservative fast paths: candidate position; bilinear:
+    // stencil corner). Empty: column order. Read by the coastal post-pass
+    // (the reference sums a row's wet weights in generation order) and
+    // released after generation.
+    DBuf<int> gen_rank;
     std::vector<float> slice_xyz;  // mean unit vector of each 32-row slice (locality hint), may be empty
     std::map<i64, SplitParams> tuned;  // nrhs -> best kernel choice
     std::mutex mu;

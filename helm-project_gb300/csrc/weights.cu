@@ -369,7 +369,8 @@ struct BilRegArgs {
     bool periodic;
 };
 
-__global__ void k_bilinear_reg(MeshView D, BilRegArgs g, int *cnt, int *col4, double *w4, int *n_unmapped) {
+__global__ void k_bilinear_reg(MeshView D, BilRegArgs g, int *cnt, int *col4, double *w4, int *gen4,
+                               int *n_unmapped) {
     const i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= D.n_cells) return;
     const int b = D.off[c], e = D.off[c + 1];
@@ -405,6 +406,7 @@ __global__ void k_bilinear_reg(MeshView D, BilRegArgs g, int *cnt, int *col4, do
     const int j1 = min(j + 1, g.nj - 1);
     int cc[4] = {j * g.ni + i, j * g.ni + i1, j1 * g.ni + i, j1 * g.ni + i1};
     double ww[4] = {(1.0 - tx) * (1.0 - ty), tx * (1.0 - ty), (1.0 - tx) * ty, tx * ty};
+    int rk[4] = {0, 1, 2, 3};  // corner = place in the generation order
     for (int a = 1; a < 4; ++a)  // stable insertion sort by column
         for (int q = a; q > 0 && cc[q - 1] > cc[q]; --q) {
             const int tc = cc[q];
@@ -413,22 +415,27 @@ __global__ void k_bilinear_reg(MeshView D, BilRegArgs g, int *cnt, int *col4, do
             const double tw = ww[q];
             ww[q] = ww[q - 1];
             ww[q - 1] = tw;
+            const int tr = rk[q];
+            rk[q] = rk[q - 1];
+            rk[q - 1] = tr;
         }
     cnt[c] = 4;
     for (int k = 0; k < 4; ++k) {
         col4[4 * c + k] = cc[k];
         w4[4 * c + k] = ww[k];
+        gen4[4 * c + k] = rk[k];
     }
 }
 
-__global__ void k_bilinear_reg_pack(const int *row_ptr, const int *cnt, const int *col4, const double *w4, i64 n_dst,
-                                    int *col, double *w, double *frac_b) {
+__global__ void k_bilinear_reg_pack(const int *row_ptr, const int *cnt, const int *col4, const double *w4,
+                                    const int *gen4, i64 n_dst, int *col, double *w, int *gen, double *frac_b) {
     const i64 c = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= n_dst) return;
     const int p = row_ptr[c];
     for (int k = 0; k < cnt[c]; ++k) {
         col[p + k] = col4[4 * c + k];
         w[p + k] = w4[4 * c + k];
+        gen[p + k] = gen4[4 * c + k];
     }
     frac_b[c] = cnt[c] ? 1.0 : 0.0;
 }
@@ -664,6 +671,7 @@ struct AssembleOpts {
     const double *area_a_out = nullptr;  // reported areas, when not the ones the weights divide by
     const double *area_b_out = nullptr;
     bool check_unmapped = true;          // the general path's UnmappedAction::Error check
+    bool keep_gen = false;               // keep each entry's candidate position (generation order)
 };
 
 // Kept pairs (overlap > 0, weight_generator.cpp:3682) of the candidate list
@@ -710,6 +718,9 @@ static void assemble(DBuf<int> &cs, DBuf<int> &cd, DBuf<double> &ov, i64 n_cand,
         radix_sort_pairs_u64(key2.p, vals2.p, nnz, cbits, s);
         k_count_keys<<<nblk(nnz, 256), 256, 0, s>>>(key2.p, nnz, ccnt.p);
         AXGB_CUDA(cudaGetLastError());
+        // vals: each CSR entry's position in the compacted candidate list,
+        // which the fast paths fill row by row in the reference's loop order
+        if (o.keep_gen) out.gen_rank = std::move(vals);
     }
     scan_exclusive_i32(rcnt.p, out.row_ptr.p, n_dst, s);
     scan_exclusive_i32(ccnt.p, col_ptr.p, n_src, s);
@@ -887,6 +898,7 @@ bool generate_conservative_regular(Mesh &src, Mesh &dst, const axgb_regrid_confi
     out.stats[0] = out.stats[1] = n_cand;
     auto t0 = Clock::now();
     AssembleOpts o;
+    o.keep_gen = true;  // rows generated in the reference's (js, is) loop order
     o.fb_pre = fb.p;
     o.check_unmapped = false;  // the fast path returns its matrix as it is (:380-415)
     assemble(cs, cd, ov, n_cand, sa.p, da.p, D, cfg, out, s, o);
@@ -946,6 +958,7 @@ bool generate_conservative_rectilinear(Mesh &src, Mesh &dst, const axgb_regrid_c
     out.stats[0] = out.stats[1] = n_cand;
     auto t0 = Clock::now();
     AssembleOpts o;
+    o.keep_gen = true;  // rows generated in the reference's (js, is) loop order
     o.fac = fac.p;
     o.fb_pre = fb.p;
     o.area_b_out = da.p;
@@ -968,10 +981,10 @@ bool generate_bilinear_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &c
     AXGB_REQUIRE(4 * n_dst < (i64(1) << 31) && n_src < (i64(1) << 31), "bilinear: meshes too large");
     BilRegArgs a{g.lon_min, g.lat_min, g.dlon, g.dlat, static_cast<int>(g.ni), static_cast<int>(g.nj),
                  std::abs((g.lon_max - g.lon_min) - 360.0) < 1.0e-10 * g.dlon};
-    DBuf<int> cnt(n_dst), col4(4 * n_dst), bad(1);
+    DBuf<int> cnt(n_dst), col4(4 * n_dst), gen4(4 * n_dst), bad(1);
     DBuf<double> w4(4 * n_dst);
     bad.zero(s);
-    k_bilinear_reg<<<nblk(n_dst, 128), 128, 0, s>>>(dst.view(), a, cnt.p, col4.p, w4.p, bad.p);
+    k_bilinear_reg<<<nblk(n_dst, 128), 128, 0, s>>>(dst.view(), a, cnt.p, col4.p, w4.p, gen4.p, bad.p);
     AXGB_CUDA(cudaGetLastError());
     int h_bad = 0;
     AXGB_CUDA(cudaMemcpy(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -987,12 +1000,13 @@ bool generate_bilinear_regular(Mesh &src, Mesh &dst, const axgb_regrid_config &c
     out.nnz = nnz;
     out.col.alloc(std::max(1, nnz));
     out.val.alloc(std::max(1, nnz));
+    out.gen_rank.alloc(std::max(1, nnz));
     out.frac_a.alloc(n_src);
     out.frac_b.alloc(n_dst);
     out.area_a.alloc(n_src);
     out.area_b.alloc(n_dst);
-    k_bilinear_reg_pack<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, cnt.p, col4.p, w4.p, n_dst, out.col.p,
-                                                         out.val.p, out.frac_b.p);
+    k_bilinear_reg_pack<<<nblk(n_dst, 256), 256, 0, s>>>(out.row_ptr.p, cnt.p, col4.p, w4.p, gen4.p, n_dst,
+                                                         out.col.p, out.val.p, out.gen_rank.p, out.frac_b.p);
     if (n_src) k_fill<<<nblk(n_src, 256), 256, 0, s>>>(out.frac_a.p, n_src, 1.0);
     out.area_a.zero(s);
     out.area_b.zero(s);

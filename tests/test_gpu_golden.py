@@ -63,6 +63,10 @@ def test_gpu_generate_golden(gpu, name):
     csr = gpu.generate_weights(ms, md, cfg).to_csr()
     rows = np.repeat(np.arange(len(csr["row_ptr"]) - 1), np.diff(csr["row_ptr"]))
     assert np.array_equal(rows, z["row"]) and np.array_equal(csr["col"], z["col"])
+    if str(z["method"]) == "bilinear":
+        # bilinear weights are bit-exact, and a masked source's coastal pass
+        # sums each row's wet weights in the generator's corner order
+        assert np.array_equal(csr["val"], z["w"]), int(np.sum(csr["val"] != z["w"]))
     # kept entries may carry weight 0 (clamped barycentric weights): exact there
     assert np.max(np.abs(csr["val"] - z["w"]) / np.maximum(np.abs(z["w"]), 1e-300), initial=0.0) < W_RTOL
     for k in ("frac_a", "frac_b", "area_a", "area_b"):
