@@ -259,12 +259,17 @@ void check_apply(const Matrix &m, const void *x, i64 ldx, const void *y, i64 ldy
 // cp.async staging; 2 or 3 buffers), 2 (blocked, bulk copies; 2 buffers),
 // 1 and 2 with 2, 4 or 8 fields per stage, 3 (blocked, producer warp and
 // mbarrier ring of 2 or 3 slots, 4 fields per stage); 4 (one fused launch
-// for few fields; the other knobs unused).
+// for few fields; the other knobs unused); 5 (segmented, lane = field, 32
+// fields per stage, 2 or 3 staging slots).
 void check_split_params(const SplitParams &p, const char *who) {
     const std::string w(who);
-    AXGB_REQUIRE(p.variant >= 0 && p.variant <= 4, w + ": variant must be 0 to 4");
+    AXGB_REQUIRE(p.variant >= 0 && p.variant <= 5, w + ": variant must be 0 to 5");
     AXGB_REQUIRE(p.fields_per_pass >= 0, w + ": fields_per_pass must be >= 0");
     if (p.variant == 4) return;
+    if (p.variant == 5) {
+        AXGB_REQUIRE(p.stages == 2 || p.stages == 3, w + ": variant 5 takes 2 or 3 staging slots");
+        return;
+    }
     if (p.variant == 0) {
         AXGB_REQUIRE(p.unroll == 1 || p.unroll == 2 || p.unroll == 4, w + ": direct unroll must be 1, 2 or 4");
         return;
@@ -292,6 +297,8 @@ SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i6
             if (u <= std::max<i64>(1, nrhs)) cands.push_back({0, static_cast<int>(t), u});
     if (nrhs == 1) cands.push_back({0, 1, 1});
     if (nrhs <= 8) cands.push_back({4, 0, 1, 2});
+    if (nrhs >= 16)
+        for (int ns : {2, 3}) cands.push_back({5, 0, 32, ns});
     cudaEvent_t e0, e1;
     AXGB_CUDA(cudaEventCreate(&e0));
     AXGB_CUDA(cudaEventCreate(&e1));
@@ -898,7 +905,7 @@ int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int6
 
 int axgb_matrix_prepare(int h, int format) {
     AXGB_TRY({
-        AXGB_REQUIRE(format >= 0 && format <= 2, "matrix_prepare: format must be 0, 1 or 2");
+        AXGB_REQUIRE(format >= 0 && format <= 3, "matrix_prepare: format must be 0, 1, 2 or 3");
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         matrix_prepare(*m, format, 0);
     });
@@ -917,10 +924,13 @@ int axgb_matrix_device_status(int h, int32_t *status) {
         AXGB_REQUIRE(status, "matrix_device_status: NULL status");
         AXGB_CUDA(cudaDeviceSynchronize());
         int v = 0;
-        if (m->blocked.status.p) {
-            AXGB_CUDA(cudaMemcpy(&v, m->blocked.status.p, sizeof(int), cudaMemcpyDeviceToHost));
-            AXGB_CUDA(cudaMemset(m->blocked.status.p, 0, sizeof(int)));
-        }
+        for (DBuf<int> *st : {&m->blocked.status, &m->seg.status})
+            if (st->p) {
+                int w = 0;
+                AXGB_CUDA(cudaMemcpy(&w, st->p, sizeof(int), cudaMemcpyDeviceToHost));
+                AXGB_CUDA(cudaMemset(st->p, 0, sizeof(int)));
+                v |= w;
+            }
         *status = v;
     });
 }
@@ -945,7 +955,7 @@ int axgb_apply_f32split_tuned(int h, const float *x, int64_t ldx, float *y, int6
     AXGB_TRY({
         auto m = Registry::get().find(Registry::get().mats, h, "matrix");
         check_apply(*m, x, ldx, y, ldy, nrhs);
-        SplitParams p{variant, fields_per_pass, unroll, variant == 3 ? 3 : 2};
+        SplitParams p{variant, fields_per_pass, unroll, variant == 3 || variant == 5 ? 3 : 2};
         check_split_params(p, "apply");
         if (nrhs > 0) apply_split(*m, x, ldx, y, ldy, nrhs, p, static_cast<cudaStream_t>(stream));
     });

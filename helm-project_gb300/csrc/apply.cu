@@ -725,6 +725,28 @@ void launch_f64_long(const Sell &S, const double *x, i64 ldx, double *y, i64 ldy
     const i64 warps = S.n_lrows * ((nrhs + kLongF - 1) / kLongF);
     k_f64_long<<<nblk(warps * 32, 256), 256, 0, s>>>(long_rows(S), x, ldx, y, ldy, nrhs);
 }
+}  // namespace
+
+// Rows of more than 32 entries given row-contiguous (the segmented layout's
+// own copy, original source numbering): k_split_long, same summation order.
+void launch_long_rows(const int *row, const int *ptr, const int *col, const float *hi, const float *lo, i64 n,
+                      const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s, float *ylo, i64 ldylo) {
+    if (n == 0 || nrhs == 0) return;
+    LongRows L{};
+    L.row = row;
+    L.ptr = ptr;
+    L.col = col;
+    L.hi = hi;
+    L.lo = lo;
+    L.n = n;
+    L.ylo = ylo;
+    L.ldylo = ldylo;
+    const i64 warps = n * ((nrhs + kLongF - 1) / kLongF);
+    k_split_long<<<nblk(warps * 32, 256), 256, 0, s>>>(L, x, ldx, y, ldy, nrhs);
+}
+
+namespace {
+
 // One launch for the whole matrix (few fields): warp per slice, then warp per long row.
 void launch_split_fused(const Matrix &m, const Sell &S, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs,
                         cudaStream_t s, float *ylo, i64 ldylo) {
@@ -1109,6 +1131,10 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
 
 void matrix_prepare(Matrix &m, int format, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(m.mu);
+    if (format == 3) {  // segmented layout (it fixes the split order through the blocked build first)
+        build_segmented(m, s);
+        return;
+    }
     if (format >= 1) build_blocked(m, s);  // fixes the split entry order (split_perm) first
     if (format == 2) {
         build_sell(m, 1, s);  // slices of blocks that do not fit the blocked kernels use the direct kernel
@@ -1165,6 +1191,11 @@ void apply_split_layouts(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, 
 void apply_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, const SplitParams &p,
                  cudaStream_t s, float *ylo, i64 ldylo) {
     if (nrhs <= 0) return;
+    if (p.variant == 5) {  // segmented: cells staged by their own ids, no renumbering gather
+        if (!m.seg.built) matrix_prepare(m, 3, s);
+        apply_segmented(m, x, ldx, y, ldy, nrhs, s, ylo, ldylo, p.stages);
+        return;
+    }
     if (!m.blocked.built) matrix_prepare(m, 2, s);
     if (!m.src_renum) {
         apply_split_layouts(m, x, ldx, y, ldy, nrhs, p, s, ylo, ldylo);

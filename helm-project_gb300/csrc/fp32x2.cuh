@@ -81,6 +81,19 @@ __device__ __forceinline__ void cstepn(F2 &s, F2 &cn, float h, F2 hp, F2 ln, flo
     s = t;
 }
 
+// The cstepn step for two rows side by side (one field each): w = (hi_a,
+// hi_b, -lo_a, -lo_b); each half is bitwise csum1 of its own row.
+__device__ __forceinline__ void cstep_pair(F2 &s, F2 &cn, float4 w, float xa, float xb) {
+    const F2 x = pk(xa, xb);
+    const F2 p = pk(__fmul_rn(w.x, xa), __fmul_rn(w.y, xb));  // not fusable (see csum2)
+    const F2 t = add2(s, p);
+    const F2 bn = sub2(s, t);
+    const F2 a = add2(t, bn);
+    const F2 e = add2(sub2(s, a), fma2(pk(w.x, w.y), x, bn));
+    cn = sub2(fma2(pk(w.z, w.w), x, cn), e);
+    s = t;
+}
+
 // Low part of a row value. The stored value is r = fl(s + c); the exact
 // rounding error of that sum (Knuth's TwoSum, exact for any operand order)
 // is returned, so r + lo represents s + c to within FP32 round-off of c's

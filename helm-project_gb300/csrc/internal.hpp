@@ -199,6 +199,52 @@ struct Blocked {
     }
 };
 
+// Segmented split-FP32 layout (staged.cu, variant 5): lane = field. Rows in
+// 8-row segments (one 32-byte sector of a field's outputs), four segments of
+// nearby rows per group (a CTA: one warp per segment, one producer warp).
+// Per group the distinct source cells of its rows (original numbering) are
+// staged cell by cell for 32 fields, transposed ([cell][field], 33 floats a
+// cell), so a warp's 32 lanes (fields) read one cell without bank
+// conflicts. A segment's rows, sorted by length, are taken in pairs summed
+// side by side with packed f32x2 arithmetic. Per entry pair: the staged
+// offsets of both cells and (hi_a, hi_b, -lo_a, -lo_b). Rows of more than
+// 32 entries, and the rows of groups with more staged cells than the
+// largest bucket, are listed for the fallback kernels (original numbering).
+struct Segmented {
+    struct Launch {
+        int usmax;     // staged-cell bucket of the launch
+        i64 begin, n;  // range in gids
+    };
+    bool built = false;
+    i64 n_groups = 0;
+    DBuf<int4> grp;       // per group: (first cell in cellmap, cells, first entry pair, entry pairs)
+    int max_ent = 0;      // entry pairs of the largest group
+    DBuf<int4> slot;      // per group and segment: (segment id or -1, first entry pair, store mask, 0)
+    DBuf<uint4> pairs;    // per group and segment: 4 x (ra | rb << 3 | has_b << 6 | length << 8)
+    DBuf<int> cellmap, gids;
+    DBuf<unsigned> eoff;  // per entry pair: staged float offsets (cell * 33) of row a | row b << 16
+    DBuf<float4> ew;      // per entry pair: (hi_a, hi_b, -lo_a, -lo_b)
+    std::vector<Launch> launches;
+    // fallback rows of at most 32 entries: row ids and row-contiguous entries
+    i64 n_fb = 0;
+    DBuf<int> fb_row, fb_ptr, fb_col;
+    DBuf<float> fb_hi, fb_lo;
+    // rows of more than 32 entries, row-contiguous (original numbering)
+    i64 n_long = 0;
+    DBuf<int> l_row, l_ptr, l_col;
+    DBuf<float> l_hi, l_lo;
+    DBuf<int> status;  // 1 = a bounded wait timed out
+    std::mutex pool_mu;
+    std::vector<cudaStream_t> pool;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
+    ~Segmented() {
+        for (auto st : pool) cudaStreamDestroy(st);
+        for (auto ev : join) cudaEventDestroy(ev);
+        if (fork) cudaEventDestroy(fork);
+    }
+};
+
 // Kernel choice for the split-FP32 apply.
 struct SplitParams {
     int variant = 1;          // 0 direct gathers, 1 blocked + cp.async chunk staging,
@@ -217,6 +263,7 @@ struct Matrix {
     double times_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     Sell sell64, sell32;
     Blocked blocked;
+    Segmented seg;
     // Order of each row's entries in the split-FP32 layouts: split_perm[rp[r] + k]
     // is the CSR index of the k-th entry of row r. Chosen by the blocked build
     // against shared-memory bank conflicts and shared by every split layout,
@@ -237,6 +284,7 @@ struct Matrix {
     // released after generation.
     DBuf<int> gen_rank;
     std::vector<float> slice_xyz;  // mean unit vector of each 32-row slice (locality hint), may be empty
+    std::vector<float> seg_xyz;    // the same for each 8-row segment (segmented layout)
     std::map<i64, SplitParams> tuned;  // nrhs -> best kernel choice
     std::mutex mu;
 };
@@ -296,6 +344,11 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
 // staged.cu
 void build_blocked(Matrix &m, cudaStream_t s);
 bool blocked_eligible(const Matrix &m, const void *x, i64 ldx, bool bulk);
+void launch_long_rows(const int *row, const int *ptr, const int *col, const float *hi, const float *lo, i64 n,
+                      const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s, float *ylo, i64 ldylo);
+void build_segmented(Matrix &m, cudaStream_t s);
+void apply_segmented(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s, float *ylo,
+                     i64 ldylo, int ns);
 void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, int kind, int T, int ns,
                    i64 fchunk, cudaStream_t s, float *ylo = nullptr, i64 ldylo = 0);
 int blocked_launches(const Matrix &m);

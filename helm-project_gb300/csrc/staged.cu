@@ -556,13 +556,15 @@ __global__ void __launch_bounds__(kRows) k_blk_bulk(BlkArgs a, const float *__re
     }
 }
 
-__global__ void k_slice_centroid(const DCap *cap, i64 n_rows, i64 n_slices, float *out) {
+// Mean cap centre of each run of `per` consecutive rows (32-row slices,
+// 8-row segments).
+__global__ void k_slice_centroid(const DCap *cap, i64 n_rows, i64 n_slices, int per, float *out) {
     i64 s = static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= n_slices) return;
     double sx = 0, sy = 0, sz = 0;
     int n = 0;
-    const i64 r1 = (n_rows < s * 32 + 32) ? n_rows : s * 32 + 32;
-    for (i64 r = s * 32; r < r1; ++r) {
+    const i64 r1 = (n_rows < s * per + per) ? n_rows : s * per + per;
+    for (i64 r = s * per; r < r1; ++r) {
         sx += cap[r].x;
         sy += cap[r].y;
         sz += cap[r].z;
@@ -727,13 +729,16 @@ void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::ve
 }  // namespace
 
 void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s) {
-    const i64 nsl = (m.n_dst + 31) / 32;
+    const i64 nsl = (m.n_dst + 31) / 32, nsg = (m.n_dst + 7) / 8;
     if (nsl == 0 || !dst.cap) return;
-    DBuf<float> d(3 * nsl);
-    k_slice_centroid<<<nblk(nsl, 256), 256, 0, s>>>(dst.cap, m.n_dst, nsl, d.p);
+    DBuf<float> d(3 * nsl), d8(3 * nsg);
+    k_slice_centroid<<<nblk(nsl, 256), 256, 0, s>>>(dst.cap, m.n_dst, nsl, 32, d.p);
+    k_slice_centroid<<<nblk(nsg, 256), 256, 0, s>>>(dst.cap, m.n_dst, nsg, 8, d8.p);
     AXGB_CUDA(cudaGetLastError());
     m.slice_xyz.resize(3 * nsl);
+    m.seg_xyz.resize(3 * nsg);
     AXGB_CUDA(cudaMemcpyAsync(m.slice_xyz.data(), d.p, sizeof(float) * 3 * nsl, cudaMemcpyDeviceToHost, s));
+    AXGB_CUDA(cudaMemcpyAsync(m.seg_xyz.data(), d8.p, sizeof(float) * 3 * nsg, cudaMemcpyDeviceToHost, s));
     AXGB_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -1235,6 +1240,457 @@ void apply_blocked(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nr
         AXGB_CUDA(cudaStreamWaitEvent(s, B.join[q], 0));
     }
     AXGB_CUDA(cudaGetLastError());
+}
+
+
+// ─── segmented layout: lane = field ────────────────────────────────────────
+namespace {
+
+constexpr int kSegRows = 8;            // rows per segment: one 32-byte sector of a field's outputs
+constexpr int kSegW = 4;               // segments per group = consumer warps of a CTA
+constexpr int kSegF = 32;              // fields per tile, one per lane
+constexpr int kSegLd = kSegF + 1;      // floats per staged cell (the extra float spreads cells over banks)
+constexpr int kSegUs[] = {160, 256};   // staged-cell buckets (launches)
+static_assert(kSegW == kWarps, "segment groups reuse the slice grouping of four");
+
+struct SegArgs {
+    const int4 *grp, *slot;
+    const uint4 *pairs;
+    const int *cellmap, *gids;
+    const unsigned *eoff;
+    const float4 *ew;
+    int *status;
+    float *ylo;
+    i64 ldylo;
+    int max_ent;  // entry pairs of the largest group (shared-memory copy of a group's entries)
+};
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+
+// One group (CTA) for all fields. Warp kSegW is the producer: for tile t (32
+// fields) it copies field f of staged cell i to xs[slot][i][f] with 4-byte
+// cp.async (lanes = consecutive staged cells, so the global side reads runs
+// of the field and the shared side writes 33-float rows without conflicts)
+// and arrives on the slot's `full` barrier as its copies land. Warp w < kSegW
+// owns segment w of the group: per tile, lane = field, it sums the
+// segment's row pairs entry by entry (both cells read conflict-free: the 32
+// lanes read one 132-byte row), releases the slot, and writes the segment's
+// 8 rows x 32 fields through a transpose buffer, 4 fields x 8 rows (four
+// 32-byte sectors) per store. Bounded waits, as k_blk_ws.
+template <int NS, int US>
+__global__ void __launch_bounds__((kSegW + 1) * 32) k_seg(SegArgs a, const float *__restrict__ x, i64 ldx,
+                                                          float *__restrict__ y, i64 ldy, i64 nrhs) {
+    constexpr int kThreads = (kSegW + 1) * 32;
+    constexpr int kOb = kSegRows + 1;  // transpose buffer row (field) stride
+    extern __shared__ __align__(128) float smem[];
+    float4 *ews = reinterpret_cast<float4 *>(smem);                           // [max_ent] the group's weights
+    unsigned *eos = reinterpret_cast<unsigned *>(ews + a.max_ent);            // [max_ent] and cell offsets
+    float *xs = reinterpret_cast<float *>(eos + a.max_ent);                   // [NS][US + 1][kSegLd]
+    float *ob = xs + NS * (US + 1) * kSegLd;                                  // [kSegW][kSegF][kOb]
+    int *cm = reinterpret_cast<int *>(ob + kSegW * kSegF * kOb);              // [US]
+    __shared__ __align__(8) std::uint64_t full[NS], empty[NS];
+    __shared__ volatile int abort_flag;
+    const int g = a.gids[blockIdx.x];
+    const int4 gd = a.grp[g];
+    const int nc = gd.y;  // staged cells; slot nc is the zero cell
+    const int e0 = gd.z, ne = gd.w;  // the group's entry pairs
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < nc; i += kThreads) cm[i] = a.cellmap[gd.x + i];
+    for (int i = tid; i < ne; i += kThreads) {
+        ews[i] = a.ew[e0 + i];
+        eos[i] = a.eoff[e0 + i];
+    }
+    for (int q = tid; q < NS * kSegLd; q += kThreads)
+        xs[(q / kSegLd) * (US + 1) * kSegLd + nc * kSegLd + q % kSegLd] = 0.f;
+    if (tid == 0) {
+        for (int st = 0; st < NS; ++st) {
+            mbar_init(&full[st], 32);
+            mbar_init(&empty[st], kSegW);
+        }
+        abort_flag = 0;
+    }
+    __syncthreads();
+    const i64 ntile = (nrhs + kSegF - 1) / kSegF;
+    if (warp == kSegW) {  // producer
+        for (i64 t = 0; t < ntile; ++t) {
+            const int st = static_cast<int>(t % NS);
+            if (t >= NS && !mbar_wait_bounded(&empty[st], static_cast<unsigned>((t / NS - 1) & 1))) {
+                abort_flag = 1;
+                atomicExch(a.status, 1);
+                break;
+            }
+            if (abort_flag) break;
+            const i64 f0 = t * kSegF;
+            const int nf = static_cast<int>(nrhs - f0 < kSegF ? nrhs - f0 : kSegF);
+            const float *xt = x + f0 * ldx;
+            float *dst = xs + st * (US + 1) * kSegLd;
+            for (int i = lane; i < nc; i += 32) {
+                const float *src = xt + cm[i];
+                float *d = dst + i * kSegLd;
+#pragma unroll 8
+                for (int f = 0; f < nf; ++f) cp_async4(d + f, src + f * ldx);
+            }
+            cp_async_mbar_arrive(&full[st]);
+        }
+        cp_async_wait<0>();
+        return;
+    }
+    const int4 sl = a.slot[static_cast<i64>(g) * kSegW + warp];
+    const uint4 pr4 = a.pairs[static_cast<i64>(g) * kSegW + warp];
+    const unsigned prs[4] = {pr4.x, pr4.y, pr4.z, pr4.w};
+    float *obw = ob + warp * kSegF * kOb;
+    const int r = lane & 7;
+    const bool store_r = ((sl.z >> r) & 1) != 0;
+    const i64 row = static_cast<i64>(sl.x) * kSegRows + r;
+    for (i64 t = 0; t < ntile; ++t) {
+        const int st = static_cast<int>(t % NS);
+        if (!mbar_wait_bounded(&full[st], static_cast<unsigned>((t / NS) & 1))) {
+            abort_flag = 1;
+            atomicExch(a.status, 1);
+            break;
+        }
+        const float *xl = xs + st * (US + 1) * kSegLd + lane;
+        F2 acc[4], cnn[4];
+        int e = sl.y - e0;
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const int len = static_cast<int>((prs[p] >> 8) & 63u);
+            F2 s2 = pk(0.f, 0.f), c2 = pk(0.f, 0.f);
+#pragma unroll 4
+            for (int k = 0; k < len; ++k) {
+                const unsigned u = eos[e + k];
+                const float4 w = ews[e + k];
+                cstep_pair(s2, c2, w, xl[u & 0xffffu], xl[u >> 16]);
+            }
+            e += len;
+            acc[p] = s2;
+            cnn[p] = c2;
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);  // the slot is no longer read by this warp
+        const i64 f0 = t * kSegF;
+        const int nf = static_cast<int>(nrhs - f0 < kSegF ? nrhs - f0 : kSegF);
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const unsigned pr = prs[p];
+            if (!(pr & 128u)) continue;
+            float ya, yb;
+            upk(sub2(acc[p], cnn[p]), ya, yb);
+            obw[lane * kOb + (pr & 7u)] = ya;
+            if (pr & 64u) obw[lane * kOb + ((pr >> 3) & 7u)] = yb;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int fb = 0; fb < kSegF / 4; ++fb) {
+            const int f = 4 * fb + (lane >> 3);
+            if (f < nf && store_r) y[(f0 + f) * ldy + row] = obw[f * kOb + r];
+        }
+        if (a.ylo) {  // low parts of the same outputs, through the same buffer
+            __syncwarp();
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const unsigned pr = prs[p];
+                if (!(pr & 128u)) continue;
+                float ya, yb, sa, sb, ca, cb;
+                upk(sub2(acc[p], cnn[p]), ya, yb);
+                upk(acc[p], sa, sb);
+                upk(cnn[p], ca, cb);
+                obw[lane * kOb + (pr & 7u)] = sum_err(sa, -ca, ya);
+                if (pr & 64u) obw[lane * kOb + ((pr >> 3) & 7u)] = sum_err(sb, -cb, yb);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int fb = 0; fb < kSegF / 4; ++fb) {
+                const int f = 4 * fb + (lane >> 3);
+                if (f < nf && store_r) a.ylo[(f0 + f) * a.ldylo + row] = obw[f * kOb + r];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Rows of at most 32 entries outside the groups: warp per (row, 32 fields),
+// lane = field, entries in the layout's order (csum1).
+__global__ void __launch_bounds__(256) k_seg_rows(const int *__restrict__ rows, const int *__restrict__ ptr,
+                                                  const int *__restrict__ col, const float *__restrict__ hi,
+                                                  const float *__restrict__ lo, i64 n, const float *__restrict__ x,
+                                                  i64 ldx, float *__restrict__ y, i64 ldy, i64 nrhs, float *ylo,
+                                                  i64 ldylo) {
+    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const i64 i = w % n, fc = w / n;
+    const i64 f = fc * 32 + (threadIdx.x & 31);
+    if (fc * 32 >= nrhs || f >= nrhs) return;
+    const int b = ptr[i], e = ptr[i + 1];
+    const float *xf = x + f * ldx;
+    float s = 0.f, c = 0.f;
+    for (int k = b; k < e; ++k) csum1(s, c, hi[k], lo[k], __ldg(xf + col[k]));
+    const float r = __fadd_rn(s, c);
+    y[f * ldy + rows[i]] = r;
+    if (ylo) ylo[f * ldylo + rows[i]] = sum_err(s, c, r);
+}
+
+template <int NS, int US>
+void launch_seg_us(const SegArgs &a, i64 grid, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs,
+                   cudaStream_t s) {
+    const size_t bytes = sizeof(float) * (static_cast<size_t>(NS) * (US + 1) * kSegLd + kSegW * kSegF * (kSegRows + 1)) +
+                         (sizeof(float4) + sizeof(unsigned)) * static_cast<size_t>(a.max_ent) + sizeof(int) * US;
+    AXGB_CUDA(cudaFuncSetAttribute(k_seg<NS, US>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+    k_seg<NS, US><<<static_cast<unsigned>(grid), (kSegW + 1) * 32, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
+}
+
+struct HostGroup {
+    int segs[kSegW];
+    int mask[kSegW];
+    unsigned pr[kSegW][4];
+    std::vector<int> cells;
+    std::vector<unsigned> eoff;
+    std::vector<float4> ew;
+    int slot_ent[kSegW];  // entry pairs of each slot (relative)
+    bool fallback = false;
+    std::vector<int> fb_rows;
+};
+
+}  // namespace
+
+void build_segmented(Matrix &m, cudaStream_t s) {
+    Segmented &G = m.seg;
+    if (G.built) return;
+    build_blocked(m, s);  // the split entry order (split_perm)
+    const i64 n = m.n_dst, nnz = m.nnz;
+    std::vector<int> rp(n + 1), col(std::max<i64>(1, nnz)), perm(std::max<i64>(1, nnz));
+    std::vector<double> val(std::max<i64>(1, nnz));
+    AXGB_CUDA(cudaMemcpy(rp.data(), m.row_ptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    if (nnz) {
+        AXGB_CUDA(cudaMemcpy(col.data(), m.col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+        AXGB_CUDA(cudaMemcpy(val.data(), m.val.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost));
+        AXGB_CUDA(cudaMemcpy(perm.data(), m.split_perm.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+    }
+    const i64 nsg = (n + kSegRows - 1) / kSegRows;
+    auto groups = group_slices(nsg, m.seg_xyz);  // four nearby segments per group (consecutive without a hint)
+    const i64 ng = static_cast<i64>(groups.size());
+    const int usmax = kSegUs[sizeof(kSegUs) / sizeof(kSegUs[0]) - 1];
+    std::vector<HostGroup> hg(ng);
+    auto split = [&](int q, float &h, float &l) {
+        h = static_cast<float>(val[q]);
+        l = static_cast<float>(val[q] - static_cast<double>(h));
+    };
+    parallel_for_host(ng, [&](i64 g0, i64 g1) {
+        std::vector<int> rows;
+        for (i64 g = g0; g < g1; ++g) {
+            HostGroup &H = hg[g];
+            H.cells.clear();
+            for (int w = 0; w < kSegW; ++w) {
+                H.segs[w] = groups[g][w];
+                H.mask[w] = 0;
+                for (int p = 0; p < 4; ++p) H.pr[w][p] = 0;
+                H.slot_ent[w] = 0;
+                const int sg = groups[g][w];
+                if (sg < 0) continue;
+                for (int r = 0; r < kSegRows; ++r) {
+                    const i64 row = static_cast<i64>(sg) * kSegRows + r;
+                    if (row >= n || rp[row + 1] - rp[row] > 32) continue;
+                    for (int q = rp[row]; q < rp[row + 1]; ++q) H.cells.push_back(col[q]);
+                }
+            }
+            std::sort(H.cells.begin(), H.cells.end());
+            H.cells.erase(std::unique(H.cells.begin(), H.cells.end()), H.cells.end());
+            const int nc = static_cast<int>(H.cells.size());
+            if (nc > usmax) {  // too many staged cells: the group's rows go to the fallback kernel
+                H.fallback = true;
+                for (int w = 0; w < kSegW; ++w) {
+                    const int sg = groups[g][w];
+                    if (sg < 0) continue;
+                    for (int r = 0; r < kSegRows; ++r) {
+                        const i64 row = static_cast<i64>(sg) * kSegRows + r;
+                        if (row < n && rp[row + 1] - rp[row] <= 32) H.fb_rows.push_back(static_cast<int>(row));
+                    }
+                }
+                H.cells.clear();
+                continue;
+            }
+            auto pos = [&](int c) {
+                return static_cast<unsigned>(std::lower_bound(H.cells.begin(), H.cells.end(), c) - H.cells.begin());
+            };
+            for (int w = 0; w < kSegW; ++w) {
+                const int sg = groups[g][w];
+                if (sg < 0) continue;
+                rows.clear();
+                for (int r = 0; r < kSegRows; ++r) {
+                    const i64 row = static_cast<i64>(sg) * kSegRows + r;
+                    if (row < n && rp[row + 1] - rp[row] <= 32) rows.push_back(r);
+                }
+                std::stable_sort(rows.begin(), rows.end(), [&](int ra, int rb) {
+                    const i64 a0 = static_cast<i64>(sg) * kSegRows + ra, b0 = static_cast<i64>(sg) * kSegRows + rb;
+                    return rp[a0 + 1] - rp[a0] > rp[b0 + 1] - rp[b0];
+                });
+                const int before = static_cast<int>(H.eoff.size());
+                for (size_t p = 0; p < rows.size(); p += 2) {
+                    const int ra = rows[p], rb = p + 1 < rows.size() ? rows[p + 1] : -1;
+                    const i64 ra0 = static_cast<i64>(sg) * kSegRows + ra;
+                    const int la = rp[ra0 + 1] - rp[ra0];
+                    const i64 rb0 = rb >= 0 ? static_cast<i64>(sg) * kSegRows + rb : -1;
+                    const int lb = rb >= 0 ? rp[rb0 + 1] - rp[rb0] : 0;
+                    H.mask[w] |= 1 << ra;
+                    if (rb >= 0) H.mask[w] |= 1 << rb;
+                    H.pr[w][p / 2] = static_cast<unsigned>(ra) | (static_cast<unsigned>(rb >= 0 ? rb : 0) << 3) |
+                                     (rb >= 0 ? 64u : 0u) | 128u | (static_cast<unsigned>(la) << 8);
+                    for (int k = 0; k < la; ++k) {
+                        const int qa = perm[rp[ra0] + k];
+                        unsigned ua = pos(col[qa]) * kSegLd, ub = static_cast<unsigned>(nc) * kSegLd;
+                        float ha, la_, hb = 0.f, lb_ = 0.f;
+                        split(qa, ha, la_);
+                        if (k < lb) {
+                            const int qb = perm[rp[rb0] + k];
+                            ub = pos(col[qb]) * kSegLd;
+                            split(qb, hb, lb_);
+                        }
+                        H.eoff.push_back(ua | (ub << 16));
+                        H.ew.push_back(make_float4(ha, hb, -la_, -lb_));
+                    }
+                }
+                H.slot_ent[w] = static_cast<int>(H.eoff.size()) - before;
+            }
+        }
+    });
+    // flatten
+    std::vector<int4> grp(ng), slot(ng * kSegW);
+    std::vector<uint4> pairs(ng * kSegW);
+    std::vector<int> cellmap, fb_rows;
+    std::vector<unsigned> eoff;
+    std::vector<float4> ew;
+    std::vector<std::vector<int>> bucket(sizeof(kSegUs) / sizeof(kSegUs[0]));
+    for (i64 g = 0; g < ng; ++g) {
+        HostGroup &H = hg[g];
+        grp[g] = make_int4(static_cast<int>(cellmap.size()), static_cast<int>(H.cells.size()),
+                           static_cast<int>(eoff.size()), static_cast<int>(H.eoff.size()));
+        if (!H.fallback) G.max_ent = std::max(G.max_ent, static_cast<int>(H.eoff.size()));
+        int ent = static_cast<int>(eoff.size());
+        for (int w = 0; w < kSegW; ++w) {
+            slot[g * kSegW + w] = make_int4(H.fallback ? -1 : H.segs[w], ent, H.fallback ? 0 : H.mask[w], 0);
+            pairs[g * kSegW + w] = make_uint4(H.pr[w][0], H.pr[w][1], H.pr[w][2], H.pr[w][3]);
+            ent += H.slot_ent[w];
+        }
+        if (H.fallback) {
+            fb_rows.insert(fb_rows.end(), H.fb_rows.begin(), H.fb_rows.end());
+            continue;
+        }
+        cellmap.insert(cellmap.end(), H.cells.begin(), H.cells.end());
+        eoff.insert(eoff.end(), H.eoff.begin(), H.eoff.end());
+        ew.insert(ew.end(), H.ew.begin(), H.ew.end());
+        int b = 0;
+        while (kSegUs[b] < static_cast<int>(H.cells.size())) ++b;
+        bucket[b].push_back(static_cast<int>(g));
+        std::vector<int>().swap(H.cells);
+        std::vector<unsigned>().swap(H.eoff);
+        std::vector<float4>().swap(H.ew);
+    }
+    std::vector<int> gids;
+    G.launches.clear();
+    G.max_ent = std::max(G.max_ent, 1);
+    for (size_t b = 0; b < bucket.size(); ++b) {
+        if (bucket[b].empty()) continue;
+        G.launches.push_back({kSegUs[b], static_cast<i64>(gids.size()), static_cast<i64>(bucket[b].size())});
+        gids.insert(gids.end(), bucket[b].begin(), bucket[b].end());
+    }
+    // fallback short rows and long rows, row-contiguous in the split order (original numbering)
+    auto rowlist = [&](const std::vector<int> &rl, DBuf<int> &drow, DBuf<int> &dptr, DBuf<int> &dcol,
+                       DBuf<float> &dhi, DBuf<float> &dlo) {
+        std::vector<int> ptr(1, 0), c;
+        std::vector<float> h, l;
+        for (int r : rl) {
+            for (int k = rp[r]; k < rp[r + 1]; ++k) {
+                const int q = perm[k];
+                float hh, ll;
+                split(q, hh, ll);
+                c.push_back(col[q]);
+                h.push_back(hh);
+                l.push_back(ll);
+            }
+            ptr.push_back(static_cast<int>(c.size()));
+        }
+        drow.upload_vec(rl, s);
+        dptr.upload_vec(ptr, s);
+        dcol.upload_vec(c, s);
+        dhi.upload_vec(h, s);
+        dlo.upload_vec(l, s);
+    };
+    std::vector<int> long_rows;
+    for (i64 r = 0; r < n; ++r)
+        if (rp[r + 1] - rp[r] > 32) long_rows.push_back(static_cast<int>(r));
+    rowlist(fb_rows, G.fb_row, G.fb_ptr, G.fb_col, G.fb_hi, G.fb_lo);
+    rowlist(long_rows, G.l_row, G.l_ptr, G.l_col, G.l_hi, G.l_lo);
+    G.n_fb = static_cast<i64>(fb_rows.size());
+    G.n_long = static_cast<i64>(long_rows.size());
+    G.grp.upload_vec(grp, s);
+    G.slot.upload_vec(slot, s);
+    G.pairs.upload_vec(pairs, s);
+    G.cellmap.upload_vec(cellmap, s);
+    G.gids.upload_vec(gids, s);
+    G.eoff.upload_vec(eoff, s);
+    G.ew.upload_vec(ew, s);
+    if (!G.status.p) {
+        G.status.alloc(1);
+        G.status.zero(s);
+    }
+    G.n_groups = ng;
+    AXGB_CUDA(cudaStreamSynchronize(s));
+    G.built = true;
+}
+
+void apply_segmented(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s, float *ylo,
+                     i64 ldylo, int ns) {
+    Segmented &G = m.seg;
+    if (nrhs <= 0) return;
+    std::lock_guard<std::mutex> lk(G.pool_mu);
+    const int nl = static_cast<int>(G.launches.size()) + (G.n_fb > 0 ? 1 : 0) + (G.n_long > 0 ? 1 : 0);
+    if (G.pool.empty()) {
+        G.pool.resize(3);
+        G.join.resize(3);
+        for (int q = 0; q < 3; ++q) {
+            AXGB_CUDA(cudaStreamCreateWithFlags(&G.pool[q], cudaStreamNonBlocking));
+            AXGB_CUDA(cudaEventCreateWithFlags(&G.join[q], cudaEventDisableTiming));
+        }
+        AXGB_CUDA(cudaEventCreateWithFlags(&G.fork, cudaEventDisableTiming));
+    }
+    const int used = std::min(3, nl);
+    AXGB_CUDA(cudaEventRecord(G.fork, s));
+    for (int q = 0; q < used; ++q) AXGB_CUDA(cudaStreamWaitEvent(G.pool[q], G.fork, 0));
+    int q = 0;
+    SegArgs a{G.grp.p, G.slot.p, G.pairs.p, G.cellmap.p, nullptr, G.eoff.p, G.ew.p, G.status.p, ylo, ldylo,
+              G.max_ent};
+    // the largest bucket first: it holds the groups with the most work
+    for (int li = static_cast<int>(G.launches.size()) - 1; li >= 0; --li) {
+        const Segmented::Launch &l = G.launches[li];
+        a.gids = G.gids.p + l.begin;
+        cudaStream_t st = G.pool[q++ % 3];
+        if (l.usmax <= kSegUs[0]) {
+            if (ns >= 3)
+                launch_seg_us<3, kSegUs[0]>(a, l.n, x, ldx, y, ldy, nrhs, st);
+            else
+                launch_seg_us<2, kSegUs[0]>(a, l.n, x, ldx, y, ldy, nrhs, st);
+        } else {
+            if (ns >= 3)
+                launch_seg_us<3, kSegUs[1]>(a, l.n, x, ldx, y, ldy, nrhs, st);
+            else
+                launch_seg_us<2, kSegUs[1]>(a, l.n, x, ldx, y, ldy, nrhs, st);
+        }
+    }
+    if (G.n_fb > 0) {
+        const i64 warps = G.n_fb * ((nrhs + 31) / 32);
+        k_seg_rows<<<nblk(warps * 32, 256), 256, 0, G.pool[q++ % 3]>>>(G.fb_row.p, G.fb_ptr.p, G.fb_col.p, G.fb_hi.p,
+                                                                      G.fb_lo.p, G.n_fb, x, ldx, y, ldy, nrhs, ylo,
+                                                                      ldylo);
+    }
+    if (G.n_long > 0)
+        launch_long_rows(G.l_row.p, G.l_ptr.p, G.l_col.p, G.l_hi.p, G.l_lo.p, G.n_long, x, ldx, y, ldy, nrhs,
+                         G.pool[q++ % 3], ylo, ldylo);
+    AXGB_CUDA(cudaGetLastError());
+    for (int k = 0; k < used; ++k) {
+        AXGB_CUDA(cudaEventRecord(G.join[k], G.pool[k]));
+        AXGB_CUDA(cudaStreamWaitEvent(s, G.join[k], 0));
+    }
 }
 
 }  // namespace axgb

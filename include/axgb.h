@@ -209,7 +209,8 @@ int axgb_matrix_import_csr(int64_t n_src, int64_t n_dst, int64_t nnz, const int6
 
 /* Builds the apply layouts of a matrix ahead of time (format 0: FP64
  * sliced-ELL, 1: split-FP32 hi+lo sliced-ELL, 2: the blocked staged
- * split-FP32 layout, which also builds 1) so that later apply calls
+ * split-FP32 layout, which also builds 1, 3: the segmented split-FP32
+ * layout of variant 5, which also builds 2) so that later apply calls
  * allocate nothing. Synchronous. */
 int axgb_matrix_prepare(int matrix_handle, int format);
 
@@ -266,7 +267,10 @@ int axgb_apply_f32split_hilo(int matrix_handle, const float *x, int64_t ld_x, fl
  * to 3 need x 16-byte aligned and ld_x a multiple of 4 (variant 2 also n_src
  * a multiple of 4); otherwise the direct kernel runs. variant 4: the whole
  * matrix in one launch (for one or a few fields); the other knobs are
- * unused. Every variant gives the same bits. */
+ * unused. variant 5: segmented, one lane per field: groups of 32 nearby
+ * rows stage their distinct source cells (original numbering, any x
+ * alignment) for 32 fields at a time; stages = staging slots (2 or 3).
+ * Every variant gives the same bits. */
 int axgb_apply_f32split_tuned(int matrix_handle, const float *x, int64_t ld_x, float *y, int64_t ld_y, int64_t nrhs,
                               int variant, int fields_per_pass, int unroll, axgb_stream_t stream);
 

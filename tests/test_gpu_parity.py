@@ -184,7 +184,7 @@ def test_apply_split_parity(gpu, oracle, cfg1):
     xs = torch.tensor(X, device="cuda")
     outs = []
     for v, fpp, u in ((0, 0, 1), (0, 0, 2), (0, 0, 4), (0, 3, 2), (0, 1, 1), (1, 0, 2), (1, 0, 4), (1, 0, 8),
-                      (2, 0, 2), (2, 0, 4), (2, 0, 8), (3, 0, 4), (3, 2, 4), (4, 0, 1)):
+                      (2, 0, 2), (2, 0, 4), (2, 0, 8), (3, 0, 4), (3, 2, 4), (4, 0, 1), (5, 0, 32)):
         y = gpu.apply_f32split(M, xs, fields_per_pass=fpp, unroll=u, variant=v).cpu().numpy()
         err = np.max(np.abs(y - ref) / np.abs(ref))
         assert err < SPLIT_RTOL, (v, fpp, u, err)
@@ -262,7 +262,7 @@ def test_kernel_choice_seed_and_read(gpu, oracle, cfg1):
     with pytest.raises(gpu.InvalidArgument):
         gpu.set_kernel_choice(M, nrhs, variant=2, fields_per_pass=0, unroll=4, stages=3)
     with pytest.raises(gpu.InvalidArgument):
-        gpu.set_kernel_choice(M, nrhs, variant=5, fields_per_pass=0, unroll=4, stages=2)
+        gpu.set_kernel_choice(M, nrhs, variant=6, fields_per_pass=0, unroll=4, stages=2)
     with pytest.raises(gpu.InvalidArgument):
         gpu.set_kernel_choice(M, nrhs, variant=3, fields_per_pass=0, unroll=4, stages=4)
     with pytest.raises(gpu.InvalidArgument):
@@ -287,7 +287,8 @@ def test_long_rows_parity(gpu, oracle):
     ref = oracle.apply_csr(wo, X.astype(np.float64), compensated=True)
     xs = torch.tensor(X, device="cuda")
     outs = [gpu.apply_f32split(M, xs, fields_per_pass=fpp, unroll=u, variant=v).cpu().numpy()
-            for v, fpp, u in ((0, 0, 1), (0, 8, 4), (1, 0, 4), (1, 16, 8), (2, 0, 4), (3, 0, 4), (4, 0, 1))]
+            for v, fpp, u in ((0, 0, 1), (0, 8, 4), (1, 0, 4), (1, 16, 8), (2, 0, 4), (3, 0, 4), (4, 0, 1),
+                              (5, 0, 32))]
     for y in outs[1:]:
         assert np.array_equal(y, outs[0])
     scale = np.abs(ref).max()
@@ -371,7 +372,8 @@ def test_apply_split_hilo(gpu, oracle, name, make):
     cond = oracle.apply_csr(wo, np.abs(X64), compensated=True)
     xd = torch.tensor(X, device="cuda")
     plain = gpu.apply_f32split(M, xd, fields_per_pass=0, unroll=1, variant=0).cpu().numpy()
-    for v, fpp, u, ns in ((0, 0, 2, 2), (0, 3, 4, 2), (1, 0, 4, 2), (1, 4, 8, 3), (3, 0, 4, 3)):
+    for v, fpp, u, ns in ((0, 0, 2, 2), (0, 3, 4, 2), (1, 0, 4, 2), (1, 4, 8, 3), (3, 0, 4, 3), (5, 0, 32, 2),
+                          (5, 0, 32, 3)):
         gpu.set_kernel_choice(M, nrhs, variant=v, fields_per_pass=fpp, unroll=u, stages=ns)
         y, ylo = gpu.apply_f32split_hilo(M, xd)
         y, ylo = y.cpu().numpy(), ylo.cpu().numpy()
@@ -413,6 +415,50 @@ def test_batch_on_two_streams(gpu, oracle, cfg1):
     torch.cuda.synchronize()
     assert np.array_equal(ya.cpu().numpy(), ra)
     assert np.array_equal(yb.cpu().numpy(), rb)
+
+
+SEG_PAIRS = [
+    ("C48->1deg", lambda: (grids.cubed_sphere(48), grids.latlon_deg(1.0))),
+    ("1deg->C48", lambda: (grids.latlon_deg(1.0), grids.cubed_sphere(48))),
+    ("0.5deg->C24 (long rows)", lambda: (grids.latlon_deg(0.5), grids.cubed_sphere(24))),
+    ("voronoi40962->2deg", lambda: (grids.voronoi(40962, seed=5), grids.latlon_deg(2.0))),
+    ("0.25deg->C12 (oversize groups)", lambda: (grids.latlon_deg(0.25), grids.cubed_sphere(12))),
+]
+
+
+@pytest.mark.parametrize("name,make", SEG_PAIRS)
+def test_segmented_variant(gpu, oracle, name, make):
+    """Variant 5 (segmented, lane = field, source cells staged by their own
+    ids) against the direct kernel bit for bit, for field counts that fill
+    and that do not fill a 32-field tile, from unaligned field starts (an
+    odd leading dimension), with and without the hi+lo output; and within
+    the split tolerance of the compensated FP64 oracle."""
+    import torch
+    src, dst = make()
+    M = gpu.generate_weights(gpu.Mesh.from_grid(src), gpu.Mesh.from_grid(dst), {"method": "conservative"})
+    wo = oracle.conservative(src, dst)
+    rng = np.random.default_rng(41)
+    nrhs = 45
+    X = rng.standard_normal((nrhs, M.n_src)).astype(np.float32)
+    ld = M.n_src + 3
+    xp = torch.zeros((nrhs, ld), dtype=torch.float32, device="cuda")
+    xp[:, :M.n_src] = torch.tensor(X, device="cuda")
+    xs = xp[:, :M.n_src]
+    ref = gpu.apply_f32split(M, xs.contiguous(), fields_per_pass=0, unroll=1, variant=0).cpu().numpy()
+    for k in (nrhs, 32, 7):
+        gpu.set_kernel_choice(M, k, variant=0, fields_per_pass=0, unroll=1, stages=2)
+        lo_ref = gpu.apply_f32split_hilo(M, xs[:k].contiguous())[1].cpu().numpy()
+        for ns in (2, 3):
+            gpu.set_kernel_choice(M, k, variant=5, fields_per_pass=0, unroll=32, stages=ns)
+            y = gpu.apply_f32split(M, xs[:k]).cpu().numpy()
+            assert np.array_equal(y, ref[:k]), (k, ns, int(np.sum(y != ref[:k])))
+            yh, yl = gpu.apply_f32split_hilo(M, xs[:k])
+            assert np.array_equal(yh.cpu().numpy(), ref[:k])
+            assert np.array_equal(yl.cpu().numpy(), lo_ref)
+    assert M.device_status() == 0
+    oref = oracle.apply_csr(wo, X.astype(np.float64), compensated=True)
+    cond = oracle.apply_csr(wo, np.abs(X.astype(np.float64)), compensated=True)
+    assert np.max(np.abs(ref - oref) / np.maximum(cond, 1e-300)) <= SPLIT_RTOL
 
 
 def test_one_dimensional_fields(gpu, oracle, cfg1):
