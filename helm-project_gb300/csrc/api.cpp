@@ -297,8 +297,6 @@ SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i6
             if (u <= std::max<i64>(1, nrhs)) cands.push_back({0, static_cast<int>(t), u});
     if (nrhs == 1) cands.push_back({0, 1, 1});
     if (nrhs <= 8) cands.push_back({4, 0, 1, 2});
-    if (nrhs >= 16)
-        for (int ns : {2, 3}) cands.push_back({5, 0, 32, ns});
     cudaEvent_t e0, e1;
     AXGB_CUDA(cudaEventCreate(&e0));
     AXGB_CUDA(cudaEventCreate(&e1));

@@ -88,6 +88,11 @@ struct Batch {
     cudaEvent_t done = nullptr;
     cudaStream_t last_stream = nullptr;
     bool launched = false;
+    // side streams and events of the captured fork/join (kernels of the graph
+    // that may run concurrently)
+    static constexpr int kSide = 4;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t fork = nullptr, join[kSide] = {};
     std::mutex mu;
     ~Batch() {
         for (auto &g : graphs) {
@@ -95,6 +100,11 @@ struct Batch {
             cudaGraphDestroy(g.second.first);
         }
         if (done) cudaEventDestroy(done);
+        for (int q = 0; q < kSide; ++q) {
+            if (side[q]) cudaStreamDestroy(side[q]);
+            if (join[q]) cudaEventDestroy(join[q]);
+        }
+        if (fork) cudaEventDestroy(fork);
     }
 };
 
@@ -1517,11 +1527,26 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
             dim3 grid(nblk(g.n, 256), static_cast<unsigned>(std::min<i64>(g.nrhs, 65535)));
             k_gather_desc<<<grid, 256, 0, cap>>>(b.d_gdesc.p + i);
         }
-        blk_batch_launch(*b.blk, cap);
+        // fork: the direct persistent kernel on its own side stream, the staged
+        // class kernels over the others, joined back before the capture ends
+        if (!b.fork) {
+            AXGB_CUDA(cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming));
+            for (int q = 0; q < Batch::kSide; ++q) {
+                AXGB_CUDA(cudaStreamCreateWithFlags(&b.side[q], cudaStreamNonBlocking));
+                AXGB_CUDA(cudaEventCreateWithFlags(&b.join[q], cudaEventDisableTiming));
+            }
+        }
+        AXGB_CUDA(cudaEventRecord(b.fork, cap));
+        for (int q = 0; q < Batch::kSide; ++q) AXGB_CUDA(cudaStreamWaitEvent(b.side[q], b.fork, 0));
         if (b.total_items > 0) {
-            cudaMemsetAsync(b.counter.p, 0, sizeof(unsigned long long), cap);
-            k_batch<<<b.blocks, 256, 0, cap>>>(b.d_desc.p, static_cast<int>(b.desc.size()), b.total_items,
-                                                b.counter.p);
+            cudaMemsetAsync(b.counter.p, 0, sizeof(unsigned long long), b.side[0]);
+            k_batch<<<b.blocks, 256, 0, b.side[0]>>>(b.d_desc.p, static_cast<int>(b.desc.size()), b.total_items,
+                                                     b.counter.p);
+        }
+        blk_batch_launch(*b.blk, b.side + 1, Batch::kSide - 1);
+        for (int q = 0; q < Batch::kSide; ++q) {
+            AXGB_CUDA(cudaEventRecord(b.join[q], b.side[q]));
+            AXGB_CUDA(cudaStreamWaitEvent(cap, b.join[q], 0));
         }
         guard.open = false;
         AXGB_CUDA(cudaStreamEndCapture(cap, &g));

@@ -359,7 +359,7 @@ std::shared_ptr<BlkBatch> blk_batch_create(const std::vector<Matrix *> &mats, co
                                            const std::vector<char> &use);
 void blk_batch_set_fields(BlkBatch &bb, const float *const *x, const i64 *ldx, float *const *y, const i64 *ldy,
                           cudaStream_t s);
-void blk_batch_launch(BlkBatch &bb, cudaStream_t s);
+void blk_batch_launch(BlkBatch &bb, const cudaStream_t *streams, int n_streams);
 void slice_centroids(const MeshView &dst, Matrix &m, cudaStream_t s);
 // get_cell_areas of src/solver/weight_generator.cpp:297-312: the mesh's own
 // areas where it has them, else planar shoelace areas in degrees (nearest.cu).

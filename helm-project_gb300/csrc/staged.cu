@@ -1194,9 +1194,18 @@ void blk_batch_set_fields(BlkBatch &bb, const float *const *x, const i64 *ldx, f
     }
 }
 
-void blk_batch_launch(BlkBatch &bb, cudaStream_t s) {
-    for (auto &g : bb.groups) {
-        if (g.total == 0) continue;
+// Class groups with the most items first, spread round-robin over the
+// given streams (each group has its own work counter, so they may run
+// concurrently; a persistent launch's tail then overlaps the next one).
+void blk_batch_launch(BlkBatch &bb, const cudaStream_t *streams, int n_streams) {
+    std::vector<int> order;
+    for (size_t q = 0; q < bb.groups.size(); ++q)
+        if (bb.groups[q].total > 0) order.push_back(static_cast<int>(q));
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return bb.groups[a].total > bb.groups[b].total; });
+    for (size_t i = 0; i < order.size(); ++i) {
+        auto &g = bb.groups[order[i]];
+        cudaStream_t s = streams[i % n_streams];
         AXGB_CUDA(cudaMemsetAsync(g.counter.p, 0, sizeof(unsigned long long), s));
         if (g.us <= kUsSmall)
             persist_dispatch<kUsSmall>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
