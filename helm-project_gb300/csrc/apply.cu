@@ -371,7 +371,30 @@ __device__ __forceinline__ void split_long_row(const LongRows &L, i64 w, const f
         s[f] = 0.f;
         c[f] = 0.f;
     }
-    for (int k = lane; k < n; k += 32) {
+    // four of the leaf's entries per step: their loads are issued together
+    // (memory-level parallelism for rows of hundreds of entries), then summed
+    // in order, as one entry per step would
+    int k = lane;
+    for (; k + 96 < n; k += 128) {
+        int cq[4];
+        float hq[4], lq[4], xq[4][kLongF];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            cq[q] = L.col[b + k + 32 * q];
+            hq[q] = L.hi[b + k + 32 * q];
+            lq[q] = L.lo[b + k + 32 * q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int f = 0; f < kLongF; ++f) xq[q][f] = f < nf ? ldg_f(x + (f0 + f) * ldx + cq[q]) : 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int f = 0; f < kLongF; ++f)
+                if (f < nf) csum1(s[f], c[f], hq[q], lq[q], xq[q][f]);
+    }
+    for (; k < n; k += 32) {
         const int col = L.col[b + k];
         const float h = L.hi[b + k], l = L.lo[b + k];
 #pragma unroll
@@ -416,7 +439,26 @@ __device__ __forceinline__ void f64_long_row(const LongRows &L, i64 w, const dou
     double s[kLongF];
 #pragma unroll
     for (int f = 0; f < kLongF; ++f) s[f] = 0.0;
-    for (int k = lane; k < n; k += 32) {
+    int k = lane;
+    for (; k + 96 < n; k += 128) {  // four entries' loads in flight, summed in order
+        int cq[4];
+        double wq[4], xq[4][kLongF];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            cq[q] = L.col[b + k + 32 * q];
+            wq[q] = L.w64[b + k + 32 * q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int f = 0; f < kLongF; ++f) xq[q][f] = f < nf ? __ldg(x + (f0 + f) * ldx + cq[q]) : 0.0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int f = 0; f < kLongF; ++f)
+                if (f < nf) s[f] = fma(wq[q], xq[q][f], s[f]);
+    }
+    for (; k < n; k += 32) {
         const int col = L.col[b + k];
         const double wv = L.w64[b + k];
 #pragma unroll

@@ -185,6 +185,7 @@ struct Blocked {
     DBuf<float> hi, lo;
     std::vector<Launch> launches;
     std::vector<int> order;  // launches by size, largest first
+    std::vector<int> h_us, h_block_ids;  // host copies: staging floats per block, block ids by class
     i64 n_fallback = 0;
     DBuf<int> status;  // device status word: 1 = a bounded wait timed out
     // stream pool for concurrent class launches (fork/join on the caller's stream)

@@ -920,6 +920,9 @@ void build_blocked(Matrix &m, cudaStream_t s) {
                      [&](int p1, int p2) { return B.launches[p1].n > B.launches[p2].n; });
     B.n_blocks = nb;
     B.n_src = m.n_src;
+    B.h_us.resize(nb);
+    for (i64 b = 0; b < nb; ++b) B.h_us[b] = hb[b].us;
+    B.h_block_ids = ids;
     B.brow.upload_vec(brow, s);
     B.wbase.upload_vec(wbase, s);
     B.wlen.upload_vec(wlen, s);
@@ -1072,6 +1075,11 @@ namespace {
 
 constexpr int kBatchT = 4, kBatchNS = 2;
 constexpr i64 kBatchFChunk = 32;  // fields per work item
+// Short-row blocks (at most 8 entries a row) whose staging needs at most
+// kUsTiny floats a field (a coarse source under a fine destination) run in a
+// batch with that stride and 8 fields per stage: 16 KB of staging instead of
+// 32 KB, so more CTAs fit, and twice the work per tile.
+constexpr int kUsTiny = 256, kTinyT = 8, kTinyMaxL = 8;
 
 BlkArgs blk_args(const Blocked &B, const Blocked::Launch &l, i64 n_src) {
     BlkArgs a{};
@@ -1093,10 +1101,10 @@ BlkArgs blk_args(const Blocked &B, const Blocked::Launch &l, i64 n_src) {
     return a;
 }
 
-template <int L, int US>
+template <int L, int US, int T = kBatchT>
 void persist_launch(const BlkDesc *d, int nd, i64 total, unsigned long long *counter, cudaStream_t s) {
-    constexpr size_t bytes = sizeof(float) * US * kBatchNS * kBatchT + sizeof(int) * (US / 4);
-    auto k = k_blk_persist<L, kBatchT, kBatchNS, US>;
+    constexpr size_t bytes = sizeof(float) * US * kBatchNS * T + sizeof(int) * (US / 4);
+    auto k = k_blk_persist<L, T, kBatchNS, US>;
     AXGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
     int dev = 0, sms = 0, per = 0;
     AXGB_CUDA(cudaGetDevice(&dev));
@@ -1123,11 +1131,16 @@ void persist_dispatch(int L, const BlkDesc *d, int nd, i64 total, unsigned long 
 }  // namespace
 
 struct BlkBatch {
+    struct Part {
+        int mat, launch;
+        std::vector<int> ids;  // the launch's blocks in this group (empty: all of them)
+    };
     struct Group {
         int L = 0, us = 0;
-        std::vector<std::pair<int, int>> parts;  // (matrix index, launch index)
+        std::vector<Part> parts;
         std::vector<BlkDesc> desc;
         DBuf<BlkDesc> d_desc;
+        DBuf<int> d_ids;  // concatenated block subsets of the parts that have one
         DBuf<unsigned long long> counter;
         i64 total = 0;
     };
@@ -1142,33 +1155,65 @@ std::shared_ptr<BlkBatch> blk_batch_create(const std::vector<Matrix *> &mats, co
     bb->mats = mats;
     bb->nrhs = nrhs;
     std::map<std::pair<int, int>, int> gi;
+    auto add = [&](int L, int us, BlkBatch::Part part) {
+        auto key = std::make_pair(L, us);
+        auto it = gi.find(key);
+        if (it == gi.end()) {
+            it = gi.emplace(key, static_cast<int>(bb->groups.size())).first;
+            bb->groups.emplace_back();
+            bb->groups.back().L = L;
+            bb->groups.back().us = us;
+        }
+        bb->groups[it->second].parts.push_back(std::move(part));
+    };
     for (size_t q = 0; q < mats.size(); ++q) {
         if (!use[q] || nrhs[q] <= 0) continue;
         const Blocked &B = mats[q]->blocked;
         for (size_t li = 0; li < B.launches.size(); ++li) {
             const Blocked::Launch &l = B.launches[li];
             if (l.n == 0) continue;
-            auto key = std::make_pair(l.L, l.us);
-            auto it = gi.find(key);
-            if (it == gi.end()) {
-                it = gi.emplace(key, static_cast<int>(bb->groups.size())).first;
-                bb->groups.emplace_back();
-                bb->groups.back().L = l.L;
-                bb->groups.back().us = l.us;
+            if (l.L <= kTinyMaxL && l.us == kUsSmall && !B.h_block_ids.empty()) {
+                std::vector<int> tiny, rest;
+                for (i64 k = l.begin; k < l.begin + l.n; ++k) {
+                    const int b = B.h_block_ids[k];
+                    (B.h_us[b] <= kUsTiny ? tiny : rest).push_back(b);
+                }
+                if (!tiny.empty() && !rest.empty()) {
+                    add(l.L, kUsTiny, {static_cast<int>(q), static_cast<int>(li), std::move(tiny)});
+                    add(l.L, l.us, {static_cast<int>(q), static_cast<int>(li), std::move(rest)});
+                    continue;
+                }
+                if (!tiny.empty()) {
+                    add(l.L, kUsTiny, {static_cast<int>(q), static_cast<int>(li), {}});
+                    continue;
+                }
             }
-            bb->groups[it->second].parts.push_back({static_cast<int>(q), static_cast<int>(li)});
+            add(l.L, l.us, {static_cast<int>(q), static_cast<int>(li), {}});
         }
     }
     for (auto &g : bb->groups) {
         g.d_desc.alloc(g.parts.size());
         g.counter.alloc(1);
         g.desc.resize(g.parts.size());
+        std::vector<int> ids;
+        std::vector<i64> off(g.parts.size(), -1);
+        for (size_t i = 0; i < g.parts.size(); ++i)
+            if (!g.parts[i].ids.empty()) {
+                off[i] = static_cast<i64>(ids.size());
+                ids.insert(ids.end(), g.parts[i].ids.begin(), g.parts[i].ids.end());
+            }
+        g.d_ids.upload_vec(ids);
         i64 items = 0;
         for (size_t i = 0; i < g.parts.size(); ++i) {
-            const int q = g.parts[i].first;
+            const int q = g.parts[i].mat;
             const Blocked &B = mats[q]->blocked;
             BlkDesc &D = g.desc[i];
-            D.a = blk_args(B, B.launches[g.parts[i].second], mats[q]->n_src);
+            D.a = blk_args(B, B.launches[g.parts[i].launch], mats[q]->n_src);
+            if (off[i] >= 0) {  // a subset of the launch's blocks
+                D.a.blocks = g.d_ids.p + off[i];
+                D.a.nbl = static_cast<i64>(g.parts[i].ids.size());
+            }
+            D.a.us = g.us;
             D.a.fchunk = std::min<i64>(kBatchFChunk, nrhs[q]);
             D.nrhs = nrhs[q];
             D.item_begin = items;
@@ -1176,6 +1221,7 @@ std::shared_ptr<BlkBatch> blk_batch_create(const std::vector<Matrix *> &mats, co
         }
         g.total = items;
     }
+    AXGB_CUDA(cudaDeviceSynchronize());  // the block subsets are uploaded before any launch reads them
     return bb;
 }
 
@@ -1183,7 +1229,7 @@ void blk_batch_set_fields(BlkBatch &bb, const float *const *x, const i64 *ldx, f
                           cudaStream_t s) {
     for (auto &g : bb.groups) {
         for (size_t i = 0; i < g.parts.size(); ++i) {
-            const int q = g.parts[i].first;
+            const int q = g.parts[i].mat;
             g.desc[i].x = x[q];
             g.desc[i].ldx = ldx[q];
             g.desc[i].y = y[q];
@@ -1207,7 +1253,12 @@ void blk_batch_launch(BlkBatch &bb, const cudaStream_t *streams, int n_streams) 
         auto &g = bb.groups[order[i]];
         cudaStream_t s = streams[i % n_streams];
         AXGB_CUDA(cudaMemsetAsync(g.counter.p, 0, sizeof(unsigned long long), s));
-        if (g.us <= kUsSmall)
+        if (g.us <= kUsTiny) {
+            if (g.L <= 4)
+                persist_launch<4, kUsTiny, kTinyT>(g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
+            else
+                persist_launch<8, kUsTiny, kTinyT>(g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
+        } else if (g.us <= kUsSmall)
             persist_dispatch<kUsSmall>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
         else
             persist_dispatch<kUsLarge>(g.L, g.d_desc.p, static_cast<int>(g.desc.size()), g.total, g.counter.p, s);
