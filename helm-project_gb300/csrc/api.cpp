@@ -258,7 +258,8 @@ void check_apply(const Matrix &m, const void *x, i64 ldx, const void *y, i64 ldy
 // Valid kernel choices: variant 0 (direct; unroll 1, 2 or 4), 1 (blocked,
 // cp.async staging; 2 or 3 buffers), 2 (blocked, bulk copies; 2 buffers),
 // 1 and 2 with 2, 4 or 8 fields per stage, 3 (blocked, producer warp and
-// mbarrier ring of 2 or 3 slots, 4 fields per stage); 4 (one fused launch
+// mbarrier ring of 2 or 3 slots, or 0: per row-length class the depth that
+// lets more CTAs fit; 4 fields per stage); 4 (one fused launch
 // for few fields; the other knobs unused); 5 (segmented, lane = field, 32
 // fields per stage, 2 or 3 staging slots).
 void check_split_params(const SplitParams &p, const char *who) {
@@ -276,8 +277,8 @@ void check_split_params(const SplitParams &p, const char *who) {
     }
     AXGB_REQUIRE(p.unroll == 2 || p.unroll == 4 || p.unroll == 8, w + ": staged fields per stage must be 2, 4 or 8");
     AXGB_REQUIRE(p.variant != 3 || p.unroll == 4, w + ": variant 3 stages 4 fields at a time");
-    AXGB_REQUIRE(p.stages == 2 || (p.stages == 3 && p.variant != 2),
-                 w + ": staging buffers must be 2 (variant 2) or 2-3 (variants 1 and 3)");
+    AXGB_REQUIRE(p.stages == 2 || (p.stages == 3 && p.variant != 2) || (p.stages == 0 && p.variant == 3),
+                 w + ": staging buffers must be 2 (variant 2), 2-3 (variant 1) or 0 (per class), 2-3 (variant 3)");
 }
 
 SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs, cudaStream_t s) {
@@ -288,7 +289,8 @@ SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i6
                 if (t <= std::max<i64>(2, nrhs) && (fc == 0 || fc < nrhs)) cands.push_back({1, fc, t, ns});
     cands.push_back({2, 64, 4, 2});
     for (int fc : {128, 64, 0})
-        if (nrhs >= 8 && (fc == 0 || fc < nrhs)) cands.push_back({3, fc, 4, 3});
+        for (int ns : {3, 0})
+            if (nrhs >= 8 && (fc == 0 || fc < nrhs)) cands.push_back({3, fc, 4, ns});
     std::vector<i64> tiles = {nrhs};
     for (i64 t : {32, 8})
         if (t < nrhs) tiles.push_back(t);

@@ -11,8 +11,10 @@
 //     warp w holds rows of similar length and loops only to its own maximum;
 //   * the block's distinct source columns are rounded out to 16-byte chunks;
 //     chunk j is staged at float offset 4*j of a field's staging area, and a
-//     zero slot follows the chunks (padding entries read it);
-//   * entries are stored k-major per warp: (staging index, hi, lo).
+//     run of 32 zero floats follows the chunks (padding entries read it);
+//   * entries are stored k-major per warp: (staging index, hi, lo), in a
+//     gather schedule that spreads each step's addresses over the banks
+//     (order_entries).
 // Kernel: one CTA (4 warps) per block. Tiles of T fields are staged into
 // shared memory double-buffered, either with cp.async.cg 16-byte copies by
 // all threads (chunk variant) or with one cp.async.bulk per run of
@@ -49,6 +51,9 @@ constexpr int kPool = 4;         // streams the class launches are spread over
 // leave the sums unchanged.
 constexpr int kGroup = 4;
 const int kUsBuckets[] = {kUsSmall, kUsLarge};
+// Zero floats staged after a block's chunks, one in every shared-memory bank:
+// a padding read can then take a bank no entry of its gather step uses.
+constexpr int kZeroRun = 32;
 
 inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
 
@@ -130,6 +135,31 @@ __device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t *bar, unsigned p
     return true;
 }
 
+// Writes the zero run (kZeroRun floats at offset zero, 16-byte aligned) of
+// each of n staging areas of stride floats.
+__device__ __forceinline__ void zero_runs(float *xs, int n, int stride, int zero, int tid, int nthreads) {
+    constexpr int kPer = kZeroRun / 4;
+    for (int q = tid; q < n * kPer; q += nthreads)
+        *reinterpret_cast<float4 *>(xs + (q / kPer) * stride + zero + 4 * (q % kPer)) = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Staging indices of a thread's L entries, two 16-bit values a register
+// (an index is below the largest staging stride, 3072 + 4). Indexed with
+// compile-time k after unrolling, so the halves are selected statically.
+template <int L>
+struct PackedIdx {
+    unsigned v[(L + 1) / 2];
+    __device__ __forceinline__ int operator[](int k) const {
+        return (k & 1) ? static_cast<int>(v[k >> 1] >> 16) : static_cast<int>(v[k >> 1] & 0xffffu);
+    }
+    __device__ __forceinline__ void set(int k, int q) {
+        if (k & 1)
+            v[k >> 1] |= static_cast<unsigned>(q) << 16;
+        else
+            v[k >> 1] = static_cast<unsigned>(q);
+    }
+};
+
 struct BlkArgs {
     const int *blocks;  // block ids of this launch
     const int *brow, *wbase, *wlen;
@@ -176,7 +206,7 @@ __device__ __forceinline__ void store_lo(float *ylo, i64 ldylo, i64 f, i64 row, 
 // shared memory). Per entry the packed weights (h, -lo) are formed once for
 // the T/2 field pairs; per pair the compensated step is 9 FMA-pipe ops.
 template <int L, int T, int US>
-__device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, const float *h, const float *lw, int wl,
+__device__ __forceinline__ void reduce_tile_c(const float *cur, const PackedIdx<L> &li, const float *h, const float *lw, int wl,
                                               i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy,
                                               float *__restrict__ ylo, i64 ldylo) {
     if (f0 + T <= nrhs) {
@@ -232,7 +262,7 @@ __device__ __forceinline__ void reduce_tile_c(const float *cur, const int *li, c
 
 // Runtime-stride version used by the bulk-copy kernel.
 template <int L, int T>
-__device__ __forceinline__ void reduce_tile(const float *cur, int us, const int *li, const float *h, const float *lw,
+__device__ __forceinline__ void reduce_tile(const float *cur, int us, const PackedIdx<L> &li, const float *h, const float *lw,
                                             int wl, i64 f0, i64 nrhs, i64 row, float *__restrict__ y, i64 ldy,
                                             float *__restrict__ ylo, i64 ldylo) {
     if (f0 + T <= nrhs) {
@@ -279,7 +309,7 @@ __device__ __forceinline__ void reduce_tile(const float *cur, int us, const int 
 }
 
 template <int L>
-__device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, int *li, float *h, float *lw, int &wl,
+__device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, PackedIdx<L> &li, float *h, float *lw, int &wl,
                                              i64 &row) {
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     row = a.brow[static_cast<i64>(b) * kRows + tid];
@@ -289,11 +319,11 @@ __device__ __forceinline__ void load_entries(const BlkArgs &a, int b, int zero, 
     for (int k = 0; k < L; ++k) {
         if (k < wl) {
             int e = base + k * 32 + lane;
-            li[k] = a.lidx[e];
+            li.set(k, a.lidx[e]);
             h[k] = a.hi[e];
             lw[k] = a.lo[e];
         } else {
-            li[k] = zero;
+            li.set(k, zero);
             h[k] = 0.f;
             lw[k] = 0.f;
         }
@@ -313,13 +343,12 @@ __device__ __forceinline__ void blk_item(const BlkArgs &a, int b, const float *_
     const int c0 = a.cstart[b], nch = a.cstart[b + 1] - c0;
     const int zero = 4 * nch;
     for (int j = threadIdx.x; j < nch; j += kRows) cc[j] = a.ccol[c0 + j];
-    int li[L];
+    PackedIdx<L> li;
     float h[L], lw[L];
     int wl;
     i64 row;
     load_entries<L>(a, b, zero, li, h, lw, wl, row);
-    for (int q = threadIdx.x; q < NS * T; q += kRows)
-        *reinterpret_cast<float4 *>(xs + q * US + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
+    zero_runs(xs, NS * T, US, zero, threadIdx.x, kRows);
     __syncthreads();
     const i64 ntile = (nrhs + T - 1) / T;
     // stage(t) commits one cp.async group (empty past the end, so group
@@ -375,8 +404,21 @@ __global__ void __launch_bounds__(kRows) k_blk_chunk(BlkArgs a, const float *__r
 // warps of different lengths are thus coupled only through the NS-slot ring,
 // not by a CTA-wide barrier per tile. Every wait is bounded (about 1 s); a
 // wait that runs out sets a.status and ends the item.
+// Resident CTAs the register allocation must allow. A CTA is five warps; a
+// sub-partition's 16K registers hold 8 of them at 64 registers a thread
+// (6 CTAs), 7 at 72 (5 CTAs), 5 at 102 (4 CTAs). Short rows need few
+// registers, so their classes are held to the counts that two staging slots
+// of 1024 floats a field also allow; the long-row classes take what they
+// need.
+template <int L, int NS>
+constexpr int ws_min_blocks() {
+#ifdef WS_MINB16
+    if (L == 16 && NS == 2) return WS_MINB16;
+#endif
+    return L <= 8 ? 6 : L <= 12 ? 5 : L <= 20 ? 4 : 1;
+}
 template <int L, int T, int NS, int US>
-__global__ void __launch_bounds__(kRows + 32) k_blk_ws(BlkArgs a, const float *__restrict__ x, i64 ldx,
+__global__ void __launch_bounds__(kRows + 32, ws_min_blocks<L, NS>()) k_blk_ws(BlkArgs a, const float *__restrict__ x, i64 ldx,
                                                       float *__restrict__ y, i64 ldy, i64 nrhs) {
     static_assert(T % 2 == 0, "fields per stage must be even");
     static_assert(NS >= 2 && NS <= 3, "two or three ring slots");
@@ -392,8 +434,7 @@ __global__ void __launch_bounds__(kRows + 32) k_blk_ws(BlkArgs a, const float *_
     const int zero = 4 * nch;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int j = tid; j < nch; j += kThreads) cc[j] = a.ccol[c0 + j];
-    for (int q = tid; q < NS * T; q += kThreads)
-        *reinterpret_cast<float4 *>(xs + q * US + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
+    zero_runs(xs, NS * T, US, zero, tid, kThreads);
     if (tid == 0) {
         for (int s = 0; s < NS; ++s) {
             mbar_init(&full[s], 32);
@@ -434,7 +475,7 @@ __global__ void __launch_bounds__(kRows + 32) k_blk_ws(BlkArgs a, const float *_
         cp_async_wait<0>();
         return;
     }
-    int li[L];
+    PackedIdx<L> li;
     float h[L], lw[L];
     int wl;
     i64 row;
@@ -506,7 +547,7 @@ __global__ void __launch_bounds__(kRows) k_blk_bulk(BlkArgs a, const float *__re
     const int zero = 4 * nch;
     const int r0 = a.rstart[b], nr = a.rstart[b + 1] - r0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int li[L];
+    PackedIdx<L> li;
     float h[L], lw[L];
     int wl;
     i64 row;
@@ -517,8 +558,7 @@ __global__ void __launch_bounds__(kRows) k_blk_bulk(BlkArgs a, const float *__re
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    for (int q = threadIdx.x; q < 2 * T; q += kRows)
-        *reinterpret_cast<float4 *>(xs + q * us + zero) = make_float4(0.f, 0.f, 0.f, 0.f);
+    zero_runs(xs, 2 * T, us, zero, threadIdx.x, kRows);
     __syncthreads();
     const i64 ntile = (nrhs + T - 1) / T;
     auto issue = [&](i64 t, int buf) {
@@ -638,7 +678,8 @@ struct HostBlock {
     int rows[kRows];
     int wlen[kWarps];
     int L;                     // row-length class (multiple of 4)
-    int us;                    // 4 * chunks + 4
+    int us;                    // 4 * chunks + kZeroRun
+    bool staged;               // taken by the staged kernels (else by the direct ones)
     std::vector<int> ccol;     // chunk start columns
     std::vector<int4> runs;    // (col, chunks, staging offset, 0)
     std::vector<unsigned short> lidx;  // k-major per warp, concatenated warps
@@ -646,83 +687,203 @@ struct HostBlock {
     int wbase_rel[kWarps];
 };
 
-struct OrderScratch {
-    std::vector<int> cand[32];  // per lane: (CSR index, staging address) of the entries not yet placed
-    std::vector<int> addr[32];
+// Gather schedule of one warp: at step k each of the 32 lanes reads one
+// staged float (one of its row's entries, or a padding read of the zero run)
+// in the same shared-memory load. Lanes reading different addresses of one
+// bank serialise, so a step costs as many wavefronts as the most addresses
+// any bank holds; lanes reading one address share it.
+struct WarpSchedule {
+    struct Cand {
+        int e;     // CSR index
+        int addr;  // staging index
+    };
+    std::vector<Cand> cand[32];  // per lane: the entries not yet placed
+    int choice[32];              // index into cand for this step, -1: none
+    int bank_addr[32], bank_users[32], bank_lane[32];
+    int press[32];               // distinct unplaced addresses per bank
+    std::vector<int> extra[32];  // further addresses of a bank this step (conflicts)
+    std::vector<int> left;       // unplaced entries per staging address
+
+    void commit(int l, int ci) {
+        const int a = cand[l][ci].addr, b = a & 31;
+        if (bank_addr[b] == a) {
+            ++bank_users[b];
+        } else {
+            bank_addr[b] = a;
+            bank_users[b] = 1;
+            bank_lane[b] = l;
+        }
+        choice[l] = ci;
+    }
+    void uncommit(int l) {
+        const int b = cand[l][choice[l]].addr & 31;
+        if (--bank_users[b] == 0) bank_addr[b] = -1;
+        choice[l] = -1;
+    }
+    // Places lane l on one of its entries without a second address in any
+    // bank: an address already chosen this step, else the free bank with the
+    // most unplaced addresses (they are the hardest to spread over the
+    // remaining steps), else by moving the single lane of a bank to another
+    // of its entries (augmenting path; seen: banks already on the path).
+    bool place(int l, unsigned &seen) {
+        const auto &c = cand[l];
+        const int n = static_cast<int>(c.size());
+        for (int i = 0; i < n; ++i)
+            if (bank_addr[c[i].addr & 31] == c[i].addr) {
+                commit(l, i);
+                return true;
+            }
+        int best = -1, bp = -1;
+        for (int i = 0; i < n; ++i) {
+            const int b = c[i].addr & 31;
+            if (bank_addr[b] < 0 && press[b] > bp) {
+                bp = press[b];
+                best = i;
+            }
+        }
+        if (best >= 0) {
+            commit(l, best);
+            return true;
+        }
+        for (int i = 0; i < n; ++i) {
+            const int b = c[i].addr & 31;
+            if (seen & (1u << b)) continue;
+            seen |= 1u << b;
+            if (bank_users[b] != 1) continue;
+            const int l2 = bank_lane[b], c2 = choice[l2];
+            uncommit(l2);
+            commit(l, i);
+            if (place(l2, seen)) return true;
+            uncommit(l);
+            commit(l2, c2);
+        }
+        return false;
+    }
 };
 
-// Order of each row's entries in the block (written to perm). At step k the
-// 32 lanes of a warp gather entry k of their rows from shared memory; lanes
-// hitting one bank at different addresses serialise. For k = 0, 1, ... each
-// row (fewest remaining entries first) takes the remaining entry whose bank
-// holds the fewest other addresses so far at this step (ties: CSR order).
-// Any order gives the same compensated row sum up to its last bits; the
-// chosen one is used by every split-FP32 layout.
+// Order of each row's entries in the block (written to perm) and the warps'
+// gather schedules (q: staging index, e: CSR index or -1 for padding, per
+// warp k-major over its wlen steps). Step by step, lanes with no slack left
+// (as many entries as steps remaining) are placed first, then the others by
+// increasing slack; a lane with slack that cannot be placed without a bank
+// conflict reads padding this step instead, as do lanes whose rows are done.
+// Padding reads the zero run (kZeroRun zero floats after the chunks, one in
+// every bank), at a bank no address of the step uses when there is one. A
+// padding step of a row is exact (weight 0 on a +0 value leaves both sums
+// unchanged), so every split-FP32 layout computes the same bits from perm.
+// Blocks the staged kernels do not take (rows longer than kMaxL, or more
+// staging than kMaxUS) keep each row's CSR order (schedule = false).
 void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::vector<int> &col,
-                   const std::vector<int> &cols, std::vector<int> &perm, OrderScratch &S) {
+                   const std::vector<int> &cols, std::vector<int> &perm, std::vector<int> &q_out,
+                   std::vector<int> &e_out, WarpSchedule &S, bool schedule) {
     const int zero = 4 * static_cast<int>(cols.size());
+    q_out.clear();
+    e_out.clear();
+    if (!schedule) {
+        for (int w = 0; w < kWarps; ++w)
+            for (int lane = 0; lane < 32; ++lane) {
+                const int r = H.rows[32 * w + lane];
+                if (r >= 0)
+                    for (int k = rp[r]; k < rp[r + 1]; ++k) perm[k] = k;
+            }
+        return;
+    }
+    S.left.assign(zero + kZeroRun, 0);
     for (int w = 0; w < kWarps; ++w) {
-        int r_of[32], n_of[32], left[32];
+        int r_of[32], placed[32];
         for (int lane = 0; lane < 32; ++lane) {
             const int r = H.rows[32 * w + lane];
             r_of[lane] = r;
-            n_of[lane] = r >= 0 ? rp[r + 1] - rp[r] : 0;
-            left[lane] = n_of[lane];
+            placed[lane] = 0;
             S.cand[lane].clear();
-            S.addr[lane].clear();
-            for (int q = 0; q < n_of[lane]; ++q) {
-                const int c = col[rp[r] + q];
+            if (r < 0) continue;
+            for (int k = rp[r]; k < rp[r + 1]; ++k) {
+                const int c = col[k];
                 const int pos =
                     static_cast<int>(std::lower_bound(cols.begin(), cols.end(), c >> 2) - cols.begin());
-                S.cand[lane].push_back(rp[r] + q);
-                S.addr[lane].push_back(4 * pos + (c & 3));
+                S.cand[lane].push_back({k, 4 * pos + (c & 3)});
             }
         }
-        for (int k = 0; k < H.wlen[w]; ++k) {
-            int bank_n[32];
-            int bank_a[32][33];
-            for (int b = 0; b < 32; ++b) bank_n[b] = 0;
-            auto present = [&](int a) {
-                const int b = a & 31;
-                for (int i = 0; i < bank_n[b]; ++i)
-                    if (bank_a[b][i] == a) return true;
-                return false;
-            };
-            auto add = [&](int a) {
-                if (!present(a)) {
-                    const int b = a & 31;
-                    bank_a[b][bank_n[b]++] = a;
-                }
-            };
-            int lanes[32], nl = 0;
-            bool pad = false;
-            for (int lane = 0; lane < 32; ++lane) {
-                if (left[lane] > 0)
-                    lanes[nl++] = lane;
-                else
-                    pad = true;
+        const int W = H.wlen[w];
+        for (int b = 0; b < 32; ++b) S.press[b] = 0;
+        for (int lane = 0; lane < 32; ++lane)
+            for (auto &c : S.cand[lane])
+                if (S.left[c.addr]++ == 0) ++S.press[c.addr & 31];
+        for (int k = 0; k < W; ++k) {
+            const int rounds = W - k;
+            for (int b = 0; b < 32; ++b) {
+                S.bank_addr[b] = -1;
+                S.bank_users[b] = 0;
+                S.extra[b].clear();
             }
-            if (pad) add(zero);
-            std::stable_sort(lanes, lanes + nl, [&](int a, int b) { return left[a] < left[b]; });
-            for (int i = 0; i < nl; ++i) {
-                const int lane = lanes[i];
-                std::vector<int> &cd = S.cand[lane], &ad = S.addr[lane];
-                int best = -1, bcost = 1 << 30;
-                for (int q = 0; q < static_cast<int>(cd.size()); ++q) {
-                    if (cd[q] < 0) continue;
-                    const int cost = present(ad[q]) ? 0 : bank_n[ad[q] & 31];
-                    if (cost < bcost) {
-                        bcost = cost;
-                        best = q;
-                        if (cost == 0) break;
+            for (int lane = 0; lane < 32; ++lane) S.choice[lane] = -1;
+            int order[32], no = 0;
+            for (int lane = 0; lane < 32; ++lane)
+                if (!S.cand[lane].empty()) order[no++] = lane;
+            std::stable_sort(order, order + no, [&](int a, int b) {
+                const int sa = rounds - static_cast<int>(S.cand[a].size());
+                const int sb = rounds - static_cast<int>(S.cand[b].size());
+                if (sa != sb) return sa < sb;
+                return S.cand[a].size() > S.cand[b].size();
+            });
+            for (int i = 0; i < no; ++i) {
+                unsigned seen = 0;
+                S.place(order[i], seen);
+            }
+            // lanes left without a conflict-free entry: those with no slack
+            // take the entry costing the fewest extra wavefronts
+            for (int i = 0; i < no; ++i) {
+                const int l = order[i];
+                if (S.choice[l] >= 0 || static_cast<int>(S.cand[l].size()) < rounds) continue;
+                int best = 0, bc = 1 << 30;
+                for (int j = 0; j < static_cast<int>(S.cand[l].size()); ++j) {
+                    const int a = S.cand[l][j].addr, b = a & 31;
+                    int cost;
+                    if (S.bank_addr[b] == a || std::find(S.extra[b].begin(), S.extra[b].end(), a) != S.extra[b].end())
+                        cost = 0;
+                    else
+                        cost = (S.bank_addr[b] >= 0 ? 1 : 0) + static_cast<int>(S.extra[b].size());
+                    if (cost < bc) {
+                        bc = cost;
+                        best = j;
                     }
                 }
-                add(ad[best]);
-                perm[rp[r_of[lane]] + (n_of[lane] - left[lane])] = cd[best];
-                cd[best] = -1;
-                --left[lane];
+                const int a = S.cand[l][best].addr, b = a & 31;
+                if (S.bank_addr[b] < 0) {
+                    S.commit(l, best);
+                } else {
+                    if (S.bank_addr[b] != a && std::find(S.extra[b].begin(), S.extra[b].end(), a) == S.extra[b].end())
+                        S.extra[b].push_back(a);
+                    S.choice[l] = best;
+                }
+            }
+            // padding: one address for all padding lanes, in the least used bank
+            int pb = 0, pc = 1 << 30;
+            for (int b = 0; b < 32; ++b) {
+                const int c = (S.bank_addr[b] >= 0 ? 1 : 0) + static_cast<int>(S.extra[b].size());
+                if (c < pc) {
+                    pc = c;
+                    pb = b;
+                }
+            }
+            const int pad = zero + ((pb - zero) & 31);
+            for (int lane = 0; lane < 32; ++lane) {
+                const int ci = S.choice[lane];
+                if (ci < 0) {
+                    q_out.push_back(pad);
+                    e_out.push_back(-1);
+                    continue;
+                }
+                auto &c = S.cand[lane];
+                q_out.push_back(c[ci].addr);
+                e_out.push_back(c[ci].e);
+                perm[rp[r_of[lane]] + placed[lane]++] = c[ci].e;
+                if (--S.left[c[ci].addr] == 0) --S.press[c[ci].addr & 31];
+                c.erase(c.begin() + ci);
             }
         }
+        for (int lane = 0; lane < 32; ++lane)
+            AXGB_REQUIRE(S.cand[lane].empty(), "blocked layout: gather schedule left entries unplaced");
     }
 }
 
@@ -799,8 +960,8 @@ void build_blocked(Matrix &m, cudaStream_t s) {
     std::vector<int> perm(std::max<i64>(1, nnz));
     parallel_for_host(nb, [&](i64 b0, i64 b1) {
         std::vector<std::pair<int, int>> rl;
-        std::vector<int> cols;
-        OrderScratch scratch;
+        std::vector<int> cols, sq, se;
+        WarpSchedule scratch;
         for (i64 b = b0; b < b1; ++b) {
             HostBlock &H = hb[b];
             rl.clear();
@@ -817,8 +978,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
             cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
             H.ccol.resize(cols.size());
             for (size_t j = 0; j < cols.size(); ++j) H.ccol[j] = cols[j] * 4;
-            H.us = 4 * static_cast<int>(cols.size()) + 4;
-            const int zero = 4 * static_cast<int>(cols.size());
+            H.us = 4 * static_cast<int>(cols.size()) + kZeroRun;
             H.runs.clear();
             for (size_t j = 0; j < cols.size();) {
                 size_t j1 = j + 1;
@@ -835,30 +995,22 @@ void build_blocked(Matrix &m, cudaStream_t s) {
                 maxlen = std::max(maxlen, mx);
             }
             H.L = std::max(4, (maxlen + 3) / 4 * 4);
-            order_entries(H, rp, col, cols, perm, scratch);
-            H.lidx.clear();
-            H.hi.clear();
-            H.lo.clear();
+            H.staged = maxlen <= kMaxL && H.us <= kMaxUS;
+            order_entries(H, rp, col, cols, perm, sq, se, scratch, H.staged);
+            if (!H.staged)  // no entries stored: the direct kernels take these slices
+                for (int w = 0; w < kWarps; ++w) H.wlen[w] = 0;
+            H.lidx.resize(sq.size());
+            H.hi.resize(sq.size());
+            H.lo.resize(sq.size());
+            for (size_t i = 0; i < sq.size(); ++i) {
+                const int e = se[i];
+                H.lidx[i] = static_cast<unsigned short>(sq[i]);
+                H.hi[i] = e >= 0 ? static_cast<float>(val[e]) : 0.f;
+                H.lo[i] = e >= 0 ? static_cast<float>(val[e] - static_cast<double>(H.hi[i])) : 0.f;
+            }
             int off = 0;
             for (int w = 0; w < kWarps; ++w) {
                 H.wbase_rel[w] = off;
-                for (int k = 0; k < H.wlen[w]; ++k)
-                    for (int lane = 0; lane < 32; ++lane) {
-                        int r = H.rows[32 * w + lane];
-                        int q = zero;
-                        float hv = 0.f, lv = 0.f;
-                        if (r >= 0 && k < rp[r + 1] - rp[r]) {
-                            int e = perm[rp[r] + k];
-                            int c = col[e];
-                            size_t pos = std::lower_bound(cols.begin(), cols.end(), c >> 2) - cols.begin();
-                            q = static_cast<int>(4 * pos) + (c & 3);
-                            hv = static_cast<float>(val[e]);
-                            lv = static_cast<float>(val[e] - static_cast<double>(hv));
-                        }
-                        H.lidx.push_back(static_cast<unsigned short>(q));
-                        H.hi.push_back(hv);
-                        H.lo.push_back(lv);
-                    }
                 off += 32 * H.wlen[w];
             }
         }
@@ -886,8 +1038,7 @@ void build_blocked(Matrix &m, cudaStream_t s) {
         lidx.insert(lidx.end(), H.lidx.begin(), H.lidx.end());
         hi.insert(hi.end(), H.hi.begin(), H.hi.end());
         lo.insert(lo.end(), H.lo.begin(), H.lo.end());
-        int maxlen = *std::max_element(H.wlen, H.wlen + kWarps);
-        if (maxlen <= kMaxL && H.us <= kMaxUS) {
+        if (H.staged) {
             int ub = 0;
             while (kUsBuckets[ub] < H.us) ++ub;
             cls[{H.L, kUsBuckets[ub]}].push_back(static_cast<int>(b));
@@ -986,10 +1137,31 @@ void launch_ws_us(const BlkArgs &a, i64 grid, const float *x, i64 ldx, float *y,
     k_blk_ws<L, T, NS, US><<<static_cast<unsigned>(grid), kRows + 32, bytes, s>>>(a, x, ldx, y, ldy, nrhs);
 }
 
+// Ring depth with the most resident CTAs: three slots unless two let more
+// CTAs fit (registers, not staging memory, often bound the count). Cached
+// per instantiation.
+template <int L, int T>
+int ws_auto_stages() {
+    static int ns = 0;
+    if (ns) return ns;
+    constexpr size_t b2 = sizeof(float) * kUsSmall * 2 * T + sizeof(int) * (kUsSmall / 4);
+    constexpr size_t b3 = sizeof(float) * kUsSmall * 3 * T + sizeof(int) * (kUsSmall / 4);
+    AXGB_CUDA(cudaFuncSetAttribute(k_blk_ws<L, T, 2, kUsSmall>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(b2)));
+    AXGB_CUDA(cudaFuncSetAttribute(k_blk_ws<L, T, 3, kUsSmall>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(b3)));
+    int o2 = 0, o3 = 0;
+    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_blk_ws<L, T, 2, kUsSmall>, kRows + 32, b2));
+    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o3, k_blk_ws<L, T, 3, kUsSmall>, kRows + 32, b3));
+    ns = o3 >= o2 ? 3 : 2;
+    return ns;
+}
+
 template <int L, int T>
 void launch_ws(const BlkArgs &a, int us, int ns, i64 grid, const float *x, i64 ldx, float *y, i64 ldy, i64 nrhs,
                cudaStream_t s) {
     if (us <= kUsSmall) {
+        if (ns == 0) ns = ws_auto_stages<L, T>();
         if (ns >= 3)
             launch_ws_us<L, T, 3, kUsSmall>(a, grid, x, ldx, y, ldy, nrhs, s);
         else

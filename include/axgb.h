@@ -284,7 +284,8 @@ int axgb_set_autotune(int enable);
 
 /* Read or seed the cached kernel choice of (matrix, nrhs) that
  * axgb_apply_f32split uses: choice[4] = variant, fields_per_pass, unroll,
- * stages (staging buffers: 2 or 3 with variants 1 and 3, else 2), as
+ * stages (staging buffers: 2 or 3 with variants 1 and 3, else 2; variant 3
+ * also 0 = per row-length class the depth that lets more CTAs fit), as
  * axgb_autotune_f32split returns
  * it. Seeding lets a caller reuse a choice tuned in an earlier process
  * without timing again. When nothing is cached for (matrix, nrhs), get
