@@ -288,7 +288,7 @@ SplitParams tune_split(Matrix &m, const float *x, i64 ldx, float *y, i64 ldy, i6
             for (int fc : {0, 128, 64, 32, 16, 8})
                 if (t <= std::max<i64>(2, nrhs) && (fc == 0 || fc < nrhs)) cands.push_back({1, fc, t, ns});
     cands.push_back({2, 64, 4, 2});
-    for (int fc : {128, 64, 0})
+    for (int fc : {256, 128, 64, 0})
         for (int ns : {3, 0})
             if (nrhs >= 8 && (fc == 0 || fc < nrhs)) cands.push_back({3, fc, 4, ns});
     std::vector<i64> tiles = {nrhs};

@@ -52,8 +52,13 @@ constexpr int kPool = 4;         // streams the class launches are spread over
 constexpr int kGroup = 4;
 const int kUsBuckets[] = {kUsSmall, kUsLarge};
 // Zero floats staged after a block's chunks, one in every shared-memory bank:
-// a padding read can then take a bank no entry of its gather step uses.
+// a padding read can then take a bank no entry of its gather step uses. A
+// block whose chunks nearly fill its staging stride gets what is left (at
+// least 4 floats): zero_run_len.
 constexpr int kZeroRun = 32;
+__host__ __device__ constexpr int zero_run_len(int stride, int zero) {
+    return stride - zero < kZeroRun ? stride - zero : kZeroRun;
+}
 
 inline unsigned nblk(i64 n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
 
@@ -135,10 +140,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t *bar, unsigned p
     return true;
 }
 
-// Writes the zero run (kZeroRun floats at offset zero, 16-byte aligned) of
-// each of n staging areas of stride floats.
+// Writes the zero run (zero_run_len floats at offset zero, 16-byte aligned)
+// of each of n staging areas of stride floats.
 __device__ __forceinline__ void zero_runs(float *xs, int n, int stride, int zero, int tid, int nthreads) {
-    constexpr int kPer = kZeroRun / 4;
+    const int kPer = zero_run_len(stride, zero) / 4;
     for (int q = tid; q < n * kPer; q += nthreads)
         *reinterpret_cast<float4 *>(xs + (q / kPer) * stride + zero + 4 * (q % kPer)) = make_float4(0.f, 0.f, 0.f, 0.f);
 }
@@ -678,7 +683,8 @@ struct HostBlock {
     int rows[kRows];
     int wlen[kWarps];
     int L;                     // row-length class (multiple of 4)
-    int us;                    // 4 * chunks + kZeroRun
+    int us;                    // 4 * chunks + zero run
+    int zrun;                  // zero run length (floats)
     bool staged;               // taken by the staged kernels (else by the direct ones)
     std::vector<int> ccol;     // chunk start columns
     std::vector<int4> runs;    // (col, chunks, staging offset, 0)
@@ -767,8 +773,8 @@ struct WarpSchedule {
 // (as many entries as steps remaining) are placed first, then the others by
 // increasing slack; a lane with slack that cannot be placed without a bank
 // conflict reads padding this step instead, as do lanes whose rows are done.
-// Padding reads the zero run (kZeroRun zero floats after the chunks, one in
-// every bank), at a bank no address of the step uses when there is one. A
+// Padding reads the zero run (up to kZeroRun zero floats after the chunks,
+// one a bank), at a bank no address of the step uses when there is one. A
 // padding step of a row is exact (weight 0 on a +0 value leaves both sums
 // unchanged), so every split-FP32 layout computes the same bits from perm.
 // Blocks the staged kernels do not take (rows longer than kMaxL, or more
@@ -788,7 +794,7 @@ void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::ve
             }
         return;
     }
-    S.left.assign(zero + kZeroRun, 0);
+    S.left.assign(zero + H.zrun, 0);
     for (int w = 0; w < kWarps; ++w) {
         int r_of[32], placed[32];
         for (int lane = 0; lane < 32; ++lane) {
@@ -857,16 +863,17 @@ void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::ve
                     S.choice[l] = best;
                 }
             }
-            // padding: one address for all padding lanes, in the least used bank
-            int pb = 0, pc = 1 << 30;
-            for (int b = 0; b < 32; ++b) {
+            // padding: one address for all padding lanes, in the least used
+            // bank the zero run covers
+            int pad = zero, pc = 1 << 30;
+            for (int i = 0; i < H.zrun; ++i) {
+                const int b = (zero + i) & 31;
                 const int c = (S.bank_addr[b] >= 0 ? 1 : 0) + static_cast<int>(S.extra[b].size());
                 if (c < pc) {
                     pc = c;
-                    pb = b;
+                    pad = zero + i;
                 }
             }
-            const int pad = zero + ((pb - zero) & 31);
             for (int lane = 0; lane < 32; ++lane) {
                 const int ci = S.choice[lane];
                 if (ci < 0) {
@@ -978,7 +985,17 @@ void build_blocked(Matrix &m, cudaStream_t s) {
             cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
             H.ccol.resize(cols.size());
             for (size_t j = 0; j < cols.size(); ++j) H.ccol[j] = cols[j] * 4;
-            H.us = 4 * static_cast<int>(cols.size()) + kZeroRun;
+            {
+                const int z = 4 * static_cast<int>(cols.size());
+                int bucket = kUsBuckets[0];
+                for (int u : kUsBuckets)
+                    if (z + 4 <= u) {
+                        bucket = u;
+                        break;
+                    }
+                H.zrun = z + 4 <= kMaxUS ? zero_run_len(bucket, z) : 4;
+                H.us = z + H.zrun;
+            }
             H.runs.clear();
             for (size_t j = 0; j < cols.size();) {
                 size_t j1 = j + 1;
