@@ -358,6 +358,7 @@ def main():
     achieved = bytes_split / (ms_step / 1e3) / 1e9
     log(f"split: {ms_step:.3f} ms/step  {achieved:.0f} GB/s ({achieved / peak:.2%} of {peak_kind} {peak:.0f})")
 
+    traffic, traffic_src = profiled_traffic(tuned) if nrhs == NRHS else (None, "not the 1016-field workload")
     workload = WORKLOAD if nrhs == NRHS else f"C768->0.25deg conservative, batched split-FP32 SpMM, {nrhs} RHS"
     result = {
         "metric": METRIC if nrhs == NRHS else METRIC.replace("1016 RHS", f"{nrhs} RHS"), "value": value,
@@ -367,8 +368,10 @@ def main():
                    "kernel": tuned, "source_renumbered": M.stats()["source_renumbered"], "l2": f"inputs {4 * M.n_src * nrhs / 1e9:.1f} GB per step > L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": profiled_traffic() if nrhs == NRHS else None,
-                     "peak_kind": peak_kind, "bytes_per_step": bytes_split},
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "peak_kind": peak_kind, "bytes_per_step": bytes_split,
+                     "unit_note": "achieved = algorithmic bytes per step / CUDA-event time per step; a step's "
+                                  "class launches run concurrently, so the step is the timed unit"},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "weightgen_c768_to_0p25": {"seconds": t_gen3, "nnz": M.nnz, "pairs_per_s": M.nnz / t_gen3,
@@ -513,19 +516,26 @@ def axgb_launches(M, variant):
     return n if n > 0 else 1
 
 
-def profiled_traffic():
-    """Per-step DRAM bytes of the apply from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "apply_split_blk_chunk_c768_0p25.md")
+def profiled_traffic(tuned):
+    """Per-step DRAM bytes of the apply from the committed ncu captures
+    (profiles/apply_split_ws_c768_0p25.md: the launches of a 128- or
+    256-field step, scaled to 1016 fields, one line per kernel choice), used
+    only when a capture of the kernel choice this run uses is there; else
+    None. Returns (bytes, source)."""
+    p = os.path.join(ROOT, "profiles", "apply_split_ws_c768_0p25.md")
     if not os.path.exists(p):
-        return None
+        return None, "no capture"
+    vals = {}
     for line in open(p):
-        if line.startswith("traffic_bytes_per_step:"):
-            try:
-                return float(line.split(":", 1)[1])
-            except ValueError:
-                return None
-    return None
-
+        if line.startswith("traffic_bytes_per_step[") and "]:" in line:
+            k, v = line[len("traffic_bytes_per_step["):].split("]:", 1)
+            vals[k.strip()] = v.strip()
+    want = ",".join(str(tuned[k]) for k in ("variant", "fields_per_pass", "unroll", "stages"))
+    if want not in vals:
+        return None, f"the committed captures are of kernels {sorted(vals)}, this run uses {want}"
+    return float(vals[want]), ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 128- or 256-field step "
+                               "of the same kernel choice, scaled to 1016 fields "
+                               "(profiles/apply_split_ws_c768_0p25.md)")
 
 def e2e_alloc(M, X):
     """Pinned host copies of the headline fields and outputs, made before the
