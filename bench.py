@@ -589,7 +589,7 @@ def link_floor_ms(M, Xh, Yh, reps=3):
 def e2e_run(M, bufs, args):
     import axgb
     Xh, Yh, nrhs = bufs
-    steps = max(3, min(args.steps, 5))
+    steps = max(7, min(args.steps, 9))
     for _ in range(1):
         axgb.batch_apply_host_f32split(M, Xh, Yh)
     t = []
@@ -597,12 +597,16 @@ def e2e_run(M, bufs, args):
         t0 = time.perf_counter()
         axgb.batch_apply_host_f32split(M, Xh, Yh)
         t.append(time.perf_counter() - t0)
-    s = statistics.mean(t)
+    s = statistics.median(t)
     floor = link_floor_ms(M, Xh, Yh)
     return {"value": M.n_dst * nrhs / s, "unit": UNIT, "h2d_bytes_per_step": 4 * M.n_src * nrhs,
-            "d2h_bytes_per_step": 4 * M.n_dst * nrhs, "ms_per_step": 1e3 * s, "nrhs": nrhs,
+            "d2h_bytes_per_step": 4 * M.n_dst * nrhs, "ms_per_step": 1e3 * s, "ms_min": 1e3 * min(t),
+            "ms_samples": [round(1e3 * v, 2) for v in t], "nrhs": nrhs,
             "link_floor_ms": floor, "frac_of_link_floor": floor / (1e3 * s),
-            "link_floor": "the same bytes by plain chunked copies, host->device and device->host concurrently",
+            "link_floor": "the same bytes by plain chunked copies, host->device and device->host concurrently "
+                          "(best of 4)",
+            "timing": "median of the timed calls (the host link is shared with other jobs on the machine: "
+                      "single calls vary; ms_min is the fastest)",
             "api": "axgb_batch_apply_host_f32split (pinned host buffers)"}
 
 
@@ -884,6 +888,26 @@ def small_configs(o):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
+    flush = None
+
+    def cold_time(fn, reps=20):
+        """Device time per call with L2 flushed before each call (a 256 MB
+        write), events around the call alone."""
+        nonlocal flush
+        if flush is None:
+            flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+        for _ in range(3):
+            fn()
+        tot = 0.0
+        for _ in range(reps):
+            flush.fill_(1.0)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps
+
     def graph_time(fn, reps=20):
         """Device time per call of fn with the host out of the loop: reps
         calls captured in one CUDA graph, replayed."""
@@ -945,6 +969,8 @@ def small_configs(o):
     ms_d = dev_time(lambda: axgb.apply_f64(M, x64, y64))
     ms_s_g = graph_time(lambda: axgb.apply_f32split(M, x32, y32))
     ms_d_g = graph_time(lambda: axgb.apply_f64(M, x64, y64))
+    ms_s_c = cold_time(lambda: axgb.apply_f32split(M, x32, y32))
+    ms_d_c = cold_time(lambda: axgb.apply_f64(M, x64, y64))
     wo = o.conservative(src, dst)
     ref = o.apply_csr(wo, x64.cpu().numpy(), compensated=True)
     cond = o.apply_csr(wo, np.abs(x64.cpu().numpy()), compensated=True)
@@ -983,8 +1009,12 @@ def small_configs(o):
         "split_ms": ms_s, "fp64_ms": ms_d, "split_speedup": ms_d / ms_s,
         "split_ms_graph": ms_s_g, "fp64_ms_graph": ms_d_g, "split_speedup_graph": ms_d_g / ms_s_g,
         "split_GBps_graph": bytes_1 / ms_s_g / 1e6,
+        "split_ms_cold": ms_s_c, "fp64_ms_cold": ms_d_c, "split_GBps_cold": bytes_1 / ms_s_c / 1e6,
+        "split_frac_cold": bytes_1 / ms_s_c / 1e6 / peaks()[0],
         "timing": "split_ms / fp64_ms: one Python call each, back to back (host call overhead included); "
-                  "*_graph: the same calls captured in a CUDA graph and replayed (device time per call)",
+                  "*_graph: the same calls captured in a CUDA graph and replayed (device time per call; the "
+                  f"{bytes_1 / 1e6:.1f} MB working set stays in L2 across calls); *_cold: one call after a 256 MB "
+                  "write that flushes L2, events around the call alone",
         "split_kernel": axgb.get_kernel_choice(M, 1),
         "split": e_s, "fp64": e_d,
         "conservation_split": axgb.check_conservation(M, x32[0], y32[0])["relative_error"],

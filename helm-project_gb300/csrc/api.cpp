@@ -382,10 +382,17 @@ SplitParams default_split_params(i64 nrhs) {
         p.stages = 2;
         return p;
     }
+    if (nrhs >= 8) {  // producer-warp staged kernel, ring depth per row-length class
+        p.variant = 3;
+        p.fields_per_pass = 128;
+        p.stages = 0;
+        p.unroll = 4;
+        return p;
+    }
     p.variant = 1;
     p.fields_per_pass = 64;
     p.stages = 2;
-    p.unroll = nrhs >= 8 ? 8 : 4;
+    p.unroll = 4;
     return p;
 }
 

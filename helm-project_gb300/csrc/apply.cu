@@ -342,6 +342,7 @@ __global__ void __launch_bounds__(256) k_f64_rows(SellArgs a, const double *__re
 }
 
 constexpr i64 kFusedMaxF64 = 2;  // FP64 applies of at most this many fields take the fused kernel
+constexpr int kFusedK = 4;        // entries a row of the fused kernels loads before gathering
 
 struct LongRows {
     const int *row, *ptr, *col;
@@ -352,32 +353,50 @@ struct LongRows {
     i64 ldylo;
 };
 constexpr int kLongF = 8;  // fields per warp in the long-row kernels
+constexpr int kLongQ1 = 8;  // entries a lane loads ahead in a single-field long row
 
 // Warp w: long row w % n, fields [F*(w / n), ...). Lane j sums entries
 // j, j+32, ... of the row for each of the F fields (leaves), then a
 // butterfly over lane offsets 1..16 combines the leaves; lane f stores
 // field f.
+template <int F = kLongF>
 __device__ __forceinline__ void split_long_row(const LongRows &L, i64 w, const float *x, i64 ldx, float *y,
                                                i64 ldy, i64 nrhs) {
     const int lane = threadIdx.x & 31;
     const i64 i = w % L.n, fc = w / L.n;
     const i64 row = L.row[i];
     const int b = L.ptr[i], n = L.ptr[i + 1] - b;
-    const i64 f0 = fc * kLongF;
-    const int nf = static_cast<int>(nrhs - f0 < kLongF ? nrhs - f0 : kLongF);
-    float s[kLongF], c[kLongF];
+    const i64 f0 = fc * F;
+    const int nf = static_cast<int>(nrhs - f0 < F ? nrhs - f0 : F);
+    float s[F], c[F];
 #pragma unroll
-    for (int f = 0; f < kLongF; ++f) {
+    for (int f = 0; f < F; ++f) {
         s[f] = 0.f;
         c[f] = 0.f;
     }
-    // four of the leaf's entries per step: their loads are issued together
-    // (memory-level parallelism for rows of hundreds of entries), then summed
-    // in order, as one entry per step would
+    // four of the leaf's entries per step (kLongQ1 for a single field): their
+    // loads are issued together (memory-level parallelism for rows of
+    // hundreds of entries), then summed in order, as one entry per step would
     int k = lane;
+    if (nf == 1) {  // warp-uniform
+        for (; k + 32 * (kLongQ1 - 1) < n; k += 32 * kLongQ1) {
+            int cq[kLongQ1];
+            float hq[kLongQ1], lq[kLongQ1], xq[kLongQ1];
+#pragma unroll
+            for (int q = 0; q < kLongQ1; ++q) {
+                cq[q] = L.col[b + k + 32 * q];
+                hq[q] = L.hi[b + k + 32 * q];
+                lq[q] = L.lo[b + k + 32 * q];
+            }
+#pragma unroll
+            for (int q = 0; q < kLongQ1; ++q) xq[q] = ldg_f(x + f0 * ldx + cq[q]);
+#pragma unroll
+            for (int q = 0; q < kLongQ1; ++q) csum1(s[0], c[0], hq[q], lq[q], xq[q]);
+        }
+    }
     for (; k + 96 < n; k += 128) {
         int cq[4];
-        float hq[4], lq[4], xq[4][kLongF];
+        float hq[4], lq[4], xq[4][F];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             cq[q] = L.col[b + k + 32 * q];
@@ -387,22 +406,22 @@ __device__ __forceinline__ void split_long_row(const LongRows &L, i64 w, const f
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int f = 0; f < kLongF; ++f) xq[q][f] = f < nf ? ldg_f(x + (f0 + f) * ldx + cq[q]) : 0.f;
+            for (int f = 0; f < F; ++f) xq[q][f] = f < nf ? ldg_f(x + (f0 + f) * ldx + cq[q]) : 0.f;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int f = 0; f < kLongF; ++f)
+            for (int f = 0; f < F; ++f)
                 if (f < nf) csum1(s[f], c[f], hq[q], lq[q], xq[q][f]);
     }
     for (; k < n; k += 32) {
         const int col = L.col[b + k];
         const float h = L.hi[b + k], l = L.lo[b + k];
 #pragma unroll
-        for (int f = 0; f < kLongF; ++f)
+        for (int f = 0; f < F; ++f)
             if (f < nf) csum1(s[f], c[f], h, l, ldg_f(x + (f0 + f) * ldx + col));
     }
 #pragma unroll
-    for (int f = 0; f < kLongF; ++f) {
+    for (int f = 0; f < F; ++f) {
         if (f < nf) {  // warp-uniform
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
@@ -428,21 +447,37 @@ __global__ void __launch_bounds__(256) k_split_long(LongRows L, const float *__r
 
 // FP64 form of split_long_row: leaves summed with fma in entry order, then
 // the butterfly with plain additions.
+template <int F = kLongF>
 __device__ __forceinline__ void f64_long_row(const LongRows &L, i64 w, const double *x, i64 ldx, double *y,
                                              i64 ldy, i64 nrhs) {
     const int lane = threadIdx.x & 31;
     const i64 i = w % L.n, fc = w / L.n;
     const i64 row = L.row[i];
     const int b = L.ptr[i], n = L.ptr[i + 1] - b;
-    const i64 f0 = fc * kLongF;
-    const int nf = static_cast<int>(nrhs - f0 < kLongF ? nrhs - f0 : kLongF);
-    double s[kLongF];
+    const i64 f0 = fc * F;
+    const int nf = static_cast<int>(nrhs - f0 < F ? nrhs - f0 : F);
+    double s[F];
 #pragma unroll
-    for (int f = 0; f < kLongF; ++f) s[f] = 0.0;
+    for (int f = 0; f < F; ++f) s[f] = 0.0;
     int k = lane;
+    if (nf == 1) {  // kLongQ1 entries' loads in flight for a single field, as split_long_row
+        for (; k + 32 * (kLongQ1 - 1) < n; k += 32 * kLongQ1) {
+            int cq[kLongQ1];
+            double wq[kLongQ1], xq[kLongQ1];
+#pragma unroll
+            for (int q = 0; q < kLongQ1; ++q) {
+                cq[q] = L.col[b + k + 32 * q];
+                wq[q] = L.w64[b + k + 32 * q];
+            }
+#pragma unroll
+            for (int q = 0; q < kLongQ1; ++q) xq[q] = __ldg(x + f0 * ldx + cq[q]);
+#pragma unroll
+            for (int q = 0; q < kLongQ1; ++q) s[0] = fma(wq[q], xq[q], s[0]);
+        }
+    }
     for (; k + 96 < n; k += 128) {  // four entries' loads in flight, summed in order
         int cq[4];
-        double wq[4], xq[4][kLongF];
+        double wq[4], xq[4][F];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             cq[q] = L.col[b + k + 32 * q];
@@ -451,22 +486,22 @@ __device__ __forceinline__ void f64_long_row(const LongRows &L, i64 w, const dou
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int f = 0; f < kLongF; ++f) xq[q][f] = f < nf ? __ldg(x + (f0 + f) * ldx + cq[q]) : 0.0;
+            for (int f = 0; f < F; ++f) xq[q][f] = f < nf ? __ldg(x + (f0 + f) * ldx + cq[q]) : 0.0;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int f = 0; f < kLongF; ++f)
+            for (int f = 0; f < F; ++f)
                 if (f < nf) s[f] = fma(wq[q], xq[q][f], s[f]);
     }
     for (; k < n; k += 32) {
         const int col = L.col[b + k];
         const double wv = L.w64[b + k];
 #pragma unroll
-        for (int f = 0; f < kLongF; ++f)
+        for (int f = 0; f < F; ++f)
             if (f < nf) s[f] = fma(wv, __ldg(x + (f0 + f) * ldx + col), s[f]);
     }
 #pragma unroll
-    for (int f = 0; f < kLongF; ++f) {
+    for (int f = 0; f < F; ++f) {
         if (f < nf) {
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) s[f] = s[f] + __shfl_xor_sync(0xffffffffu, s[f], off);
@@ -489,38 +524,70 @@ __global__ void __launch_bounds__(256) k_f64_long(LongRows L, const double *__re
 // n_lrows): one row of more than 32 entries each, for all fields, 8 at a time
 // (split_long_row / f64_long_row). Same summation order as the class
 // kernels, so the same bits, in one launch instead of one per class.
-__global__ void __launch_bounds__(256) k_split_fused(SellArgs a, LongRows L, i64 n_slices, const float *__restrict__ x,
-                                                     i64 ldx, float *__restrict__ y, i64 ldy, i64 nrhs) {
+// F: fields a long-row warp carries (the call's field count, at most
+// kLongF); few fields need few registers, so more warps fit.
+template <int F>
+__global__ void __launch_bounds__(256, F <= 2 ? 4 : 2) k_split_fused(SellArgs a, LongRows L, i64 n_slices,
+                                                                   const float *__restrict__ x, i64 ldx,
+                                                                   float *__restrict__ y, i64 ldy, i64 nrhs) {
     const int lane = threadIdx.x & 31;
-    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const i64 wg = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    // the long rows' warps come first in the grid: each is a long chain of
+    // dependent loads, and starting them with the first wave overlaps them
+    // with the short rows instead of leaving them as the tail
+    if (wg < L.n) {
+        for (i64 fc = 0; fc * F < nrhs; ++fc) split_long_row<F>(L, fc * L.n + wg, x, ldx, y, ldy, nrhs);
+        return;
+    }
+    const i64 w = wg - L.n;
     if (w < n_slices) {
         const i64 row = w * 32 + lane;
         if (row >= a.n_rows) return;
         const int n = a.rlen[row];
-        if (n > 32) return;  // a long row: its own warp below
+        if (n > 32) return;  // a long row: its own warp above
         const int e0 = a.base[w] + lane;
         for (i64 f = 0; f < nrhs; ++f) {
             const float *xf = x + f * ldx;
             float s = 0.f, c = 0.f;
-            for (int k = 0; k < n; ++k) {
-                const int e = e0 + 32 * k;
-                csum1(s, c, a.hi[e], a.lo[e], ldg_f(xf + a.col[e]));
+            // kFusedK entries at a time: their loads, then their gathers, then
+            // the compensated steps in entry order (two memory round trips a
+            // chunk instead of two an entry)
+            for (int k0 = 0; k0 < n; k0 += kFusedK) {
+                int cl[kFusedK];
+                float hv[kFusedK], lv[kFusedK], xv[kFusedK];
+#pragma unroll
+                for (int j = 0; j < kFusedK; ++j)
+                    if (k0 + j < n) {
+                        const int e = e0 + 32 * (k0 + j);
+                        cl[j] = a.col[e];
+                        hv[j] = a.hi[e];
+                        lv[j] = a.lo[e];
+                    }
+#pragma unroll
+                for (int j = 0; j < kFusedK; ++j)
+                    if (k0 + j < n) xv[j] = ldg_f(xf + cl[j]);
+#pragma unroll
+                for (int j = 0; j < kFusedK; ++j)
+                    if (k0 + j < n) csum1(s, c, hv[j], lv[j], xv[j]);
             }
             const float r = __fadd_rn(s, c);
             y[f * ldy + row] = r;
             if (a.ylo) a.ylo[f * a.ldylo + row] = sum_err(s, c, r);
         }
-        return;
     }
-    const i64 i = w - n_slices;
-    if (i >= L.n) return;
-    for (i64 fc = 0; fc * kLongF < nrhs; ++fc) split_long_row(L, fc * L.n + i, x, ldx, y, ldy, nrhs);
 }
 
-__global__ void __launch_bounds__(256) k_f64_fused(SellArgs a, LongRows L, i64 n_slices, const double *__restrict__ x,
-                                                   i64 ldx, double *__restrict__ y, i64 ldy, i64 nrhs) {
+template <int F>
+__global__ void __launch_bounds__(256, F <= 2 ? 4 : 2) k_f64_fused(SellArgs a, LongRows L, i64 n_slices,
+                                                                 const double *__restrict__ x, i64 ldx,
+                                                                 double *__restrict__ y, i64 ldy, i64 nrhs) {
     const int lane = threadIdx.x & 31;
-    const i64 w = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const i64 wg = (static_cast<i64>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (wg < L.n) {  // long rows first, as k_split_fused
+        for (i64 fc = 0; fc * F < nrhs; ++fc) f64_long_row<F>(L, fc * L.n + wg, x, ldx, y, ldy, nrhs);
+        return;
+    }
+    const i64 w = wg - L.n;
     if (w < n_slices) {
         const i64 row = w * 32 + lane;
         if (row >= a.n_rows) return;
@@ -530,17 +597,26 @@ __global__ void __launch_bounds__(256) k_f64_fused(SellArgs a, LongRows L, i64 n
         for (i64 f = 0; f < nrhs; ++f) {
             const double *xf = x + f * ldx;
             double s = 0.0;
-            for (int k = 0; k < n; ++k) {
-                const int e = e0 + 32 * k;
-                s = fma(a.w64[e], __ldg(xf + a.col[e]), s);
+            for (int k0 = 0; k0 < n; k0 += kFusedK) {  // as k_split_fused
+                int cl[kFusedK];
+                double wv[kFusedK], xv[kFusedK];
+#pragma unroll
+                for (int j = 0; j < kFusedK; ++j)
+                    if (k0 + j < n) {
+                        const int e = e0 + 32 * (k0 + j);
+                        cl[j] = a.col[e];
+                        wv[j] = a.w64[e];
+                    }
+#pragma unroll
+                for (int j = 0; j < kFusedK; ++j)
+                    if (k0 + j < n) xv[j] = __ldg(xf + cl[j]);
+#pragma unroll
+                for (int j = 0; j < kFusedK; ++j)
+                    if (k0 + j < n) s = fma(wv[j], xv[j], s);
             }
             y[f * ldy + row] = s;
         }
-        return;
     }
-    const i64 i = w - n_slices;
-    if (i >= L.n) return;
-    for (i64 fc = 0; fc * kLongF < nrhs; ++fc) f64_long_row(L, fc * L.n + i, x, ldx, y, ldy, nrhs);
 }
 
 // Row-contiguous copy of the long rows' entries (in the layout's order).
@@ -807,15 +883,30 @@ void launch_split_fused(const Matrix &m, const Sell &S, const float *x, i64 ldx,
     LongRows L = long_rows(S);
     L.ylo = ylo;
     L.ldylo = ldylo;
-    k_split_fused<<<nblk(warps * 32, 256), 256, 0, s>>>(sell_args(m, S, 0, ylo, ldylo), L, S.n_slices, x, ldx, y, ldy,
-                                                        nrhs);
+    const SellArgs a = sell_args(m, S, 0, ylo, ldylo);
+    const unsigned g = nblk(warps * 32, 256);
+    if (nrhs == 1)
+        k_split_fused<1><<<g, 256, 0, s>>>(a, L, S.n_slices, x, ldx, y, ldy, nrhs);
+    else if (nrhs == 2)
+        k_split_fused<2><<<g, 256, 0, s>>>(a, L, S.n_slices, x, ldx, y, ldy, nrhs);
+    else if (nrhs <= 4)
+        k_split_fused<4><<<g, 256, 0, s>>>(a, L, S.n_slices, x, ldx, y, ldy, nrhs);
+    else
+        k_split_fused<kLongF><<<g, 256, 0, s>>>(a, L, S.n_slices, x, ldx, y, ldy, nrhs);
 }
 void launch_f64_fused(const Matrix &m, const Sell &S, const double *x, i64 ldx, double *y, i64 ldy, i64 nrhs,
                       cudaStream_t s) {
     const i64 warps = S.n_slices + S.n_lrows;
     if (warps == 0 || nrhs == 0) return;
-    k_f64_fused<<<nblk(warps * 32, 256), 256, 0, s>>>(sell_args(m, S, 0), long_rows(S), S.n_slices, x, ldx, y, ldy,
-                                                      nrhs);
+    const SellArgs a = sell_args(m, S, 0);
+    const LongRows L = long_rows(S);
+    const unsigned g = nblk(warps * 32, 256);
+    if (nrhs == 1)
+        k_f64_fused<1><<<g, 256, 0, s>>>(a, L, S.n_slices, x, ldx, y, ldy, nrhs);
+    else if (nrhs == 2)
+        k_f64_fused<2><<<g, 256, 0, s>>>(a, L, S.n_slices, x, ldx, y, ldy, nrhs);
+    else
+        k_f64_fused<kLongF><<<g, 256, 0, s>>>(a, L, S.n_slices, x, ldx, y, ldy, nrhs);
 }
 
 template <int L>

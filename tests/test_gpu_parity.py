@@ -267,7 +267,10 @@ def test_kernel_choice_seed_and_read(gpu, oracle, cfg1):
         gpu.set_kernel_choice(M, nrhs, variant=3, fields_per_pass=0, unroll=4, stages=4)
     with pytest.raises(gpu.InvalidArgument):
         gpu.set_kernel_choice(M, nrhs, variant=3, fields_per_pass=0, unroll=8, stages=3)
-    for v, ns in ((3, 2), (3, 3), (4, 2)):  # producer-warp ring, fused single launch
+    with pytest.raises(gpu.InvalidArgument):  # per-class ring depth is variant 3's only
+        gpu.set_kernel_choice(M, nrhs, variant=1, fields_per_pass=0, unroll=4, stages=0)
+    # producer-warp ring (2, 3 slots, or per row-length class), fused single launch
+    for v, ns in ((3, 2), (3, 3), (3, 0), (4, 2)):
         gpu.set_kernel_choice(M, nrhs, variant=v, fields_per_pass=0, unroll=4, stages=ns)
         assert np.array_equal(gpu.apply_f32split(M, X).cpu().numpy().astype(np.float64), y)
 
