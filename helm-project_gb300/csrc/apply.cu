@@ -65,11 +65,15 @@ struct Batch {
     };
     std::vector<std::shared_ptr<Matrix>> mats;
     std::vector<i64> nrhs;
+    // descriptors: the slice items (mode 0) first, then the row items
+    // (modes 1, 2); each group has its own persistent kernel and counter
     std::vector<Desc> desc;
     DBuf<Desc> d_desc;
-    DBuf<unsigned long long> counter;
-    i64 total_items = 0;
-    int blocks = 0;
+    DBuf<unsigned long long> counter;  // [0]: slice items, [1]: row items
+    i64 total_items = 0;               // both groups
+    i64 total_slice_items = 0, total_row_items = 0;
+    int n_slice_desc = 0;
+    int blocks_slices = 0, blocks_rows = 0;
     // matrices whose fields take the persistent staged kernels (blocked
     // layout) in the current plan, and that plan
     std::vector<char> use;
@@ -90,7 +94,7 @@ struct Batch {
     bool launched = false;
     // side streams and events of the captured fork/join (kernels of the graph
     // that may run concurrently)
-    static constexpr int kSide = 4;
+    static constexpr int kSide = 5;
     cudaStream_t side[kSide] = {};
     cudaEvent_t fork = nullptr, join[kSide] = {};
     std::mutex mu;
@@ -354,6 +358,7 @@ struct LongRows {
 };
 constexpr int kLongF = 8;  // fields per warp in the long-row kernels
 constexpr int kLongQ1 = 8;  // entries a lane loads ahead in a single-field long row
+constexpr int kBatchLongF = 4;  // fields per long-row item of the persistent batch kernel (k_batch<true>)
 
 // Warp w: long row w % n, fields [F*(w / n), ...). Lane j sums entries
 // j, j+32, ... of the row for each of the F fields (leaves), then a
@@ -1187,7 +1192,15 @@ double *noalloc_scratch() {
 // Items of all matrices are handed out by one atomic counter (no waiting):
 // item -> (matrix, tile, slice). Entries of up to 32 per row are cached in
 // registers; longer rows are read from global memory.
-__global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ desc, int n_desc, i64 total,
+// ROWS: the row items (modes 1, 2), else the slice items (mode 0). The two
+// run as separate kernels: the slice items cache 16 entries a lane and need
+// about 128 registers (two blocks an SM); the row items are chains of
+// dependent gathers that want warps, so their kernel carries four fields a
+// long-row item and is held to 64 registers, four blocks an SM (measured on
+// the 17-pair batch: 1.14 ms, against 1.18 ms at three blocks, 1.23 ms with
+// two fields an item at five, 1.45 ms with eight fields at two).
+template <bool ROWS>
+__global__ void __launch_bounds__(256, ROWS ? 4 : 2) k_batch(const Batch::Desc *__restrict__ desc, int n_desc, i64 total,
                                                unsigned long long *counter) {
     const int lane = threadIdx.x & 31;
     while (true) {
@@ -1199,6 +1212,7 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
         while (m + 1 < n_desc && desc[m + 1].item_begin <= static_cast<i64>(it)) ++m;
         const Batch::Desc &d = desc[m];
         const i64 local = static_cast<i64>(it) - d.item_begin;
+        if constexpr (ROWS) {
         if (d.mode == 2) {  // rows of more than 32 entries
             LongRows L{};
             L.row = d.lrow;
@@ -1208,7 +1222,7 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
             L.lo = d.llo;
             L.w64 = nullptr;
             L.n = d.n_ids;
-            split_long_row(L, local, d.x, d.ldx, d.y, d.ldy, d.nrhs);
+            split_long_row<kBatchLongF>(L, local, d.x, d.ldx, d.y, d.ldy, d.nrhs);
             continue;
         }
         if (d.mode == 1) {  // short rows of long-class slices: lane = field
@@ -1234,6 +1248,7 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
             }
             continue;
         }
+        } else {
         const i64 t = local / d.n_ids;
         const i64 sid = d.ids[local - t * d.n_ids];
         const i64 row = sid * 32 + lane;
@@ -1268,6 +1283,7 @@ __global__ void __launch_bounds__(256) k_batch(const Batch::Desc *__restrict__ d
                 csum1(s, cc, d.hi[e], d.lo[e], __ldg(xf + d.col[e]));
             }
             if (store) d.y[f * d.ldy + row] = __fadd_rn(s, cc);
+        }
         }
     }
 }
@@ -1485,9 +1501,11 @@ std::shared_ptr<Batch> batch_create(const std::vector<std::shared_ptr<Matrix>> &
     AXGB_CUDA(cudaGetDevice(&dev));
     AXGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int per_sm = 0;
-    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, 256, 0));
-    b->blocks = std::max(1, sms * std::max(1, per_sm));
-    b->counter.alloc(1);
+    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<false>, 256, 0));
+    b->blocks_slices = std::max(1, sms * std::max(1, per_sm));
+    AXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<true>, 256, 0));
+    b->blocks_rows = std::max(1, sms * std::max(1, per_sm));
+    b->counter.alloc(2);
     return b;
 }
 
@@ -1499,11 +1517,16 @@ namespace {
 void plan_direct(Batch &b) {
     b.desc.clear();
     i64 items = 0;
+    b.n_slice_desc = 0;
+    b.total_slice_items = 0;
+    for (int group = 0; group < 2; ++group) {  // slice items (mode 0), then row items (modes 1, 2)
+    items = 0;
     for (size_t q = 0; q < b.mats.size(); ++q) {
         Matrix &m = *b.mats[q];
         const Sell &S = m.sell32;
         const i64 k = b.nrhs[q];
         for (int mode = 0; mode < 3; ++mode) {
+            if ((mode == 0) != (group == 0)) continue;
             Batch::Desc d{};
             d.base = S.base.p;
             d.len = nullptr;
@@ -1537,14 +1560,21 @@ void plan_direct(Batch &b) {
             }
             const i64 n_items = mode == 0   ? d.n_tiles * d.n_ids
                                 : mode == 1 ? d.n_ids * 32 * ((k + 31) / 32)
-                                            : d.n_ids * ((k + kLongF - 1) / kLongF);
+                                            : d.n_ids * ((k + kBatchLongF - 1) / kBatchLongF);
             if (n_items == 0) continue;
             d.item_begin = items;
             items += n_items;
             b.desc.push_back(d);
         }
     }
-    b.total_items = items;
+    if (group == 0) {
+        b.n_slice_desc = static_cast<int>(b.desc.size());
+        b.total_slice_items = items;
+    } else {
+        b.total_row_items = items;
+    }
+    }
+    b.total_items = b.total_slice_items + b.total_row_items;
     b.d_desc.alloc(std::max<size_t>(1, b.desc.size()));
 }
 
@@ -1673,12 +1703,18 @@ void batch_apply(Batch &b, const float *const *x, const i64 *ldx, float *const *
         }
         AXGB_CUDA(cudaEventRecord(b.fork, cap));
         for (int q = 0; q < Batch::kSide; ++q) AXGB_CUDA(cudaStreamWaitEvent(b.side[q], b.fork, 0));
-        if (b.total_items > 0) {
-            cudaMemsetAsync(b.counter.p, 0, sizeof(unsigned long long), b.side[0]);
-            k_batch<<<b.blocks, 256, 0, b.side[0]>>>(b.d_desc.p, static_cast<int>(b.desc.size()), b.total_items,
-                                                     b.counter.p);
+        if (b.total_row_items > 0) {  // the row items (long chains of gathers) on their own side stream
+            AXGB_CUDA(cudaMemsetAsync(b.counter.p + 1, 0, sizeof(unsigned long long), b.side[0]));
+            k_batch<true><<<b.blocks_rows, 256, 0, b.side[0]>>>(
+                b.d_desc.p + b.n_slice_desc, static_cast<int>(b.desc.size()) - b.n_slice_desc, b.total_row_items,
+                b.counter.p + 1);
         }
-        blk_batch_launch(*b.blk, b.side + 1, Batch::kSide - 1);
+        if (b.total_slice_items > 0) {
+            AXGB_CUDA(cudaMemsetAsync(b.counter.p, 0, sizeof(unsigned long long), b.side[1]));
+            k_batch<false><<<b.blocks_slices, 256, 0, b.side[1]>>>(b.d_desc.p, b.n_slice_desc, b.total_slice_items,
+                                                                   b.counter.p);
+        }
+        blk_batch_launch(*b.blk, b.side + 2, Batch::kSide - 2);
         for (int q = 0; q < Batch::kSide; ++q) {
             AXGB_CUDA(cudaEventRecord(b.join[q], b.side[q]));
             AXGB_CUDA(cudaStreamWaitEvent(cap, b.join[q], 0));
