@@ -330,9 +330,11 @@ int axgb_batch_apply_host_f32split(int matrix_handle, const float *src, int64_t 
 
 /* ─── Many grid pairs in one persistent launch ───────────────────────────
  * A batch groups k matrices, each with its own field count. axgb_batch_apply
- * runs all of them (split-FP32) in one persistent kernel fed by a work queue
- * over (matrix, row slice, field tile) items, replayed from a CUDA graph
- * captured on first use per stream and per pointer set. A batch's graphs
+ * runs all of them (split-FP32) in persistent kernels fed by work queues: one
+ * per row-length class of the staged layout over (matrix, field chunk, block)
+ * items, and two direct ones over the rows and slices that layout leaves out,
+ * replayed from a CUDA graph captured on first use per stream and per
+ * pointer set. A batch's graphs
  * share its work counters and descriptors: a call on another stream than
  * the previous call's waits on the GPU for the previous call's work, so one
  * batch never runs on two streams at once. No reference counterpart: the
