@@ -35,7 +35,7 @@ UNITS = [
     ("bilinear.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["api.cpp", "esmf_io.cpp"]  # host C++ (g++)
-HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", "lbvh.cuh", os.path.join("..", "..", "include", "axgb.h")]
+HEADERS = ["internal.hpp", "geom.cuh", "fp32x2.cuh", "lbvh.cuh", "gather_schedule.hpp", os.path.join("..", "..", "include", "axgb.h")]
 
 
 def _nvcc():

@@ -29,6 +29,7 @@
 #include <thread>
 
 #include "fp32x2.cuh"
+#include "gather_schedule.hpp"
 #include "internal.hpp"
 
 namespace axgb {
@@ -693,92 +694,15 @@ struct HostBlock {
     int wbase_rel[kWarps];
 };
 
-// Gather schedule of one warp: at step k each of the 32 lanes reads one
-// staged float (one of its row's entries, or a padding read of the zero run)
-// in the same shared-memory load. Lanes reading different addresses of one
-// bank serialise, so a step costs as many wavefronts as the most addresses
-// any bank holds; lanes reading one address share it.
-struct WarpSchedule {
-    struct Cand {
-        int e;     // CSR index
-        int addr;  // staging index
-    };
-    std::vector<Cand> cand[32];  // per lane: the entries not yet placed
-    int choice[32];              // index into cand for this step, -1: none
-    int bank_addr[32], bank_users[32], bank_lane[32];
-    int press[32];               // distinct unplaced addresses per bank
-    std::vector<int> extra[32];  // further addresses of a bank this step (conflicts)
-    std::vector<int> left;       // unplaced entries per staging address
-
-    void commit(int l, int ci) {
-        const int a = cand[l][ci].addr, b = a & 31;
-        if (bank_addr[b] == a) {
-            ++bank_users[b];
-        } else {
-            bank_addr[b] = a;
-            bank_users[b] = 1;
-            bank_lane[b] = l;
-        }
-        choice[l] = ci;
-    }
-    void uncommit(int l) {
-        const int b = cand[l][choice[l]].addr & 31;
-        if (--bank_users[b] == 0) bank_addr[b] = -1;
-        choice[l] = -1;
-    }
-    // Places lane l on one of its entries without a second address in any
-    // bank: an address already chosen this step, else the free bank with the
-    // most unplaced addresses (they are the hardest to spread over the
-    // remaining steps), else by moving the single lane of a bank to another
-    // of its entries (augmenting path; seen: banks already on the path).
-    bool place(int l, unsigned &seen) {
-        const auto &c = cand[l];
-        const int n = static_cast<int>(c.size());
-        for (int i = 0; i < n; ++i)
-            if (bank_addr[c[i].addr & 31] == c[i].addr) {
-                commit(l, i);
-                return true;
-            }
-        int best = -1, bp = -1;
-        for (int i = 0; i < n; ++i) {
-            const int b = c[i].addr & 31;
-            if (bank_addr[b] < 0 && press[b] > bp) {
-                bp = press[b];
-                best = i;
-            }
-        }
-        if (best >= 0) {
-            commit(l, best);
-            return true;
-        }
-        for (int i = 0; i < n; ++i) {
-            const int b = c[i].addr & 31;
-            if (seen & (1u << b)) continue;
-            seen |= 1u << b;
-            if (bank_users[b] != 1) continue;
-            const int l2 = bank_lane[b], c2 = choice[l2];
-            uncommit(l2);
-            commit(l, i);
-            if (place(l2, seen)) return true;
-            uncommit(l);
-            commit(l2, c2);
-        }
-        return false;
-    }
-};
-
 // Order of each row's entries in the block (written to perm) and the warps'
 // gather schedules (q: staging index, e: CSR index or -1 for padding, per
-// warp k-major over its wlen steps). Step by step, lanes with no slack left
-// (as many entries as steps remaining) are placed first, then the others by
-// increasing slack; a lane with slack that cannot be placed without a bank
-// conflict reads padding this step instead, as do lanes whose rows are done.
+// warp k-major over its wlen steps), by WarpSchedule (gather_schedule.hpp).
 // Padding reads the zero run (up to kZeroRun zero floats after the chunks,
-// one a bank), at a bank no address of the step uses when there is one. A
-// padding step of a row is exact (weight 0 on a +0 value leaves both sums
-// unchanged), so every split-FP32 layout computes the same bits from perm.
-// Blocks the staged kernels do not take (rows longer than kMaxL, or more
-// staging than kMaxUS) keep each row's CSR order (schedule = false).
+// one a bank). A padding step of a row is exact (weight 0 on a +0 value
+// leaves both sums unchanged), so every split-FP32 layout computes the same
+// bits from perm. Blocks the staged kernels do not take (rows longer than
+// kMaxL, or more staging than kMaxUS) keep each row's CSR order (schedule =
+// false).
 void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::vector<int> &col,
                    const std::vector<int> &cols, std::vector<int> &perm, std::vector<int> &q_out,
                    std::vector<int> &e_out, WarpSchedule &S, bool schedule) {
@@ -796,11 +720,8 @@ void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::ve
     }
     S.left.assign(zero + H.zrun, 0);
     for (int w = 0; w < kWarps; ++w) {
-        int r_of[32], placed[32];
         for (int lane = 0; lane < 32; ++lane) {
             const int r = H.rows[32 * w + lane];
-            r_of[lane] = r;
-            placed[lane] = 0;
             S.cand[lane].clear();
             if (r < 0) continue;
             for (int k = rp[r]; k < rp[r + 1]; ++k) {
@@ -810,87 +731,13 @@ void order_entries(const HostBlock &H, const std::vector<int> &rp, const std::ve
                 S.cand[lane].push_back({k, 4 * pos + (c & 3)});
             }
         }
-        const int W = H.wlen[w];
-        for (int b = 0; b < 32; ++b) S.press[b] = 0;
-        for (int lane = 0; lane < 32; ++lane)
-            for (auto &c : S.cand[lane])
-                if (S.left[c.addr]++ == 0) ++S.press[c.addr & 31];
-        for (int k = 0; k < W; ++k) {
-            const int rounds = W - k;
-            for (int b = 0; b < 32; ++b) {
-                S.bank_addr[b] = -1;
-                S.bank_users[b] = 0;
-                S.extra[b].clear();
-            }
-            for (int lane = 0; lane < 32; ++lane) S.choice[lane] = -1;
-            int order[32], no = 0;
-            for (int lane = 0; lane < 32; ++lane)
-                if (!S.cand[lane].empty()) order[no++] = lane;
-            std::stable_sort(order, order + no, [&](int a, int b) {
-                const int sa = rounds - static_cast<int>(S.cand[a].size());
-                const int sb = rounds - static_cast<int>(S.cand[b].size());
-                if (sa != sb) return sa < sb;
-                return S.cand[a].size() > S.cand[b].size();
-            });
-            for (int i = 0; i < no; ++i) {
-                unsigned seen = 0;
-                S.place(order[i], seen);
-            }
-            // lanes left without a conflict-free entry: those with no slack
-            // take the entry costing the fewest extra wavefronts
-            for (int i = 0; i < no; ++i) {
-                const int l = order[i];
-                if (S.choice[l] >= 0 || static_cast<int>(S.cand[l].size()) < rounds) continue;
-                int best = 0, bc = 1 << 30;
-                for (int j = 0; j < static_cast<int>(S.cand[l].size()); ++j) {
-                    const int a = S.cand[l][j].addr, b = a & 31;
-                    int cost;
-                    if (S.bank_addr[b] == a || std::find(S.extra[b].begin(), S.extra[b].end(), a) != S.extra[b].end())
-                        cost = 0;
-                    else
-                        cost = (S.bank_addr[b] >= 0 ? 1 : 0) + static_cast<int>(S.extra[b].size());
-                    if (cost < bc) {
-                        bc = cost;
-                        best = j;
-                    }
-                }
-                const int a = S.cand[l][best].addr, b = a & 31;
-                if (S.bank_addr[b] < 0) {
-                    S.commit(l, best);
-                } else {
-                    if (S.bank_addr[b] != a && std::find(S.extra[b].begin(), S.extra[b].end(), a) == S.extra[b].end())
-                        S.extra[b].push_back(a);
-                    S.choice[l] = best;
-                }
-            }
-            // padding: one address for all padding lanes, in the least used
-            // bank the zero run covers
-            int pad = zero, pc = 1 << 30;
-            for (int i = 0; i < H.zrun; ++i) {
-                const int b = (zero + i) & 31;
-                const int c = (S.bank_addr[b] >= 0 ? 1 : 0) + static_cast<int>(S.extra[b].size());
-                if (c < pc) {
-                    pc = c;
-                    pad = zero + i;
-                }
-            }
-            for (int lane = 0; lane < 32; ++lane) {
-                const int ci = S.choice[lane];
-                if (ci < 0) {
-                    q_out.push_back(pad);
-                    e_out.push_back(-1);
-                    continue;
-                }
-                auto &c = S.cand[lane];
-                q_out.push_back(c[ci].addr);
-                e_out.push_back(c[ci].e);
-                perm[rp[r_of[lane]] + placed[lane]++] = c[ci].e;
-                if (--S.left[c[ci].addr] == 0) --S.press[c[ci].addr & 31];
-                c.erase(c.begin() + ci);
-            }
+        AXGB_REQUIRE(S.run(H.wlen[w], zero, H.zrun, q_out, e_out),
+                     "blocked layout: gather schedule left entries unplaced");
+        for (int lane = 0; lane < 32; ++lane) {
+            const int r = H.rows[32 * w + lane];
+            if (r < 0) continue;
+            for (size_t j = 0; j < S.placed[lane].size(); ++j) perm[rp[r] + j] = S.placed[lane][j];
         }
-        for (int lane = 0; lane < 32; ++lane)
-            AXGB_REQUIRE(S.cand[lane].empty(), "blocked layout: gather schedule left entries unplaced");
     }
 }
 
