@@ -11,16 +11,19 @@
 //     warp w holds rows of similar length and loops only to its own maximum;
 //   * the block's distinct source columns are rounded out to 16-byte chunks;
 //     chunk j is staged at float offset 4*j of a field's staging area, and a
-//     run of 32 zero floats follows the chunks (padding entries read it);
+//     run of up to 32 zero floats follows the chunks (padding entries read
+//     it);
 //   * entries are stored k-major per warp: (staging index, hi, lo), in a
 //     gather schedule that spreads each step's addresses over the banks
-//     (order_entries).
-// Kernel: one CTA (4 warps) per block. Tiles of T fields are staged into
-// shared memory double-buffered, either with cp.async.cg 16-byte copies by
-// all threads (chunk variant) or with one cp.async.bulk per run of
-// consecutive chunks and field, completing on an mbarrier (bulk variant).
-// Each thread then reduces its row for the T fields with packed f32x2
-// compensated arithmetic (fp32x2.cuh).
+//     (order_entries, gather_schedule.hpp).
+// Kernels: one CTA per block (or per work item of a persistent launch).
+// Tiles of T fields are staged into shared memory ring slots: by a producer
+// warp with cp.async.cg 16-byte copies and full/empty mbarriers per slot
+// (k_blk_ws, the headline kernel), by all threads with one barrier per tile
+// (k_blk_chunk, and the persistent batch kernel k_blk_persist), or with one
+// cp.async.bulk per run of consecutive chunks and field, completing on an
+// mbarrier (k_blk_bulk). Each row warp then reduces its rows for the T fields
+// with packed f32x2 compensated arithmetic (fp32x2.cuh).
 #include <algorithm>
 #include <array>
 #include <cstdint>
